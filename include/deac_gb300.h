@@ -1,0 +1,215 @@
+/*
+ * deac_gb300.h -- C-ABI of the GB300-native DEAC engine.
+ *
+ * DEAC (differential evolution for analytic continuation) reconstructs a
+ * spectrum S(omega) from imaginary-time correlation data F(tau) +- sigma(tau)
+ * by self-adaptive differential evolution (jDE) over a population of
+ * discretised spectra ("genomes").
+ *
+ * This header is the drop-in boundary for the per-generation loop of
+ * nscottnichols/deac-cpp.  In the reference that loop is the C++ function
+ *     void deac(xoshiro256p_state*, double* imaginary_time, double* isf,
+ *               double* isf_error, double* frequency, ... 27 arguments)
+ * (src/deac/src/deac.cpp:218-229), which drives 19 C++-linkage launchers
+ * `gpu_*(cudaStream_t, ...)` (src/deac/include/deac_gpu.cuh:6-27).  The
+ * reference selects the spectral model, zero temperature, the one-sided
+ * (bosonic) genome and signed weights at compile time
+ * (src/deac/CMakeLists.txt:18-35, 98-109, 227-232); here they are fields of
+ * `deac_config`, so one library serves every variant.
+ *
+ * Conventions
+ *  - plain C types only; every function returns 0 on success or a negative
+ *    DEAC_E_* code, with a message available from deac_last_error()
+ *    (the reference asserts on CUDA return codes instead, common_gpu.hpp:51);
+ *  - host arrays are caller owned and only read/written during the call;
+ *  - a batch owns its device memory; kernels run on the stream given to
+ *    deac_batch_create (NULL = the legacy default stream);
+ *  - one host thread per batch.
+ */
+#ifndef DEAC_GB300_H
+#define DEAC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ------------------------------------------------------- */
+#define DEAC_OK 0
+#define DEAC_E_INVALID (-1)   /* bad argument or configuration */
+#define DEAC_E_CUDA (-2)      /* a CUDA runtime call failed */
+#define DEAC_E_NOMEM (-3)     /* host or device allocation failed */
+#define DEAC_E_STATE (-4)     /* call out of order (e.g. run before setup) */
+#define DEAC_E_NODEVICE (-5)  /* no usable sm_103 device */
+
+/* ---- variants ---------------------------------------------------------- */
+/* DEAC_MODEL (src/deac/CMakeLists.txt:98-109) */
+#define DEAC_MODEL_STANDARD 0
+#define DEAC_MODEL_HYPERBOLIC 1
+#define DEAC_MODEL_NORMALIZATION 2
+
+/* --spectra_type (deac.cpp:2016-2023, 2040-2058).  BDSF is the only type of
+ * the one-sided (bosonic) genome; the other four are two-sided. */
+#define DEAC_SPECTRA_SPBSF 0
+#define DEAC_SPECTRA_SPFSF 1
+#define DEAC_SPECTRA_BFULL 2
+#define DEAC_SPECTRA_FFULL 3
+#define DEAC_SPECTRA_BDSF 4
+
+/* Evaluation engines of a batch.
+ *  PLAIN_FP64: every step in FP64 in the order of the reference CUDA path;
+ *              bit-identical to the reference semantics (the default). */
+#define DEAC_ENGINE_PLAIN_FP64 0
+
+/* Everything the reference reads from its command line (deac.cpp:1926-2024)
+ * plus the compile-time variant switches. */
+typedef struct deac_config {
+    int32_t model;                 /* DEAC_MODEL_* */
+    int32_t zero_temperature;      /* ZeroT build type: K = df*exp(-tau*omega) */
+    int32_t bosonic;               /* one-sided genome (detailed balance) */
+    int32_t allow_negative_weight; /* no fabs() in the mutation */
+    int32_t spectra_type;          /* DEAC_SPECTRA_* */
+    int32_t normalize;             /* --normalize */
+    int32_t use_negative_first_moment; /* --use_negative_first_moment */
+    int32_t track_stats;           /* --track_stats */
+    double temperature;            /* -T */
+    double first_moment;           /* --first_moment (<0: unused) */
+    double third_moment;           /* --third_moment (<0: unused) */
+    double third_moment_error;     /* --third_moment_error */
+    double crossover_probability;  /* -r, initial CR */
+    double self_adapting_crossover_probability;           /* -u, tau_CR */
+    double differential_weight;                           /* -F, initial F */
+    double self_adapting_differential_weight_probability; /* -v, tau_F */
+    double self_adapting_differential_weight_shift;       /* -l, accepted and unused, as in the reference */
+    double self_adapting_differential_weight;             /* -m, accepted and unused, as in the reference */
+    double stop_minimum_fitness;   /* --stop_minimum_fitness */
+    uint64_t number_of_generations; /* -N */
+    uint64_t population_size;       /* -P */
+    uint64_t seed;                  /* --seed; the PRNG is seeded with 1407513600 + seed */
+} deac_config;
+
+/* Result of one run, as the reference reports it (deac.cpp:1592, 1677-1685,
+ * 1760-1763). */
+typedef struct deac_run_result {
+    uint64_t generation;      /* the `generation:` value of the log */
+    double minimum_fitness;   /* the `minimum_fitness:` value */
+    uint64_t best_index;      /* first member with the minimum fitness */
+    uint64_t spectrum_length; /* 2M-1 (two-sided) or M (one-sided) */
+    uint64_t stats_length;    /* generation+1 when track_stats, else 0 */
+    uint64_t population_size;
+    uint64_t genome_size;
+    uint64_t number_of_timeslices;
+    int32_t sides;            /* 2 two-sided, 1 one-sided */
+    int32_t finished;         /* 1 once the run stopped or used all generations */
+} deac_run_result;
+
+/* Fill `cfg` with the reference command-line defaults (deac.cpp:1927-2024):
+ * T=0, N=100000, P=512, CR=0.9, tau_CR=0.1, F=0.9, tau_F=0.1, stop=1.0,
+ * seed=0, standard model, two-sided, spectra_type spfsf. */
+void deac_config_default(deac_config* cfg);
+
+/* Validate a configuration against the checks the reference applies before
+ * calling deac() (deac.cpp:2093-2106, 2143-2153) and the variant rules
+ * (e.g. zero temperature needs the one-sided genome, as in the reference
+ * where the two-sided ZeroT build does not compile).  Returns DEAC_OK or
+ * DEAC_E_INVALID with the reference's message in deac_last_error(). */
+int deac_config_check(const deac_config* cfg);
+
+/* Message for the last failing call on this thread. */
+const char* deac_last_error(void);
+
+/* ---- batch engine: the deac() loop for one or many independent runs ----- */
+typedef struct deac_batch deac_batch;
+
+/* Create an empty batch on `device` that launches on `cuda_stream`
+ * (a cudaStream_t; NULL for the default stream).  Replaces the stream and
+ * buffer set-up of deac.cpp:256-301. */
+int deac_batch_create(int device, void* cuda_stream, int32_t engine, deac_batch** out);
+
+/* Add one run: the configuration plus the arrays main() hands to deac()
+ * (deac.cpp:2184-2192): tau, F(tau), sigma(tau) of length
+ * number_of_timeslices, and the frequency grid of length genome_size.
+ * Writes the run's index to *run_index. */
+int deac_batch_add_run(deac_batch* b, const deac_config* cfg,
+                       const double* imaginary_time, const double* isf,
+                       const double* isf_error, uint64_t number_of_timeslices,
+                       const double* frequency, uint64_t genome_size,
+                       uint32_t* run_index);
+
+/* Build the kernel matrices and moment terms (deac.cpp:310-401, 478-827),
+ * draw the initial populations and the per-gene PRNG state tables
+ * (deac.cpp:418-458, 1114-1135), upload everything and evaluate the initial
+ * fitness (deac.cpp:829-976).  Synchronous. */
+int deac_batch_setup(deac_batch* b);
+
+/* Enqueue up to `generations` generations of every unfinished run on the
+ * batch stream and return without waiting.  Runs that reach their stop
+ * fitness or their generation limit stop on the device. */
+int deac_batch_launch(deac_batch* b, uint64_t generations);
+
+/* Wait for the stream, then report how many runs have finished. */
+int deac_batch_sync(deac_batch* b, uint32_t* runs_finished);
+
+/* setup (if not done) + launch/sync until every run has finished. */
+int deac_batch_run(deac_batch* b);
+
+/* Number of runs in the batch. */
+int deac_batch_size(const deac_batch* b, uint32_t* runs);
+
+/* Summary of run `run` (valid once it finished). */
+int deac_batch_result(deac_batch* b, uint32_t run, deac_run_result* out);
+
+/* Outputs of run `run`, as the reference writes them (deac.cpp:1594-1717):
+ * best_dsf and best_frequency of spectrum_length doubles; the three stats
+ * arrays of stats_length doubles (only with track_stats).  Any pointer may
+ * be NULL. */
+int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf,
+                     double* best_frequency, double* stats_mean,
+                     double* stats_minimum, double* stats_squared_mean);
+
+/* Current state of run `run`: population [side][member][gene] (S*P*M
+ * doubles), fitness (P), crossover rates and differential weights
+ * ([side][member], S*P each).  Any pointer may be NULL. */
+int deac_batch_fetch_state(deac_batch* b, uint32_t run, double* population,
+                           double* fitness, double* crossover_rates,
+                           double* differential_weights);
+
+/* Record, for run `run`, the trial fitness of every member at every
+ * generation up to `max_generations` (a test aid; call before setup). */
+int deac_batch_enable_trace(deac_batch* b, uint32_t run, uint64_t max_generations);
+
+/* Copy the recorded trace: trial_fitness[g*P + i] for generations
+ * g < min(executed, max_generations). */
+int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness,
+                           uint64_t capacity);
+
+/* Device time of the kernels of the last deac_batch_launch call, per kernel
+ * kind, measured with CUDA events on the batch stream (ms). kind 0 = trial
+ * kernel, 1 = contraction kernel.  Only when timing was enabled. */
+int deac_batch_enable_timing(deac_batch* b, int32_t enable);
+int deac_batch_kernel_time(deac_batch* b, int32_t kind, double* ms, uint64_t* launches);
+
+int deac_batch_destroy(deac_batch* b);
+
+/* ---- one-call form of deac() ------------------------------------------- */
+/* Run one reconstruction to completion and return its outputs: the drop-in
+ * for deac() (deac.cpp:218-1923) minus the file writing, which the deac.e
+ * front end does.  Output arrays as in deac_batch_fetch. */
+int deac_reconstruct(const deac_config* cfg, const double* imaginary_time,
+                     const double* isf, const double* isf_error,
+                     uint64_t number_of_timeslices, const double* frequency,
+                     uint64_t genome_size, deac_run_result* result,
+                     double* best_dsf, double* best_frequency,
+                     double* stats_mean, double* stats_minimum,
+                     double* stats_squared_mean);
+
+/* Library version string. */
+const char* deac_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEAC_GB300_H */
