@@ -1,0 +1,693 @@
+// deac_engine.cu -- host side of the GB300 DEAC engine and its C-ABI
+// (include/deac_gb300.h).
+//
+// A batch holds any number of independent runs (seeds, temperatures, grids,
+// models).  Set-up builds each run's constant terms on the host in FP64
+// (deac_model.cpp), draws its initial population and per-gene PRNG table
+// exactly as the reference does (deac.cpp:418-458, 1114-1135), uploads
+// everything once and evaluates the initial fitness on the device.  Each
+// generation of all runs is then two kernel launches (deac_kernels.cu);
+// blocks of generations are captured once into a CUDA graph and replayed.
+// The stop test runs on the device, so the host never synchronises inside
+// a block -- the reference does a D2H copy and ~10 stream syncs per
+// generation (deac.cpp:1140-1147 and the deac_wait calls of 1168-1574).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "deac_gb300.h"
+#include "deac_kernels.cuh"
+#include "deac_model.hpp"
+#include "deac_rng.cuh"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(DEAC_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                               \
+    } while (0)
+
+constexpr uint64_t kGraphBlock = 16;          // generations per captured graph
+constexpr uint64_t kTrialSmemCapGenes = 20480;  // 160 KB of trial genes in shared memory
+
+uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+struct Arena {
+    uint64_t size = 0;
+    uint64_t take(uint64_t bytes) {
+        const uint64_t off = size;
+        size = align256(size + bytes);
+        return off;
+    }
+};
+
+// Device copy of a kernel matrix, shared by runs with identical inputs.
+struct KernelMatrix {
+    double* k_pos = nullptr;
+    double* k_neg = nullptr;
+};
+
+struct RunHost {
+    deac_config cfg;
+    std::vector<double> tau, isf, err, freq;
+    uint64_t Nt = 0, M = 0, P = 0;
+    int S = 2;
+    deac::Model model;
+    std::vector<double> pop0;            // [S][P][M] initial parents
+    std::vector<uint64_t> rng_table;     // 4 x n_states word-major
+    uint64_t n_states = 0;
+    uint64_t trace_cap = 0;
+    char* arena = nullptr;               // device allocation of this run
+    deac::RunDev dev{};                  // host copy of the descriptor
+    // results
+    bool finished = false;
+};
+
+}  // namespace
+
+struct deac_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;     // launch stream (caller's or own)
+    bool own_stream = false;
+    cudaStream_t capture_stream = nullptr;
+    int32_t engine = DEAC_ENGINE_PLAIN_FP64;
+    std::vector<std::unique_ptr<RunHost>> runs;
+    std::map<std::string, KernelMatrix> kcache;
+    deac::RunDev* d_runs = nullptr;
+    deac::Work* d_trial_work = nullptr;
+    deac::Work* d_contract_work = nullptr;
+    uint32_t n_trial_ctas = 0, n_contract_ctas = 0, contract_threads = 32;
+    int smem_genes = 0;
+    size_t trial_smem_bytes = 0;
+    bool set_up = false;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<deac::RunDev> status;  // host mirror of d_runs
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double kernel_ms[2] = {0.0, 0.0};
+    uint64_t kernel_launches[2] = {0, 0};
+};
+
+namespace {
+
+int launch_generation(deac_batch* b, cudaStream_t s, int init_mode) {
+    deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
+                                                                          init_mode, b->smem_genes);
+    deac::contract_kernel<<<b->n_contract_ctas, b->contract_threads, 0, s>>>(b->d_runs, b->d_contract_work,
+                                                                             init_mode);
+    return DEAC_OK;
+}
+
+int launch_generation_timed(deac_batch* b) {
+    CUDA_TRY(cudaEventRecord(b->ev[0], b->stream));
+    deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, b->stream>>>(
+        b->d_runs, b->d_trial_work, 0, b->smem_genes);
+    CUDA_TRY(cudaEventRecord(b->ev[1], b->stream));
+    deac::contract_kernel<<<b->n_contract_ctas, b->contract_threads, 0, b->stream>>>(
+        b->d_runs, b->d_contract_work, 0);
+    CUDA_TRY(cudaEventRecord(b->ev[2], b->stream));
+    CUDA_TRY(cudaEventSynchronize(b->ev[2]));
+    float a = 0.f, c = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&a, b->ev[0], b->ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(&c, b->ev[1], b->ev[2]));
+    b->kernel_ms[0] += a;
+    b->kernel_ms[1] += c;
+    b->kernel_launches[0] += 1;
+    b->kernel_launches[1] += 1;
+    return DEAC_OK;
+}
+
+std::string kernel_key(const RunHost& r) {
+    std::string k;
+    auto put = [&k](const void* p, size_t n) { k.append(static_cast<const char*>(p), n); };
+    put(&r.cfg.model, sizeof r.cfg.model);
+    put(&r.cfg.zero_temperature, sizeof r.cfg.zero_temperature);
+    put(&r.cfg.bosonic, sizeof r.cfg.bosonic);
+    put(&r.model.beta, sizeof r.model.beta);
+    put(&r.model.periodicity, sizeof r.model.periodicity);
+    put(r.tau.data(), r.tau.size() * sizeof(double));
+    put(r.freq.data(), r.freq.size() * sizeof(double));
+    return k;
+}
+
+// Host part of one run's set-up: constants, initial population, PRNG table.
+void prepare_run(RunHost& r) {
+    const deac_config& c = r.cfg;
+    deac::build_model(c, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model);
+    const uint64_t P = r.P, M = r.M;
+    const int S = r.S;
+    // initial population: one stream seeded with 1407513600 + seed
+    // (deac.cpp:2089-2091), member-major, a draw per side per gene
+    // (deac.cpp:429-446), zero frequency matched (deac.cpp:447-456)
+    deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + c.seed);
+    r.pop0.assign((uint64_t)S * P * M, 0.0);
+    for (uint64_t i = 0; i < P; ++i)
+        for (uint64_t j = 0; j < M; ++j)
+            for (int s = 0; s < S; ++s) {
+                double v = deac::to_unit(g.next());
+                if (c.allow_negative_weight) v -= 0.5;
+                r.pop0[(uint64_t)s * P * M + i * M + j] = v;
+            }
+    if (S == 2)
+        for (uint64_t i = 0; i < P; ++i) r.pop0[P * M + i * M] = r.pop0[i * M];
+    // per-gene states: state k = jump^k(generator after the initial draws)
+    // (deac.cpp:1114-1126), stored in this engine's member-major slots
+    r.n_states = P * (1 + (uint64_t)S * M);
+    r.rng_table.assign(4 * r.n_states, 0);
+    for (uint64_t k = 0; k < r.n_states; ++k) {
+        const uint64_t slot = deac::rng_slot((uint32_t)P, (uint32_t)M, (uint32_t)S, k);
+        for (int w = 0; w < 4; ++w) r.rng_table[(uint64_t)w * r.n_states + slot] = g.s[w];
+        g.jump();
+    }
+}
+
+int upload_run(deac_batch* b, RunHost& r) {
+    const uint64_t P = r.P, M = r.M, Nt = r.Nt, N = r.cfg.number_of_generations;
+    const int S = r.S;
+    const deac::Model& m = r.model;
+    // constant kernel matrix, shared between runs with the same inputs
+    const std::string key = kernel_key(r);
+    auto it = b->kcache.find(key);
+    if (it == b->kcache.end()) {
+        KernelMatrix km;
+        CUDA_TRY(cudaMalloc(&km.k_pos, Nt * M * sizeof(double)));
+        CUDA_TRY(cudaMemcpy(km.k_pos, m.k_pos.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
+        if (S == 2) {
+            CUDA_TRY(cudaMalloc(&km.k_neg, Nt * M * sizeof(double)));
+            CUDA_TRY(cudaMemcpy(km.k_neg, m.k_neg.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        it = b->kcache.emplace(key, km).first;
+    }
+
+    Arena a;
+    const uint64_t o_isf = a.take(Nt * 8), o_err = a.take(Nt * 8), o_tw = a.take(Nt * 8);
+    const uint64_t o_np = a.take(M * 8), o_nn = a.take(M * 8), o_fp = a.take(M * 8), o_fn = a.take(M * 8);
+    const uint64_t o_tp = a.take(M * 8), o_tn = a.take(M * 8);
+    const uint64_t o_pop = a.take(2ull * S * P * M * 8);
+    const uint64_t o_cur = a.take(P);
+    const uint64_t o_rng = a.take(4 * r.n_states * 8);
+    const uint64_t o_cr = a.take(2ull * S * P * 8), o_fw = a.take(2ull * S * P * 8);
+    const uint64_t o_fo = a.take(P * 8), o_fnw = a.take(P * 8);
+    const uint64_t o_E = a.take(P * Nt * 8), o_mom = a.take(2 * P * 8);
+    const uint64_t o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
+    const uint64_t o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
+    CUDA_TRY(cudaMalloc(&r.arena, a.size));
+    CUDA_TRY(cudaMemset(r.arena, 0, a.size));
+    char* base = r.arena;
+    auto up = [&](uint64_t off, const std::vector<double>& v) -> int {
+        if (!v.empty()) CUDA_TRY(cudaMemcpy(base + off, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+        return DEAC_OK;
+    };
+    int rc = DEAC_OK;
+    if ((rc = up(o_isf, r.isf)) || (rc = up(o_err, r.err)) || (rc = up(o_tw, m.tau_weight)) ||
+        (rc = up(o_np, m.norm_pos)) || (rc = up(o_nn, m.norm_neg)) || (rc = up(o_fp, m.first_pos)) ||
+        (rc = up(o_fn, m.first_neg)) || (rc = up(o_tp, m.third_pos)) || (rc = up(o_tn, m.third_neg)) ||
+        (rc = up(o_pop, r.pop0)))
+        return rc;
+    CUDA_TRY(cudaMemcpy(base + o_rng, r.rng_table.data(), r.rng_table.size() * 8, cudaMemcpyHostToDevice));
+    std::vector<double> crfw(2ull * S * P, 0.0);
+    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.crossover_probability;
+    if ((rc = up(o_cr, crfw))) return rc;
+    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
+    if ((rc = up(o_fw, crfw))) return rc;
+
+    deac::RunDev& d = r.dev;
+    d = deac::RunDev{};
+    d.P = (uint32_t)P;
+    d.M = (uint32_t)M;
+    d.Nt = (uint32_t)Nt;
+    d.S = (uint32_t)S;
+    d.flags = (r.cfg.normalize ? deac::kNormalize : 0) | (m.use_first_moment ? deac::kFirstMoment : 0) |
+              (m.use_third_moment ? deac::kThirdMoment : 0) |
+              (m.use_negative_first_moment ? deac::kNegativeFirstMoment : 0) |
+              (r.cfg.allow_negative_weight ? deac::kSignedWeights : 0) |
+              (r.cfg.track_stats ? deac::kTrackStats : 0) | (r.trace_cap ? deac::kTrace : 0);
+    d.member_tile = (uint32_t)std::min<uint64_t>(P, 256);
+    d.tau_tile = std::max<uint32_t>(1, 32 / d.member_tile);
+    const uint32_t member_tiles = (d.P + d.member_tile - 1) / d.member_tile;
+    const uint32_t tau_tiles = (d.Nt + d.tau_tile - 1) / d.tau_tile;
+    d.contract_ctas = member_tiles * tau_tiles;
+    d.N = N;
+    d.tau_cr = r.cfg.self_adapting_crossover_probability;
+    d.tau_f = r.cfg.self_adapting_differential_weight_probability;
+    d.alpha = 1.0 / m.zeroth_moment;
+    d.stop = r.cfg.stop_minimum_fitness;
+    d.first_target = r.cfg.first_moment;
+    d.third_target = r.cfg.third_moment;
+    d.third_error = r.cfg.third_moment_error;
+    d.negfirst_target = m.negative_first_moment;
+    d.negfirst_error = m.negative_first_moment_error;
+    d.k_pos = it->second.k_pos;
+    d.k_neg = it->second.k_neg;
+    auto ptr = [&](uint64_t off) { return reinterpret_cast<double*>(base + off); };
+    d.isf = ptr(o_isf);
+    d.err = ptr(o_err);
+    d.tau_w = ptr(o_tw);
+    d.norm_pos = ptr(o_np);
+    d.norm_neg = ptr(o_nn);
+    d.first_pos = ptr(o_fp);
+    d.first_neg = ptr(o_fn);
+    d.third_pos = ptr(o_tp);
+    d.third_neg = ptr(o_tn);
+    d.pop = ptr(o_pop);
+    d.cur = reinterpret_cast<uint8_t*>(base + o_cur);
+    d.rng = reinterpret_cast<uint64_t*>(base + o_rng);
+    d.n_states = r.n_states;
+    d.cr = ptr(o_cr);
+    d.fw = ptr(o_fw);
+    d.fit_old = ptr(o_fo);
+    d.fit_new = ptr(o_fnw);
+    d.model_isf = ptr(o_E);
+    d.moments = ptr(o_mom);
+    d.stats = ptr(o_stats);
+    d.trace = ptr(o_trace);
+    d.trace_cap = r.trace_cap;
+    // host copies are no longer needed
+    std::vector<uint64_t>().swap(r.rng_table);
+    return DEAC_OK;
+}
+
+int refresh_status(deac_batch* b) {
+    b->status.resize(b->runs.size());
+    CUDA_TRY(cudaMemcpyAsync(b->status.data(), b->d_runs, b->runs.size() * sizeof(deac::RunDev),
+                             cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return DEAC_OK;
+}
+
+int build_graph(deac_batch* b) {
+    if (b->graph) return DEAC_OK;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal));
+    for (uint64_t k = 0; k < kGraphBlock; ++k) launch_generation(b, b->capture_stream, 0);
+    CUDA_TRY(cudaStreamEndCapture(b->capture_stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(DEAC_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    return DEAC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* deac_last_error(void) { return g_error.c_str(); }
+
+const char* deac_version(void) { return "deac-gb300 0.1.0 (sm_103a)"; }
+
+void deac_config_default(deac_config* c) {
+    std::memset(c, 0, sizeof *c);
+    c->model = DEAC_MODEL_STANDARD;
+    c->spectra_type = DEAC_SPECTRA_SPFSF;
+    c->temperature = 0.0;
+    c->first_moment = -1.0;
+    c->third_moment = -1.0;
+    c->third_moment_error = 0.0;
+    c->crossover_probability = 0.9;
+    c->self_adapting_crossover_probability = 0.1;
+    c->differential_weight = 0.9;
+    c->self_adapting_differential_weight_probability = 0.1;
+    c->self_adapting_differential_weight_shift = 0.1;
+    c->self_adapting_differential_weight = 0.9;
+    c->stop_minimum_fitness = 1.0;
+    c->number_of_generations = 100000;
+    c->population_size = 512;
+    c->seed = 0;
+}
+
+int deac_config_check(const deac_config* c) {
+    if (!c) return fail(DEAC_E_INVALID, "null configuration");
+    const std::string msg = deac::check_config(*c);
+    if (!msg.empty()) return fail(DEAC_E_INVALID, "%s", msg.c_str());
+    return DEAC_OK;
+}
+
+int deac_batch_create(int device, void* cuda_stream, int32_t engine, deac_batch** out) {
+    if (!out) return fail(DEAC_E_INVALID, "null output pointer");
+    *out = nullptr;
+    if (engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "unknown engine %d", engine);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0)
+        return fail(DEAC_E_NODEVICE, "no CUDA device %d", device);
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(DEAC_E_NODEVICE, "device %d is sm_%d%d; this library is built for sm_103a (GB300)", device,
+                    prop.major, prop.minor);
+    CUDA_TRY(cudaSetDevice(device));
+    auto b = std::make_unique<deac_batch>();
+    b->device = device;
+    b->engine = engine;
+    if (cuda_stream) {
+        b->stream = static_cast<cudaStream_t>(cuda_stream);
+    } else {
+        CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        b->own_stream = true;
+    }
+    CUDA_TRY(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+    for (auto& e : b->ev) CUDA_TRY(cudaEventCreate(&e));
+    *out = b.release();
+    return DEAC_OK;
+}
+
+int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau, const double* isf,
+                       const double* err, uint64_t nt, const double* freq, uint64_t m, uint32_t* run_index) {
+    if (!b || !cfg || !tau || !isf || !err || !freq) return fail(DEAC_E_INVALID, "null argument");
+    if (b->set_up) return fail(DEAC_E_STATE, "runs must be added before deac_batch_setup");
+    int rc = deac_config_check(cfg);
+    if (rc) return rc;
+    if (nt < 2) return fail(DEAC_E_INVALID, "ISF input file must contain at least two timeslices");
+    if (m < 2) return fail(DEAC_E_INVALID, "genome_size must be at least 2");
+    if (cfg->population_size > (1u << 20) || m > (1u << 26) || nt > (1u << 20))
+        return fail(DEAC_E_INVALID, "problem size beyond the engine's limits");
+    if (isf[0] == 0.0 && cfg->normalize) return fail(DEAC_E_INVALID, "--normalize needs a nonzero F(0)");
+    auto r = std::make_unique<RunHost>();
+    r->cfg = *cfg;
+    r->tau.assign(tau, tau + nt);
+    r->isf.assign(isf, isf + nt);
+    r->err.assign(err, err + nt);
+    r->freq.assign(freq, freq + m);
+    r->Nt = nt;
+    r->M = m;
+    r->P = cfg->population_size;
+    r->S = cfg->bosonic ? 1 : 2;
+    if (run_index) *run_index = (uint32_t)b->runs.size();
+    b->runs.push_back(std::move(r));
+    return DEAC_OK;
+}
+
+int deac_batch_enable_trace(deac_batch* b, uint32_t run, uint64_t max_generations) {
+    if (!b || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad run index");
+    if (b->set_up) return fail(DEAC_E_STATE, "enable the trace before deac_batch_setup");
+    b->runs[run]->trace_cap = max_generations;
+    return DEAC_OK;
+}
+
+int deac_batch_setup(deac_batch* b) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    if (b->set_up) return DEAC_OK;
+    if (b->runs.empty()) return fail(DEAC_E_STATE, "empty batch");
+    CUDA_TRY(cudaSetDevice(b->device));
+    // host preparation, one thread per run (the PRNG table is a serial chain
+    // of jumps per run, as in the reference)
+    {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        std::vector<std::thread> pool;
+        size_t next = 0;
+        while (next < b->runs.size()) {
+            pool.clear();
+            for (unsigned t = 0; t < hw && next < b->runs.size(); ++t, ++next)
+                pool.emplace_back(prepare_run, std::ref(*b->runs[next]));
+            for (auto& th : pool) th.join();
+        }
+    }
+    uint64_t max_genes = 0;
+    uint32_t max_threads = 32;
+    std::vector<deac::Work> tw, cw;
+    for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+        RunHost& r = *b->runs[ri];
+        int rc = upload_run(b, r);
+        if (rc) return rc;
+        for (uint32_t i = 0; i < r.dev.P; ++i) tw.push_back({ri, i});
+        for (uint32_t k = 0; k < r.dev.contract_ctas; ++k) cw.push_back({ri, k});
+        max_threads = std::max(max_threads, r.dev.member_tile * r.dev.tau_tile);
+        const uint64_t genes = (uint64_t)r.S * r.M;
+        if (genes <= kTrialSmemCapGenes) max_genes = std::max(max_genes, genes);
+    }
+    b->contract_threads = (max_threads + 31) / 32 * 32;
+    b->smem_genes = (int)max_genes;
+    b->trial_smem_bytes = max_genes * sizeof(double);
+    CUDA_TRY(cudaFuncSetAttribute(deac::trial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
+    b->n_trial_ctas = (uint32_t)tw.size();
+    b->n_contract_ctas = (uint32_t)cw.size();
+    CUDA_TRY(cudaMalloc(&b->d_trial_work, tw.size() * sizeof(deac::Work)));
+    CUDA_TRY(cudaMalloc(&b->d_contract_work, cw.size() * sizeof(deac::Work)));
+    CUDA_TRY(cudaMemcpy(b->d_trial_work, tw.data(), tw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b->d_contract_work, cw.data(), cw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+    std::vector<deac::RunDev> descs;
+    for (auto& r : b->runs) descs.push_back(r->dev);
+    CUDA_TRY(cudaMalloc(&b->d_runs, descs.size() * sizeof(deac::RunDev)));
+    CUDA_TRY(cudaMemcpy(b->d_runs, descs.data(), descs.size() * sizeof(deac::RunDev), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaDeviceSynchronize());
+    // initial fitness, statistics of generation 0 and the first stop test
+    launch_generation(b, b->stream, 1);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->set_up = true;
+    return refresh_status(b);
+}
+
+int deac_batch_launch(deac_batch* b, uint64_t generations) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    if (b->timing) {
+        for (uint64_t g = 0; g < generations; ++g) {
+            int rc = launch_generation_timed(b);
+            if (rc) return rc;
+        }
+        CUDA_TRY(cudaGetLastError());
+        return DEAC_OK;
+    }
+    int rc = build_graph(b);
+    if (rc) return rc;
+    for (uint64_t g = 0; g < generations; g += kGraphBlock) CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+    return DEAC_OK;
+}
+
+int deac_batch_sync(deac_batch* b, uint32_t* runs_finished) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaGetLastError());
+    int rc = refresh_status(b);
+    if (rc) return rc;
+    uint32_t n = 0;
+    for (auto& s : b->status) n += s.done ? 1 : 0;
+    if (runs_finished) *runs_finished = n;
+    return DEAC_OK;
+}
+
+int deac_batch_run(deac_batch* b) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    int rc = deac_batch_setup(b);
+    if (rc) return rc;
+    uint32_t done = 0;
+    if ((rc = deac_batch_sync(b, &done))) return rc;
+    // a run needs at most N-1 generations; poll every few graph blocks
+    uint64_t block = kGraphBlock * 4;
+    while (done < b->runs.size()) {
+        if ((rc = deac_batch_launch(b, block))) return rc;
+        if ((rc = deac_batch_sync(b, &done))) return rc;
+        block = std::min<uint64_t>(block * 2, kGraphBlock * 256);
+    }
+    return DEAC_OK;
+}
+
+int deac_batch_size(const deac_batch* b, uint32_t* runs) {
+    if (!b || !runs) return fail(DEAC_E_INVALID, "null argument");
+    *runs = (uint32_t)b->runs.size();
+    return DEAC_OK;
+}
+
+// Copy a run's parents and fitness back and locate the best member.
+static int gather(deac_batch* b, uint32_t run, std::vector<double>& pop, std::vector<double>& fit,
+                  std::vector<double>* crfw, deac::RunDev& st) {
+    RunHost& r = *b->runs[run];
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    const uint64_t P = r.P, M = r.M, S = r.S;
+    std::vector<uint8_t> cur(P);
+    std::vector<double> both(2 * S * P * M);
+    fit.assign(P, 0.0);
+    CUDA_TRY(cudaMemcpy(cur.data(), st.cur, P, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(both.data(), st.pop, both.size() * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, P * 8, cudaMemcpyDeviceToHost));
+    pop.assign(S * P * M, 0.0);
+    for (uint64_t s = 0; s < S; ++s)
+        for (uint64_t i = 0; i < P; ++i)
+            std::memcpy(&pop[(s * P + i) * M], &both[((uint64_t)cur[i] * S * P + s * P + i) * M], M * 8);
+    if (crfw) {
+        crfw->assign(4 * S * P, 0.0);
+        CUDA_TRY(cudaMemcpy(crfw->data(), st.cr, S * P * 8, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(crfw->data() + 2 * S * P, st.fw, S * P * 8, cudaMemcpyDeviceToHost));
+    }
+    return DEAC_OK;
+}
+
+static void summarize(const RunHost& r, const deac::RunDev& st, const std::vector<double>& fit,
+                      deac_run_result* out) {
+    // argmin_and_min: first index of the strict minimum (deac.cpp:146-158)
+    uint64_t best = 0;
+    double mn = fit[0];
+    for (uint64_t i = 0; i < fit.size(); ++i)
+        if (fit[i] < mn) {
+            mn = fit[i];
+            best = i;
+        }
+    uint64_t gen = st.generation;
+    if (st.done && gen == r.cfg.number_of_generations - 2) gen += 1;  // deac.cpp:1677-1679
+    std::memset(out, 0, sizeof *out);
+    out->generation = gen;
+    out->minimum_fitness = mn;
+    out->best_index = best;
+    out->spectrum_length = r.S == 2 ? 2 * r.M - 1 : r.M;
+    out->stats_length = r.cfg.track_stats ? gen + 1 : 0;
+    out->population_size = r.P;
+    out->genome_size = r.M;
+    out->number_of_timeslices = r.Nt;
+    out->sides = r.S;
+    out->finished = st.done ? 1 : 0;
+}
+
+int deac_batch_result(deac_batch* b, uint32_t run, deac_run_result* out) {
+    if (!b || !out || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    std::vector<double> pop, fit;
+    deac::RunDev st;
+    int rc = gather(b, run, pop, fit, nullptr, st);
+    if (rc) return rc;
+    summarize(*b->runs[run], st, fit, out);
+    return DEAC_OK;
+}
+
+int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best_frequency,
+                     double* stats_mean, double* stats_minimum, double* stats_squared_mean) {
+    if (!b || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    RunHost& r = *b->runs[run];
+    std::vector<double> pop, fit;
+    deac::RunDev st;
+    int rc = gather(b, run, pop, fit, nullptr, st);
+    if (rc) return rc;
+    deac_run_result res;
+    summarize(r, st, fit, &res);
+    const uint64_t P = r.P, M = r.M;
+    const uint64_t L = res.spectrum_length;
+    std::vector<double> dsf(L), fr(L);
+    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, &pop[res.best_index * M],
+                        r.S == 2 ? &pop[P * M + res.best_index * M] : nullptr, dsf.data(), fr.data());
+    if (best_dsf) std::memcpy(best_dsf, dsf.data(), L * 8);
+    if (best_frequency) std::memcpy(best_frequency, fr.data(), L * 8);
+    if (r.cfg.track_stats && (stats_mean || stats_minimum || stats_squared_mean)) {
+        const uint64_t N = r.cfg.number_of_generations, n = res.stats_length;
+        std::vector<double> stats(3 * N);
+        CUDA_TRY(cudaMemcpy(stats.data(), st.stats, 3 * N * 8, cudaMemcpyDeviceToHost));
+        if (st.done && st.generation == N - 2) {
+            // last entry from the host, with the sequential mean
+            // (deac.cpp:1677-1685)
+            stats[N - 1] = deac::sequential_mean(fit.data(), P);
+            stats[2 * N - 1] = res.minimum_fitness;
+            stats[3 * N - 1] = deac::sequential_squared_mean(fit.data(), P);
+        }
+        if (stats_mean) std::memcpy(stats_mean, stats.data(), n * 8);
+        if (stats_minimum) std::memcpy(stats_minimum, stats.data() + N, n * 8);
+        if (stats_squared_mean) std::memcpy(stats_squared_mean, stats.data() + 2 * N, n * 8);
+    }
+    return DEAC_OK;
+}
+
+int deac_batch_fetch_state(deac_batch* b, uint32_t run, double* population, double* fitness,
+                           double* crossover_rates, double* differential_weights) {
+    if (!b || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    RunHost& r = *b->runs[run];
+    std::vector<double> pop, fit, crfw;
+    deac::RunDev st;
+    int rc = gather(b, run, pop, fit, &crfw, st);
+    if (rc) return rc;
+    const uint64_t SP = (uint64_t)r.S * r.P;
+    if (population) std::memcpy(population, pop.data(), pop.size() * 8);
+    if (fitness) std::memcpy(fitness, fit.data(), fit.size() * 8);
+    if (crossover_rates) std::memcpy(crossover_rates, crfw.data(), SP * 8);
+    if (differential_weights) std::memcpy(differential_weights, crfw.data() + 2 * SP, SP * 8);
+    return DEAC_OK;
+}
+
+int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness, uint64_t capacity) {
+    if (!b || run >= b->runs.size() || !trial_fitness) return fail(DEAC_E_INVALID, "bad argument");
+    RunHost& r = *b->runs[run];
+    if (!b->set_up || !r.trace_cap) return fail(DEAC_E_STATE, "no trace recorded");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    deac::RunDev st;
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    const uint64_t rows = std::min(std::min(st.ii, r.trace_cap), capacity);
+    if (rows) CUDA_TRY(cudaMemcpy(trial_fitness, st.trace, rows * r.P * 8, cudaMemcpyDeviceToHost));
+    return DEAC_OK;
+}
+
+int deac_batch_enable_timing(deac_batch* b, int32_t enable) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    b->timing = enable != 0;
+    b->kernel_ms[0] = b->kernel_ms[1] = 0.0;
+    b->kernel_launches[0] = b->kernel_launches[1] = 0;
+    return DEAC_OK;
+}
+
+int deac_batch_kernel_time(deac_batch* b, int32_t kind, double* ms, uint64_t* launches) {
+    if (!b || kind < 0 || kind > 1) return fail(DEAC_E_INVALID, "bad argument");
+    if (ms) *ms = b->kernel_ms[kind];
+    if (launches) *launches = b->kernel_launches[kind];
+    return DEAC_OK;
+}
+
+int deac_batch_destroy(deac_batch* b) {
+    if (!b) return DEAC_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& r : b->runs)
+        if (r->arena) cudaFree(r->arena);
+    for (auto& kv : b->kcache) {
+        cudaFree(kv.second.k_pos);
+        if (kv.second.k_neg) cudaFree(kv.second.k_neg);
+    }
+    cudaFree(b->d_runs);
+    cudaFree(b->d_trial_work);
+    cudaFree(b->d_contract_work);
+    for (auto& e : b->ev)
+        if (e) cudaEventDestroy(e);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return DEAC_OK;
+}
+
+int deac_reconstruct(const deac_config* cfg, const double* tau, const double* isf, const double* err,
+                     uint64_t nt, const double* freq, uint64_t m, deac_run_result* result, double* best_dsf,
+                     double* best_frequency, double* stats_mean, double* stats_minimum,
+                     double* stats_squared_mean) {
+    deac_batch* b = nullptr;
+    int rc = deac_batch_create(0, nullptr, DEAC_ENGINE_PLAIN_FP64, &b);
+    if (rc) return rc;
+    std::unique_ptr<deac_batch, int (*)(deac_batch*)> guard(b, deac_batch_destroy);
+    if ((rc = deac_batch_add_run(b, cfg, tau, isf, err, nt, freq, m, nullptr))) return rc;
+    if ((rc = deac_batch_run(b))) return rc;
+    if (result && (rc = deac_batch_result(b, 0, result))) return rc;
+    return deac_batch_fetch(b, 0, best_dsf, best_frequency, stats_mean, stats_minimum, stats_squared_mean);
+}
+
+}  // extern "C"

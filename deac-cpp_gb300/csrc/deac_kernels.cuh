@@ -1,0 +1,118 @@
+// deac_kernels.cuh -- device data layout and kernels of the plain FP64
+// engine.  One generation of every run in a batch is two launches:
+//
+//   trial_kernel     one CTA per (run, member): jDE self-adaptation of CR and
+//                    F, mutant indices, per-gene crossover draws, DE/rand/1
+//                    mutation with fabs, zero-frequency matching, and the
+//                    normalisation / moment row sums of the new trial.
+//                    Replaces gpu_set_crossover_probabilities_new,
+//                    gpu_set_differential_weights_new, gpu_set_mutant_indices,
+//                    gpu_set_mutate_indices, gpu_set_population_new,
+//                    gpu_match_population_zero, gpu_deac_gemv and
+//                    gpu_deac_dgmmDiv1D (deac_gpu.cu:345-374, 406-415,
+//                    514-549, 584-643).
+//   contract_kernel  one CTA per (run, member tile, tau tile): the
+//                    population x K contraction as order-exact FP64 FMA
+//                    chains; the last CTA of each run then forms chi^2 with
+//                    the reference's reduction tree, adds the moment terms,
+//                    does greedy selection by swapping the member's buffer
+//                    index, records statistics and sets the run's stop flag.
+//                    Replaces gpu_matmul, gpu_deac_reduced_chi_squared,
+//                    gpu_deac_add_scalar_reduced_chi_squared,
+//                    gpu_set_rejection_indices, gpu_swap_control_parameters,
+//                    gpu_swap_populations, gpu_get_minimum and
+//                    gpu_set_fitness_(squared_)mean (deac_gpu.cu:277-315,
+//                    376-404, 417-512, 551-582).
+//
+// Arithmetic is FP64 in the reference's order; the file is compiled with
+// --fmad=false and every fused multiply-add of the reference is an explicit
+// fma().  The selection step never copies a genome: each member owns two
+// buffers and an index saying which one holds its parent.
+#pragma once
+
+#include <cstdint>
+
+namespace deac {
+
+enum : uint32_t {
+    kNormalize = 1u << 0,
+    kFirstMoment = 1u << 1,
+    kThirdMoment = 1u << 2,
+    kNegativeFirstMoment = 1u << 3,
+    kSignedWeights = 1u << 4,
+    kTrackStats = 1u << 5,
+    kTrace = 1u << 6,
+};
+
+// Per-run descriptor, resident in device memory.
+struct RunDev {
+    uint32_t P, M, Nt, S;
+    uint32_t flags;
+    uint32_t contract_ctas;  // CTAs of contract_kernel for this run
+    uint32_t member_tile;    // members per contract CTA
+    uint32_t tau_tile;       // timeslices per contract CTA
+    uint64_t N;              // number_of_generations
+    double tau_cr, tau_f;    // self-adaptation probabilities
+    double alpha;            // 1 / F(0), the normalisation scale
+    double stop;             // stop_minimum_fitness
+    double first_target, third_target, third_error;
+    double negfirst_target, negfirst_error;
+    const double* k_pos;     // [Nt][M]
+    const double* k_neg;     // [Nt][M] (two-sided)
+    const double* isf;       // [Nt]
+    const double* err;       // [Nt]
+    const double* tau_w;     // [Nt] negative-first-moment weights
+    const double* norm_pos;  // [M]
+    const double* norm_neg;
+    const double* first_pos;
+    const double* first_neg;
+    const double* third_pos;
+    const double* third_neg;
+    double* pop;             // [2 buffers][S][P][M]
+    uint8_t* cur;            // [P] buffer holding each member's parent
+    uint64_t* rng;           // 4 words x n_states, word-major
+    uint64_t n_states;       // P * (1 + S*M)
+    double* cr;              // [old|new][S][P]
+    double* fw;              // [old|new][S][P]
+    double* fit_old;         // [P]
+    double* fit_new;         // [P]
+    double* model_isf;       // [P][Nt]
+    double* moments;         // [P][2]: first, third
+    double* stats;           // [mean|minimum|squared mean][N]
+    double* trace;           // [trace_cap][P]
+    uint64_t trace_cap;
+    // status, owned by the kernels
+    uint64_t ii;             // next generation index to execute
+    uint64_t generation;     // generation reported when done
+    uint32_t ticket;         // CTAs of contract_kernel done this launch
+    int32_t done;
+};
+
+// Per-member PRNG slot layout.  The reference keeps one state per
+// (member, gene, side) plus P extra states, in the order
+//   state i                       CR(+) and mutant indices of member i
+//   state P + s*P*M + j*P + i     crossover draw of gene j, side s, member i
+// (deac.cpp:1116-1126, 1170-1174, 1219-1222).  Here member i owns the
+// contiguous slots  base(i) + q,  base(i) = i*(1+S*M):
+//   q = 0            reference state i
+//   q = 1 + s*M + j  reference state P + s*P*M + j*P + i
+// The jDE kernels of the reference use states P+i, 2P+i, 3P+i for F(+),
+// CR(-), F(-); they are member i's slots q = 1, 2, 3.
+__host__ __device__ inline uint64_t rng_slot(uint32_t P, uint32_t M, uint32_t S, uint64_t ref_state) {
+    if (ref_state < P) return ref_state * (1ull + (uint64_t)S * M);
+    const uint64_t m = ref_state - P;
+    const uint64_t pm = (uint64_t)P * M;
+    const uint64_t s = m / pm, rem = m % pm;
+    const uint64_t j = rem / P, i = rem % P;
+    return i * (1ull + (uint64_t)S * M) + 1 + s * M + j;
+}
+
+struct Work {
+    uint32_t run;
+    uint32_t index;  // member (trial) or tile (contract)
+};
+
+__global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes);
+__global__ void contract_kernel(RunDev* runs, const Work* work, int init_mode);
+
+}  // namespace deac

@@ -1,0 +1,84 @@
+// deac_rng.cuh -- the reference PRNG, usable on host and device.
+//
+// xoshiro256+ seeded through splitmix64 exactly as the reference does it
+// (src/deac/include/rng.hpp:10-59): each 64-bit splitmix output fills two
+// state words with its low and high 32-bit halves.  The 2^128 jump
+// (rng.hpp:64-87) separates the per-gene states of the GPU path
+// (deac.cpp:1114-1135).  Uniform doubles are (x >> 11) * 2^-53
+// (rng.hpp:129-131).
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define DEAC_HD __host__ __device__ __forceinline__
+#else
+#define DEAC_HD inline
+#endif
+
+namespace deac {
+
+DEAC_HD uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+// One xoshiro256+ step on four words held by the caller.
+DEAC_HD uint64_t xoshiro_next(uint64_t& s0, uint64_t& s1, uint64_t& s2, uint64_t& s3) {
+    const uint64_t result = s0 + s3;
+    const uint64_t t = s1 << 17;
+    s2 ^= s0;
+    s3 ^= s1;
+    s1 ^= s2;
+    s0 ^= s3;
+    s2 ^= t;
+    s3 = rotl64(s3, 45);
+    return result;
+}
+
+DEAC_HD double to_unit(uint64_t x) { return static_cast<double>(x >> 11) * 0x1.0p-53; }
+
+struct Xoshiro {
+    uint64_t s[4];
+
+    DEAC_HD uint64_t next() { return xoshiro_next(s[0], s[1], s[2], s[3]); }
+
+    static uint64_t splitmix(uint64_t& x) {
+        uint64_t r = (x += 0x9E3779B97f4A7C15ULL);
+        r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        r = (r ^ (r >> 27)) * 0x94D049BB133111EBULL;
+        return r ^ (r >> 31);
+    }
+
+    static Xoshiro seeded(uint64_t seed) {
+        Xoshiro g;
+        uint64_t x = seed;
+        const uint64_t a = splitmix(x);
+        g.s[0] = static_cast<uint32_t>(a);
+        g.s[1] = a >> 32;
+        const uint64_t b = splitmix(x);
+        g.s[2] = static_cast<uint32_t>(b);
+        g.s[3] = b >> 32;
+        return g;
+    }
+
+    // Advance by 2^128 steps (the published xoshiro256 jump polynomial).
+    void jump() {
+        static const uint64_t kJump[4] = {0x180ec6d33cfd0abaULL, 0xd5a61266f0c9392cULL,
+                                          0xa9582618e03fc9aaULL, 0x39abdc4529b1661cULL};
+        uint64_t a = 0, b = 0, c = 0, d = 0;
+        for (int w = 0; w < 4; ++w)
+            for (int bit = 0; bit < 64; ++bit) {
+                if (kJump[w] & (1ULL << bit)) {
+                    a ^= s[0];
+                    b ^= s[1];
+                    c ^= s[2];
+                    d ^= s[3];
+                }
+                next();
+            }
+        s[0] = a;
+        s[1] = b;
+        s[2] = c;
+        s[3] = d;
+    }
+};
+
+}  // namespace deac

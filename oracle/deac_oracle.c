@@ -50,7 +50,9 @@
  * (deac.cpp:120-126), squared_mean (deac.cpp:177-183), the
  * negative-first-moment target (deac.cpp:888), and the inlined
  * matrix_multiply_* sites whose destination it keeps in a register (the
- * one-sided contraction, the negative first moment and third moment sums).
+ * normalisation of the initial population, the one-sided contraction inside
+ * the loop, the one-sided row sums, the negative-first-moment and the
+ * third-moment sums).
  * This map was established by comparing against the reference CPU build
  * (g++ 13, -O3 -march=native, x86-64) bit for bit, stats arrays included;
  * another host compiler may fuse differently.  nvcc fuses every a*b+c of
@@ -379,10 +381,11 @@ static double gemv_gpu(const oracle_t* o, uint64_t i, double* const pop[2],
 }
 
 /* CPU-order row sum: one chain over the positive then the negative side
- * (matrix_multiply_MxN_by_Nx1 called twice into the same accumulator). */
+ * (matrix_multiply_MxN_by_Nx1 called twice into the same accumulator); the
+ * one-sided build keeps its single call's accumulator in a register. */
 static double gemv_cpu(const oracle_t* o, uint64_t i, double* const pop[2],
                        const double* tp, const double* tn) {
-    double y = chain(pop[0] + i * o->M, tp, o->M, 0.0);
+    double y = (o->S == 1) ? chain_unfused(pop[0] + i * o->M, tp, o->M, 0.0) : chain(pop[0] + i * o->M, tp, o->M, 0.0);
     if (o->S == 2) y = chain(pop[1] + i * o->M, tn, o->M, y);
     return y;
 }
@@ -399,10 +402,12 @@ static void normalize_gpu(oracle_t* o, double* pop[2]) {
     }
 }
 
-/* --normalize of the initial population on the CPU path, deac.cpp:581-601 */
+/* --normalize of the initial population on the CPU path, deac.cpp:581-601
+ * (its accumulator lives in a register in the reference build: unfused) */
 static void normalize_cpu(oracle_t* o, double* pop[2]) {
     for (uint64_t i = 0; i < o->P; i++) {
-        const double norm = gemv_cpu(o, i, pop, o->np_, o->nn_);
+        double norm = chain_unfused(pop[0] + i * o->M, o->np_, o->M, 0.0);
+        if (o->S == 2) norm = chain_unfused(pop[1] + i * o->M, o->nn_, o->M, norm);
         for (uint64_t j = 0; j < o->M; j++) {
             pop[0][i * o->M + j] *= o->zeroth / norm;
             if (o->S == 2) pop[1][i * o->M + j] *= o->zeroth / norm;
@@ -424,11 +429,11 @@ static double fitness_of(oracle_t* o, uint64_t i, double* pop[2], int setup) {
             E[t] = e;
         } else {
             /* one continued chain (deac.cpp:857-865, 1386-1394).  The
-             * one-sided build carries it in a register, unfused, except at
-             * the set-up site of the non-standard models, which stays fused */
+             * one-sided build fuses it at the set-up site and carries it in a
+             * register, unfused, inside the loop */
             double e;
             if (o->S == 2) e = chain(o->Kn + t * M, pop[1] + i * M, M, chain(o->Kp + t * M, pop[0] + i * M, M, 0.0));
-            else if (setup && (o->c->model != DEAC_MODEL_STANDARD || o->c->zero_temperature))
+            else if (setup)
                 e = chain(o->Kp + t * M, pop[0] + i * M, M, 0.0);
             else e = chain_unfused(o->Kp + t * M, pop[0] + i * M, M, 0.0);
             E[t] = e;

@@ -16,6 +16,7 @@ import os
 import re
 import struct
 import subprocess
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -24,70 +25,12 @@ REPO = Path(__file__).resolve().parents[1]
 ORACLE_SO = REPO / "oracle" / "_build" / "libdeac_oracle.so"
 REF_DIR = REPO / "oracle" / "_ref"
 
-MODEL = {"standard": 0, "hyperbolic": 1, "normalization": 2}
-SPECTRA = {"spbsf": 0, "spfsf": 1, "bfull": 2, "ffull": 3, "bdsf": 4}
 GPU_ORDER, CPU_ORDER = 0, 1
 
-
-class DeacConfig(ctypes.Structure):
-    _fields_ = [
-        ("model", ctypes.c_int32),
-        ("zero_temperature", ctypes.c_int32),
-        ("bosonic", ctypes.c_int32),
-        ("allow_negative_weight", ctypes.c_int32),
-        ("spectra_type", ctypes.c_int32),
-        ("normalize", ctypes.c_int32),
-        ("use_negative_first_moment", ctypes.c_int32),
-        ("track_stats", ctypes.c_int32),
-        ("temperature", ctypes.c_double),
-        ("first_moment", ctypes.c_double),
-        ("third_moment", ctypes.c_double),
-        ("third_moment_error", ctypes.c_double),
-        ("crossover_probability", ctypes.c_double),
-        ("self_adapting_crossover_probability", ctypes.c_double),
-        ("differential_weight", ctypes.c_double),
-        ("self_adapting_differential_weight_probability", ctypes.c_double),
-        ("self_adapting_differential_weight_shift", ctypes.c_double),
-        ("self_adapting_differential_weight", ctypes.c_double),
-        ("stop_minimum_fitness", ctypes.c_double),
-        ("number_of_generations", ctypes.c_uint64),
-        ("population_size", ctypes.c_uint64),
-        ("seed", ctypes.c_uint64),
-    ]
-
-
-def make_config(**kw) -> DeacConfig:
-    """Reference CLI defaults (deac.cpp:1927-2024), overridden by ``kw``.
-
-    ``model`` and ``spectra_type`` accept names."""
-    c = DeacConfig()
-    c.model = 0
-    c.spectra_type = SPECTRA["spfsf"]
-    c.temperature = 0.0
-    c.first_moment = -1.0
-    c.third_moment = -1.0
-    c.third_moment_error = 0.0
-    c.crossover_probability = 0.9
-    c.self_adapting_crossover_probability = 0.1
-    c.differential_weight = 0.9
-    c.self_adapting_differential_weight_probability = 0.1
-    c.self_adapting_differential_weight_shift = 0.1
-    c.self_adapting_differential_weight = 0.9
-    c.stop_minimum_fitness = 1.0
-    c.number_of_generations = 100000
-    c.population_size = 512
-    c.seed = 0
-    for k, v in kw.items():
-        if k == "model" and isinstance(v, str):
-            v = MODEL[v]
-        if k == "spectra_type" and isinstance(v, str):
-            v = SPECTRA[v]
-        if isinstance(v, bool):
-            v = int(v)
-        setattr(c, k, v)
-    if kw.get("bosonic") and "spectra_type" not in kw:
-        c.spectra_type = SPECTRA["bdsf"]
-    return c
+PKG_DIR = REPO / "deac-cpp_gb300"
+if str(PKG_DIR) not in sys.path:
+    sys.path.insert(0, str(PKG_DIR))
+from deac_gb300 import MODEL, SPECTRA, DeacConfig, make_config  # noqa: E402
 
 
 class OracleOut(ctypes.Structure):
