@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark: DEAC generations/s summed over runs on GB300.
+
+Workload (the reference's production scale, BASELINE config 1): 8 runs,
+seeds 1-8, standard model, two-sided (--spectra_type bfull), T = 1.35,
+N_tau = 128 on [0, beta], M = 4096 on omega in [0, 512], P = 8, --normalize,
+stop fitness 1.0 (not reached in the timed generations).  Synthetic data by
+the benchmark recipe (deac_gb300.data.config1_data).
+
+A step is G generations of every run of the batch (plain FP64 engine,
+bit-identical to the reference CUDA-path semantics).  Timing: W untimed
+warm-up steps, then K steps, each bracketed by CUDA events on the batch
+stream, with a 256 MB L2 flush before each step (outside the events); the
+K steps sit between a barrier + device synchronize on both sides; value is
+the max over ranks.  With --gpus N (torchrun), each rank runs its own 8
+seeds (weak scaling, no data-path collective).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+--impl reference times the reference's own CPU implementation of the path
+(the CPU-order oracle, a restatement of the reference's CPU code path, since
+the reference sources are not on the GPU host) on the host cores, one
+process per run, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+for p in (REPO / "deac-cpp_gb300", REPO / "tests"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "generations/s summed over runs: batched split-precision vs plain FP64, same χ²"
+UNIT = "generations/s"
+RUNS_PER_GPU = 8
+P, M, NT, OMEGA_MAX, T = 8, 4096, 128, 512.0, 1.35
+GENS_PER_STEP = 32
+WORKLOAD = ("deac config 1: 8 runs (seeds 1-8), standard model, two-sided bfull, T=1.35, "
+            "N_tau=128, M=4096 on [0,512], P=8, --normalize, plain FP64 engine")
+DATA = "synthetic (benchmark recipe: 0.7 N(5,1) + 0.3 N(20,3), sigma = 1e-4 F, numpy default_rng(seed))"
+CPU_SAMPLE_GENERATIONS = 1000
+
+
+def run_configs(rank):
+    import deac_gb300
+    from deac_gb300.data import config1_data, uniform_grid
+
+    freq = uniform_grid(M, OMEGA_MAX)
+    out = []
+    for k in range(RUNS_PER_GPU):
+        seed = rank * RUNS_PER_GPU + k + 1
+        cfg = deac_gb300.make_config(temperature=T, spectra_type="bfull", population_size=P,
+                                     number_of_generations=1_600_000, normalize=True, stop_minimum_fitness=1.0,
+                                     seed=seed)
+        tau, isf, err = config1_data(seed, T)
+        out.append((cfg, tau, isf, err, freq))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier_max(value, world, device):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world, device):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.barrier(device_ids=[device])
+    import torch
+    torch.cuda.synchronize()
+
+
+# ------------------------------------------------------------------ CPU side
+
+def _cpu_worker(args):
+    """One reconstruction of `gens` generations with the CPU-order oracle (the
+    reference's CPU path); returns (generations executed, seconds)."""
+    seed, gens = args
+    sys.path.insert(0, str(REPO / "tests"))
+    sys.path.insert(0, str(REPO / "deac-cpp_gb300"))
+    from deac_testlib import CPU_ORDER, Oracle
+    import deac_gb300
+    from deac_gb300.data import config1_data, uniform_grid
+    cfg = deac_gb300.make_config(temperature=T, spectra_type="bfull", population_size=P,
+                                 number_of_generations=gens + 1, normalize=True, stop_minimum_fitness=-1.0,
+                                 seed=seed)
+    tau, isf, err = config1_data(seed, T)
+    t0 = time.perf_counter()
+    r = Oracle().run(cfg, tau, isf, err, uniform_grid(M, OMEGA_MAX), order=CPU_ORDER)
+    return r["executed"], time.perf_counter() - t0
+
+
+def ensure_oracle():
+    subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "all"], check=True)
+
+
+def cpu_baseline():
+    """Bounded single-core sample of the reference CPU path on the workload."""
+    ensure_oracle()
+    gens, secs = _cpu_worker((1, CPU_SAMPLE_GENERATIONS))
+    return {"value": gens / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"seed 1 of the workload, {gens} generations, one core "
+                      f"(CPU-order oracle = the reference's CPU code path), {secs:.1f} s"}
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    ensure_oracle()
+    gens = 48  # per run per step: ~0.6 s of CPU work per run
+    cores = min(RUNS_PER_GPU, os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_cpu_worker, [(s + 1, gens) for s in range(RUNS_PER_GPU)])
+        t0 = time.perf_counter()
+        total = 0
+        for _ in range(args.steps):
+            res = pool.map(_cpu_worker, [(s + 1, gens) for s in range(RUNS_PER_GPU)])
+            total += sum(g for g, _ in res)
+        dt = time.perf_counter() - t0
+    value = total / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD + " (reference CPU path)", "runs": RUNS_PER_GPU,
+                   "generations_per_run_per_step": gens, "processes": cores},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{RUNS_PER_GPU} runs x {gens} generations per step, one process per run "
+                                   f"(CPU-order oracle: the reference's CPU code path restated; the reference "
+                                   f"sources are not present on the GPU host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+
+def engine_arm(args, world, rank, local):
+    import torch
+    import deac_gb300
+
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=device)
+    configs = run_configs(rank)
+    G = args.generations_per_step
+
+    batch = deac_gb300.Batch(device=local, stream=stream.cuda_stream)
+    for cfg, tau, isf, err, freq in configs:
+        batch.add_run(cfg, tau, isf, err, freq)
+    batch.setup()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    for _ in range(args.warmup):
+        batch.launch(G)
+    torch.cuda.synchronize()
+    assert batch.sync() == 0, "a run finished during warm-up"
+
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world, local)
+    with ClockSampler(local) as clocks:
+        for e0, e1 in events:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0.record(stream)
+            batch.launch(G)
+            e1.record(stream)
+        stream.synchronize()
+        barrier(world, local)
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in events)
+    finished = batch.sync()
+    assert finished == 0, "a run finished inside the timed region; its generations would not count"
+    ms = barrier_max(ms, world, device)
+    gens_total = world * RUNS_PER_GPU * args.steps * G
+    value = gens_total / (ms / 1e3)
+
+    # per-kernel device time (separate pass, individually launched kernels
+    # bracketed by events on the batch stream)
+    batch.enable_timing(True)
+    batch.launch(G)
+    trial_ms, trial_n = batch.kernel_time(0)
+    contract_ms, contract_n = batch.kernel_time(1)
+    batch.enable_timing(False)
+    batch.close()
+
+    flops_per_launch = RUNS_PER_GPU * 2.0 * 2 * P * NT * M  # 2*S*P*Nt*M per run-generation
+    contract_s = contract_ms / contract_n / 1e3
+    achieved = flops_per_launch / contract_s / 1e12
+    peak = 1.196  # TFLOP/s, measured DFMA throughput (profiles/fp64_pipe_gb300.md)
+    traffic = None
+    tpath = REPO / "profiles" / "contract_kernel_traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get("bytes_per_launch")
+
+    # end to end through the public API with host buffers: create + add runs
+    # (host arrays) + setup (host build, H2D) + K steps of (G generations,
+    # then every run's best spectrum and minimum fitness read back)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b2 = deac_gb300.Batch(device=local, stream=stream.cuda_stream)
+    h2d = 0
+    for cfg, tau, isf, err, freq in configs:
+        b2.add_run(cfg, tau, isf, err, freq)
+        s = 2
+        h2d += 8 * (3 * NT + 2 * s * P * M + 4 * P * (1 + s * M) + 4 * s * P)
+    h2d += 8 * 2 * NT * M  # shared kernel matrix
+    b2.setup()
+    d2h = 0
+    for _ in range(args.steps):
+        b2.launch(G)
+        for r in range(len(configs)):
+            out = b2.fetch(r)
+            d2h += 8 * (len(out["dsf"]) + P) + P
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    b2.close()
+    e2e_value = gens_total / barrier_max(e2e_s, world, device)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD, "runs_per_gpu": RUNS_PER_GPU, "population_size": P, "genome_size": M,
+                   "number_of_timeslices": NT, "normalize": True, "generations_per_step": G,
+                   "engine": "plain_fp64", "l2": "flushed before every timed step (256 MB write, untimed)"},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "contract_kernel",
+                     "peak_source": "measured DFMA throughput (profiles/fp64_pipe_gb300.md); the driver's "
+                                    "peak file has no FP64 figure",
+                     "flops_per_launch": flops_per_launch, "launch_us": contract_s * 1e6,
+                     "trial_kernel_launch_us": trial_ms / trial_n * 1e3},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
+        "gpu_launches": 2 * G * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--generations-per-step", type=int, default=GENS_PER_STEP)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        # CPU only: rank 0 measures, the other ranks exit without work
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        reference_arm(args, world, int(os.environ.get("RANK", "0")))
+        return
+    world, rank, local = dist_setup()
+    engine_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -566,11 +566,13 @@ static void summarize(const RunHost& r, const deac::RunDev& st, const std::vecto
 int deac_batch_result(deac_batch* b, uint32_t run, deac_run_result* out) {
     if (!b || !out || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
-    std::vector<double> pop, fit;
+    RunHost& r = *b->runs[run];
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     deac::RunDev st;
-    int rc = gather(b, run, pop, fit, nullptr, st);
-    if (rc) return rc;
-    summarize(*b->runs[run], st, fit, out);
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    std::vector<double> fit(r.P);
+    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, r.P * 8, cudaMemcpyDeviceToHost));
+    summarize(r, st, fit, out);
     return DEAC_OK;
 }
 
@@ -579,33 +581,44 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
     if (!b || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
     RunHost& r = *b->runs[run];
-    std::vector<double> pop, fit;
+    const uint64_t P = r.P, M = r.M, S = r.S;
+    // only the fitness, the buffer indices and the best member's genes cross
+    // the bus (the reference copies the whole population, deac.cpp:1577-1590)
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     deac::RunDev st;
-    int rc = gather(b, run, pop, fit, nullptr, st);
-    if (rc) return rc;
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    std::vector<double> fit(P);
+    std::vector<uint8_t> cur(P);
+    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, P * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(cur.data(), st.cur, P, cudaMemcpyDeviceToHost));
     deac_run_result res;
     summarize(r, st, fit, &res);
-    const uint64_t P = r.P, M = r.M;
+    const uint64_t best = res.best_index;
+    std::vector<double> genes(S * M);
+    for (uint64_t s = 0; s < S; ++s)
+        CUDA_TRY(cudaMemcpy(&genes[s * M], st.pop + ((uint64_t)cur[best] * S * P + s * P + best) * M, M * 8,
+                            cudaMemcpyDeviceToHost));
     const uint64_t L = res.spectrum_length;
     std::vector<double> dsf(L), fr(L);
-    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, &pop[res.best_index * M],
-                        r.S == 2 ? &pop[P * M + res.best_index * M] : nullptr, dsf.data(), fr.data());
+    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes.data(), S == 2 ? &genes[M] : nullptr, dsf.data(),
+                        fr.data());
     if (best_dsf) std::memcpy(best_dsf, dsf.data(), L * 8);
     if (best_frequency) std::memcpy(best_frequency, fr.data(), L * 8);
     if (r.cfg.track_stats && (stats_mean || stats_minimum || stats_squared_mean)) {
         const uint64_t N = r.cfg.number_of_generations, n = res.stats_length;
-        std::vector<double> stats(3 * N);
-        CUDA_TRY(cudaMemcpy(stats.data(), st.stats, 3 * N * 8, cudaMemcpyDeviceToHost));
+        std::vector<double> stats(3 * n);
+        for (int k = 0; k < 3; ++k)
+            if (n) CUDA_TRY(cudaMemcpy(&stats[k * n], st.stats + k * N, n * 8, cudaMemcpyDeviceToHost));
         if (st.done && st.generation == N - 2) {
             // last entry from the host, with the sequential mean
             // (deac.cpp:1677-1685)
-            stats[N - 1] = deac::sequential_mean(fit.data(), P);
-            stats[2 * N - 1] = res.minimum_fitness;
-            stats[3 * N - 1] = deac::sequential_squared_mean(fit.data(), P);
+            stats[n - 1] = deac::sequential_mean(fit.data(), P);
+            stats[2 * n - 1] = res.minimum_fitness;
+            stats[3 * n - 1] = deac::sequential_squared_mean(fit.data(), P);
         }
         if (stats_mean) std::memcpy(stats_mean, stats.data(), n * 8);
-        if (stats_minimum) std::memcpy(stats_minimum, stats.data() + N, n * 8);
-        if (stats_squared_mean) std::memcpy(stats_squared_mean, stats.data() + 2 * N, n * 8);
+        if (stats_minimum) std::memcpy(stats_minimum, stats.data() + n, n * 8);
+        if (stats_squared_mean) std::memcpy(stats_squared_mean, stats.data() + 2 * n, n * 8);
     }
     return DEAC_OK;
 }

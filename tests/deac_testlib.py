@@ -134,49 +134,8 @@ class Oracle:
 
 
 # ----------------------------------------------------------------- data recipe
-
-def gaussian(w, mean, sd):
-    return np.exp(-0.5 * ((w - mean) / sd) ** 2) / (sd * np.sqrt(2 * np.pi))
-
-
-def make_isf(n_tau, temperature, peaks, rel_error=1e-4, seed=1, omega_max_data=None,
-             n_omega_data=20001, tau_max=None):
-    """Synthetic ISF of the benchmark recipe.
-
-    peaks: list of (weight, mean, sd).  F(tau) = sum_w [e^{-tau w} + e^{-(beta-tau) w}]
-    S(w) dw on a fine grid; sigma = rel_error*F; F_data = F + sigma*N(0,1) drawn
-    with numpy.random.default_rng(seed).  tau is uniform on [0, tau_max]
-    (default beta)."""
-    beta = 1.0 / temperature
-    if omega_max_data is None:
-        omega_max_data = max(m + 8 * s for _, m, s in peaks)
-    w = np.linspace(0.0, omega_max_data, n_omega_data)
-    dw = w[1] - w[0]
-    s = sum(a * gaussian(w, m, sd) for a, m, sd in peaks)
-    tau = np.linspace(0.0, beta if tau_max is None else tau_max, n_tau)
-    kern = np.exp(-np.outer(tau, w)) + np.exp(-np.outer(beta - tau, w))
-    f = kern @ (s * dw)
-    sigma = rel_error * np.abs(f)
-    rng = np.random.default_rng(seed)
-    f_data = f + sigma * rng.standard_normal(n_tau)
-    return tau, f_data, sigma
-
-
-def config0_data(seed=1):
-    """Plain FP64, standard model, T=1.35, N_tau=64 on [0, beta],
-    S = 0.7 N(5,1) + 0.3 N(20,3), sigma = 1e-4 F."""
-    return make_isf(64, 1.35, [(0.7, 5.0, 1.0), (0.3, 20.0, 3.0)], 1e-4, seed)
-
-
-def config1_data(seed=1, temperature=1.35):
-    """Reference production scale: the config-0 recipe with N_tau = 128."""
-    return make_isf(128, temperature, [(0.7, 5.0, 1.0), (0.3, 20.0, 3.0)], 1e-4, seed)
-
-
-def uniform_grid(m, omega_max):
-    """Frequency grid of deac.cpp:2123-2126: i * (omega_max / (M - 1))."""
-    d = omega_max / (m - 1)
-    return np.array([i * d for i in range(m)], dtype=np.float64)
+from deac_gb300.data import (config0_data, config1_data, config2_data, gaussian, make_isf,  # noqa: E402,F401
+                             uniform_grid)
 
 
 # ------------------------------------------------------------ files / binaries
