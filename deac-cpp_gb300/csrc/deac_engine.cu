@@ -50,8 +50,9 @@ int fail(int code, const char* fmt, ...) {
                         __FILE__, __LINE__);                                               \
     } while (0)
 
-constexpr uint64_t kGraphBlock = 16;          // generations per captured graph
-constexpr uint64_t kTrialSmemCapGenes = 20480;  // 160 KB of trial genes in shared memory
+constexpr uint64_t kGraphBlock = 16;             // generations per captured graph
+constexpr uint64_t kTrialSmemCapDoubles = 25600;  // 200 KB: trial genes + one row of weights
+constexpr uint64_t kTailSlotsBytes = 4 * 1024 * 8;  // reduction slots of the finishing CTA
 
 uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 
@@ -99,9 +100,10 @@ struct deac_batch {
     deac::RunDev* d_runs = nullptr;
     deac::Work* d_trial_work = nullptr;
     deac::Work* d_contract_work = nullptr;
-    uint32_t n_trial_ctas = 0, n_contract_ctas = 0, contract_threads = 32;
-    int smem_genes = 0;
+    uint32_t n_trial_ctas = 0, n_contract_ctas = 0;
+    int smem_doubles = 0;
     size_t trial_smem_bytes = 0;
+    size_t contract_smem_bytes = 0;
     bool set_up = false;
     cudaGraphExec_t graph = nullptr;
     std::vector<deac::RunDev> status;  // host mirror of d_runs
@@ -116,18 +118,18 @@ namespace {
 
 int launch_generation(deac_batch* b, cudaStream_t s, int init_mode) {
     deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
-                                                                          init_mode, b->smem_genes);
-    deac::contract_kernel<<<b->n_contract_ctas, b->contract_threads, 0, s>>>(b->d_runs, b->d_contract_work,
-                                                                             init_mode);
+                                                                          init_mode, b->smem_doubles);
+    deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s>>>(
+        b->d_runs, b->d_contract_work, init_mode);
     return DEAC_OK;
 }
 
 int launch_generation_timed(deac_batch* b) {
     CUDA_TRY(cudaEventRecord(b->ev[0], b->stream));
     deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, b->stream>>>(
-        b->d_runs, b->d_trial_work, 0, b->smem_genes);
+        b->d_runs, b->d_trial_work, 0, b->smem_doubles);
     CUDA_TRY(cudaEventRecord(b->ev[1], b->stream));
-    deac::contract_kernel<<<b->n_contract_ctas, b->contract_threads, 0, b->stream>>>(
+    deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, b->stream>>>(
         b->d_runs, b->d_contract_work, 0);
     CUDA_TRY(cudaEventRecord(b->ev[2], b->stream));
     CUDA_TRY(cudaEventSynchronize(b->ev[2]));
@@ -246,8 +248,18 @@ int upload_run(deac_batch* b, RunHost& r) {
               (m.use_negative_first_moment ? deac::kNegativeFirstMoment : 0) |
               (r.cfg.allow_negative_weight ? deac::kSignedWeights : 0) |
               (r.cfg.track_stats ? deac::kTrackStats : 0) | (r.trace_cap ? deac::kTrace : 0);
-    d.member_tile = (uint32_t)std::min<uint64_t>(P, 256);
-    d.tau_tile = std::max<uint32_t>(1, 32 / d.member_tile);
+    // contraction tile: a power-of-two number of members times timeslices
+    // filling the CTA's 64 (two-sided) or 128 (one-sided) chain pairs, and a
+    // staging chunk that keeps two stages within 96 KB of shared memory
+    const uint32_t pairs = deac::contract_pairs((uint32_t)S);
+    uint32_t mt = 1;
+    while (mt * 2 <= std::min<uint64_t>(P, pairs)) mt *= 2;
+    d.member_tile = mt;
+    d.tau_tile = pairs / mt;
+    const uint64_t rows = (uint64_t)S * (d.member_tile + d.tau_tile);
+    uint64_t chunk = (96 * 1024 / 8) / (2 * rows) - 2;
+    chunk = std::min<uint64_t>(chunk, 128) & ~uint64_t(1);
+    d.chunk = (uint32_t)std::max<uint64_t>(chunk, 8);
     const uint32_t member_tiles = (d.P + d.member_tile - 1) / d.member_tile;
     const uint32_t tau_tiles = (d.Nt + d.tau_tile - 1) / d.tau_tile;
     d.contract_ctas = member_tiles * tau_tiles;
@@ -425,8 +437,7 @@ int deac_batch_setup(deac_batch* b) {
             for (auto& th : pool) th.join();
         }
     }
-    uint64_t max_genes = 0;
-    uint32_t max_threads = 32;
+    uint64_t trial_doubles = 0, contract_bytes = kTailSlotsBytes;
     std::vector<deac::Work> tw, cw;
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         RunHost& r = *b->runs[ri];
@@ -434,15 +445,22 @@ int deac_batch_setup(deac_batch* b) {
         if (rc) return rc;
         for (uint32_t i = 0; i < r.dev.P; ++i) tw.push_back({ri, i});
         for (uint32_t k = 0; k < r.dev.contract_ctas; ++k) cw.push_back({ri, k});
-        max_threads = std::max(max_threads, r.dev.member_tile * r.dev.tau_tile);
+        // trial genes, plus one row of weights when a row sum is formed
         const uint64_t genes = (uint64_t)r.S * r.M;
-        if (genes <= kTrialSmemCapGenes) max_genes = std::max(max_genes, genes);
+        const bool sums = (r.dev.flags & (deac::kNormalize | deac::kFirstMoment | deac::kThirdMoment)) != 0;
+        if (sums && 2 * genes <= kTrialSmemCapDoubles) trial_doubles = std::max(trial_doubles, 2 * genes);
+        else if (genes <= kTrialSmemCapDoubles) trial_doubles = std::max(trial_doubles, genes);
+        const uint64_t stage =
+            deac::stage_doubles(r.dev.S, r.dev.member_tile, r.dev.tau_tile, r.dev.chunk) * 2 * sizeof(double);
+        contract_bytes = std::max<uint64_t>(contract_bytes, stage);
     }
-    b->contract_threads = (max_threads + 31) / 32 * 32;
-    b->smem_genes = (int)max_genes;
-    b->trial_smem_bytes = max_genes * sizeof(double);
+    b->smem_doubles = (int)trial_doubles;
+    b->trial_smem_bytes = trial_doubles * sizeof(double);
+    b->contract_smem_bytes = contract_bytes;
     CUDA_TRY(cudaFuncSetAttribute(deac::trial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
+    CUDA_TRY(cudaFuncSetAttribute(deac::contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)b->contract_smem_bytes));
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
     CUDA_TRY(cudaMalloc(&b->d_trial_work, tw.size() * sizeof(deac::Work)));

@@ -11,7 +11,6 @@ namespace deac {
 namespace {
 
 constexpr int kTrialThreads = 256;
-constexpr int kTailWarps = 2;      // warps of the last contract CTA that reduce chi^2
 constexpr int kTreeSlots = 1024;   // GPU_BLOCK_SIZE of the reference reductions
 
 __device__ __forceinline__ void load_state(const RunDev& R, uint64_t slot, uint64_t s[4]) {
@@ -34,22 +33,53 @@ __device__ __forceinline__ double draw(uint64_t s[4]) {
     return to_unit(xoshiro_next(s[0], s[1], s[2], s[3]));
 }
 
-// k-ascending FMA chain from 0.0 (the inner loop of gpu_deac_gemv,
-// deac_gpu.cu:359-363).
-__device__ double row_chain(const double* __restrict__ x, const double* __restrict__ w, uint32_t n) {
-    double acc = 0.0;
+// k-ascending FMA chain continuing from `acc` (the inner loops of
+// gpu_matmul and gpu_deac_gemv, deac_gpu.cu:302-304, 359-363).  Operands of
+// the next 8 steps are loaded while the current 8 are fused, so a dependent
+// DFMA (64 cycles on this part) never waits for memory.
+__device__ __forceinline__ double chain(const double* x, const double* w, uint32_t n, double acc) {
+    constexpr uint32_t U = 8;
     uint32_t k = 0;
-    for (; k + 4 <= n; k += 4) {
-        const double x0 = x[k], x1 = x[k + 1], x2 = x[k + 2], x3 = x[k + 3];
-        const double w0 = __ldg(w + k), w1 = __ldg(w + k + 1), w2 = __ldg(w + k + 2), w3 = __ldg(w + k + 3);
-        acc = fma(x0, w0, acc);
-        acc = fma(x1, w1, acc);
-        acc = fma(x2, w2, acc);
-        acc = fma(x3, w3, acc);
+    if (n >= U) {
+        double xa[U], wa[U];
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u) {
+            xa[u] = x[u];
+            wa[u] = w[u];
+        }
+        for (k = U; k + U <= n; k += U) {
+            double xb[U], wb[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                xb[u] = x[k + u];
+                wb[u] = w[k + u];
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) acc = fma(xa[u], wa[u], acc);
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                xa[u] = xb[u];
+                wa[u] = wb[u];
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u) acc = fma(xa[u], wa[u], acc);
     }
-    for (; k < n; ++k) acc = fma(x[k], __ldg(w + k), acc);
+    for (; k < n; ++k) acc = fma(x[k], w[k], acc);
     return acc;
 }
+
+__device__ __forceinline__ void cp_async16(double* dst, const double* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Row sum of the gemv pair the reference issues for normalisation and
 // moments: y = alpha*s_pos (beta = 0), then y = alpha*s_neg + 1*y, which
@@ -88,9 +118,13 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
 }  // namespace
 
 // ---------------------------------------------------------------- trial
+// Dynamic shared memory: the member's S*M trial genes, then S*M weights of
+// the row sum being formed (normalisation, first or third moment), when the
+// batch's capacity `smem_doubles` allows; otherwise the chains read global
+// memory (still k-ascending).
 __global__ void __launch_bounds__(kTrialThreads)
-trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
-    extern __shared__ double trial_s[];  // S*M trial genes when they fit
+trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
+    extern __shared__ __align__(16) double trial_s[];
     __shared__ double s_cr[2], s_fw[2], s_sum[4];
     __shared__ uint32_t s_mut[3];
 
@@ -100,11 +134,14 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
     const uint32_t i = w.index;
     const uint32_t P = R.P, M = R.M, S = R.S;
     const uint64_t PM = (uint64_t)P * M;
+    const uint64_t SM = (uint64_t)S * M;
     const uint32_t parent_buf = R.cur[i];
     const uint32_t dst_buf = init_mode ? parent_buf : 1u - parent_buf;
     double* dst = R.pop + ((uint64_t)dst_buf * S) * PM + (uint64_t)i * M;  // side s at + s*PM
-    const bool in_smem = (uint64_t)S * M <= (uint64_t)smem_genes;
-    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
+    const bool in_smem = SM <= (uint64_t)smem_doubles;
+    const bool terms_in_smem = 2 * SM <= (uint64_t)smem_doubles;
+    double* terms_s = trial_s + SM;
+    const uint64_t base = (uint64_t)i * (1ull + SM);
 
     if (!init_mode) {
         if (threadIdx.x == 0) {
@@ -135,6 +172,8 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
                 s_fw[s] = fw;
                 R.fw[(uint64_t)S * P + s * P + i] = fw;
             }
+            // rejection sampling as in the reference; P >= 4 is enforced on
+            // the host, so every loop has an admissible outcome
             uint64_t r0 = i, r1 = i, r2 = i;
             while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
             while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
@@ -147,32 +186,53 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
         __syncthreads();
 
         // crossover draw + DE/rand/1 mutation per gene
-        // (deac_gpu.cu:514-539, 635-643)
+        // (deac_gpu.cu:514-539, 635-643).  Two genes per thread per pass so
+        // that their state and parent loads are in flight together.
         const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
-        const uint8_t b0 = R.cur[r0], b1 = R.cur[r1], b2 = R.cur[r2];
+        const uint64_t buf = (uint64_t)S * PM;  // stride between the two buffers
+        const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
+        const double* pb = R.pop + (uint64_t)R.cur[r1] * buf + (uint64_t)r1 * M;
+        const double* pc = R.pop + (uint64_t)R.cur[r2] * buf + (uint64_t)r2 * M;
+        const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
         const bool keep_sign = (R.flags & kSignedWeights) != 0;
-        const uint64_t SM = (uint64_t)S * M;
-        for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
-            const uint32_t s = (uint32_t)(q / M);
-            const uint32_t j = (uint32_t)(q - (uint64_t)s * M);
-            uint64_t st[4];
-            load_state(R, base + 1 + q, st);
-            const bool mutate = draw(st) < s_cr[s];
-            store_state(R, base + 1 + q, st);
-            const double* side = R.pop + (uint64_t)s * PM;
-            const uint64_t buf = (uint64_t)S * PM;  // stride between the two buffers
-            double v;
-            if (mutate) {
-                const double a = side[b0 * buf + (uint64_t)r0 * M + j];
-                const double b = side[b1 * buf + (uint64_t)r1 * M + j];
-                const double c = side[b2 * buf + (uint64_t)r2 * M + j];
-                v = fma(s_fw[s], b - c, a);
-                if (!keep_sign) v = fabs(v);
-            } else {
-                v = side[parent_buf * buf + (uint64_t)i * M + j];
+        const uint64_t n = R.n_states;
+        for (uint64_t q0 = threadIdx.x; q0 < SM; q0 += 2 * blockDim.x) {
+            uint64_t st[2][4];
+            double a[2], b[2], c[2], x[2];
+            uint32_t sd[2], jj[2];
+            bool ok[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint64_t q = q0 + (uint64_t)h * blockDim.x;
+                ok[h] = q < SM;
+                const uint64_t qq = ok[h] ? q : q0;
+                sd[h] = (uint32_t)(qq / M);
+                jj[h] = (uint32_t)(qq - (uint64_t)sd[h] * M);
+                const uint64_t slot = base + 1 + qq;
+                st[h][0] = R.rng[slot];
+                st[h][1] = R.rng[n + slot];
+                st[h][2] = R.rng[2 * n + slot];
+                st[h][3] = R.rng[3 * n + slot];
+                const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
+                a[h] = pa[off];
+                b[h] = pb[off];
+                c[h] = pc[off];
+                x[h] = px[off];
             }
-            dst[(uint64_t)s * PM + j] = v;
-            if (in_smem) trial_s[q] = v;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (!ok[h]) continue;
+                const uint64_t q = q0 + (uint64_t)h * blockDim.x;
+                const bool mutate = draw(st[h]) < s_cr[sd[h]];
+                store_state(R, base + 1 + q, st[h]);
+                double v = x[h];
+                if (mutate) {
+                    v = fma(s_fw[sd[h]], b[h] - c[h], a[h]);
+                    if (!keep_sign) v = fabs(v);
+                }
+                dst[(uint64_t)sd[h] * PM + jj[h]] = v;
+                if (in_smem) trial_s[q] = v;
+            }
         }
         __syncthreads();
         if (S == 2 && threadIdx.x == 0) {
@@ -183,7 +243,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
         }
         __syncthreads();
     } else if (in_smem) {
-        for (uint64_t q = threadIdx.x; q < (uint64_t)S * M; q += blockDim.x) {
+        for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
             trial_s[q] = dst[(uint64_t)s * PM + (q - (uint64_t)s * M)];
         }
@@ -194,15 +254,32 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
     const double* gene_neg = in_smem ? trial_s + M : dst + PM;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
 
+    // weights of one row sum, staged next to the genes when they fit
+    auto weights = [&](const double* wp, const double* wn, const double*& tp, const double*& tn) {
+        if (terms_in_smem) {
+            for (uint32_t k = threadIdx.x; k < M; k += blockDim.x) {
+                terms_s[k] = wp[k];
+                if (S == 2) terms_s[M + k] = wn[k];
+            }
+            tp = terms_s;
+            tn = terms_s + M;
+        } else {
+            tp = wp;
+            tn = wn;
+        }
+    };
+
     if (R.flags & kNormalize) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
-        if (lane == 0 && warp < S) s_sum[warp] = row_chain(warp == 0 ? gene_pos : gene_neg,
-                                                           warp == 0 ? R.norm_pos : R.norm_neg, M);
+        const double *tp, *tn;
+        weights(R.norm_pos, R.norm_neg, tp, tn);
+        __syncthreads();
+        if (lane == 0 && warp < S) s_sum[warp] = chain(warp == 0 ? gene_pos : gene_neg, warp == 0 ? tp : tn, M, 0.0);
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
-        for (uint64_t q = threadIdx.x; q < (uint64_t)S * M; q += blockDim.x) {
+        for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
             const uint64_t g = (uint64_t)s * PM + (q - (uint64_t)s * M);
             const double v = (in_smem ? trial_s[q] : dst[g]) * recip;
@@ -212,76 +289,99 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes) {
         __syncthreads();
     }
 
-    if (R.flags & (kFirstMoment | kThirdMoment)) {
-        // moment row sums with alpha = 1 (deac.cpp:1418-1477)
-        if (lane == 0) {
-            const bool first = warp < 2 && (R.flags & kFirstMoment);
-            const bool third = warp >= 2 && warp < 4 && (R.flags & kThirdMoment);
-            const uint32_t side = warp & 1u;
-            if ((first || third) && side < S) {
-                const double* t = first ? (side ? R.first_neg : R.first_pos) : (side ? R.third_neg : R.third_pos);
-                s_sum[warp] = row_chain(side ? gene_neg : gene_pos, t, M);
-            }
-        }
+    // moment row sums with alpha = 1 (deac.cpp:1418-1477)
+    for (int which = 0; which < 2; ++which) {
+        const uint32_t flag = which == 0 ? kFirstMoment : kThirdMoment;
+        if (!(R.flags & flag)) continue;
+        const double *tp, *tn;
+        weights(which == 0 ? R.first_pos : R.third_pos, which == 0 ? R.first_neg : R.third_neg, tp, tn);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            if (R.flags & kFirstMoment)
-                R.moments[2 * i] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
-            if (R.flags & kThirdMoment)
-                R.moments[2 * i + 1] = gemv_pair(s_sum[2], S == 2 ? s_sum[3] : 0.0, 1.0, S == 2);
-        }
+        if (lane == 0 && warp < S) s_sum[warp] = chain(warp == 0 ? gene_pos : gene_neg, warp == 0 ? tp : tn, M, 0.0);
+        __syncthreads();
+        if (threadIdx.x == 0) R.moments[2 * i + which] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
+        __syncthreads();
     }
 }
 
 // ------------------------------------------------------------- contract
-__global__ void __launch_bounds__(256) contract_kernel(RunDev* runs, const Work* work, int init_mode) {
-    __shared__ double slots[kTailWarps][kTreeSlots];
+// Dynamic shared memory: two stages of `chunk` genes of every pop row and K
+// row the CTA needs ([S][member_tile] pop rows, then [S][tau_tile] K rows,
+// row stride chunk+2), reused by the finishing CTA as 4 x 1024 reduction
+// slots.
+__global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int init_mode) {
+    extern __shared__ __align__(16) double dyn[];
     __shared__ int s_last;
 
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
     if (R.done) return;
     const uint32_t P = R.P, M = R.M, Nt = R.Nt, S = R.S;
+    const uint32_t MT = R.member_tile, TT = R.tau_tile, CH = R.chunk;
     const uint64_t PM = (uint64_t)P * M;
-    const uint32_t member_tiles = (P + R.member_tile - 1) / R.member_tile;
+    const uint32_t member_tiles = (P + MT - 1) / MT;
     const uint32_t mt = w.index % member_tiles, tt = w.index / member_tiles;
-    const uint32_t i = mt * R.member_tile + threadIdx.x % R.member_tile;
-    const uint32_t t = tt * R.tau_tile + threadIdx.x / R.member_tile;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t pair = S == 2 ? warp * 16 + (lane & 15u) : threadIdx.x;
+    const uint32_t side = S == 2 ? (lane >> 4) : 0u;
+    const uint32_t mi = pair % MT, ti = pair / MT;
+    const uint32_t i = mt * MT + mi, t = tt * TT + ti;
+    const bool valid = ti < TT && i < P && t < Nt;
+    const uint32_t stride = stage_stride(CH);
+    const uint32_t rows = S * (MT + TT);
+    double* stage0 = dyn;
+    double* stage1 = dyn + (uint64_t)rows * stride;
+    const bool vec = (M & 1u) == 0;  // 16-byte copies need 16-byte aligned rows
 
-    if (threadIdx.x < R.member_tile * R.tau_tile && i < P && t < Nt) {
-        // E[i,t]: two k-ascending FMA chains (gpu_matmul, deac_gpu.cu:277-315,
-        // called once per side: C = 1*c_pos + 0*C, then C = 1*c_neg + 1*C)
-        const uint32_t buf = init_mode ? R.cur[i] : 1u - R.cur[i];
-        const double* xp = R.pop + (uint64_t)buf * S * PM + (uint64_t)i * M;
-        const double* kp = R.k_pos + (uint64_t)t * M;
-        double cp = 0.0, cn = 0.0;
-        if (S == 2) {
-            const double* xn = xp + PM;
-            const double* kn = R.k_neg + (uint64_t)t * M;
-            uint32_t k = 0;
-            // 16-byte loads need every row start 16-byte aligned: M even
-            // (buffers come from cudaMalloc, 256-byte aligned)
-            const uint32_t vec_end = (M & 1u) ? 0u : M;
-            for (; k + 2 <= vec_end; k += 2) {
-                const double2 a = *reinterpret_cast<const double2*>(xp + k);
-                const double2 b = __ldg(reinterpret_cast<const double2*>(kp + k));
-                const double2 c = *reinterpret_cast<const double2*>(xn + k);
-                const double2 d = __ldg(reinterpret_cast<const double2*>(kn + k));
-                cp = fma(a.x, b.x, cp);
-                cn = fma(c.x, d.x, cn);
-                cp = fma(a.y, b.y, cp);
-                cn = fma(c.y, d.y, cn);
+    // stage `CH` genes starting at k0 of every row into buffer `b`
+    auto issue = [&](double* b, uint32_t k0) {
+        const uint32_t n = min(CH, M - k0);
+        const uint32_t units = vec ? (n + 1) / 2 : n;
+        for (uint32_t e = threadIdx.x; e < rows * units; e += blockDim.x) {
+            const uint32_t r = e / units, u = e - r * units;
+            const double* src;
+            if (r < S * MT) {
+                const uint32_t s = r / MT, m = mt * MT + (r - s * MT);
+                if (m >= P) continue;
+                const uint32_t bsel = init_mode ? R.cur[m] : 1u - R.cur[m];
+                src = R.pop + ((uint64_t)bsel * S + s) * PM + (uint64_t)m * M + k0;
+            } else {
+                const uint32_t rr = r - S * MT;
+                const uint32_t s = rr / TT, tau = tt * TT + (rr - s * TT);
+                if (tau >= Nt) continue;
+                src = (s ? R.k_neg : R.k_pos) + (uint64_t)tau * M + k0;
             }
-            for (; k < M; ++k) {
-                cp = fma(xp[k], __ldg(kp + k), cp);
-                cn = fma(xn[k], __ldg(kn + k), cn);
-            }
-            R.model_isf[(uint64_t)i * Nt + t] = cn + cp;
-        } else {
-            for (uint32_t k = 0; k < M; ++k) cp = fma(xp[k], __ldg(kp + k), cp);
-            R.model_isf[(uint64_t)i * Nt + t] = cp;
+            double* d = b + (uint64_t)r * stride;
+            if (vec) cp_async16(d + 2 * u, src + 2 * u);
+            else cp_async8(d + u, src + u);
         }
+        cp_async_commit();
+    };
+
+    // E[i,t]: one k-ascending FMA chain per side from 0 (gpu_matmul,
+    // deac_gpu.cu:277-315), staged through shared memory, double-buffered
+    double acc = 0.0;
+    const uint32_t nst = (M + CH - 1) / CH;
+    issue(stage0, 0);
+    for (uint32_t st = 0; st < nst; ++st) {
+        double* cur = (st & 1u) ? stage1 : stage0;
+        if (st + 1 < nst) {
+            issue((st & 1u) ? stage0 : stage1, (st + 1) * CH);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        if (valid) {
+            const double* xr = cur + (uint64_t)(side * MT + mi) * stride;
+            const double* kr = cur + (uint64_t)(S * MT + side * TT + ti) * stride;
+            acc = chain(xr, kr, min(CH, M - st * CH), acc);
+        }
+        __syncthreads();
     }
+    // the two gpu_matmul calls: C = 1*c_pos + 0*C, then C = 1*c_neg + 1*C
+    double e = acc;
+    if (S == 2) e = __shfl_xor_sync(0xffffffffu, acc, 16) + acc;
+    if (valid && side == 0) R.model_isf[(uint64_t)i * Nt + t] = e;
 
     // the last CTA of this run finishes the generation
     __threadfence();
@@ -294,49 +394,45 @@ __global__ void __launch_bounds__(256) contract_kernel(RunDev* runs, const Work*
     if (!s_last) return;
     __threadfence();
 
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t lanes = Nt < kTreeSlots ? Nt : kTreeSlots;
     const uint32_t width = pow2_ceil(lanes);
     double* fit_dst = init_mode ? R.fit_old : R.fit_new;
+    double* sl = dyn + (uint64_t)warp * kTreeSlots;
 
     // reduced chi^2 (deac_gpu.cu:417-448) plus the moment terms
-    // (deac_gpu.cu:450-456; order of deac.cpp:1479-1499)
-    if (warp < kTailWarps) {
-        double* sl = slots[warp];
-        const volatile double* E_all = R.model_isf;
-        for (uint32_t m = warp; m < P; m += (nwarps < kTailWarps ? nwarps : kTailWarps)) {
-            for (uint32_t s = lane; s < width; s += 32) {
-                double v = 0.0;
-                for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
-                    const double term = (R.isf[idx] - E_all[(uint64_t)m * Nt + idx]) / R.err[idx];
-                    v = fma(term, term, v);
-                }
-                sl[s] = v;
+    // (deac_gpu.cu:450-456; order of deac.cpp:1479-1499), a warp per member
+    const volatile double* E_all = R.model_isf;
+    for (uint32_t m = warp; m < P; m += nwarps) {
+        for (uint32_t s = lane; s < width; s += 32) {
+            double v = 0.0;
+            for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
+                const double term = (R.isf[idx] - E_all[(uint64_t)m * Nt + idx]) / R.err[idx];
+                v = fma(term, term, v);
             }
-            __syncwarp();
-            const double total = warp_tree(sl, width);
-            if (lane == 0) {
-                double fit = total / (double)Nt;
-                if (R.flags & kNegativeFirstMoment) {
-                    double mom = 0.0;
-                    for (uint32_t idx = 0; idx < Nt; ++idx)
-                        mom = fma(E_all[(uint64_t)m * Nt + idx], R.tau_w[idx], mom);
-                    const double term = (R.negfirst_target - mom) / R.negfirst_error;
-                    fit = fma(term, term, fit);
-                }
-                if (R.flags & kFirstMoment) {
-                    const double term = (R.first_target - R.moments[2 * m]) / 1.0;
-                    fit = fma(term, term, fit);
-                }
-                if (R.flags & kThirdMoment) {
-                    const double term = (R.third_target - R.moments[2 * m + 1]) / R.third_error;
-                    fit = fma(term, term, fit);
-                }
-                fit_dst[m] = fit;
-            }
-            __syncwarp();
+            sl[s] = v;
         }
+        __syncwarp();
+        const double total = warp_tree(sl, width);
+        if (lane == 0) {
+            double fit = total / (double)Nt;
+            if (R.flags & kNegativeFirstMoment) {
+                double mom = 0.0;
+                for (uint32_t idx = 0; idx < Nt; ++idx) mom = fma(E_all[(uint64_t)m * Nt + idx], R.tau_w[idx], mom);
+                const double term = (R.negfirst_target - mom) / R.negfirst_error;
+                fit = fma(term, term, fit);
+            }
+            if (R.flags & kFirstMoment) {
+                const double term = (R.first_target - R.moments[2 * m]) / 1.0;
+                fit = fma(term, term, fit);
+            }
+            if (R.flags & kThirdMoment) {
+                const double term = (R.third_target - R.moments[2 * m + 1]) / R.third_error;
+                fit = fma(term, term, fit);
+            }
+            fit_dst[m] = fit;
+        }
+        __syncwarp();
     }
     __syncthreads();
 
@@ -370,7 +466,6 @@ __global__ void __launch_bounds__(256) contract_kernel(RunDev* runs, const Work*
                 // fitness mean and mean of squares (deac_gpu.cu:458-512)
                 const uint32_t pl = P < kTreeSlots ? P : kTreeSlots;
                 const uint32_t pw = pow2_ceil(pl);
-                double* sl = slots[0];
                 for (int sq = 0; sq < 2; ++sq) {
                     for (uint32_t s = lane; s < pw; s += 32) {
                         double v = 0.0;

@@ -49,8 +49,9 @@ struct RunDev {
     uint32_t P, M, Nt, S;
     uint32_t flags;
     uint32_t contract_ctas;  // CTAs of contract_kernel for this run
-    uint32_t member_tile;    // members per contract CTA
+    uint32_t member_tile;    // members per contract CTA (power of two)
     uint32_t tau_tile;       // timeslices per contract CTA
+    uint32_t chunk;          // genes per shared-memory stage of contract_kernel
     uint64_t N;              // number_of_generations
     double tau_cr, tau_f;    // self-adaptation probabilities
     double alpha;            // 1 / F(0), the normalisation scale
@@ -107,12 +108,25 @@ __host__ __device__ inline uint64_t rng_slot(uint32_t P, uint32_t M, uint32_t S,
     return i * (1ull + (uint64_t)S * M) + 1 + s * M + j;
 }
 
+// contract_kernel: 128 threads, one FMA chain per thread.  Two-sided runs
+// put the positive-side chain of an (member, timeslice) pair in lane l and
+// the negative-side chain in lane l+16 of the same warp, so a CTA covers 64
+// pairs; one-sided runs cover 128.
+constexpr int kContractThreads = 128;
+__host__ __device__ inline uint32_t contract_pairs(uint32_t S) { return S == 2 ? 64u : 128u; }
+// shared-memory row stride of a staged chunk (even, so rows stay 16-byte
+// aligned; the 2-double pad spreads rows over the banks)
+__host__ __device__ inline uint32_t stage_stride(uint32_t chunk) { return chunk + 2; }
+__host__ __device__ inline uint64_t stage_doubles(uint32_t S, uint32_t mt, uint32_t tt, uint32_t chunk) {
+    return (uint64_t)S * (mt + tt) * stage_stride(chunk);
+}
+
 struct Work {
     uint32_t run;
     uint32_t index;  // member (trial) or tile (contract)
 };
 
-__global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_genes);
+__global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
 __global__ void contract_kernel(RunDev* runs, const Work* work, int init_mode);
 
 }  // namespace deac
