@@ -117,7 +117,7 @@ struct deac_batch {
 namespace {
 
 int launch_generation(deac_batch* b, cudaStream_t s, int init_mode) {
-    deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
+    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
                                                                           init_mode, b->smem_doubles);
     deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s>>>(
         b->d_runs, b->d_contract_work, init_mode);
@@ -126,7 +126,7 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode) {
 
 int launch_generation_timed(deac_batch* b) {
     CUDA_TRY(cudaEventRecord(b->ev[0], b->stream));
-    deac::trial_kernel<<<b->n_trial_ctas, 256, b->trial_smem_bytes, b->stream>>>(
+    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, b->stream>>>(
         b->d_runs, b->d_trial_work, 0, b->smem_doubles);
     CUDA_TRY(cudaEventRecord(b->ev[1], b->stream));
     deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, b->stream>>>(
@@ -437,7 +437,7 @@ int deac_batch_setup(deac_batch* b) {
             for (auto& th : pool) th.join();
         }
     }
-    uint64_t trial_doubles = 0, contract_bytes = kTailSlotsBytes;
+    uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         RunHost& r = *b->runs[ri];

@@ -10,7 +10,6 @@ namespace deac {
 
 namespace {
 
-constexpr int kTrialThreads = 256;
 constexpr int kTreeSlots = 1024;   // GPU_BLOCK_SIZE of the reference reductions
 
 __device__ __forceinline__ void load_state(const RunDev& R, uint64_t slot, uint64_t s[4]) {
@@ -31,6 +30,15 @@ __device__ __forceinline__ void store_state(const RunDev& R, uint64_t slot, cons
 
 __device__ __forceinline__ double draw(uint64_t s[4]) {
     return to_unit(xoshiro_next(s[0], s[1], s[2], s[3]));
+}
+
+// Integer form of the crossover test  (x >> 11) * 2^-53 < cr
+// (deac_gpu.cu:641): with m = x >> 11 < 2^53 and X = cr * 2^53 (exact),
+// m < X  <=>  m < ceil(X).  Keeps the FP64 pipe free for the row-sum chain.
+__device__ __forceinline__ uint64_t crossover_threshold(double cr) {
+    if (!(cr > 0.0)) return 0;
+    if (cr >= 1.0) return 1ull << 53;
+    return (uint64_t)ceil(cr * 0x1.0p53);
 }
 
 // k-ascending FMA chain continuing from `acc` (the inner loops of
@@ -126,6 +134,7 @@ __global__ void __launch_bounds__(kTrialThreads)
 trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     extern __shared__ __align__(16) double trial_s[];
     __shared__ double s_cr[2], s_fw[2], s_sum[4];
+    __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
 
     const Work w = work[blockIdx.x];
@@ -143,116 +152,8 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     double* terms_s = trial_s + SM;
     const uint64_t base = (uint64_t)i * (1ull + SM);
 
-    if (!init_mode) {
-        if (threadIdx.x == 0) {
-            // jDE (deac_gpu.cu:584-606): CR(+) on slot 0, F(+) slot 1,
-            // CR(-) slot 2, F(-) slot 3; then mutant indices on slot 0
-            // (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.
-            uint64_t st[4];
-            load_state(R, base, st);
-            for (uint32_t s = 0; s < S; ++s) {
-                uint64_t* cur = st;
-                uint64_t tmp[4];
-                if (s == 1) {
-                    load_state(R, base + 2, tmp);
-                    cur = tmp;
-                }
-                const double cr_old = R.cr[s * P + i];
-                const double cr = draw(cur) < R.tau_cr ? draw(cur) : cr_old;
-                if (s == 1) store_state(R, base + 2, tmp);
-                s_cr[s] = cr;
-                R.cr[(uint64_t)S * P + s * P + i] = cr;
-
-                uint64_t fs[4];
-                const uint64_t fslot = base + (s == 0 ? 1 : 3);
-                load_state(R, fslot, fs);
-                const double fw_old = R.fw[s * P + i];
-                const double fw = draw(fs) < R.tau_f ? 2.0 * draw(fs) : fw_old;
-                store_state(R, fslot, fs);
-                s_fw[s] = fw;
-                R.fw[(uint64_t)S * P + s * P + i] = fw;
-            }
-            // rejection sampling as in the reference; P >= 4 is enforced on
-            // the host, so every loop has an admissible outcome
-            uint64_t r0 = i, r1 = i, r2 = i;
-            while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-            while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-            while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-            store_state(R, base, st);
-            s_mut[0] = (uint32_t)r0;
-            s_mut[1] = (uint32_t)r1;
-            s_mut[2] = (uint32_t)r2;
-        }
-        __syncthreads();
-
-        // crossover draw + DE/rand/1 mutation per gene
-        // (deac_gpu.cu:514-539, 635-643).  Two genes per thread per pass so
-        // that their state and parent loads are in flight together.
-        const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
-        const uint64_t buf = (uint64_t)S * PM;  // stride between the two buffers
-        const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
-        const double* pb = R.pop + (uint64_t)R.cur[r1] * buf + (uint64_t)r1 * M;
-        const double* pc = R.pop + (uint64_t)R.cur[r2] * buf + (uint64_t)r2 * M;
-        const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
-        const bool keep_sign = (R.flags & kSignedWeights) != 0;
-        const uint64_t n = R.n_states;
-        for (uint64_t q0 = threadIdx.x; q0 < SM; q0 += 2 * blockDim.x) {
-            uint64_t st[2][4];
-            double a[2], b[2], c[2], x[2];
-            uint32_t sd[2], jj[2];
-            bool ok[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const uint64_t q = q0 + (uint64_t)h * blockDim.x;
-                ok[h] = q < SM;
-                const uint64_t qq = ok[h] ? q : q0;
-                sd[h] = (uint32_t)(qq / M);
-                jj[h] = (uint32_t)(qq - (uint64_t)sd[h] * M);
-                const uint64_t slot = base + 1 + qq;
-                st[h][0] = R.rng[slot];
-                st[h][1] = R.rng[n + slot];
-                st[h][2] = R.rng[2 * n + slot];
-                st[h][3] = R.rng[3 * n + slot];
-                const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
-                a[h] = pa[off];
-                b[h] = pb[off];
-                c[h] = pc[off];
-                x[h] = px[off];
-            }
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (!ok[h]) continue;
-                const uint64_t q = q0 + (uint64_t)h * blockDim.x;
-                const bool mutate = draw(st[h]) < s_cr[sd[h]];
-                store_state(R, base + 1 + q, st[h]);
-                double v = x[h];
-                if (mutate) {
-                    v = fma(s_fw[sd[h]], b[h] - c[h], a[h]);
-                    if (!keep_sign) v = fabs(v);
-                }
-                dst[(uint64_t)sd[h] * PM + jj[h]] = v;
-                if (in_smem) trial_s[q] = v;
-            }
-        }
-        __syncthreads();
-        if (S == 2 && threadIdx.x == 0) {
-            // gpu_match_population_zero (deac_gpu.cu:541-549)
-            const double z = in_smem ? trial_s[0] : dst[0];
-            dst[PM] = z;
-            if (in_smem) trial_s[M] = z;
-        }
-        __syncthreads();
-    } else if (in_smem) {
-        for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
-            const uint32_t s = (uint32_t)(q / M);
-            trial_s[q] = dst[(uint64_t)s * PM + (q - (uint64_t)s * M)];
-        }
-        __syncthreads();
-    }
-
-    const double* gene_pos = in_smem ? trial_s : dst;
-    const double* gene_neg = in_smem ? trial_s + M : dst + PM;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const bool normalize = (R.flags & kNormalize) != 0;
 
     // weights of one row sum, staged next to the genes when they fit
     auto weights = [&](const double* wp, const double* wn, const double*& tp, const double*& tn) {
@@ -268,14 +169,160 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             tn = wn;
         }
     };
+    const double *norm_p = nullptr, *norm_n = nullptr;
+    if (normalize) weights(R.norm_pos, R.norm_neg, norm_p, norm_n);
 
-    if (R.flags & kNormalize) {
+    if (!init_mode && threadIdx.x == 0) {
+        // jDE (deac_gpu.cu:584-606): CR(+) on slot 0, F(+) slot 1,
+        // CR(-) slot 2, F(-) slot 3; then mutant indices on slot 0
+        // (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.
+        uint64_t st[4];
+        load_state(R, base, st);
+        for (uint32_t s = 0; s < S; ++s) {
+            uint64_t* cur = st;
+            uint64_t tmp[4];
+            if (s == 1) {
+                load_state(R, base + 2, tmp);
+                cur = tmp;
+            }
+            const double cr_old = R.cr[s * P + i];
+            const double cr = draw(cur) < R.tau_cr ? draw(cur) : cr_old;
+            if (s == 1) store_state(R, base + 2, tmp);
+            s_cr[s] = cr;
+            s_thr[s] = crossover_threshold(cr);
+            R.cr[(uint64_t)S * P + s * P + i] = cr;
+
+            uint64_t fs[4];
+            const uint64_t fslot = base + (s == 0 ? 1 : 3);
+            load_state(R, fslot, fs);
+            const double fw_old = R.fw[s * P + i];
+            const double fw = draw(fs) < R.tau_f ? 2.0 * draw(fs) : fw_old;
+            store_state(R, fslot, fs);
+            s_fw[s] = fw;
+            R.fw[(uint64_t)S * P + s * P + i] = fw;
+        }
+        // rejection sampling as in the reference; P >= 4 is enforced on
+        // the host, so every loop has an admissible outcome
+        uint64_t r0 = i, r1 = i, r2 = i;
+        while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+        while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+        while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+        store_state(R, base, st);
+        s_mut[0] = (uint32_t)r0;
+        s_mut[1] = (uint32_t)r1;
+        s_mut[2] = (uint32_t)r2;
+    }
+    __syncthreads();
+
+    const double* gene_pos = in_smem ? trial_s : dst;
+    const double* gene_neg = in_smem ? trial_s + M : dst + PM;
+    // row-sum chains of the normalisation: lane 0 of warp 0 the positive
+    // side, lane 1 the negative side (one FP64 instruction per step for both)
+    double chain_acc = 0.0;
+    const bool chain_lane = warp == 0 && lane < S;
+    const double* chain_x = lane == 0 ? gene_pos : gene_neg;
+    const double* chain_w = lane == 0 ? norm_p : norm_n;
+
+    if (!init_mode) {
+        // crossover draw + DE/rand/1 mutation per gene (deac_gpu.cu:514-539,
+        // 635-643), in chunks of kGeneChunk genes per side.  With
+        // --normalize, warp 0 runs the row-sum chains over chunk c while the
+        // other warps produce chunk c+1; one barrier per chunk.
+        const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
+        const uint64_t buf = (uint64_t)S * PM;  // stride between the two buffers
+        const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
+        const double* pb = R.pop + (uint64_t)R.cur[r1] * buf + (uint64_t)r1 * M;
+        const double* pc = R.pop + (uint64_t)R.cur[r2] * buf + (uint64_t)r2 * M;
+        const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
+        const bool keep_sign = (R.flags & kSignedWeights) != 0;
+        const uint64_t n = R.n_states;
+        constexpr uint32_t kGeneChunk = 256;
+        const uint32_t nchunks = (M + kGeneChunk - 1) / kGeneChunk;
+
+        // genes [c*kGeneChunk, ...) of both sides, by worker `wid` of `nt`
+        auto produce = [&](uint32_t c, uint32_t wid, uint32_t nt) {
+            const uint32_t j0 = c * kGeneChunk;
+            const uint32_t len = min(kGeneChunk, M - j0);
+            const uint32_t items = S * len;
+            for (uint32_t e0 = wid; e0 < items; e0 += 2 * nt) {
+                uint64_t st[2][4];
+                double a[2], b[2], cc[2], x[2];
+                uint32_t sd[2], jj[2];
+                bool ok[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t e = e0 + (uint32_t)h * nt;
+                    ok[h] = e < items;
+                    const uint32_t ee = ok[h] ? e : e0;
+                    sd[h] = ee / len;
+                    jj[h] = j0 + (ee - sd[h] * len);
+                    const uint64_t slot = base + 1 + (uint64_t)sd[h] * M + jj[h];
+                    st[h][0] = R.rng[slot];
+                    st[h][1] = R.rng[n + slot];
+                    st[h][2] = R.rng[2 * n + slot];
+                    st[h][3] = R.rng[3 * n + slot];
+                    const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
+                    a[h] = pa[off];
+                    b[h] = pb[off];
+                    cc[h] = pc[off];
+                    x[h] = px[off];
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!ok[h]) continue;
+                    const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
+                    store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
+                    double v = x[h];
+                    if (mutate) {
+                        v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
+                        if (!keep_sign) v = fabs(v);
+                    }
+                    dst[(uint64_t)sd[h] * PM + jj[h]] = v;
+                    if (in_smem) trial_s[(uint64_t)sd[h] * M + jj[h]] = v;
+                }
+            }
+        };
+
+        produce(0, threadIdx.x, blockDim.x);
+        __syncthreads();
+        if (S == 2 && threadIdx.x == 0) {
+            // gpu_match_population_zero (deac_gpu.cu:541-549)
+            const double z = in_smem ? trial_s[0] : dst[0];
+            dst[PM] = z;
+            if (in_smem) trial_s[M] = z;
+        }
+        __syncthreads();
+        for (uint32_t c = 0; c < nchunks; ++c) {
+            if (normalize) {
+                if (chain_lane) {
+                    const uint32_t j0 = c * kGeneChunk;
+                    chain_acc = chain(chain_x + j0, chain_w + j0, min(kGeneChunk, M - j0), chain_acc);
+                }
+                // producers keep off the chain warp's SM sub-partition
+                // (warps 4, 8, 12 share it with warp 0 and stay idle)
+                const uint32_t nwarps = blockDim.x >> 5;
+                if ((warp & 3u) != 0 && c + 1 < nchunks)
+                    produce(c + 1, (warp - (warp >> 2) - 1) * 32 + lane, (nwarps - (nwarps + 3) / 4) * 32);
+            } else if (c + 1 < nchunks) {
+                produce(c + 1, threadIdx.x, blockDim.x);
+            }
+            __syncthreads();
+        }
+    } else if (in_smem) {
+        for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
+            const uint32_t s = (uint32_t)(q / M);
+            trial_s[q] = dst[(uint64_t)s * PM + (q - (uint64_t)s * M)];
+        }
+        __syncthreads();
+        if (normalize && chain_lane) chain_acc = chain(chain_x, chain_w, M, 0.0);
+    } else if (normalize && chain_lane) {
+        chain_acc = chain(chain_x, chain_w, M, 0.0);
+    }
+
+    if (normalize) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
-        const double *tp, *tn;
-        weights(R.norm_pos, R.norm_neg, tp, tn);
-        __syncthreads();
-        if (lane == 0 && warp < S) s_sum[warp] = chain(warp == 0 ? gene_pos : gene_neg, warp == 0 ? tp : tn, M, 0.0);
+        if (chain_lane) s_sum[lane] = chain_acc;
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
@@ -296,7 +343,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         const double *tp, *tn;
         weights(which == 0 ? R.first_pos : R.third_pos, which == 0 ? R.first_neg : R.third_neg, tp, tn);
         __syncthreads();
-        if (lane == 0 && warp < S) s_sum[warp] = chain(warp == 0 ? gene_pos : gene_neg, warp == 0 ? tp : tn, M, 0.0);
+        if (chain_lane) s_sum[lane] = chain(chain_x, lane == 0 ? tp : tn, M, 0.0);
         __syncthreads();
         if (threadIdx.x == 0) R.moments[2 * i + which] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
         __syncthreads();
@@ -332,27 +379,50 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     double* stage1 = dyn + (uint64_t)rows * stride;
     const bool vec = (M & 1u) == 0;  // 16-byte copies need 16-byte aligned rows
 
-    // stage `CH` genes starting at k0 of every row into buffer `b`
-    auto issue = [&](double* b, uint32_t k0) {
-        const uint32_t n = min(CH, M - k0);
-        const uint32_t units = vec ? (n + 1) / 2 : n;
-        for (uint32_t e = threadIdx.x; e < rows * units; e += blockDim.x) {
-            const uint32_t r = e / units, u = e - r * units;
-            const double* src;
+    // Each thread owns fixed rows of every stage (at most two, since a stage
+    // has at most 2*(64+1) rows) and a fixed stride of 16-byte units within
+    // them, so issuing a copy costs one address add; resolved once here.
+    const uint32_t tpr = rows >= blockDim.x ? 1u : blockDim.x / rows;  // threads per row
+    const uint32_t sub = threadIdx.x % tpr;
+    const uint32_t rstep = blockDim.x / tpr;
+    const double* src_row[2] = {nullptr, nullptr};
+    uint32_t dst_row[2] = {0u, 0u};
+    {
+        double* const pop = R.pop;
+        const double* const kp = R.k_pos;
+        const double* const kn = R.k_neg;
+        for (uint32_t j = 0; j < 2; ++j) {
+            const uint32_t r = threadIdx.x / tpr + j * rstep;
+            if (r >= rows) break;
+            dst_row[j] = r;
             if (r < S * MT) {
                 const uint32_t s = r / MT, m = mt * MT + (r - s * MT);
-                if (m >= P) continue;
-                const uint32_t bsel = init_mode ? R.cur[m] : 1u - R.cur[m];
-                src = R.pop + ((uint64_t)bsel * S + s) * PM + (uint64_t)m * M + k0;
+                if (m < P) {
+                    const uint32_t bsel = init_mode ? R.cur[m] : 1u - R.cur[m];
+                    src_row[j] = pop + ((uint64_t)bsel * S + s) * PM + (uint64_t)m * M;
+                }
             } else {
                 const uint32_t rr = r - S * MT;
                 const uint32_t s = rr / TT, tau = tt * TT + (rr - s * TT);
-                if (tau >= Nt) continue;
-                src = (s ? R.k_neg : R.k_pos) + (uint64_t)tau * M + k0;
+                if (tau < Nt) src_row[j] = (s ? kn : kp) + (uint64_t)tau * M;
             }
-            double* d = b + (uint64_t)r * stride;
-            if (vec) cp_async16(d + 2 * u, src + 2 * u);
-            else cp_async8(d + u, src + u);
+        }
+    }
+
+    // stage `CH` genes starting at k0 of every row into buffer `b`
+    auto issue = [&](double* b, uint32_t k0) {
+        const uint32_t n = min(CH, M - k0);
+        const uint32_t units = vec ? n / 2 : n;  // M even => k0 and n even
+#pragma unroll
+        for (uint32_t j = 0; j < 2; ++j) {
+            if (src_row[j] == nullptr) continue;
+            double* d = b + (uint64_t)dst_row[j] * stride;
+            const double* src = src_row[j] + k0;
+            if (vec) {
+                for (uint32_t u = sub; u < units; u += tpr) cp_async16(d + 2 * u, src + 2 * u);
+            } else {
+                for (uint32_t u = sub; u < units; u += tpr) cp_async8(d + u, src + u);
+            }
         }
         cp_async_commit();
     };

@@ -108,11 +108,16 @@ __host__ __device__ inline uint64_t rng_slot(uint32_t P, uint32_t M, uint32_t S,
     return i * (1ull + (uint64_t)S * M) + 1 + s * M + j;
 }
 
-// contract_kernel: 128 threads, one FMA chain per thread.  Two-sided runs
-// put the positive-side chain of an (member, timeslice) pair in lane l and
-// the negative-side chain in lane l+16 of the same warp, so a CTA covers 64
-// pairs; one-sided runs cover 128.
+// contract_kernel: 128 threads (4 warps), one FMA chain per thread.
+// Two-sided runs put the positive-side chain of a (member, timeslice) pair in
+// lane l and the negative-side chain in lane l+16 of the same warp, so a CTA
+// covers 64 pairs; one-sided runs cover 128.  Each SM sub-partition retires
+// one FP64 warp-instruction per ~64 cycles, and a second CTA on the same SM
+// lands its warps on the same sub-partitions, doubling the cost of a chain
+// step.  The host therefore requests enough shared memory to keep one CTA
+// per SM: 4 warps, one per sub-partition, ~80 cycles per dependent step.
 constexpr int kContractThreads = 128;
+constexpr uint32_t kContractMinSmemBytes = 116 * 1024;  // > half of an SM's 228 KB
 __host__ __device__ inline uint32_t contract_pairs(uint32_t S) { return S == 2 ? 64u : 128u; }
 // shared-memory row stride of a staged chunk (even, so rows stay 16-byte
 // aligned; the 2-double pad spreads rows over the banks)
@@ -120,6 +125,8 @@ __host__ __device__ inline uint32_t stage_stride(uint32_t chunk) { return chunk 
 __host__ __device__ inline uint64_t stage_doubles(uint32_t S, uint32_t mt, uint32_t tt, uint32_t chunk) {
     return (uint64_t)S * (mt + tt) * stage_stride(chunk);
 }
+
+constexpr int kTrialThreads = 512;
 
 struct Work {
     uint32_t run;
