@@ -27,6 +27,7 @@
 #include "deac_kernels.cuh"
 #include "deac_model.hpp"
 #include "deac_rng.cuh"
+#include "deac_split.cuh"
 
 namespace {
 
@@ -65,10 +66,15 @@ struct Arena {
     }
 };
 
-// Device copy of a kernel matrix, shared by runs with identical inputs.
+// Device copy of a kernel matrix, shared by runs with identical inputs,
+// with its BF16 digit planes for the split engine.
 struct KernelMatrix {
     double* k_pos = nullptr;
     double* k_neg = nullptr;
+    uint16_t* kdig = nullptr;   // [kDigits][S][Nt][M]
+    int16_t* kexp = nullptr;    // [Nt][M/kChunk]
+    int16_t* kexp_max = nullptr;  // [Nt]
+    uint32_t group = 0;         // index of the runs sharing it (split tiles)
 };
 
 struct RunHost {
@@ -82,7 +88,10 @@ struct RunHost {
     uint64_t n_states = 0;
     uint64_t trace_cap = 0;
     char* arena = nullptr;               // device allocation of this run
+    char* split_arena = nullptr;         // split-engine buffers of this run
     deac::RunDev dev{};                  // host copy of the descriptor
+    deac::SplitRun split{};              // host copy of the split descriptor
+    uint32_t kgroup = 0;                 // kernel-matrix group (split tiles)
     // results
     bool finished = false;
 };
@@ -107,39 +116,74 @@ struct deac_batch {
     bool set_up = false;
     cudaGraphExec_t graph = nullptr;
     std::vector<deac::RunDev> status;  // host mirror of d_runs
-    // timing
+    // split engine
+    deac::SplitRun* d_split = nullptr;
+    deac::SplitTile* d_tiles = nullptr;
+    deac::SplitRow* d_rows = nullptr;
+    uint32_t n_tiles = 0;
+    int* d_status = nullptr;            // set when a bounded wait gave up
+    // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
+    // passes), 2 digitize, 3 split contraction, 4 split decisions
     bool timing = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    double kernel_ms[2] = {0.0, 0.0};
-    uint64_t kernel_launches[2] = {0, 0};
+    cudaEvent_t ev[8] = {};
+    double kernel_ms[5] = {};
+    uint64_t kernel_launches[5] = {};
 };
 
 namespace {
 
-int launch_generation(deac_batch* b, cudaStream_t s, int init_mode) {
-    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
-                                                                          init_mode, b->smem_doubles);
+void launch_contract(deac_batch* b, cudaStream_t s, int mode) {
     deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s>>>(
-        b->d_runs, b->d_contract_work, init_mode);
-    return DEAC_OK;
+        b->d_runs, b->d_contract_work, mode);
 }
 
-int launch_generation_timed(deac_batch* b) {
-    CUDA_TRY(cudaEventRecord(b->ev[0], b->stream));
-    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, b->stream>>>(
-        b->d_runs, b->d_trial_work, 0, b->smem_doubles);
-    CUDA_TRY(cudaEventRecord(b->ev[1], b->stream));
-    deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, b->stream>>>(
-        b->d_runs, b->d_contract_work, 0);
-    CUDA_TRY(cudaEventRecord(b->ev[2], b->stream));
-    CUDA_TRY(cudaEventSynchronize(b->ev[2]));
-    float a = 0.f, c = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&a, b->ev[0], b->ev[1]));
-    CUDA_TRY(cudaEventElapsedTime(&c, b->ev[1], b->ev[2]));
-    b->kernel_ms[0] += a;
-    b->kernel_ms[1] += c;
-    b->kernel_launches[0] += 1;
-    b->kernel_launches[1] += 1;
+// One generation of every run: two launches for the plain engine; for the
+// split engine trial, digits, tensor-core estimate, interval decisions and
+// the exact passes for what the intervals left open.  With `timed`, events
+// bracket every launch and their device times are accumulated per kind.
+int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed = false) {
+    int e = 0;
+    auto mark = [&](int kind) -> int {
+        if (!timed) return DEAC_OK;
+        CUDA_TRY(cudaEventRecord(b->ev[e + 1], s));
+        CUDA_TRY(cudaEventSynchronize(b->ev[e + 1]));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, b->ev[e], b->ev[e + 1]));
+        b->kernel_ms[kind] += ms;
+        b->kernel_launches[kind] += 1;
+        ++e;
+        return DEAC_OK;
+    };
+    if (timed) CUDA_TRY(cudaEventRecord(b->ev[0], s));
+    int rc;
+    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
+                                                                                        init_mode, b->smem_doubles);
+    if ((rc = mark(0))) return rc;
+    if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
+        launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
+        return mark(1);
+    }
+    deac::digitize_kernel<<<b->n_trial_ctas, 256, 0, s>>>(b->d_runs, b->d_split, b->d_trial_work, 0);
+    if ((rc = mark(2))) return rc;
+    deac::split_contract_kernel<<<b->n_tiles, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
+        b->d_runs, b->d_split, b->d_tiles, b->d_rows, b->d_status);
+    if ((rc = mark(3))) return rc;
+    deac::split_decide_kernel<<<(uint32_t)b->runs.size(), 256, 0, s>>>(b->d_runs, b->d_split, 0);
+    if ((rc = mark(4))) return rc;
+    launch_contract(b, s, deac::kModeParents);
+    launch_contract(b, s, deac::kModeTrials);
+    return mark(1);
+}
+
+int launch_generation_timed(deac_batch* b) { return launch_generation(b, b->stream, 0, true); }
+
+// Split engine: make every parent's fitness exact (the final argmin, the
+// reported minimum and the state fetches read them).
+int finalize_split(deac_batch* b) {
+    if (b->engine != DEAC_ENGINE_SPLIT_BF16) return DEAC_OK;
+    launch_contract(b, b->stream, deac::kModeFinal);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     return DEAC_OK;
 }
 
@@ -202,8 +246,42 @@ int upload_run(deac_batch* b, RunHost& r) {
             CUDA_TRY(cudaMalloc(&km.k_neg, Nt * M * sizeof(double)));
             CUDA_TRY(cudaMemcpy(km.k_neg, m.k_neg.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
         }
+        if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+            // digit planes of K: one scale per (timeslice, 32-gene chunk)
+            // shared by both sides, six 7-bit digits per value
+            const uint64_t C = M / deac::kChunk;
+            std::vector<uint16_t> kdig((uint64_t)deac::kDigits * S * Nt * M);
+            std::vector<int16_t> kexp(Nt * C), kmax(Nt, -1000);
+            for (uint64_t t = 0; t < Nt; ++t)
+                for (uint64_t c = 0; c < C; ++c) {
+                    int e = -2000;
+                    for (int sd = 0; sd < S; ++sd)
+                        for (uint64_t j = c * deac::kChunk; j < (c + 1) * deac::kChunk; ++j) {
+                            const double v = (sd ? m.k_neg : m.k_pos)[t * M + j];
+                            if (v != 0.0 && std::isnormal(v)) e = std::max(e, std::ilogb(v));
+                        }
+                    e = e <= -1500 ? -1000 : e + 1;
+                    kexp[t * C + c] = (int16_t)e;
+                    kmax[t] = (int16_t)std::max<int>(kmax[t], e);
+                    for (int sd = 0; sd < S; ++sd)
+                        for (uint64_t j = c * deac::kChunk; j < (c + 1) * deac::kChunk; ++j) {
+                            uint16_t dg[deac::kDigits];
+                            deac::digits_of((sd ? m.k_neg : m.k_pos)[t * M + j], e, dg);
+                            for (int d = 0; d < deac::kDigits; ++d)
+                                kdig[(((uint64_t)d * S + sd) * Nt + t) * M + j] = dg[d];
+                        }
+                }
+            CUDA_TRY(cudaMalloc(&km.kdig, kdig.size() * 2));
+            CUDA_TRY(cudaMemcpy(km.kdig, kdig.data(), kdig.size() * 2, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMalloc(&km.kexp, kexp.size() * 2));
+            CUDA_TRY(cudaMemcpy(km.kexp, kexp.data(), kexp.size() * 2, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMalloc(&km.kexp_max, kmax.size() * 2));
+            CUDA_TRY(cudaMemcpy(km.kexp_max, kmax.data(), kmax.size() * 2, cudaMemcpyHostToDevice));
+        }
+        km.group = (uint32_t)b->kcache.size();
         it = b->kcache.emplace(key, km).first;
     }
+    r.kgroup = it->second.group;
 
     Arena a;
     const uint64_t o_isf = a.take(Nt * 8), o_err = a.take(Nt * 8), o_tw = a.take(Nt * 8);
@@ -298,6 +376,39 @@ int upload_run(deac_batch* b, RunHost& r) {
     d.stats = ptr(o_stats);
     d.trace = ptr(o_trace);
     d.trace_cap = r.trace_cap;
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        const uint64_t C = M / deac::kChunk;
+        Arena sa;
+        const uint64_t o_xd = sa.take((uint64_t)deac::kDigits * S * P * M * 2);
+        const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 2);
+        const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
+        const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
+        const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
+        const uint64_t o_cnt = sa.take(3 * 8);
+        CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
+        CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
+        char* sb = r.split_arena;
+        deac::SplitRun& x = r.split;
+        x.xdig = reinterpret_cast<uint16_t*>(sb + o_xd);
+        x.xexp = reinterpret_cast<int16_t*>(sb + o_xe);
+        x.xexp_max = reinterpret_cast<int16_t*>(sb + o_xm);
+        x.kdig = it->second.kdig;
+        x.kexp = it->second.kexp;
+        x.kexp_max = it->second.kexp_max;
+        x.e_mp = reinterpret_cast<double*>(sb + o_em);
+        x.e_bound = reinterpret_cast<double*>(sb + o_eb);
+        x.changed = reinterpret_cast<uint8_t*>(sb + o_ch);
+        x.recheck = reinterpret_cast<uint8_t*>(sb + o_rc);
+        x.f_lo = reinterpret_cast<double*>(sb + o_fl);
+        x.f_hi = reinterpret_cast<double*>(sb + o_fh);
+        x.t_lo = reinterpret_cast<double*>(sb + o_tl);
+        x.t_hi = reinterpret_cast<double*>(sb + o_th);
+        x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
+        d.changed = x.changed;
+        d.recheck = x.recheck;
+        d.f_lo = x.f_lo;
+        d.f_hi = x.f_hi;
+    }
     // host copies are no longer needed
     std::vector<uint64_t>().swap(r.rng_table);
     return DEAC_OK;
@@ -361,7 +472,8 @@ int deac_config_check(const deac_config* c) {
 int deac_batch_create(int device, void* cuda_stream, int32_t engine, deac_batch** out) {
     if (!out) return fail(DEAC_E_INVALID, "null output pointer");
     *out = nullptr;
-    if (engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "unknown engine %d", engine);
+    if (engine != DEAC_ENGINE_PLAIN_FP64 && engine != DEAC_ENGINE_SPLIT_BF16)
+        return fail(DEAC_E_INVALID, "unknown engine %d", engine);
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0)
         return fail(DEAC_E_NODEVICE, "no CUDA device %d", device);
@@ -397,6 +509,13 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau,
     if (cfg->population_size > (1u << 20) || m > (1u << 26) || nt > (1u << 20))
         return fail(DEAC_E_INVALID, "problem size beyond the engine's limits");
     if (isf[0] == 0.0 && cfg->normalize) return fail(DEAC_E_INVALID, "--normalize needs a nonzero F(0)");
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        if (m % deac::kChunk != 0)
+            return fail(DEAC_E_INVALID, "the split engine needs genome_size a multiple of %d", deac::kChunk);
+        if (cfg->first_moment >= 0.0 || cfg->third_moment >= 0.0 ||
+            (cfg->use_negative_first_moment && cfg->bosonic && !cfg->zero_temperature))
+            return fail(DEAC_E_INVALID, "the split engine does not support moment terms; use the plain engine");
+    }
     auto r = std::make_unique<RunHost>();
     r->cfg = *cfg;
     r->tau.assign(tau, tau + nt);
@@ -471,6 +590,40 @@ int deac_batch_setup(deac_batch* b) {
     for (auto& r : b->runs) descs.push_back(r->dev);
     CUDA_TRY(cudaMalloc(&b->d_runs, descs.size() * sizeof(deac::RunDev)));
     CUDA_TRY(cudaMemcpy(b->d_runs, descs.data(), descs.size() * sizeof(deac::RunDev), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&b->d_status, sizeof(int)));
+    CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int)));
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        std::vector<deac::SplitRun> xs;
+        for (auto& r : b->runs) xs.push_back(r->split);
+        CUDA_TRY(cudaMalloc(&b->d_split, xs.size() * sizeof(deac::SplitRun)));
+        CUDA_TRY(cudaMemcpy(b->d_split, xs.data(), xs.size() * sizeof(deac::SplitRun), cudaMemcpyHostToDevice));
+        // MMA tiles: the members of all runs that share a kernel matrix, 128
+        // rows at a time, times 64 timeslices
+        std::vector<deac::SplitRow> rows;
+        std::vector<deac::SplitTile> tiles;
+        for (uint32_t g = 0; g < b->kcache.size(); ++g) {
+            std::vector<deac::SplitRow> grp;
+            uint32_t nt = 0;
+            for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+                if (b->runs[ri]->kgroup != g) continue;
+                nt = (uint32_t)b->runs[ri]->Nt;
+                for (uint32_t m = 0; m < b->runs[ri]->P; ++m) grp.push_back({ri, m});
+            }
+            for (size_t r0 = 0; r0 < grp.size(); r0 += deac::kSplitRows) {
+                const uint32_t nrow = (uint32_t)std::min<size_t>(deac::kSplitRows, grp.size() - r0);
+                for (uint32_t t0 = 0; t0 < nt; t0 += deac::kSplitTau)
+                    tiles.push_back({(uint32_t)(rows.size() + r0), nrow, t0, grp[r0].run});
+            }
+            rows.insert(rows.end(), grp.begin(), grp.end());
+        }
+        b->n_tiles = (uint32_t)tiles.size();
+        CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
+        CUDA_TRY(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
+        CUDA_TRY(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaFuncSetAttribute(deac::split_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)deac::split_smem_bytes(2)));
+    }
     CUDA_TRY(cudaDeviceSynchronize());
     // initial fitness, statistics of generation 0 and the first stop test
     launch_generation(b, b->stream, 1);
@@ -501,6 +654,11 @@ int deac_batch_sync(deac_batch* b, uint32_t* runs_finished) {
     if (!b) return fail(DEAC_E_INVALID, "null batch");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(cudaGetLastError());
+    if (b->d_status) {
+        int st = 0;
+        CUDA_TRY(cudaMemcpy(&st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
+        if (st) return fail(DEAC_E_CUDA, "a tensor-core wait gave up (status %d)", st);
+    }
     int rc = refresh_status(b);
     if (rc) return rc;
     uint32_t n = 0;
@@ -535,7 +693,8 @@ int deac_batch_size(const deac_batch* b, uint32_t* runs) {
 static int gather(deac_batch* b, uint32_t run, std::vector<double>& pop, std::vector<double>& fit,
                   std::vector<double>* crfw, deac::RunDev& st) {
     RunHost& r = *b->runs[run];
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int rc = finalize_split(b);
+    if (rc) return rc;
     CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     const uint64_t P = r.P, M = r.M, S = r.S;
     std::vector<uint8_t> cur(P);
@@ -585,7 +744,8 @@ int deac_batch_result(deac_batch* b, uint32_t run, deac_run_result* out) {
     if (!b || !out || run >= b->runs.size()) return fail(DEAC_E_INVALID, "bad argument");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
     RunHost& r = *b->runs[run];
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int rc = finalize_split(b);
+    if (rc) return rc;
     deac::RunDev st;
     CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     std::vector<double> fit(r.P);
@@ -602,7 +762,8 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
     const uint64_t P = r.P, M = r.M, S = r.S;
     // only the fitness, the buffer indices and the best member's genes cross
     // the bus (the reference copies the whole population, deac.cpp:1577-1590)
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int rc0 = finalize_split(b);
+    if (rc0) return rc0;
     deac::RunDev st;
     CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     std::vector<double> fit(P);
@@ -670,16 +831,26 @@ int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness, u
     return DEAC_OK;
 }
 
+int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]) {
+    if (!b || run >= b->runs.size() || !counts) return fail(DEAC_E_INVALID, "bad argument");
+    if (b->engine != DEAC_ENGINE_SPLIT_BF16 || !b->set_up) return fail(DEAC_E_STATE, "not a set-up split batch");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaMemcpy(counts, b->runs[run]->split.counts, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return DEAC_OK;
+}
+
 int deac_batch_enable_timing(deac_batch* b, int32_t enable) {
     if (!b) return fail(DEAC_E_INVALID, "null batch");
     b->timing = enable != 0;
-    b->kernel_ms[0] = b->kernel_ms[1] = 0.0;
-    b->kernel_launches[0] = b->kernel_launches[1] = 0;
+    for (int k = 0; k < 5; ++k) {
+        b->kernel_ms[k] = 0.0;
+        b->kernel_launches[k] = 0;
+    }
     return DEAC_OK;
 }
 
 int deac_batch_kernel_time(deac_batch* b, int32_t kind, double* ms, uint64_t* launches) {
-    if (!b || kind < 0 || kind > 1) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b || kind < 0 || kind > 4) return fail(DEAC_E_INVALID, "bad argument");
     if (ms) *ms = b->kernel_ms[kind];
     if (launches) *launches = b->kernel_launches[kind];
     return DEAC_OK;
@@ -690,12 +861,21 @@ int deac_batch_destroy(deac_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    for (auto& r : b->runs)
+    for (auto& r : b->runs) {
         if (r->arena) cudaFree(r->arena);
+        if (r->split_arena) cudaFree(r->split_arena);
+    }
     for (auto& kv : b->kcache) {
         cudaFree(kv.second.k_pos);
         if (kv.second.k_neg) cudaFree(kv.second.k_neg);
+        if (kv.second.kdig) cudaFree(kv.second.kdig);
+        if (kv.second.kexp) cudaFree(kv.second.kexp);
+        if (kv.second.kexp_max) cudaFree(kv.second.kexp_max);
     }
+    cudaFree(b->d_split);
+    cudaFree(b->d_tiles);
+    cudaFree(b->d_rows);
+    cudaFree(b->d_status);
     cudaFree(b->d_runs);
     cudaFree(b->d_trial_work);
     cudaFree(b->d_contract_work);

@@ -240,6 +240,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         const uint32_t nchunks = (M + kGeneChunk - 1) / kGeneChunk;
 
         // genes [c*kGeneChunk, ...) of both sides, by worker `wid` of `nt`
+        bool mutated = false;
         auto produce = [&](uint32_t c, uint32_t wid, uint32_t nt) {
             const uint32_t j0 = c * kGeneChunk;
             const uint32_t len = min(kGeneChunk, M - j0);
@@ -276,6 +277,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
                     if (mutate) {
                         v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
                         if (!keep_sign) v = fabs(v);
+                        mutated = true;
                     }
                     dst[(uint64_t)sd[h] * PM + jj[h]] = v;
                     if (in_smem) trial_s[(uint64_t)sd[h] * M + jj[h]] = v;
@@ -308,6 +310,9 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             }
             __syncthreads();
         }
+        // the split engine skips the evaluation of a trial equal to its parent
+        if (__syncthreads_or(mutated) && threadIdx.x == 0 && R.changed) R.changed[i] = 1;
+        else if (threadIdx.x == 0 && R.changed) R.changed[i] = 0;
     } else if (in_smem) {
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
@@ -326,6 +331,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
+        if (!init_mode && threadIdx.x == 0 && R.changed && recip != 1.0) R.changed[i] = 1;
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
             const uint64_t g = (uint64_t)s * PM + (q - (uint64_t)s * M);
@@ -355,13 +361,22 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 // row the CTA needs ([S][member_tile] pop rows, then [S][tau_tile] K rows,
 // row stride chunk+2), reused by the finishing CTA as 4 x 1024 reduction
 // slots.
-__global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int init_mode) {
+__global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int mode) {
     extern __shared__ __align__(16) double dyn[];
-    __shared__ int s_last;
+    __shared__ int s_last, s_any;
 
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
-    if (R.done) return;
+    if (R.done && mode != kModeFinal) return;
+    const bool init_mode = mode == kModeInit;
+    // members evaluated by this launch, and which of their two buffers
+    const bool use_parent = mode == kModeInit || mode == kModeParents || mode == kModeFinal;
+    auto wanted = [&](uint32_t m) -> bool {
+        if (mode == kModeGeneration || mode == kModeInit) return true;
+        if (mode == kModeTrials) return R.recheck[m] != 0;
+        const bool inexact = R.f_lo[m] != R.f_hi[m];
+        return mode == kModeFinal ? inexact : (R.recheck[m] != 0 && inexact);
+    };
     const uint32_t P = R.P, M = R.M, Nt = R.Nt, S = R.S;
     const uint32_t MT = R.member_tile, TT = R.tau_tile, CH = R.chunk;
     const uint64_t PM = (uint64_t)P * M;
@@ -372,7 +387,11 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     const uint32_t side = S == 2 ? (lane >> 4) : 0u;
     const uint32_t mi = pair % MT, ti = pair / MT;
     const uint32_t i = mt * MT + mi, t = tt * TT + ti;
-    const bool valid = ti < TT && i < P && t < Nt;
+    const bool valid = ti < TT && i < P && t < Nt && wanted(i);
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    if (valid) s_any = 1;
+    __syncthreads();
     const uint32_t stride = stage_stride(CH);
     const uint32_t rows = S * (MT + TT);
     double* stage0 = dyn;
@@ -397,8 +416,8 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
             dst_row[j] = r;
             if (r < S * MT) {
                 const uint32_t s = r / MT, m = mt * MT + (r - s * MT);
-                if (m < P) {
-                    const uint32_t bsel = init_mode ? R.cur[m] : 1u - R.cur[m];
+                if (m < P && wanted(m)) {
+                    const uint32_t bsel = use_parent ? R.cur[m] : 1u - R.cur[m];
                     src_row[j] = pop + ((uint64_t)bsel * S + s) * PM + (uint64_t)m * M;
                 }
             } else {
@@ -430,8 +449,8 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     // E[i,t]: one k-ascending FMA chain per side from 0 (gpu_matmul,
     // deac_gpu.cu:277-315), staged through shared memory, double-buffered
     double acc = 0.0;
-    const uint32_t nst = (M + CH - 1) / CH;
-    issue(stage0, 0);
+    const uint32_t nst = s_any ? (M + CH - 1) / CH : 0u;  // nothing wanted in this tile
+    if (nst) issue(stage0, 0);
     for (uint32_t st = 0; st < nst; ++st) {
         double* cur = (st & 1u) ? stage1 : stage0;
         if (st + 1 < nst) {
@@ -467,13 +486,14 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t lanes = Nt < kTreeSlots ? Nt : kTreeSlots;
     const uint32_t width = pow2_ceil(lanes);
-    double* fit_dst = init_mode ? R.fit_old : R.fit_new;
+    double* fit_dst = use_parent ? R.fit_old : R.fit_new;
     double* sl = dyn + (uint64_t)warp * kTreeSlots;
 
     // reduced chi^2 (deac_gpu.cu:417-448) plus the moment terms
     // (deac_gpu.cu:450-456; order of deac.cpp:1479-1499), a warp per member
     const volatile double* E_all = R.model_isf;
     for (uint32_t m = warp; m < P; m += nwarps) {
+        if (!wanted(m)) continue;  // warp-uniform
         for (uint32_t s = lane; s < width; s += 32) {
             double v = 0.0;
             for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
@@ -501,19 +521,27 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
                 fit = fma(term, term, fit);
             }
             fit_dst[m] = fit;
+            if (use_parent && R.f_lo) R.f_lo[m] = R.f_hi[m] = fit;  // now exact
         }
         __syncwarp();
     }
     __syncthreads();
+    if (mode == kModeParents || mode == kModeFinal) {
+        if (threadIdx.x == 0) R.ticket = 0;
+        return;  // no selection and no bookkeeping in these passes
+    }
 
     uint64_t ii = R.ii;
     if (!init_mode) {
-        // greedy selection, ties accept (deac_gpu.cu:551-582)
+        // greedy selection, ties accept (deac_gpu.cu:551-582); the split
+        // engine's trial pass settles only the members the intervals left open
         for (uint32_t m = threadIdx.x; m < P; m += blockDim.x) {
+            if (!wanted(m)) continue;
             const double fn = R.fit_new[m];
             if ((R.flags & kTrace) && ii < R.trace_cap) R.trace[ii * P + m] = fn;
             if (fn <= R.fit_old[m]) {
                 R.fit_old[m] = fn;
+                if (R.f_lo) R.f_lo[m] = R.f_hi[m] = fn;
                 for (uint32_t s = 0; s < S; ++s) {
                     R.cr[s * P + m] = R.cr[(uint64_t)S * P + s * P + m];
                     R.fw[s * P + m] = R.fw[(uint64_t)S * P + s * P + m];

@@ -82,6 +82,11 @@ struct RunDev {
     double* stats;           // [mean|minimum|squared mean][N]
     double* trace;           // [trace_cap][P]
     uint64_t trace_cap;
+    // split engine only (null otherwise): see deac_split.cuh
+    uint8_t* changed;        // [P] trial differs from its parent
+    const uint8_t* recheck;  // [P] decision left to the exact FP64 value
+    double* f_lo;            // [P] interval holding the parent's exact fitness
+    double* f_hi;
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
@@ -133,7 +138,16 @@ struct Work {
     uint32_t index;  // member (trial) or tile (contract)
 };
 
+// contract_kernel modes
+enum ContractMode : int {
+    kModeGeneration = 0,  // trials of every member, selection, next-generation bookkeeping
+    kModeInit = 1,        // fitness of the initial population, bookkeeping of generation 0
+    kModeParents = 2,     // split engine: exact fitness of undecided members' inexact parents
+    kModeTrials = 3,      // split engine: exact fitness and selection of undecided trials, bookkeeping
+    kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
+};
+
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
-__global__ void contract_kernel(RunDev* runs, const Work* work, int init_mode);
+__global__ void contract_kernel(RunDev* runs, const Work* work, int mode);
 
 }  // namespace deac

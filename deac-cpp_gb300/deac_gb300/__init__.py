@@ -26,6 +26,7 @@ EXE_PATH = PKG / "bin" / "deac.e"
 MODEL = {"standard": 0, "hyperbolic": 1, "normalization": 2}
 SPECTRA = {"spbsf": 0, "spfsf": 1, "bfull": 2, "ffull": 3, "bdsf": 4}
 ENGINE_PLAIN_FP64 = 0
+ENGINE_SPLIT_BF16 = 1
 
 
 class DeacConfig(ctypes.Structure):
@@ -132,6 +133,7 @@ SIGNATURES = {
     "deac_batch_enable_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]),
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "deac_batch_split_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "deac_reconstruct": (ctypes.c_int, [ctypes.POINTER(DeacConfig), _dp, _dp, _dp, ctypes.c_uint64, _dp,
@@ -234,6 +236,11 @@ class Batch:
         n = ctypes.c_uint64()
         _check(self._lib.deac_batch_kernel_time(self._h, kind, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def split_counts(self, run: int) -> dict:
+        c = (ctypes.c_uint64 * 3)()
+        _check(self._lib.deac_batch_split_counts(self._h, run, c))
+        return {"equal_to_parent": c[0], "interval": c[1], "exact": c[2]}
 
     def result(self, run: int) -> dict:
         r = RunResult()

@@ -60,8 +60,16 @@ extern "C" {
 
 /* Evaluation engines of a batch.
  *  PLAIN_FP64: every step in FP64 in the order of the reference CUDA path;
- *              bit-identical to the reference semantics (the default). */
+ *              bit-identical to the reference semantics (the default).
+ *  SPLIT_BF16: the contraction of each trial is first evaluated on the
+ *              tcgen05 tensor cores from exact BF16 digit slices, with a
+ *              rigorous bound on its distance from the FP64 value; only
+ *              decisions that bound leaves open are settled by the FP64
+ *              chains.  Selection, generation count, minimum fitness and
+ *              spectrum are identical to PLAIN_FP64.  Needs genome_size a
+ *              multiple of 32 and no moment terms. */
 #define DEAC_ENGINE_PLAIN_FP64 0
+#define DEAC_ENGINE_SPLIT_BF16 1
 
 /* Everything the reference reads from its command line (deac.cpp:1926-2024)
  * plus the compile-time variant switches. */
@@ -185,9 +193,17 @@ int deac_batch_enable_trace(deac_batch* b, uint32_t run, uint64_t max_generation
 int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness,
                            uint64_t capacity);
 
-/* Device time of the kernels of the last deac_batch_launch call, per kernel
- * kind, measured with CUDA events on the batch stream (ms). kind 0 = trial
- * kernel, 1 = contraction kernel.  Only when timing was enabled. */
+/* Split engine: how the trials of run `run` were decided so far --
+ * counts[0] equal to their parent (no gene changed), counts[1] settled by the
+ * tensor-core estimate's interval, counts[2] settled by the exact FP64 value. */
+int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]);
+
+/* Device time of the kernels launched since timing was enabled, per kernel
+ * kind, measured with CUDA events on the batch stream (ms): 0 trial kernel,
+ * 1 contraction kernel (plain generation or the split engine's exact
+ * passes), 2 digit slicing, 3 tensor-core contraction, 4 interval decisions.
+ * While timing is enabled, generations are launched one by one instead of
+ * as CUDA graphs. */
 int deac_batch_enable_timing(deac_batch* b, int32_t enable);
 int deac_batch_kernel_time(deac_batch* b, int32_t kind, double* ms, uint64_t* launches);
 

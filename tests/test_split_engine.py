@@ -1,0 +1,120 @@
+"""Split-precision engine (tcgen05 BF16 digit slices + intervals) vs the plain
+FP64 engine: every selection decision must be the FP64 one, so the two
+engines must produce bit-identical results -- generation count, minimum
+fitness, best spectrum, final population and final fitness -- on the same
+runs.  Each case also checks that the tensor-core intervals settled most
+trials (the exact FP64 chains only see the undecided ones)."""
+import numpy as np
+import pytest
+
+from deac_testlib import config0_data, make_isf, uniform_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(kind, seed=1):
+    if kind == "cfg0":
+        return config0_data(seed)
+    if kind == "neg":
+        tau, isf, err = config0_data(seed)
+        return tau, -isf, err
+    if kind == "odd":
+        return make_isf(50, 0.5, [(0.6, 3.0, 1.0), (0.4, 9.0, 2.0)], 1e-3, seed)
+    if kind == "tight":  # sigma = 1e-5 F, three peaks
+        return make_isf(96, 1.35, [(0.5, 3.0, 0.5), (0.3, 40.0, 5.0), (0.2, 200.0, 30.0)], 1e-5, seed,
+                        omega_max_data=512.0)
+    raise KeyError(kind)
+
+
+CASES = {
+    # name: (data kind, M, omega_max, N, overrides)
+    "standard-bfull": ("cfg0", 64, 64.0, 1500, dict(spectra_type="bfull")),
+    "normalize": ("cfg0", 64, 64.0, 800, dict(spectra_type="bfull", normalize=True)),
+    "hyperbolic": ("cfg0", 96, 64.0, 800, dict(model="hyperbolic", spectra_type="bfull")),
+    "fermionic-negative-K": ("neg", 64, 64.0, 800, dict(spectra_type="spfsf")),
+    "bosonic": ("cfg0", 64, 64.0, 800, dict(bosonic=True)),
+    "zero-temperature": ("cfg0", 64, 64.0, 800, dict(bosonic=True, zero_temperature=True)),
+    "signed-weights": ("cfg0", 64, 64.0, 800, dict(spectra_type="bfull", allow_negative_weight=True)),
+    "odd-population-and-timeslices": ("odd", 64, 20.0, 800, dict(spectra_type="bfull", population_size=13)),
+    "track-stats": ("cfg0", 64, 64.0, 500, dict(spectra_type="bfull", track_stats=True)),
+    "wide-genome-tight-errors": ("tight", 512, 512.0, 300, dict(spectra_type="bfull", population_size=64)),
+    "early-stop": ("cfg0", 64, 64.0, 20000, dict(spectra_type="bfull", stop_minimum_fitness=5e4)),
+}
+
+
+def _results(engine, kind, specs):
+    out = []
+    with engine.Batch(engine=kind) as b:
+        ids = [b.add_run(cfg, *data, freq) for cfg, data, freq in specs]
+        b.run()
+        for r in ids:
+            res = b.fetch(r)
+            res.update(b.fetch_state(r))
+            if kind == engine.ENGINE_SPLIT_BF16:
+                res["counts"] = b.split_counts(r)
+            out.append(res)
+    return out
+
+
+def _same(a, b):
+    assert a["generation"] == b["generation"]
+    assert a["minimum_fitness"] == b["minimum_fitness"]
+    assert a["best_index"] == b["best_index"]
+    assert np.array_equal(a["dsf"], b["dsf"])
+    assert np.array_equal(a["population"], b["population"])
+    assert np.array_equal(a["fitness"], b["fitness"])
+    assert np.array_equal(a["crossover"], b["crossover"])
+    assert np.array_equal(a["weights"], b["weights"])
+    for k in ("stats_mean", "stats_minimum", "stats_squared_mean"):
+        if k in a:
+            assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_split_matches_plain(name, engine):
+    kind, m, omax, n, over = CASES[name]
+    kw = dict(temperature=1.35 if kind != "odd" else 0.5, population_size=8, number_of_generations=n, seed=5,
+              stop_minimum_fitness=1.0)
+    kw.update(over)
+    cfg = engine.make_config(**kw)
+    spec = [(cfg, _data(kind), uniform_grid(m, omax))]
+    plain = _results(engine, engine.ENGINE_PLAIN_FP64, spec)[0]
+    split = _results(engine, engine.ENGINE_SPLIT_BF16, spec)[0]
+    _same(plain, split)
+    c = split["counts"]
+    total = sum(c.values())
+    assert total > 0
+    # the intervals, not the FP64 chains, must settle most changed trials
+    assert c["interval"] >= c["exact"], c
+
+
+def test_split_batch_shares_tiles_across_runs(engine):
+    """Several runs sharing one kernel matrix are packed into the same
+    128-row MMA tiles; another run has its own matrix.  Each must still match
+    its plain-engine twin."""
+    tau, isf, err = config0_data(1)
+    freq = uniform_grid(64, 64.0)
+    specs = []
+    for seed, p in ((1, 40), (2, 40), (3, 64), (4, 8)):
+        cfg = engine.make_config(temperature=1.35, spectra_type="bfull", population_size=p,
+                                 number_of_generations=400, seed=seed)
+        specs.append((cfg, config0_data(seed), freq))
+    cfg = engine.make_config(temperature=0.5, spectra_type="bfull", population_size=16, number_of_generations=400,
+                             seed=9)
+    specs.append((cfg, make_isf(64, 0.5, [(1.0, 4.0, 1.0)], 1e-4, 9), uniform_grid(96, 30.0)))
+    plain = _results(engine, engine.ENGINE_PLAIN_FP64, specs)
+    split = _results(engine, engine.ENGINE_SPLIT_BF16, specs)
+    for a, b in zip(plain, split):
+        _same(a, b)
+
+
+def test_split_rejects_unsupported(engine):
+    cfg = engine.make_config(temperature=1.35, spectra_type="bfull", population_size=8, number_of_generations=10,
+                             first_moment=1.0)
+    tau, isf, err = config0_data(1)
+    with engine.Batch(engine=engine.ENGINE_SPLIT_BF16) as b:
+        with pytest.raises(engine.DeacError):
+            b.add_run(cfg, tau, isf, err, uniform_grid(64, 64.0))
+        cfg.first_moment = -1.0
+        with pytest.raises(engine.DeacError):
+            b.add_run(cfg, tau, isf, err, uniform_grid(50, 64.0))
