@@ -16,8 +16,9 @@ constexpr int kGroups = 2 * kDigits - 1;  // a+b = 0..10; groups above kDigits-1
 constexpr int kKept = kDigits;            // groups 0..5 kept
 constexpr uint32_t kTmemCols = 512;       // 6 groups x 64 + bound x 64 = 448 used
 constexpr uint32_t kBoundCol = kKept * kSplitTau;
-constexpr uint32_t kWaitLimit = 1u << 26;  // bounded mbarrier waits (~seconds)
+constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier waits: 2 s
 constexpr uint32_t kFlush = 16;            // chunks per double-float run before the FP64 fold
+constexpr int kStatusWait = 1;             // status: a tensor-core completion wait gave up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -48,15 +49,27 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the completion of the mbarrier phase with parity `phase`, giving
+// up after kWaitNs of wall time (the caller then reports an error).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kWaitLimit && !done; ++it) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        uint32_t done;
         asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(phase));
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > kWaitNs) return false;
+        __nanosleep(64);
     }
-    return done != 0;
 }
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
@@ -170,6 +183,9 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     __shared__ int s_kmax[kSplitTau];
     __shared__ int s_live;
 
+    // a failed wait in an earlier launch leaves the status set: do nothing
+    // more until the host has seen it
+    if (*reinterpret_cast<volatile int*>(status) != 0) return;
     const SplitTile tile = tiles[blockIdx.x];
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const RunDev& R0 = runs[tile.run0];
@@ -341,13 +357,14 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     }
     flush();
 
-    if (ok && live) {
+    if (ok) {  // CTA-uniform: the .sync.aligned TMEM loads need whole warps
         // bound sums sum_c 2^(e_x + e_K), then the interval half-width
         const uint32_t lane_base = tmem + ((warp * 32u) << 16);
         for (uint32_t ts = 0; ts < kSplitTau / 8; ++ts) {
             uint32_t d[8];
             tmem_ld8(lane_base + kBoundCol + ts * 8, d);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            if (!live) continue;
             for (int j = 0; j < 8; ++j) {
                 const uint32_t t = tau0 + ts * 8 + j;
                 if (t >= Nt) continue;
@@ -363,7 +380,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
             }
         }
     }
-    if (!ok && tid == 0) atomicExch(status, 1);
+    if (!ok && tid == 0) atomicCAS(status, 0, kStatusWait);
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
