@@ -43,6 +43,16 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+namespace deac {
+// The last-error message of this thread, for the C-ABI entry points that
+// live in other translation units.
+__attribute__((visibility("hidden"))) int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace deac
+
+namespace {
+
 #define CUDA_TRY(call)                                                                     \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \

@@ -138,6 +138,10 @@ SIGNATURES = {
     "deac_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "deac_reconstruct": (ctypes.c_int, [ctypes.POINTER(DeacConfig), _dp, _dp, _dp, ctypes.c_uint64, _dp,
                                         ctypes.c_uint64, ctypes.POINTER(RunResult), _dp, _dp, _dp, _dp, _dp]),
+    "deac_population_fitness_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                                       ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                       ctypes.c_uint64, ctypes.c_void_p]),
 }
 
 

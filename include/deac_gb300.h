@@ -221,6 +221,45 @@ int deac_reconstruct(const deac_config* cfg, const double* imaginary_time,
                      double* stats_mean, double* stats_minimum,
                      double* stats_squared_mean);
 
+/* ---- fitness of a device-resident population, allocating nothing -------- */
+/* No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory when they need fitness
+ * values: a framework that reserves most of the GPU at start-up, or a pool
+ * allocator that owns every buffer, makes a cudaMalloc from this library fail
+ * although the caller already holds all inputs and outputs; and cudaFree
+ * waits for the whole device, stalling the caller's other streams.
+ *
+ * Writes fitness[i] = (1/Nt) sum_t ((isf[t] - E[i,t]) / isf_error[t])^2 with
+ * E = population x kernel^T (both sides), the reduced chi^2 without moment
+ * terms, computed by the batch engine's contraction kernel in the same order,
+ * so the values equal deac_batch_fetch_state's fitness for the same
+ * population.  Every pointer is device memory of `device`:
+ *   population  [sides][population_size][genome_size], 16-byte aligned;
+ *   kernel_pos, kernel_neg  [number_of_timeslices][genome_size], 16-byte
+ *               aligned (kernel_neg ignored when sides == 1);
+ *   isf, isf_error  [number_of_timeslices];  fitness  [population_size].
+ * Enqueued on `cuda_stream` (NULL: the legacy default stream); returns
+ * without waiting.
+ *
+ * The kernel's scratch (run descriptor, work list and the population x
+ * timeslice model-ISF matrix) lives in one static device array of
+ * DEAC_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits: population_size x number_of_timeslices x 8 bytes plus a
+ * few KB must fit in it, and larger calls fail with DEAC_E_INVALID.  The first
+ * call on a device looks up the array's device address and raises the
+ * kernel's shared-memory limit; make that first call before any stream
+ * capture.  All calls on a device share the one array, which keeps the last
+ * call's contents: calls that overlap on the GPU (different streams or host
+ * threads) race and must be ordered by the caller. */
+#define DEAC_NOALLOC_SCRATCH_BYTES (16u << 20)
+int deac_population_fitness_noalloc(int device, void* cuda_stream, int32_t sides,
+                                    const double* population, uint64_t population_size,
+                                    uint64_t genome_size, const double* kernel_pos,
+                                    const double* kernel_neg, const double* isf,
+                                    const double* isf_error, uint64_t number_of_timeslices,
+                                    double* fitness);
+
 /* Library version string. */
 const char* deac_version(void);
 
