@@ -129,8 +129,10 @@ struct deac_batch {
     // split engine
     deac::SplitRun* d_split = nullptr;
     deac::SplitTile* d_tiles = nullptr;
+    deac::SplitWork* d_split_work = nullptr;
     deac::SplitRow* d_rows = nullptr;
-    uint32_t n_tiles = 0;
+    float4* d_partial = nullptr;       // partial sums of the split contraction CTAs
+    uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
     // passes), 2 digitize, 3 split contraction, 4 split decisions
@@ -173,12 +175,15 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
         return mark(1);
     }
-    deac::digitize_kernel<<<b->n_trial_ctas, 256, 0, s>>>(b->d_runs, b->d_split, b->d_trial_work, 0);
+    deac::digitize_kernel<<<b->n_trial_ctas, deac::kDigitizeThreads, 0, s>>>(b->d_runs, b->d_split,
+                                                                           b->d_trial_work, 0);
     if ((rc = mark(2))) return rc;
-    deac::split_contract_kernel<<<b->n_tiles, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
-        b->d_runs, b->d_split, b->d_tiles, b->d_rows, b->d_status);
+    deac::split_contract_kernel<<<b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
+        b->d_runs, b->d_split, b->d_tiles, b->d_split_work, b->d_rows, b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
-    deac::split_decide_kernel<<<(uint32_t)b->runs.size(), 256, 0, s>>>(b->d_runs, b->d_split, 0);
+    deac::split_combine_kernel<<<b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s>>>(
+        b->d_runs, b->d_split, b->d_tiles, b->d_rows, b->d_partial);
+    deac::split_decide_kernel<<<(uint32_t)b->runs.size(), deac::kDecideThreads, 0, s>>>(b->d_runs, b->d_split);
     if ((rc = mark(4))) return rc;
     launch_contract(b, s, deac::kModeParents);
     launch_contract(b, s, deac::kModeTrials);
@@ -607,28 +612,52 @@ int deac_batch_setup(deac_batch* b) {
         for (auto& r : b->runs) xs.push_back(r->split);
         CUDA_TRY(cudaMalloc(&b->d_split, xs.size() * sizeof(deac::SplitRun)));
         CUDA_TRY(cudaMemcpy(b->d_split, xs.data(), xs.size() * sizeof(deac::SplitRun), cudaMemcpyHostToDevice));
-        // MMA tiles: the members of all runs that share a kernel matrix, 128
-        // rows at a time, times 64 timeslices
+        // output tiles: the members of all runs that share a kernel matrix,
+        // 64 rows at a time, times 128 timeslices
         std::vector<deac::SplitRow> rows;
         std::vector<deac::SplitTile> tiles;
+        std::vector<uint32_t> tile_chunks;
         for (uint32_t g = 0; g < b->kcache.size(); ++g) {
             std::vector<deac::SplitRow> grp;
-            uint32_t nt = 0;
+            uint32_t nt = 0, chunks = 0;
             for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
                 if (b->runs[ri]->kgroup != g) continue;
                 nt = (uint32_t)b->runs[ri]->Nt;
+                chunks = (uint32_t)(b->runs[ri]->M / deac::kChunk);
                 for (uint32_t m = 0; m < b->runs[ri]->P; ++m) grp.push_back({ri, m});
             }
-            for (size_t r0 = 0; r0 < grp.size(); r0 += deac::kSplitRows) {
-                const uint32_t nrow = (uint32_t)std::min<size_t>(deac::kSplitRows, grp.size() - r0);
-                for (uint32_t t0 = 0; t0 < nt; t0 += deac::kSplitTau)
-                    tiles.push_back({(uint32_t)(rows.size() + r0), nrow, t0, grp[r0].run});
+            for (size_t r0 = 0; r0 < grp.size(); r0 += deac::kRowTile) {
+                const uint32_t nrow = (uint32_t)std::min<size_t>(deac::kRowTile, grp.size() - r0);
+                for (uint32_t t0 = 0; t0 < nt; t0 += deac::kTauTile) {
+                    tiles.push_back({t0, (uint32_t)(rows.size() + r0), nrow, grp[r0].run, 0, 0});
+                    tile_chunks.push_back(chunks);
+                }
             }
             rows.insert(rows.end(), grp.begin(), grp.end());
         }
+        // split every tile's chunks over CTAs so that the launch fills the
+        // SMs about once (one CTA per SM: the kernel uses ~214 KB of shared
+        // memory and all of TMEM)
+        int sms = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+        const uint64_t want = std::max<uint64_t>(1, (uint64_t)sms / tiles.size());
+        std::vector<deac::SplitWork> work;
+        uint32_t blocks = 0;
+        for (uint32_t t = 0; t < tiles.size(); ++t) {
+            const uint32_t C = tile_chunks[t];
+            const uint32_t per = (uint32_t)((C + std::min<uint64_t>(want, C) - 1) / std::min<uint64_t>(want, C));
+            tiles[t].block0 = blocks;
+            for (uint32_t c0 = 0; c0 < C; c0 += per) work.push_back({t, c0, std::min(C, c0 + per), blocks++});
+            tiles[t].nsplit = blocks - tiles[t].block0;
+        }
         b->n_tiles = (uint32_t)tiles.size();
+        b->n_split_ctas = (uint32_t)work.size();
         CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
         CUDA_TRY(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_split_work, work.size() * sizeof(deac::SplitWork)));
+        CUDA_TRY(cudaMemcpy(b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork),
+                            cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_partial, (uint64_t)blocks * deac::kPartialBlock * sizeof(float4)));
         CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
         CUDA_TRY(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
         CUDA_TRY(cudaFuncSetAttribute(deac::split_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -884,6 +913,8 @@ int deac_batch_destroy(deac_batch* b) {
     }
     cudaFree(b->d_split);
     cudaFree(b->d_tiles);
+    cudaFree(b->d_split_work);
+    cudaFree(b->d_partial);
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
     cudaFree(b->d_runs);

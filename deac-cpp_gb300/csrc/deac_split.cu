@@ -12,12 +12,10 @@ namespace deac {
 
 namespace {
 
-constexpr int kGroups = 2 * kDigits - 1;  // a+b = 0..10; groups above kDigits-1 are dropped
 constexpr int kKept = kDigits;            // groups 0..5 kept
-constexpr uint32_t kTmemCols = 512;       // 6 groups x 64 + bound x 64 = 448 used
-constexpr uint32_t kBoundCol = kKept * kSplitTau;
+constexpr uint32_t kTmemCols = 512;       // 6 groups x 64 rows + bound x 64 rows = 448 used
+constexpr uint32_t kBoundCol = kKept * kRowTile;
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier waits: 2 s
-constexpr uint32_t kFlush = 16;            // chunks per double-float run before the FP64 fold
 constexpr int kStatusWait = 1;             // status: a tensor-core completion wait gave up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -104,14 +102,44 @@ __device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
     return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
 }
 
-__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float a, float b) {
-    // (hi, lo) += (a, b) in double-float arithmetic
-    const float s = hi + a;
-    const float bp = s - hi;
-    float e = (hi - (s - bp)) + (a - bp);
-    e += lo + b;
-    hi = s + e;
-    lo = e - (hi - s);
+// Error-free transformations in FP32 (IEEE round-to-nearest; the file is
+// compiled without FMA contraction): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+    s = a + b;
+    e = b - (s - a);
+}
+
+// (ah, al) += (bh, bl): the accurate double-float sum of Joldes, Muller and
+// Popescu (ACM TOMS 44(2), 2017, Alg. 6), relative error below 3 * 2^-48.
+__device__ __forceinline__ void dw_add(float& ah, float& al, float bh, float bl) {
+    float sh, sl, th, tl, vh, vl;
+    two_sum(ah, bh, sh, sl);
+    two_sum(al, bl, th, tl);
+    sl += th;
+    fast_two_sum(sh, sl, vh, vl);
+    vl += tl;
+    fast_two_sum(vh, vl, ah, al);
+}
+
+__device__ __forceinline__ float exp2_int(int n) {  // 2^n for -126 <= n <= 127
+    return __uint_as_float((uint32_t)(n + 127) << 23);
+}
+
+// (hi, lo) *= 2^k for k <= 60: exact unless the result is subnormal (then
+// each factor rounds once, by at most 2^-150)
+__device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
+    const int k1 = k < -126 ? -126 : k;
+    int k2 = k - k1;
+    k2 = k2 < -126 ? -126 : k2;
+    const float f1 = __uint_as_float((uint32_t)(k1 + 127) << 23);
+    const float f2 = __uint_as_float((uint32_t)(k2 + 127) << 23);
+    hi = hi * f1 * f2;
+    lo = lo * f1 * f2;
 }
 
 }  // namespace
@@ -119,9 +147,9 @@ __device__ __forceinline__ void two_sum_add(float& hi, float& lo, float a, float
 // -------------------------------------------------------------- digitize
 // One CTA per (run, member): a warp per 32-gene chunk computes the chunk's
 // scale exponent (max over both sides) and writes the six 7-bit digit planes.
-__global__ void __launch_bounds__(256) digitize_kernel(RunDev* runs, SplitRun* split, const Work* work,
-                                                       int all_members) {
-    __shared__ int s_max[8];
+__global__ void __launch_bounds__(kDigitizeThreads) digitize_kernel(RunDev* runs, SplitRun* split, const Work* work,
+                                                                    int all_members) {
+    __shared__ int s_max[kDigitizeThreads / 32];
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
     if (R.done) return;
@@ -137,26 +165,38 @@ __global__ void __launch_bounds__(256) digitize_kernel(RunDev* runs, SplitRun* s
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
     const uint32_t C = M / kChunk;
     int wmax = -2000;
-    for (uint32_t c = warp; c < C; c += nw) {
-        const uint32_t j = c * kChunk + lane;
-        double v[2];
-        int e = -2000;
-        for (uint32_t s = 0; s < S; ++s) {
-            v[s] = row[(uint64_t)s * PM + j];
-            e = max(e, exp_of(v[s]));
-        }
-        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-        e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
-        for (uint32_t s = 0; s < S; ++s) {
-            const uint64_t f = frac42(v[s], e);
-            const bool neg = v[s] < 0.0;
-            for (int b = 0; b < kDigits; ++b) {
-                const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
-                X.xdig[((uint64_t)b * S + s) * PM + (uint64_t)i * M + j] = bf16_digit(d, neg);
+    constexpr uint32_t kAhead = 4;  // chunks in flight per warp
+    for (uint32_t c0 = warp * kAhead; c0 < C; c0 += nw * kAhead) {
+        double v[kAhead][2];
+#pragma unroll
+        for (uint32_t u = 0; u < kAhead; ++u)
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s)
+                v[u][s] = (c0 + u < C && s < S) ? row[(uint64_t)s * PM + (c0 + u) * kChunk + lane] : 0.0;
+#pragma unroll
+        for (uint32_t u = 0; u < kAhead; ++u) {
+            const uint32_t c = c0 + u;
+            if (c >= C) break;  // warp-uniform
+            const uint32_t j = c * kChunk + lane;
+            int e = -2000;
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s)
+                if (s < S) e = max(e, exp_of(v[u][s]));
+            for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+            e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s) {
+                if (s >= S) break;
+                const uint64_t f = frac42(v[u][s], e);
+                const bool neg = v[u][s] < 0.0;
+                for (int b = 0; b < kDigits; ++b) {
+                    const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
+                    X.xdig[((uint64_t)b * S + s) * PM + (uint64_t)i * M + j] = bf16_digit(d, neg);
+                }
             }
+            if (lane == 0) X.xexp[(uint64_t)i * C + c] = (int16_t)e;
+            wmax = max(wmax, e);
         }
-        if (lane == 0) X.xexp[(uint64_t)i * C + c] = (int16_t)e;
-        wmax = max(wmax, e);
     }
     if (lane == 0) s_max[warp] = wmax;
     __syncthreads();
@@ -168,55 +208,110 @@ __global__ void __launch_bounds__(256) digitize_kernel(RunDev* runs, SplitRun* s
 }
 
 // ----------------------------------------------------- split contraction
-// One CTA per tile of up to 128 (run, member) rows that share a kernel
-// matrix, times 64 timeslices.  Thread t owns row t (TMEM lane t).  For each
-// 32-gene chunk: stage the digit tiles of both operands, issue the kept digit
-// pairs into six TMEM group accumulators plus one rank-1 MMA of the chunk
-// scales into the bound accumulator, wait, and fold the exact group sums into
-// double-float accumulators.
+// One CTA per (tile, chunk range).  The tile is 128 timeslices (MMA M, one
+// TMEM lane each) x 64 trial rows (MMA N) of runs that share K.  Per 32-gene
+// chunk: stage the digit planes of both operands, issue the kept digit pairs
+// into six TMEM group accumulators plus one rank-1 MMA of the chunk scales
+// into the bound accumulator, wait, and fold the exact group sums into
+// double-float accumulators in shared memory; the next chunk's digits load
+// while the current one is folded.  The CTA ends by writing its partial sums
+// (hi, lo, bound) for the combine kernel.
 __global__ void __launch_bounds__(kSplitThreads, 1)
-split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows, int* status) {
+split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
+                      const SplitRow* rows, float4* partial, int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t s_tmem;
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_kexp[kSplitTau];
-    __shared__ int s_kmax[kSplitTau];
+    __shared__ int s_ek[kTauTile], s_kmax[kTauTile];
+    __shared__ int s_ex[kRowTile], s_xmax[kRowTile];
     __shared__ int s_live;
 
-    // a failed wait in an earlier launch leaves the status set: do nothing
-    // more until the host has seen it
-    if (*reinterpret_cast<volatile int*>(status) != 0) return;
-    const SplitTile tile = tiles[blockIdx.x];
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const SplitWork wk = work[blockIdx.x];
+    const SplitTile tile = tiles[wk.tile];
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     const RunDev& R0 = runs[tile.run0];
     const SplitRun& X0 = split[tile.run0];
     const uint32_t S = R0.S, M = R0.M, Nt = R0.Nt;
     const uint32_t C = M / kChunk;
+    const uint32_t tau0 = tile.tau0;
 
-    // which rows of the tile need an estimate this generation
-    const bool has_row = tid < tile.rows;
-    SplitRow my = has_row ? rows[tile.first_row + tid] : SplitRow{tile.run0, 0};
-    const RunDev& R = runs[my.run];
-    const SplitRun& X = split[my.run];
-    const bool live = has_row && !R.done && X.changed[my.member];
-    if (tid == 0) s_live = 0;
+    // is any row of the tile a changed trial of a running run?  (Nothing is
+    // done either after a failed wait in an earlier launch, until the host
+    // has seen the status; one thread reads it so the CTA agrees.)
+    if (tid == 0) s_live = *reinterpret_cast<volatile int*>(status) != 0 ? -1 : 0;
     __syncthreads();
-    if (live) atomicOr(&s_live, 1);
+    if (s_live == 0 && tid < tile.rows) {
+        const SplitRow rw = rows[tile.first_row + tid];
+        if (!runs[rw.run].done && split[rw.run].changed[rw.member]) atomicOr(&s_live, 1);
+    }
     __syncthreads();
-    if (!s_live) return;
+    if (s_live <= 0) return;
 
-    // shared memory: A digits [6][S] x (128 x 32), B digits [6][S] x (64 x 32),
-    // bound operands A (128 x 16) and B (64 x 16), FP64 rows 128 x 64
-    const uint32_t a_tile = kSplitRows * kChunk * 2;  // 8 KB
-    const uint32_t b_tile = kSplitTau * kChunk * 2;   // 4 KB
+    // shared memory: K digits [6][S] x (128 x 32), trial digits [6][S] x
+    // (64 x 32), bound operands (128 x 16) and (64 x 16), accumulators
+    const uint32_t a_tile = kTauTile * kChunk * 2;  // 8 KB
+    const uint32_t b_tile = kRowTile * kChunk * 2;  // 4 KB
     uint8_t* sA = smem;
     uint8_t* sB = sA + kDigits * S * a_tile;
     uint8_t* sAb = sB + kDigits * S * b_tile;
-    uint8_t* sBb = sAb + kSplitRows * 16 * 2;
+    uint8_t* sBb = sAb + kTauTile * 16 * 2;
+    float2* acc = reinterpret_cast<float2*>(sBb + kRowTile * 16 * 2);  // [row][tau]
 
     // zero the rank-1 bound operands once (only k = 0 is written per chunk)
-    for (uint32_t e = tid; e < (kSplitRows + kSplitTau) * 16; e += blockDim.x)
+    for (uint32_t e = tid; e < (kTauTile + kRowTile) * 16; e += blockDim.x)
         reinterpret_cast<uint16_t*>(sAb)[e] = 0;
+
+    // staging roles: K digits -> (timeslice row, two 16-byte units);
+    // trial digits -> (trial row, one unit)
+    const uint32_t a_row = tid >> 1, a_u0 = (tid & 1u) * 2;
+    const bool a_ok = tau0 + a_row < Nt;
+    const uint16_t* a_src = X0.kdig + (uint64_t)(tau0 + (a_ok ? a_row : 0)) * M;
+    const uint64_t a_plane = (uint64_t)Nt * M;
+    const uint32_t b_row = tid >> 2, b_u = tid & 3u;
+    const bool b_ok = b_row < tile.rows;
+    const uint16_t* b_src = nullptr;
+    uint64_t b_plane = 0;
+    if (b_ok) {
+        const SplitRow rw = rows[tile.first_row + b_row];
+        b_plane = (uint64_t)runs[rw.run].P * M;
+        b_src = split[rw.run].xdig + (uint64_t)rw.member * M;
+    }
+    auto stage = [&](uint32_t c) {
+        const uint32_t g0 = c * kChunk;
+        for (uint32_t q = 0; q < (uint32_t)kDigits * S; ++q) {
+            if (a_ok) {
+                uint8_t* dst = sA + q * a_tile;
+                const uint16_t* src = a_src + q * a_plane + g0;
+                cp16(dst + canon(a_row, a_u0 * 8, kChunk), src + a_u0 * 8);
+                cp16(dst + canon(a_row, a_u0 * 8 + 8, kChunk), src + a_u0 * 8 + 8);
+            }
+            if (b_ok) cp16(sB + q * b_tile + canon(b_row, b_u * 8, kChunk), b_src + q * b_plane + g0 + b_u * 8);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    // chunk exponents and the bound operands 2^(e - max) at k = 0
+    auto scales = [&](uint32_t c) {
+        if (tid < kTauTile) {
+            const bool ok = tau0 + tid < Nt;
+            const int ek = ok ? X0.kexp[(uint64_t)(tau0 + tid) * C + c] : -1000;
+            s_ek[tid] = ek;
+            const int d = ek - s_kmax[tid];
+            const float v = (ok && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
+            *reinterpret_cast<uint16_t*>(sAb + canon(tid, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
+        } else if (tid < kTauTile + kRowTile) {
+            const uint32_t r = tid - kTauTile;
+            const bool ok = r < tile.rows;
+            int e = -1000;
+            if (ok) {
+                const SplitRow rw = rows[tile.first_row + r];
+                e = split[rw.run].xexp[(uint64_t)rw.member * C + c];
+            }
+            s_ex[r] = e;
+            const int d = e - s_xmax[r];
+            const float v = (ok && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
+            *reinterpret_cast<uint16_t*>(sBb + canon(r, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
+        }
+    };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_tmem)),
@@ -227,156 +322,122 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar)));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
+    if (tid < kTauTile) s_kmax[tid] = (tau0 + tid < Nt) ? X0.kexp_max[tau0 + tid] : 0;
+    if (tid >= kTauTile && tid < kTauTile + kRowTile) {
+        const uint32_t r = tid - kTauTile;
+        int m = 0;
+        if (r < tile.rows) {
+            const SplitRow rw = rows[tile.first_row + r];
+            m = split[rw.run].xexp_max[rw.member];
+        }
+        s_xmax[r] = m;
+    }
+    // this thread's TMEM lane (timeslice) and rows
+    const uint32_t quarter = warp & 3u, half = warp >> 2;
+    const uint32_t tl = quarter * 32 + lane;  // timeslice within the tile
+    const uint32_t r0 = half * 32;            // first of this thread's 32 rows
+    for (uint32_t r = 0; r < 32; ++r) acc[(r0 + r) * kTauTile + tl] = make_float2(0.0f, 0.0f);
+
+    stage(wk.c0);
+    __syncthreads();  // s_kmax / s_xmax
+    scales(wk.c0);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     const uint32_t tmem = s_tmem;
+    const uint32_t idesc = idesc_bf16(kTauTile, kRowTile);
+    const uint32_t lane_base = tmem + ((quarter * 32u) << 16);
 
-    const uint64_t PM = (uint64_t)R.P * M;
-    const uint16_t* xrow = X.xdig + (uint64_t)my.member * M;  // + (b*S + s)*PM
-    const int16_t* xexp = X.xexp + (uint64_t)my.member * C;
-    const int xmax = live ? X.xexp_max[my.member] : 0;
-    const uint32_t tau0 = tile.tau0;
-    if (tid < kSplitTau) s_kmax[tid] = (tau0 + tid < Nt) ? X0.kexp_max[tau0 + tid] : 0;
-
-    // per-row accumulators: a double-float pair per timeslice in registers,
-    // folded into an FP64 row in shared memory every kFlush chunks
-    double* e64 = reinterpret_cast<double*>(sBb + kSplitTau * 16 * 2) + (uint64_t)tid * kSplitTau;
-    for (int t = 0; t < kSplitTau; ++t) e64[t] = 0.0;
-    float acc_hi[kSplitTau], acc_lo[kSplitTau];
-#pragma unroll
-    for (int t = 0; t < kSplitTau; ++t) acc_hi[t] = acc_lo[t] = 0.0f;
-    auto flush = [&]() {
-#pragma unroll
-        for (int t = 0; t < kSplitTau; ++t) {
-            e64[t] += (double)acc_hi[t] + (double)acc_lo[t];
-            acc_hi[t] = acc_lo[t] = 0.0f;
-        }
-    };
-
-    const uint32_t idesc = idesc_bf16(kSplitRows, kSplitTau);
     bool ok = true;
-    for (uint32_t c = 0; c < C && ok; ++c) {
-        const uint32_t g0 = c * kChunk;
-        // --- stage this chunk's digits (16-byte units = 8 genes of a row)
-        if (live) {
-            for (uint32_t b = 0; b < kDigits; ++b)
-                for (uint32_t s = 0; s < S; ++s) {
-                    const uint16_t* src = xrow + ((uint64_t)b * S + s) * PM + g0;
-                    uint8_t* dst = sA + (b * S + s) * a_tile;
-#pragma unroll
-                    for (uint32_t u = 0; u < kChunk / 8; ++u) cp16(dst + canon(tid, u * 8, kChunk), src + u * 8);
-                }
-        }
-        {
-            // B: thread -> (timeslice row, half of the digit/side planes)
-            const uint32_t trow = tid & (kSplitTau - 1), half = tid / kSplitTau;
-            if (tau0 + trow < Nt) {
-                for (uint32_t q = half; q < kDigits * S; q += 2) {
-                    const uint32_t b = q / S, s = q % S;
-                    const uint16_t* src = X0.kdig + (((uint64_t)b * S + s) * Nt + tau0 + trow) * M + g0;
-                    uint8_t* dst = sB + q * b_tile;
-#pragma unroll
-                    for (uint32_t u = 0; u < kChunk / 8; ++u) cp16(dst + canon(trow, u * 8, kChunk), src + u * 8);
-                }
-            }
-        }
-        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-        // bound operands: 2^(e_x - max_x) and 2^(e_K - max_K) at k = 0
-        const int ex = live ? xexp[c] : -1000;
-        {
-            const int d = ex - xmax;
-            const float v = (live && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
-            *reinterpret_cast<uint16_t*>(sAb + canon(tid, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
-        }
-        if (tid < kSplitTau) {
-            const int ek = (tau0 + tid < Nt) ? X0.kexp[(uint64_t)(tau0 + tid) * C + c] : -1000;
-            s_kexp[tid] = ek;
-            const int d = ek - s_kmax[tid];
-            const float v = (tau0 + tid < Nt && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
-            *reinterpret_cast<uint16_t*>(sBb + canon(tid, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
-        }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-
-        // --- MMAs (one thread)
+    for (uint32_t c = wk.c0; c < wk.c1; ++c) {
+        const uint32_t it = c - wk.c0;
+        // --- MMAs (one thread): group g accumulates every digit pair a+b=g
         if (tid == 0) {
             const uint32_t lbo = 128, sbo = (kChunk / 8) * 128;
             for (uint32_t g = 0; g < (uint32_t)kKept; ++g) {
                 uint32_t first = 1;
                 for (uint32_t a = 0; a <= g; ++a) {
-                    const uint32_t b = g - a;
-                    if (a >= (uint32_t)kDigits || b >= (uint32_t)kDigits) continue;
+                    const uint32_t bq = g - a;  // K digit index
                     for (uint32_t s = 0; s < S; ++s)
                         for (uint32_t ks = 0; ks < kChunk / 16; ++ks) {
-                            const uint64_t da =
-                                smem_desc(smem_u32(sA + (a * S + s) * a_tile) + ks * 256, lbo, sbo);
-                            const uint64_t db =
-                                smem_desc(smem_u32(sB + (b * S + s) * b_tile) + ks * 256, lbo, sbo);
-                            mma_bf16(tmem + g * kSplitTau, da, db, idesc, first ? 0u : 1u);
+                            const uint64_t da = smem_desc(smem_u32(sA + (bq * S + s) * a_tile) + ks * 256, lbo, sbo);
+                            const uint64_t db = smem_desc(smem_u32(sB + (a * S + s) * b_tile) + ks * 256, lbo, sbo);
+                            mma_bf16(tmem + g * kRowTile, da, db, idesc, first ? 0u : 1u);
                             first = 0;
                         }
                 }
             }
             const uint64_t dab = smem_desc(smem_u32(sAb), 128, 256);
             const uint64_t dbb = smem_desc(smem_u32(sBb), 128, 256);
-            mma_bf16(tmem + kBoundCol, dab, dbb, idesc, c > 0 ? 1u : 0u);
+            mma_bf16(tmem + kBoundCol, dab, dbb, idesc, it > 0 ? 1u : 0u);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 smem_u32(&s_bar)));
         }
-        ok = __syncthreads_and(mbar_wait(&s_bar, c & 1u)) != 0;  // uniform across the CTA
+        ok = __syncthreads_and(mbar_wait(&s_bar, it & 1u)) != 0;  // uniform across the CTA
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         if (!ok) break;
+        // the staging buffers are free again: load the next chunk meanwhile
+        if (c + 1 < wk.c1) stage(c + 1);
 
         // --- fold the six exact group sums of this chunk into the accumulators
-        const uint32_t lane_base = tmem + ((warp * 32u) << 16);
-#pragma unroll
-        for (uint32_t ts = 0; ts < kSplitTau / 8; ++ts) {
+        const int ek = s_ek[tl];
+#pragma unroll 1
+        for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
             uint32_t d[kKept][8];
 #pragma unroll
-            for (int g = 0; g < kKept; ++g) tmem_ld8(lane_base + g * kSplitTau + ts * 8, d[g]);
+            for (int g = 0; g < kKept; ++g) tmem_ld8(lane_base + g * kRowTile + r0 + j8, d[g]);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                // sum_g D_g 2^(7(5-g)): exact in 64 bits (every D_g < 2^24)
-                long long s = 0;
+                const uint32_t r = r0 + j8 + j;
+                // sum_g D_g 2^(7(5-g)) as a double-float: every term is exact
+                float sh = __uint_as_float(d[0][j]) * 0x1p35f, sl = 0.0f;
 #pragma unroll
-                for (int g = 0; g < kKept; ++g) s += (long long)(int)__uint_as_float(d[g][j]) << (7 * (kKept - 1 - g));
-                const float hi = (float)s;
-                const float lo = (float)(s - (long long)hi);
-                const int sc = ex + s_kexp[ts * 8 + j] - 7 * (kKept + 1);  // weight of g = 5 is 2^-49
-                two_sum_add(acc_hi[ts * 8 + j], acc_lo[ts * 8 + j], ldexpf(hi, sc), ldexpf(lo, sc));
+                for (int g = 1; g < kKept; ++g) {
+                    float e;
+                    two_sum(sh, __uint_as_float(d[g][j]) * exp2_int(7 * (kKept - 1 - g)), sh, e);
+                    sl += e;
+                }
+                float hi, lo;
+                fast_two_sum(sh, sl, hi, lo);
+                // weight of the lowest kept group: 2^(e_x + e_K - 49)
+                const int k = s_ex[r] + ek - 7 * (kKept + 1);
+                if (k > 60) {  // beyond any sane data: make the estimate unusable
+                    hi = __int_as_float(0x7fc00000);
+                    lo = 0.0f;
+                } else {
+                    scale_pow2(hi, lo, k);
+                }
+                float2 a = acc[r * kTauTile + tl];
+                dw_add(a.x, a.y, hi, lo);
+                acc[r * kTauTile + tl] = a;
             }
         }
-        if ((c + 1) % kFlush == 0) flush();
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();  // every read of s_ek/s_ex and of TMEM is done
+        if (c + 1 < wk.c1) {
+            scales(c + 1);
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        }
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;\n");
     }
-    flush();
 
-    if (ok) {  // CTA-uniform: the .sync.aligned TMEM loads need whole warps
-        // bound sums sum_c 2^(e_x + e_K), then the interval half-width
-        const uint32_t lane_base = tmem + ((warp * 32u) << 16);
-        for (uint32_t ts = 0; ts < kSplitTau / 8; ++ts) {
+    if (ok) {
+        // partial sums and the bound accumulator sum_c 2^(e_x-max_x + e_K-max_K)
+        float4* out = partial + (uint64_t)wk.block * kPartialBlock;
+        for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
             uint32_t d[8];
-            tmem_ld8(lane_base + kBoundCol + ts * 8, d);
+            tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-            if (!live) continue;
             for (int j = 0; j < 8; ++j) {
-                const uint32_t t = tau0 + ts * 8 + j;
-                if (t >= Nt) continue;
-                const double scale = ldexp(1.0, xmax + s_kmax[ts * 8 + j]);
-                // FP32 accumulation of C terms: relative error < C * 2^-24;
-                // terms that underflowed are each < 2^-126
-                const double bsum = ((double)__uint_as_float(d[j]) * (1.0 + 1e-4) + (double)C * 0x1.0p-126) * scale;
-                const uint64_t o = (uint64_t)my.member * Nt + t;
-                X.e_mp[o] = e64[ts * 8 + j];
-                // |estimate - FP64 chain| <= (2^-33.2 digits + 2^-33 chain
-                // rounding + 2^-35.4 double-float + 2^-42 FP64 folds) * B_sum
-                X.e_bound[o] = 0x1.0p-31 * bsum + (double)C * 0x1.0p-140;
+                const uint32_t r = r0 + j8 + j;
+                const float2 a = acc[r * kTauTile + tl];
+                out[(uint64_t)r * kTauTile + tl] = make_float4(a.x, a.y, __uint_as_float(d[j]), 0.0f);
             }
         }
     }
@@ -386,49 +447,112 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
 }
 
+// ------------------------------------------------------------- combine
+// One thread per (row, timeslice) of a tile: add the tile's partial sums over
+// its chunk splits and turn them into the estimate and its error bound.
+__global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
+                                                            const SplitRow* rows, const float4* partial) {
+    const SplitTile tile = tiles[blockIdx.x / kCombineCtasPerTile];
+    const uint32_t idx = (blockIdx.x % kCombineCtasPerTile) * blockDim.x + threadIdx.x;
+    const uint32_t r = idx / kTauTile, tl = idx % kTauTile;
+    if (r >= tile.rows) return;
+    const SplitRow rw = rows[tile.first_row + r];
+    const RunDev& R = runs[rw.run];
+    SplitRun& X = split[rw.run];
+    const uint32_t t = tile.tau0 + tl;
+    if (R.done || t >= R.Nt || !X.changed[rw.member]) return;
+    float hi = 0.0f, lo = 0.0f, b = 0.0f;
+    const float4* p = partial + (uint64_t)tile.block0 * kPartialBlock + idx;
+    // eight loads in flight per thread: the sum is latency-bound otherwise
+    constexpr uint32_t kAhead = 8;
+    for (uint32_t s0 = 0; s0 < tile.nsplit; s0 += kAhead) {
+        float4 v[kAhead];
+#pragma unroll
+        for (uint32_t u = 0; u < kAhead; ++u)
+            v[u] = s0 + u < tile.nsplit ? p[(uint64_t)(s0 + u) * kPartialBlock] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (uint32_t u = 0; u < kAhead; ++u) {
+            dw_add(hi, lo, v[u].x, v[u].y);
+            b += v[u].z;
+        }
+    }
+    const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
+    const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
+    // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
+    // below 2^-23 per addition), terms under 2^-126 dropped
+    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 1.0) * 0x1p-23) + C * 0x1p-126), emax);
+    // |estimate - FP64 chain| <= B * (digits 2^-33 + FP64 chain M 2^-47 +
+    // digit-group sums 2^-37 + double-float additions (C + nsplit + 2) 2^-40
+    // + final FP64 sum 2^-46), plus what underflowed in FP32
+    const double rel = 0x1p-33 + M * 0x1p-47 + 0x1p-37 + (C + ks + 2.0) * 0x1p-40 + 0x1p-46;
+    const uint64_t o = (uint64_t)rw.member * R.Nt + t;
+    X.e_mp[o] = (double)hi + (double)lo;
+    X.e_bound[o] = bsum * rel + (C + ks + 2.0) * 0x1p-140;
+}
+
 // ---------------------------------------------------------------- decide
-// One CTA per run: the estimate's chi^2 and its interval, then the
-// selection decisions that the interval settles.  Undecided members are
-// flagged for the exact FP64 evaluation (contract_kernel, recheck mode).
-__global__ void __launch_bounds__(256) split_decide_kernel(RunDev* runs, SplitRun* split, int init_mode) {
+// One CTA per run, a warp per member: the estimate's chi^2 and its interval,
+// then the selection decisions that the interval settles.  Undecided members
+// are flagged for the exact FP64 evaluation (contract_kernel, recheck mode).
+__global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* runs, SplitRun* split) {
+    __shared__ unsigned long long s_n[3];
+    __shared__ double s_inv_err[kDecideMaxTau];
     RunDev& R = runs[blockIdx.x];
     if (R.done) return;
     SplitRun& X = split[blockIdx.x];
     const uint32_t P = R.P, Nt = R.Nt, S = R.S;
     const bool force_exact = (R.flags & kTrackStats) != 0;
-    unsigned long long n_tie = 0, n_interval = 0, n_exact = 0;
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-        X.recheck[i] = 0;
-        if (!X.changed[i]) {
-            // the trial is the parent: the same fitness, and ties accept
-            X.t_lo[i] = X.f_lo[i];
-            X.t_hi[i] = X.f_hi[i];
-            R.fit_new[i] = X.f_lo[i];
-            for (uint32_t s = 0; s < S; ++s) {
-                R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
-                R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
+    if (threadIdx.x < 3) s_n[threadIdx.x] = 0;
+    // 1/sigma once per timeslice (a relative error of 2^-53, covered below)
+    const bool inv_ok = Nt <= kDecideMaxTau;
+    if (inv_ok)
+        for (uint32_t t = threadIdx.x; t < Nt; t += blockDim.x) s_inv_err[t] = 1.0 / R.err[t];
+    __syncthreads();
+    for (uint32_t i = warp; i < P; i += nw) {
+        const bool changed = X.changed[i] != 0;
+        if (!changed) {
+            if (lane == 0) {
+                // the trial is the parent: the same fitness, and ties accept
+                X.recheck[i] = 0;
+                X.t_lo[i] = X.f_lo[i];
+                X.t_hi[i] = X.f_hi[i];
+                R.fit_new[i] = X.f_lo[i];
+                for (uint32_t s = 0; s < S; ++s) {
+                    R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
+                    R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
+                }
+                R.cur[i] = (uint8_t)(1u - R.cur[i]);
+                atomicAdd(&s_n[0], 1ull);
             }
-            R.cur[i] = (uint8_t)(1u - R.cur[i]);
-            ++n_tie;
             continue;
         }
         // chi^2 of the estimate and a bound on its distance from the value
-        // the FP64 engine computes
+        // the FP64 engine computes (any summation order: the rounding term
+        // covers n-term sums)
         double chi = 0.0, dchi = 0.0;
-        for (uint32_t t = 0; t < Nt; ++t) {
+        for (uint32_t t = lane; t < Nt; t += 32) {
             const uint64_t o = (uint64_t)i * Nt + t;
-            const double r = (R.isf[t] - X.e_mp[o]) / R.err[t];
-            const double dr = X.e_bound[o] / R.err[t] * (1.0 + 0x1.0p-50) + fabs(r) * 0x1.0p-51;
+            const double ie = inv_ok ? s_inv_err[t] : 1.0 / R.err[t];
+            // r and dr carry up to three roundings of 2^-53 each
+            const double r = (R.isf[t] - X.e_mp[o]) * ie;
+            const double dr = X.e_bound[o] * ie * (1.0 + 0x1.0p-50) + fabs(r) * 0x1.0p-51;
             chi = fma(r, r, chi);
             dchi += (2.0 * fabs(r) + dr) * dr;
         }
+        for (int o = 16; o > 0; o >>= 1) {
+            chi += __shfl_xor_sync(0xffffffffu, chi, o);
+            dchi += __shfl_xor_sync(0xffffffffu, dchi, o);
+        }
+        if (lane != 0) continue;
+        X.recheck[i] = 0;
         chi /= (double)Nt;
         dchi = dchi / (double)Nt * (1.0 + 0x1.0p-40) + chi * (double)(Nt + 8) * 0x1.0p-52;
-        double lo = chi - dchi, hi = chi + dchi;
+        const double lo = chi - dchi, hi = chi + dchi;
         X.t_lo[i] = lo;
         X.t_hi[i] = hi;
         if (lo > X.f_hi[i]) {  // certainly worse: reject
-            ++n_interval;
+            atomicAdd(&s_n[1], 1ull);
             continue;
         }
         const bool certain_accept = hi <= X.f_lo[i];
@@ -442,16 +566,14 @@ __global__ void __launch_bounds__(256) split_decide_kernel(RunDev* runs, SplitRu
                 R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
             }
             R.cur[i] = (uint8_t)(1u - R.cur[i]);
-            ++n_interval;
+            atomicAdd(&s_n[1], 1ull);
             continue;
         }
         X.recheck[i] = 1;  // settle with the exact FP64 value
-        ++n_exact;
+        atomicAdd(&s_n[2], 1ull);
     }
-    if (n_tie) atomicAdd(&X.counts[0], n_tie);
-    if (n_interval) atomicAdd(&X.counts[1], n_interval);
-    if (n_exact) atomicAdd(&X.counts[2], n_exact);
-    (void)init_mode;
+    __syncthreads();
+    if (threadIdx.x < 3 && s_n[threadIdx.x]) atomicAdd(&X.counts[threadIdx.x], s_n[threadIdx.x]);
 }
 
 // ------------------------------------------------------------------ host
