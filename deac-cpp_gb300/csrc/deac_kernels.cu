@@ -3,6 +3,7 @@
 // fma() calls, placed where the reference's nvcc build fuses.
 #include <cuda_runtime.h>
 
+#include "deac_chain.cuh"
 #include "deac_kernels.cuh"
 #include "deac_rng.cuh"
 
@@ -216,18 +217,17 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 
     const double* gene_pos = in_smem ? trial_s : dst;
     const double* gene_neg = in_smem ? trial_s + M : dst + PM;
-    // row-sum chains of the normalisation: lane 0 of warp 0 the positive
-    // side, lane 1 the negative side (one FP64 instruction per step for both)
+    // row-sum chains (normalisation and moments): warp 0 the positive side,
+    // warp 1 the negative side, each by the exact warp-parallel evaluation
+    // of the sequential FMA chain (deac_chain.cuh)
     double chain_acc = 0.0;
-    const bool chain_lane = warp == 0 && lane < S;
-    const double* chain_x = lane == 0 ? gene_pos : gene_neg;
-    const double* chain_w = lane == 0 ? norm_p : norm_n;
+    const bool chain_warp = warp < S;
+    const double* chain_x = warp == 0 ? gene_pos : gene_neg;
+    const double* chain_w = warp == 0 ? norm_p : norm_n;
 
     if (!init_mode) {
         // crossover draw + DE/rand/1 mutation per gene (deac_gpu.cu:514-539,
-        // 635-643), in chunks of kGeneChunk genes per side.  With
-        // --normalize, warp 0 runs the row-sum chains over chunk c while the
-        // other warps produce chunk c+1; one barrier per chunk.
+        // 635-643), in chunks of kGeneChunk genes per side
         const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
         const uint64_t buf = (uint64_t)S * PM;  // stride between the two buffers
         const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
@@ -285,30 +285,13 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             }
         };
 
-        produce(0, threadIdx.x, blockDim.x);
+        for (uint32_t c = 0; c < nchunks; ++c) produce(c, threadIdx.x, blockDim.x);
         __syncthreads();
         if (S == 2 && threadIdx.x == 0) {
             // gpu_match_population_zero (deac_gpu.cu:541-549)
             const double z = in_smem ? trial_s[0] : dst[0];
             dst[PM] = z;
             if (in_smem) trial_s[M] = z;
-        }
-        __syncthreads();
-        for (uint32_t c = 0; c < nchunks; ++c) {
-            if (normalize) {
-                if (chain_lane) {
-                    const uint32_t j0 = c * kGeneChunk;
-                    chain_acc = chain(chain_x + j0, chain_w + j0, min(kGeneChunk, M - j0), chain_acc);
-                }
-                // producers keep off the chain warp's SM sub-partition
-                // (warps 4, 8, 12 share it with warp 0 and stay idle)
-                const uint32_t nwarps = blockDim.x >> 5;
-                if ((warp & 3u) != 0 && c + 1 < nchunks)
-                    produce(c + 1, (warp - (warp >> 2) - 1) * 32 + lane, (nwarps - (nwarps + 3) / 4) * 32);
-            } else if (c + 1 < nchunks) {
-                produce(c + 1, threadIdx.x, blockDim.x);
-            }
-            __syncthreads();
         }
         // the split engine skips the evaluation of a trial equal to its parent
         if (__syncthreads_or(mutated) && threadIdx.x == 0 && R.changed) R.changed[i] = 1;
@@ -319,15 +302,15 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             trial_s[q] = dst[(uint64_t)s * PM + (q - (uint64_t)s * M)];
         }
         __syncthreads();
-        if (normalize && chain_lane) chain_acc = chain(chain_x, chain_w, M, 0.0);
-    } else if (normalize && chain_lane) {
-        chain_acc = chain(chain_x, chain_w, M, 0.0);
     }
 
     if (normalize) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
-        if (chain_lane) s_sum[lane] = chain_acc;
+        if (chain_warp) {
+            chain_acc = warp_fma_chain(chain_x, chain_w, M, 0.0);
+            if (lane == 0) s_sum[warp] = chain_acc;
+        }
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
@@ -349,7 +332,10 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         const double *tp, *tn;
         weights(which == 0 ? R.first_pos : R.third_pos, which == 0 ? R.first_neg : R.third_neg, tp, tn);
         __syncthreads();
-        if (chain_lane) s_sum[lane] = chain(chain_x, lane == 0 ? tp : tn, M, 0.0);
+        if (chain_warp) {
+            const double v = warp_fma_chain(chain_x, warp == 0 ? tp : tn, M, 0.0);
+            if (lane == 0) s_sum[warp] = v;
+        }
         __syncthreads();
         if (threadIdx.x == 0) R.moments[2 * i + which] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
         __syncthreads();
