@@ -7,11 +7,14 @@ N_tau = 128 on [0, beta], M = 4096 on omega in [0, 512], P = 8, --normalize,
 stop fitness 1.0 (not reached in the timed generations).  Synthetic data by
 the benchmark recipe (deac_gb300.data.config1_data).
 
-A step is G generations of every run of the batch (plain FP64 engine,
-bit-identical to the reference CUDA-path semantics).  Timing: W untimed
+A step is G generations of every run of the batch.  The headline is the
+split-precision engine (contraction from exact BF16 digit slices on the
+tcgen05 tensor cores, every selection decision equal to FP64); the plain
+FP64 engine runs the same generations beside it, and the line records
+whether both ended with identical chi^2 and spectra.  Timing: W untimed
 warm-up steps, then K steps, each bracketed by CUDA events on the batch
-stream, with a 256 MB L2 flush before each step (outside the events); the
-K steps sit between a barrier + device synchronize on both sides; value is
+stream, with a 256 MB L2 flush before each step (outside the events); the K
+steps sit between a barrier + device synchronize on both sides; value is
 the max over ranks.  With --gpus N (torchrun), each rank runs its own 8
 seeds (weak scaling, no data-path collective).
 
@@ -46,7 +49,7 @@ RUNS_PER_GPU = 8
 P, M, NT, OMEGA_MAX, T = 8, 4096, 128, 512.0, 1.35
 GENS_PER_STEP = 32
 WORKLOAD = ("deac config 1: 8 runs (seeds 1-8), standard model, two-sided bfull, T=1.35, "
-            "N_tau=128, M=4096 on [0,512], P=8, --normalize, plain FP64 engine")
+            "N_tau=128, M=4096 on [0,512], P=8, --normalize; split-precision engine, plain FP64 engine beside it")
 DATA = "synthetic (benchmark recipe: 0.7 N(5,1) + 0.3 N(20,3), sigma = 1e-4 F, numpy default_rng(seed))"
 CPU_SAMPLE_GENERATIONS = 1000
 
@@ -221,6 +224,102 @@ def reference_arm(args, world, rank):
 
 # ---------------------------------------------------------------- GPU side
 
+# Algorithmic work per launch of each kernel kind of the split engine
+# (deac_batch_kernel_time kinds), for the roofline of the dominant one.
+BYTES_PER_TRIAL_GENE = 4 * 8 + 2 * 32 + 2 * 8 + 8  # parent+3 donors, PRNG state in/out, gene out twice, weight
+BYTES_PER_DIGITIZED_GENE = 8 + 6 * 2                # gene in, six BF16 digits out
+KEPT_DIGIT_PAIRS = 21                               # digit pairs a+b <= 5 of six 7-bit digits
+
+
+def kernel_roofline(kind, launch_s, peaks, split_ctas):
+    S, rows = 2, RUNS_PER_GPU * P
+    genes = RUNS_PER_GPU * P * S * M
+    if kind == 0:
+        work, unit, bound, peak = genes * BYTES_PER_TRIAL_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
+        achieved = work / launch_s / 1e9
+        name = "trial_kernel"
+    elif kind == 2:
+        work, unit, bound, peak = genes * BYTES_PER_DIGITIZED_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
+        achieved = work / launch_s / 1e9
+        name = "digitize_kernel"
+    elif kind == 3:
+        work = 2.0 * rows * NT * M * S * KEPT_DIGIT_PAIRS
+        unit, bound, peak = "TFLOP/s", "tensor", peaks["bf16_tflops"]
+        achieved = work / launch_s / 1e12
+        name = "split_contract_kernel"
+    elif kind == 4:
+        work = 16.0 * rows * NT * split_ctas + rows * NT * 16  # partial sums in, estimate + bound out
+        unit, bound, peak = "GB/s", "hbm", peaks["hbm_gbs"]
+        achieved = work / launch_s / 1e9
+        name = "split_combine_kernel+split_decide_kernel"
+    else:
+        work = 2.0 * 2 * rows * NT * M  # FP64 FMA chains, were every trial re-evaluated
+        unit, bound, peak = "TFLOP/s", "fp64", 1.196
+        achieved = work / launch_s / 1e12
+        name = "contract_kernel (exact passes)"
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+            "kernel": name, "work_per_launch": work, "launch_us": launch_s * 1e6}
+
+
+def load_peaks():
+    path = REPO / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured (MEASURED_PEAKS.json)"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def timed_engine(engine_kind, configs, args, local, stream, flush, world, sample_clocks):
+    """Set up a batch of the workload on `engine_kind`, run the warm-up steps,
+    then time K steps of G generations (events on the batch stream, L2
+    flushed before every step)."""
+    import torch
+    import deac_gb300
+
+    G = args.generations_per_step
+    batch = deac_gb300.Batch(engine=engine_kind, device=local, stream=stream.cuda_stream)
+    for cfg, tau, isf, err, freq in configs:
+        batch.add_run(cfg, tau, isf, err, freq)
+    batch.setup()
+    for _ in range(args.warmup):
+        batch.launch(G)
+    torch.cuda.synchronize()
+    assert batch.sync() == 0, "a run finished during warm-up"
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world, local)
+    clocks = ClockSampler(local) if sample_clocks else None
+    if clocks:
+        clocks.__enter__()
+    try:
+        for e0, e1 in events:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0.record(stream)
+            batch.launch(G)
+            e1.record(stream)
+        stream.synchronize()
+        barrier(world, local)
+    finally:
+        if clocks:
+            clocks.__exit__(None, None, None)
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in events)
+    assert batch.sync() == 0, "a run finished inside the timed region; its generations would not count"
+    return batch, ms, (clocks.summary() if clocks else None)
+
+
+def same_results(a, b, runs):
+    """Both batches ran the same generations: identical minimum fitness (chi^2),
+    best member and best spectrum for every run."""
+    import numpy as np
+    for r in range(runs):
+        x, y = a.fetch(r), b.fetch(r)
+        if x["generation"] != y["generation"] or x["minimum_fitness"] != y["minimum_fitness"]:
+            return False
+        if x["best_index"] != y["best_index"] or not np.array_equal(x["dsf"], y["dsf"]):
+            return False
+    return True
+
+
 def engine_arm(args, world, rank, local):
     import torch
     import deac_gb300
@@ -230,65 +329,60 @@ def engine_arm(args, world, rank, local):
     stream = torch.cuda.Stream(device=device)
     configs = run_configs(rank)
     G = args.generations_per_step
-
-    batch = deac_gb300.Batch(device=local, stream=stream.cuda_stream)
-    for cfg, tau, isf, err, freq in configs:
-        batch.add_run(cfg, tau, isf, err, freq)
-    batch.setup()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
-    for _ in range(args.warmup):
-        batch.launch(G)
-    torch.cuda.synchronize()
-    assert batch.sync() == 0, "a run finished during warm-up"
 
-    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier(world, local)
-    with ClockSampler(local) as clocks:
-        for e0, e1 in events:
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            e0.record(stream)
-            batch.launch(G)
-            e1.record(stream)
-        stream.synchronize()
-        barrier(world, local)
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in events)
-    finished = batch.sync()
-    assert finished == 0, "a run finished inside the timed region; its generations would not count"
+    # the headline: the split-precision engine; beside it the plain FP64
+    # engine on the same runs and the same generations
+    split, ms, clocks = timed_engine(deac_gb300.ENGINE_SPLIT_BF16, configs, args, local, stream, flush, world, True)
+    plain, ms_plain, _ = timed_engine(deac_gb300.ENGINE_PLAIN_FP64, configs, args, local, stream, flush, world,
+                                      False)
+    identical = same_results(split, plain, len(configs))
+    counts = [split.split_counts(r) for r in range(len(configs))]
+    plain.close()
     ms = barrier_max(ms, world, device)
+    ms_plain = barrier_max(ms_plain, world, device)
     gens_total = world * RUNS_PER_GPU * args.steps * G
     value = gens_total / (ms / 1e3)
+    value_plain = gens_total / (ms_plain / 1e3)
 
-    # per-kernel device time (separate pass, individually launched kernels
+    # per-kernel device time (separate pass, kernels launched one by one and
     # bracketed by events on the batch stream)
-    batch.enable_timing(True)
-    batch.launch(G)
-    trial_ms, trial_n = batch.kernel_time(0)
-    contract_ms, contract_n = batch.kernel_time(1)
-    batch.enable_timing(False)
-    batch.close()
-
-    flops_per_launch = RUNS_PER_GPU * 2.0 * 2 * P * NT * M  # 2*S*P*Nt*M per run-generation
-    contract_s = contract_ms / contract_n / 1e3
-    achieved = flops_per_launch / contract_s / 1e12
-    peak = 1.196  # TFLOP/s, measured DFMA throughput (profiles/fp64_pipe_gb300.md)
-    traffic = None
-    tpath = REPO / "profiles" / "contract_kernel_traffic.json"
-    if tpath.exists():
-        traffic = json.loads(tpath.read_text()).get("bytes_per_launch")
+    split.enable_timing(True)
+    split.launch(G)
+    kt = {k: split.kernel_time(k) for k in range(5)}
+    split.enable_timing(False)
+    split.close()
+    # CTAs of the split contraction: one tile (64 rows x 128 timeslices) whose
+    # M/32 chunks are spread over about one CTA per SM
+    chunks = M // 32
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    per = -(-chunks // min(max(1, sms), chunks))
+    split_ctas = -(-chunks // per)
+    per_gen_us = {k: ms_k / G * 1e3 for k, (ms_k, n) in kt.items() if n}
+    dominant = max(per_gen_us, key=per_gen_us.get)
+    ms_d, n_d = kt[dominant]
+    peaks = load_peaks()
+    roof = kernel_roofline(dominant, ms_d / n_d / 1e3, peaks, split_ctas)
+    roof["peak_source"] = peaks["source"] + (" burst figure" if roof["bound"] != "fp64" else
+                                             "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
+    tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_traffic.json"
+    roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
+    names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "digitize_kernel",
+             3: "split_contract_kernel", 4: "split_combine_kernel+split_decide_kernel"}
+    roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs
     # (host arrays) + setup (host build, H2D) + K steps of (G generations,
     # then every run's best spectrum and minimum fitness read back)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b2 = deac_gb300.Batch(device=local, stream=stream.cuda_stream)
+    b2 = deac_gb300.Batch(engine=deac_gb300.ENGINE_SPLIT_BF16, device=local, stream=stream.cuda_stream)
     h2d = 0
     for cfg, tau, isf, err, freq in configs:
         b2.add_run(cfg, tau, isf, err, freq)
         s = 2
         h2d += 8 * (3 * NT + 2 * s * P * M + 4 * P * (1 + s * M) + 4 * s * P)
-    h2d += 8 * 2 * NT * M  # shared kernel matrix
+    h2d += 8 * 2 * NT * M + 2 * 6 * 2 * NT * M  # shared kernel matrix and its digit planes
     b2.setup()
     d2h = 0
     for _ in range(args.steps):
@@ -304,21 +398,22 @@ def engine_arm(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "vs_baseline": None, "dtype": "f64 (FP64-identical results; contraction from exact bf16 digit slices)",
+        "data": DATA,
         "config": {"workload": WORKLOAD, "runs_per_gpu": RUNS_PER_GPU, "population_size": P, "genome_size": M,
                    "number_of_timeslices": NT, "normalize": True, "generations_per_step": G,
-                   "engine": "plain_fp64", "l2": "flushed before every timed step (256 MB write, untimed)"},
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "contract_kernel",
-                     "peak_source": "measured DFMA throughput (profiles/fp64_pipe_gb300.md); the driver's "
-                                    "peak file has no FP64 figure",
-                     "flops_per_launch": flops_per_launch, "launch_us": contract_s * 1e6,
-                     "trial_kernel_launch_us": trial_ms / trial_n * 1e3},
+                   "engine": "split_bf16", "l2": "flushed before every timed step (256 MB write, untimed)"},
+        "plain_fp64": {"value": value_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
+                       "split_over_plain": value / value_plain,
+                       "same_chi2_and_spectra": identical},
+        "split_decisions": {"equal_to_parent": sum(c["equal_to_parent"] for c in counts),
+                            "by_interval": sum(c["interval"] for c in counts),
+                            "by_exact_fp64": sum(c["exact"] for c in counts)},
+        "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
-        "gpu_launches": 2 * G * args.steps,
-        "clocks": clocks.summary(),
+        "gpu_launches": 7 * G * args.steps,
+        "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
