@@ -17,14 +17,15 @@
 // the new binade.  Zero, subnormal and non-finite states also step plainly.
 //
 // Everything is integer arithmetic on the IEEE fields, so the host and the
-// device share the per-step code below; the device form scans 32 lanes at a
-// time (warp_fma_chain), the host form walks the same blocks sequentially and
-// is the CPU check of the arithmetic.
+// device share the per-step code below; the device form scans a group of
+// warps at a time (group_fma_chain), the host form walks blocks sequentially
+// and is the CPU check of the arithmetic.
 #pragma once
 
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #ifndef __CUDACC__
 #define __host__
@@ -45,6 +46,13 @@ struct Term {
     uint32_t flags;    // kGtHalf | kTie | kGtZero | kNeg | kBad
 };
 constexpr uint32_t kGtHalf = 1u, kTie = 2u, kGtZero = 4u, kNeg = 8u, kBad = 16u;
+
+// A term packed in one word (F < 2^54 in the low bits, the flags above) to
+// keep the per-thread caches of the group form in registers.
+__host__ __device__ __forceinline__ uint64_t pack(const Term& t) { return t.F | ((uint64_t)t.flags << 56); }
+__host__ __device__ __forceinline__ Term unpack(uint64_t v) {
+    return Term{v & ((1ull << 54) - 1), (uint32_t)(v >> 56)};
+}
 
 __host__ __device__ __forceinline__ uint64_t bits_of(double d) {
 #ifdef __CUDA_ARCH__
@@ -175,6 +183,26 @@ __host__ __device__ __forceinline__ bool step(const Term& t, uint64_t A, uint32_
     return true;
 }
 
+// the grid of a state moved up by d binades: v' = v / 2^d
+__host__ __device__ __forceinline__ void shift_term(Term& t, int d) {
+    if (d == 0 || (t.flags & kBad)) return;
+    const uint32_t neg = t.flags & kNeg;
+    const uint32_t below_old = (t.flags & kGtZero) != 0;  // anything under the old integer part
+    uint64_t F = t.F;
+    uint32_t half, sticky;
+    if (d >= 64) {
+        half = 0;
+        sticky = (F != 0) || below_old;
+        F = 0;
+    } else {
+        half = (uint32_t)(F >> (d - 1)) & 1u;
+        sticky = (d > 1 && (F & ((1ull << (d - 1)) - 1)) != 0) || below_old;
+        F >>= d;
+    }
+    t.F = F;
+    t.flags = (half && sticky ? kGtHalf : 0u) | (half && !sticky ? kTie : 0u) | (half || sticky ? kGtZero : 0u) | neg;
+}
+
 }  // namespace chain_detail
 
 // Host form: the same blocks of `block` steps as the device form, walked one
@@ -215,109 +243,252 @@ inline double host_fma_chain(const double* x, const double* w, uint64_t n, doubl
     return acc;
 }
 
-#ifdef __CUDACC__
-// Device form: one warp evaluates the chain over x[0..n), w[0..n) (shared or
-// global memory) starting from `acc`; every lane returns the result.  Blocks
-// of 32*kChainPerLane steps; lane j owns steps j*kChainPerLane + i.
-constexpr uint32_t kChainPerLane = 8;
-
-__device__ __forceinline__ double warp_fma_chain(const double* x, const double* w, uint32_t n, double acc) {
+// Host form of group_fma_chain: the same super-blocks, plain first steps,
+// rounds and term shifts, with the scans walked sequentially.
+inline double host_group_fma_chain(const double* x, const double* w, uint64_t n, double acc, uint64_t SB,
+                                   uint64_t* rounds_out = nullptr) {
     using namespace chain_detail;
-    const uint32_t lane = threadIdx.x & 31u;
-    constexpr uint32_t E = kChainPerLane, B = 32 * kChainPerLane;
-    uint32_t k = 0;
-    uint32_t plain_run = 0;  // steps to run plainly before scanning again
-    while (k < n) {
-        if (plain_run > 0 || !state_ok(acc)) {
-            acc = fma(x[k], w[k], acc);
-            ++k;
-            if (plain_run > 0) --plain_run;
-            continue;
+    uint64_t rounds = 0;
+    std::vector<uint64_t> tp(SB);
+    for (uint64_t base = 0; base < n; base += SB) {
+        const uint64_t len = n - base < SB ? n - base : SB;
+        uint64_t k0 = 0;
+        const uint64_t early = base == 0 ? (len < 32 ? len : 32) : 0;
+        while (k0 < early || (k0 < len && !state_ok(acc))) {
+            acc = std::fma(x[base + k0], w[base + k0], acc);
+            ++k0;
         }
+        if (k0 >= len) continue;
         uint32_t neg;
         uint64_t A0;
         int ea;
         state_split(acc, neg, A0, ea);
-        const uint32_t L = n - k < B ? n - k : B;
-        // this lane's steps: terms, parity map (a, b): par' = (a & par) ^ b
-        Term t[E];
-        uint32_t pa = 1u, pb = 0u;
-#pragma unroll
-        for (uint32_t i = 0; i < E; ++i) {
-            const uint32_t s = lane * E + i;
-            t[i] = s < L ? term(x[k + s], w[k + s], ea, neg) : Term{0ull, 0u};
-            if (t[i].flags & kTie) {
-                pa = 0u;
-                pb = 0u;
-            } else {
-                pb ^= parity_flip(t[i]);
+        for (uint64_t s = 0; s < len; ++s) tp[s] = s >= k0 ? pack(term(x[base + s], w[base + s], ea, neg)) : 0ull;
+        for (;;) {
+            ++rounds;
+            uint64_t A = A0, bad = len;
+            for (uint64_t s = k0; s < len; ++s) {
+                int64_t q;
+                if (!step(unpack(tp[s]), A, (uint32_t)(A & 1u), q)) {
+                    bad = s;
+                    break;
+                }
+                A = (uint64_t)((int64_t)A + q);
             }
-        }
-        // inclusive scan of the maps over lanes, then the exclusive one
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t qa = __shfl_up_sync(0xffffffffu, pa, o), qb = __shfl_up_sync(0xffffffffu, pb, o);
-            if (lane >= o) {
-                pb = (pa & qb) ^ pb;
-                pa = qa & pa;
+            acc = state_join(neg, A, ea);
+            if (bad == len) break;
+            acc = std::fma(x[base + bad], w[base + bad], acc);
+            k0 = bad + 1;
+            while (k0 < len && !state_ok(acc)) {
+                acc = std::fma(x[base + k0], w[base + k0], acc);
+                ++k0;
             }
-        }
-        uint32_t ea_map = __shfl_up_sync(0xffffffffu, pa, 1), eb_map = __shfl_up_sync(0xffffffffu, pb, 1);
-        if (lane == 0) {
-            ea_map = 1u;
-            eb_map = 0u;
-        }
-        uint32_t par = (ea_map & (uint32_t)(A0 & 1u)) ^ eb_map;
-        // the integer steps (garbage after an invalid one, never used)
-        int64_t q[E];
-        int64_t lane_sum = 0;
-#pragma unroll
-        for (uint32_t i = 0; i < E; ++i) {
-            const uint64_t mag = t[i].F + ((t[i].flags & kGtHalf) ? 1u : 0u) +
-                                 ((t[i].flags & kTie) ? (par ^ (uint32_t)(t[i].F & 1u)) : 0u);
-            q[i] = (t[i].flags & kNeg) ? -(int64_t)mag : (int64_t)mag;
-            par = (t[i].flags & kTie) ? 0u : par ^ parity_flip(t[i]);
-            lane_sum += q[i];
-        }
-        int64_t incl = lane_sum;
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const int64_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        // validity of each step from the exact running integer
-        uint64_t A = (uint64_t)((int64_t)A0 + incl - lane_sum);
-        uint32_t first_bad = 0xFFFFFFFFu;
-        uint64_t A_at_bad = 0;
-#pragma unroll
-        for (uint32_t i = 0; i < E; ++i) {
-            const uint32_t s = lane * E + i;
-            if (s < L && first_bad == 0xFFFFFFFFu) {
-                int64_t qq;
-                // the tie parity is already folded into q[i]; step() is used
-                // for the range checks only
-                if (!step(t[i], A, (uint32_t)(A & 1u), qq)) {
-                    first_bad = s;
-                    A_at_bad = A;
+            if (k0 >= len) break;
+            uint32_t neg2;
+            uint64_t A2;
+            int ea2;
+            state_split(acc, neg2, A2, ea2);
+            const bool shift = neg2 == neg && ea2 >= ea;
+            for (uint64_t s = k0; s < len; ++s) {
+                Term t = unpack(tp[s]);
+                if (shift && !(t.flags & kBad)) {
+                    shift_term(t, ea2 - ea);
+                    tp[s] = pack(t);
                 } else {
-                    A = (uint64_t)((int64_t)A + q[i]);
+                    tp[s] = pack(term(x[base + s], w[base + s], ea2, neg2));
                 }
             }
+            neg = neg2;
+            A0 = A2;
+            ea = ea2;
         }
-        const uint32_t bad = __reduce_min_sync(0xffffffffu, first_bad);
-        uint64_t A_end;
-        if (bad == 0xFFFFFFFFu) {
-            A_end = (uint64_t)((int64_t)A0 + __shfl_sync(0xffffffffu, incl, 31));
-        } else {
-            A_end = __shfl_sync(0xffffffffu, A_at_bad, bad / E);
+    }
+    if (rounds_out) *rounds_out = rounds;
+    return acc;
+}
+
+#ifdef __CUDACC__
+// Scratch of one warp group running group_fma_chain (shared memory).
+struct ChainScratch {
+    uint32_t map_a[8], map_b[8];  // per-warp parity maps
+    long long sum[8];             // per-warp integer sums
+    uint32_t bad[8];              // per-warp first invalid step
+    unsigned long long a_bad;     // running integer at the first invalid step
+};
+
+namespace chain_detail {
+
+__device__ __forceinline__ void group_bar(int id, int threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+}  // namespace chain_detail
+
+// CTA-cooperative form: the W warps starting at warp `w0` evaluate the chain
+// over x[0..n), w[0..n) from `acc`; every thread of the group returns the
+// result.  Steps are split into super-blocks of W*32*E, each thread owning E
+// consecutive steps; a round scans the parity maps and the integer steps of
+// the whole super-block at once, and a binade change (a new round) shifts the
+// thread's cached terms instead of decoding them again.  Synchronises the
+// group with named barrier `bar_id` (not 0).
+template <int W, int E>
+__device__ __forceinline__ double group_fma_chain(const double* x, const double* w, uint32_t n, double acc,
+                                                  uint32_t w0, int bar_id, ChainScratch& sc) {
+    using namespace chain_detail;
+    constexpr uint32_t NT = W * 32, SB = NT * E;
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    const uint32_t tg = threadIdx.x - w0 * 32, lane = tg & 31u, wg = tg >> 5;
+    for (uint32_t base = 0; base < n; base += SB) {
+        const uint32_t len = n - base < SB ? n - base : SB;
+        uint32_t k0 = 0;
+        // the first steps change binade every few steps: run them plainly
+        const uint32_t early = base == 0 ? (len < 32u ? len : 32u) : 0u;
+        while (k0 < early || (k0 < len && !state_ok(acc))) {
+            acc = fma(x[base + k0], w[base + k0], acc);
+            ++k0;
         }
-        acc = state_join(neg, A_end, ea);
-        if (bad == 0xFFFFFFFFu) {
-            k += L;
-        } else {
-            acc = fma(x[k + bad], w[k + bad], acc);
-            k += bad + 1;
-            if (bad < 16) plain_run = 32;  // little progress: step plainly for a while
+        if (k0 >= len) continue;
+        uint32_t neg;
+        uint64_t A0;
+        int ea;
+        state_split(acc, neg, A0, ea);
+        const uint32_t my0 = tg * E;  // first step of this thread within the super-block
+        uint64_t tp[E];               // packed terms
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            const uint32_t s = my0 + i;
+            tp[i] = (s >= k0 && s < len) ? pack(term(x[base + s], w[base + s], ea, neg)) : 0ull;
+        }
+        for (;;) {
+            // --- parity maps: par' = (a & par) ^ b; steps before k0 are identity
+            uint32_t pa = 1u, pb = 0u;
+#pragma unroll
+            for (uint32_t i = 0; i < E; ++i) {
+                const Term t = unpack(tp[i]);
+                if (t.flags & kTie) {
+                    pa = 0u;
+                    pb = 0u;
+                } else {
+                    pb ^= parity_flip(t);
+                }
+            }
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t qa = __shfl_up_sync(0xffffffffu, pa, o), qb = __shfl_up_sync(0xffffffffu, pb, o);
+                if (lane >= o) {
+                    pb = (pa & qb) ^ pb;
+                    pa = qa & pa;
+                }
+            }
+            if (lane == 31) {
+                sc.map_a[wg] = pa;
+                sc.map_b[wg] = pb;
+            }
+            uint32_t xa = __shfl_up_sync(0xffffffffu, pa, 1), xb = __shfl_up_sync(0xffffffffu, pb, 1);
+            if (lane == 0) {
+                xa = 1u;
+                xb = 0u;
+            }
+            group_bar(bar_id, NT);
+            // maps of the warps before this one, then this warp's exclusive part
+            uint32_t ga = 1u, gb = 0u;
+            for (uint32_t v = 0; v < wg; ++v) {
+                gb = (sc.map_a[v] & gb) ^ sc.map_b[v];
+                ga = sc.map_a[v] & ga;
+            }
+            const uint32_t ca = xa & ga, cb = (xa & gb) ^ xb;
+            const uint32_t par = (ca & (uint32_t)(A0 & 1u)) ^ cb;
+            // --- integer steps
+            long long lane_sum = 0;
+            {
+                uint32_t p = par;
+#pragma unroll
+                for (uint32_t i = 0; i < E; ++i) {
+                    const Term t = unpack(tp[i]);
+                    const uint64_t mag = t.F + ((t.flags & kGtHalf) ? 1u : 0u) +
+                                         ((t.flags & kTie) ? (p ^ (uint32_t)(t.F & 1u)) : 0u);
+                    lane_sum += (t.flags & kNeg) ? -(long long)mag : (long long)mag;
+                    p = (t.flags & kTie) ? 0u : p ^ parity_flip(t);
+                }
+            }
+            long long incl = lane_sum;
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane == 31) sc.sum[wg] = incl;
+            group_bar(bar_id, NT);
+            long long before = 0, total = 0;
+            for (uint32_t v = 0; v < (uint32_t)W; ++v) {
+                const long long sv = sc.sum[v];
+                if (v < wg) before += sv;
+                total += sv;
+            }
+            // --- validity of each step from the exact running integer
+            uint64_t A = (uint64_t)((long long)A0 + before + incl - lane_sum);
+            uint32_t first_bad = kNone;
+            uint64_t A_at_bad = 0;
+            {
+                uint32_t p = par;
+#pragma unroll
+                for (uint32_t i = 0; i < E; ++i) {
+                    const uint32_t s = my0 + i;
+                    const Term t = unpack(tp[i]);
+                    if (first_bad == kNone && s >= k0 && s < len) {
+                        int64_t q;
+                        if (!step(t, A, p, q)) {
+                            first_bad = s;
+                            A_at_bad = A;
+                        } else {
+                            A = (uint64_t)((long long)A + q);
+                        }
+                    }
+                    p = (t.flags & kTie) ? 0u : p ^ parity_flip(t);
+                }
+            }
+            const uint32_t wbad = __reduce_min_sync(0xffffffffu, first_bad);
+            if (lane == 0) sc.bad[wg] = wbad;
+            group_bar(bar_id, NT);
+            uint32_t bad = kNone;
+            for (uint32_t v = 0; v < (uint32_t)W; ++v) bad = sc.bad[v] < bad ? sc.bad[v] : bad;
+            if (bad == kNone) {
+                acc = state_join(neg, (uint64_t)((long long)A0 + total), ea);
+                group_bar(bar_id, NT);  // the scratch is reused by the next super-block
+                break;
+            }
+            if (first_bad == bad) sc.a_bad = A_at_bad;
+            group_bar(bar_id, NT);
+            acc = state_join(neg, (uint64_t)sc.a_bad, ea);
+            acc = fma(x[base + bad], w[base + bad], acc);
+            k0 = bad + 1;
+            while (k0 < len && !state_ok(acc)) {
+                acc = fma(x[base + k0], w[base + k0], acc);
+                ++k0;
+            }
+            group_bar(bar_id, NT);  // every thread has read the scratch
+            if (k0 >= len) break;
+            uint32_t neg2;
+            uint64_t A2;
+            int ea2;
+            state_split(acc, neg2, A2, ea2);
+            const bool shift = neg2 == neg && ea2 >= ea;
+#pragma unroll
+            for (uint32_t i = 0; i < E; ++i) {
+                const uint32_t s = my0 + i;
+                Term t = unpack(tp[i]);
+                if (s < k0 || s >= len) {
+                    tp[i] = 0ull;
+                } else if (shift && !(t.flags & kBad)) {
+                    shift_term(t, ea2 - ea);
+                    tp[i] = pack(t);
+                } else {
+                    tp[i] = pack(term(x[base + s], w[base + s], ea2, neg2));
+                }
+            }
+            neg = neg2;
+            A0 = A2;
+            ea = ea2;
         }
     }
     return acc;

@@ -6,6 +6,7 @@
 #include "deac_chain.cuh"
 #include "deac_gb300.h"
 #include "deac_gb300_debug.h"
+#include "deac_kernels.cuh"
 
 namespace deac {
 __attribute__((visibility("hidden"))) int set_error(int code, const char* msg);
@@ -13,16 +14,19 @@ __attribute__((visibility("hidden"))) int set_error(int code, const char* msg);
 
 namespace {
 
-// warp 0: the exact parallel chain; warp 1, lane 0: the plain chain
+// warps 0-7: the exact parallel chain in the configuration of trial_kernel;
+// warp 8, lane 0: the plain chain
 __global__ void fma_chains_kernel(const double* x, const double* w, uint64_t n, const double* start, double* fast,
                                   double* plain) {
+    __shared__ deac::ChainScratch sc;
     const uint64_t c = blockIdx.x;
     const double* xc = x + c * n;
     const double* wc = w + c * n;
-    if (threadIdx.x < 32) {
-        const double r = deac::warp_fma_chain(xc, wc, (uint32_t)n, start[c]);
+    if (threadIdx.x < 32 * deac::kChainWarps) {
+        const double r = deac::group_fma_chain<deac::kChainWarps, deac::kChainSteps>(xc, wc, (uint32_t)n, start[c],
+                                                                                      0, 1, sc);
         if (threadIdx.x == 0) fast[c] = r;
-    } else if (threadIdx.x == 32) {
+    } else if (threadIdx.x == 32 * deac::kChainWarps) {
         double acc = start[c];
         for (uint64_t k = 0; k < n; ++k) acc = fma(xc[k], wc[k], acc);
         plain[c] = acc;
@@ -63,7 +67,7 @@ extern "C" int deac_debug_fma_chains(const double* x, const double* w, uint64_t 
             rc = cuda_fail(e, "cudaMemcpy");
             break;
         }
-        fma_chains_kernel<<<count, 64>>>(dx, dw, n, ds, df, dp);
+        fma_chains_kernel<<<count, 32 * deac::kChainWarps + 32>>>(dx, dw, n, ds, df, dp);
         if ((e = cudaGetLastError()) || (e = cudaDeviceSynchronize())) {
             rc = cuda_fail(e, "fma_chains_kernel");
             break;

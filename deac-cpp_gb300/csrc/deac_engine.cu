@@ -135,7 +135,7 @@ struct deac_batch {
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
-    // passes), 2 digitize, 3 split contraction, 4 split decisions
+    // passes), 2 unused, 3 split contraction, 4 combine + decisions
     bool timing = false;
     cudaEvent_t ev[8] = {};
     double kernel_ms[5] = {};
@@ -175,9 +175,6 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
         return mark(1);
     }
-    deac::digitize_kernel<<<b->n_trial_ctas, deac::kDigitizeThreads, 0, s>>>(b->d_runs, b->d_split,
-                                                                           b->d_trial_work, 0);
-    if ((rc = mark(2))) return rc;
     deac::split_contract_kernel<<<b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
         b->d_runs, b->d_split, b->d_tiles, b->d_split_work, b->d_rows, b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
@@ -420,6 +417,9 @@ int upload_run(deac_batch* b, RunHost& r) {
         x.t_hi = reinterpret_cast<double*>(sb + o_th);
         x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
         d.changed = x.changed;
+        d.xdig = x.xdig;
+        d.xexp = x.xexp;
+        d.xexp_max = x.xexp_max;
         d.recheck = x.recheck;
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;

@@ -6,6 +6,7 @@
 #include "deac_chain.cuh"
 #include "deac_kernels.cuh"
 #include "deac_rng.cuh"
+#include "deac_split.cuh"
 
 namespace deac {
 
@@ -137,6 +138,8 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     __shared__ double s_cr[2], s_fw[2], s_sum[4];
     __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
+    __shared__ ChainScratch s_chain[2];
+    __shared__ int s_digit_max[kTrialThreads / 32];
 
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
@@ -215,15 +218,20 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     }
     __syncthreads();
 
+    bool trial_changed = false;  // uniform over the CTA
     const double* gene_pos = in_smem ? trial_s : dst;
     const double* gene_neg = in_smem ? trial_s + M : dst + PM;
-    // row-sum chains (normalisation and moments): warp 0 the positive side,
-    // warp 1 the negative side, each by the exact warp-parallel evaluation
-    // of the sequential FMA chain (deac_chain.cuh)
-    double chain_acc = 0.0;
-    const bool chain_warp = warp < S;
-    const double* chain_x = warp == 0 ? gene_pos : gene_neg;
-    const double* chain_w = warp == 0 ? norm_p : norm_n;
+    // row-sum chains (normalisation and moments): warps 0-7 the positive
+    // side, warps 8-15 the negative side, each group by the exact parallel
+    // evaluation of the sequential FMA chain (deac_chain.cuh)
+    const uint32_t chain_side = warp / kChainWarps;
+    const bool chain_warp = chain_side < S;
+    const double* chain_x = chain_side == 0 ? gene_pos : gene_neg;
+    const double* chain_w = chain_side == 0 ? norm_p : norm_n;
+    auto row_sum = [&](const double* wts) -> double {
+        return group_fma_chain<kChainWarps, kChainSteps>(chain_x, wts, M, 0.0, chain_side * kChainWarps,
+                                                         1 + (int)chain_side, s_chain[chain_side]);
+    };
 
     if (!init_mode) {
         // crossover draw + DE/rand/1 mutation per gene (deac_gpu.cu:514-539,
@@ -294,8 +302,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             if (in_smem) trial_s[M] = z;
         }
         // the split engine skips the evaluation of a trial equal to its parent
-        if (__syncthreads_or(mutated) && threadIdx.x == 0 && R.changed) R.changed[i] = 1;
-        else if (threadIdx.x == 0 && R.changed) R.changed[i] = 0;
+        trial_changed = __syncthreads_or(mutated) != 0;
     } else if (in_smem) {
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
@@ -308,13 +315,13 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
         if (chain_warp) {
-            chain_acc = warp_fma_chain(chain_x, chain_w, M, 0.0);
-            if (lane == 0) s_sum[warp] = chain_acc;
+            const double v = row_sum(chain_w);
+            if (warp % kChainWarps == 0 && lane == 0) s_sum[chain_side] = v;
         }
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
-        if (!init_mode && threadIdx.x == 0 && R.changed && recip != 1.0) R.changed[i] = 1;
+        trial_changed = trial_changed || recip != 1.0;
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
             const uint64_t g = (uint64_t)s * PM + (q - (uint64_t)s * M);
@@ -333,12 +340,21 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         weights(which == 0 ? R.first_pos : R.third_pos, which == 0 ? R.first_neg : R.third_neg, tp, tn);
         __syncthreads();
         if (chain_warp) {
-            const double v = warp_fma_chain(chain_x, warp == 0 ? tp : tn, M, 0.0);
-            if (lane == 0) s_sum[warp] = v;
+            const double v = row_sum(chain_side == 0 ? tp : tn);
+            if (warp % kChainWarps == 0 && lane == 0) s_sum[chain_side] = v;
         }
         __syncthreads();
         if (threadIdx.x == 0) R.moments[2 * i + which] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
         __syncthreads();
+    }
+
+    // split engine: flag the trial and slice a changed one into BF16 digits
+    // for the tensor-core contraction
+    if (!init_mode && R.changed) {
+        if (threadIdx.x == 0) R.changed[i] = trial_changed ? 1 : 0;
+        if (trial_changed)
+            digitize_trial(in_smem ? trial_s : dst, in_smem ? (uint64_t)M : PM, S, M, R.xdig + (uint64_t)i * M, PM,
+                           R.xexp + (uint64_t)i * (M / kChunk), R.xexp_max + i, s_digit_max);
     }
 }
 
@@ -354,6 +370,7 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
     if (R.done && mode != kModeFinal) return;
+    if ((mode == kModeParents || mode == kModeTrials) && R.exact_idle) return;
     const bool init_mode = mode == kModeInit;
     // members evaluated by this launch, and which of their two buffers
     const bool use_parent = mode == kModeInit || mode == kModeParents || mode == kModeFinal;

@@ -87,11 +87,17 @@ struct RunDev {
     const uint8_t* recheck;  // [P] decision left to the exact FP64 value
     double* f_lo;            // [P] interval holding the parent's exact fitness
     double* f_hi;
+    uint16_t* xdig;          // [6][S][P][M] digit planes of the changed trials
+    int16_t* xexp;           // [P][M/32] their chunk scale exponents
+    int16_t* xexp_max;       // [P]
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
     uint32_t ticket;         // CTAs of contract_kernel done this launch
     int32_t done;
+    int32_t exact_idle;      // split engine: this generation needs no exact pass
+                             // (set by split_decide_kernel, which then also did
+                             // the generation's bookkeeping)
 };
 
 // Per-member PRNG slot layout.  The reference keeps one state per
@@ -132,6 +138,10 @@ __host__ __device__ inline uint64_t stage_doubles(uint32_t S, uint32_t mt, uint3
 }
 
 constexpr int kTrialThreads = 512;
+// row-sum chains of trial_kernel: a group of 8 warps per side, 16 steps per
+// thread in a round (2048 steps)
+constexpr int kChainWarps = 8;
+constexpr int kChainSteps = 8;
 
 struct Work {
     uint32_t run;

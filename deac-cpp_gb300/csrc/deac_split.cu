@@ -80,28 +80,6 @@ __device__ __forceinline__ void cp16(void* dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 
-// exponent field of |v| (unbiased), or -2000 for zero / subnormal
-__device__ __forceinline__ int exp_of(double v) {
-    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    const int ef = (int)(b >> 52);
-    return ef == 0 ? -2000 : ef - 1023;
-}
-
-// fixed-point fraction floor(|v| * 2^(42-e)) for a scale 2^e > |v|
-__device__ __forceinline__ uint64_t frac42(double v, int e) {
-    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    const int ef = (int)(b >> 52);
-    if (ef == 0) return 0;  // zero or subnormal: below every scale used here
-    const uint64_t mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int shift = 10 + e - (ef - 1023);
-    return shift >= 64 ? 0 : (mant >> shift);
-}
-
-__device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
-    const uint32_t f = __float_as_uint((float)d);  // exact: d < 128
-    return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
-}
-
 // Error-free transformations in FP32 (IEEE round-to-nearest; the file is
 // compiled without FMA contraction): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -143,69 +121,6 @@ __device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
 }
 
 }  // namespace
-
-// -------------------------------------------------------------- digitize
-// One CTA per (run, member): a warp per 32-gene chunk computes the chunk's
-// scale exponent (max over both sides) and writes the six 7-bit digit planes.
-__global__ void __launch_bounds__(kDigitizeThreads) digitize_kernel(RunDev* runs, SplitRun* split, const Work* work,
-                                                                    int all_members) {
-    __shared__ int s_max[kDigitizeThreads / 32];
-    const Work w = work[blockIdx.x];
-    RunDev& R = runs[w.run];
-    if (R.done) return;
-    SplitRun& X = split[w.run];
-    const uint32_t i = w.index;
-    if (!all_members && !X.changed[i]) return;
-    const uint32_t P = R.P, M = R.M, S = R.S;
-    const uint64_t PM = (uint64_t)P * M;
-    // digitize the member's trial (buffer 1-cur) or, with all_members, its
-    // parent (initial population)
-    const uint32_t buf = all_members ? R.cur[i] : 1u - R.cur[i];
-    const double* row = R.pop + (uint64_t)buf * S * PM + (uint64_t)i * M;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
-    const uint32_t C = M / kChunk;
-    int wmax = -2000;
-    constexpr uint32_t kAhead = 4;  // chunks in flight per warp
-    for (uint32_t c0 = warp * kAhead; c0 < C; c0 += nw * kAhead) {
-        double v[kAhead][2];
-#pragma unroll
-        for (uint32_t u = 0; u < kAhead; ++u)
-#pragma unroll
-            for (uint32_t s = 0; s < 2; ++s)
-                v[u][s] = (c0 + u < C && s < S) ? row[(uint64_t)s * PM + (c0 + u) * kChunk + lane] : 0.0;
-#pragma unroll
-        for (uint32_t u = 0; u < kAhead; ++u) {
-            const uint32_t c = c0 + u;
-            if (c >= C) break;  // warp-uniform
-            const uint32_t j = c * kChunk + lane;
-            int e = -2000;
-#pragma unroll
-            for (uint32_t s = 0; s < 2; ++s)
-                if (s < S) e = max(e, exp_of(v[u][s]));
-            for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-            e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
-#pragma unroll
-            for (uint32_t s = 0; s < 2; ++s) {
-                if (s >= S) break;
-                const uint64_t f = frac42(v[u][s], e);
-                const bool neg = v[u][s] < 0.0;
-                for (int b = 0; b < kDigits; ++b) {
-                    const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
-                    X.xdig[((uint64_t)b * S + s) * PM + (uint64_t)i * M + j] = bf16_digit(d, neg);
-                }
-            }
-            if (lane == 0) X.xexp[(uint64_t)i * C + c] = (int16_t)e;
-            wmax = max(wmax, e);
-        }
-    }
-    if (lane == 0) s_max[warp] = wmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int m = -2000;
-        for (uint32_t k = 0; k < nw; ++k) m = max(m, s_max[k]);
-        X.xexp_max[i] = (int16_t)m;
-    }
-}
 
 // ----------------------------------------------------- split contraction
 // One CTA per (tile, chunk range).  The tile is 128 timeslices (MMA M, one
@@ -448,46 +363,61 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
 }
 
 // ------------------------------------------------------------- combine
-// One thread per (row, timeslice) of a tile: add the tile's partial sums over
-// its chunk splits and turn them into the estimate and its error bound.
+// A CTA per 32 (row, timeslice) outputs of a tile: warp w adds the partial
+// sums of the splits w, w+8, ... for its lane's output (coalesced 512-byte
+// loads, eight in flight), then lane-wise the eight warps' sums are added in
+// a fixed order and turned into the estimate and its error bound.
 __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
                                                             const SplitRow* rows, const float4* partial) {
+    __shared__ float4 s_part[8][32];
     const SplitTile tile = tiles[blockIdx.x / kCombineCtasPerTile];
-    const uint32_t idx = (blockIdx.x % kCombineCtasPerTile) * blockDim.x + threadIdx.x;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t idx = (blockIdx.x % kCombineCtasPerTile) * 32 + lane;
     const uint32_t r = idx / kTauTile, tl = idx % kTauTile;
-    if (r >= tile.rows) return;
-    const SplitRow rw = rows[tile.first_row + r];
-    const RunDev& R = runs[rw.run];
-    SplitRun& X = split[rw.run];
-    const uint32_t t = tile.tau0 + tl;
-    if (R.done || t >= R.Nt || !X.changed[rw.member]) return;
+    // rows and timeslices outside the tile or not evaluated this generation
+    // are summed anyway (uniform control flow) and not written
     float hi = 0.0f, lo = 0.0f, b = 0.0f;
     const float4* p = partial + (uint64_t)tile.block0 * kPartialBlock + idx;
-    // eight loads in flight per thread: the sum is latency-bound otherwise
     constexpr uint32_t kAhead = 8;
-    for (uint32_t s0 = 0; s0 < tile.nsplit; s0 += kAhead) {
+    for (uint32_t s0 = warp; s0 < tile.nsplit; s0 += 8 * kAhead) {
         float4 v[kAhead];
 #pragma unroll
-        for (uint32_t u = 0; u < kAhead; ++u)
-            v[u] = s0 + u < tile.nsplit ? p[(uint64_t)(s0 + u) * kPartialBlock] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (uint32_t u = 0; u < kAhead; ++u) {
+            const uint32_t s = s0 + 8 * u;
+            v[u] = s < tile.nsplit ? p[(uint64_t)s * kPartialBlock] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
         for (uint32_t u = 0; u < kAhead; ++u) {
             dw_add(hi, lo, v[u].x, v[u].y);
             b += v[u].z;
         }
     }
+    s_part[warp][lane] = make_float4(hi, lo, b, 0.0f);
+    __syncthreads();
+    if (warp != 0 || r >= tile.rows) return;
+    hi = lo = b = 0.0f;
+    for (uint32_t w = 0; w < 8; ++w) {
+        const float4 v = s_part[w][lane];
+        dw_add(hi, lo, v.x, v.y);
+        b += v.z;
+    }
+    const SplitRow rw = rows[tile.first_row + r];
+    const RunDev& R = runs[rw.run];
+    SplitRun& X = split[rw.run];
+    const uint32_t t = tile.tau0 + tl;
+    if (R.done || t >= R.Nt || !X.changed[rw.member]) return;
     const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
     const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
     // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
     // below 2^-23 per addition), terms under 2^-126 dropped
-    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 1.0) * 0x1p-23) + C * 0x1p-126), emax);
+    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
     // |estimate - FP64 chain| <= B * (digits 2^-33 + FP64 chain M 2^-47 +
-    // digit-group sums 2^-37 + double-float additions (C + nsplit + 2) 2^-40
+    // digit-group sums 2^-37 + double-float additions (C + nsplit + 10) 2^-40
     // + final FP64 sum 2^-46), plus what underflowed in FP32
-    const double rel = 0x1p-33 + M * 0x1p-47 + 0x1p-37 + (C + ks + 2.0) * 0x1p-40 + 0x1p-46;
+    const double rel = 0x1p-33 + M * 0x1p-47 + 0x1p-37 + (C + ks + 10.0) * 0x1p-40 + 0x1p-46;
     const uint64_t o = (uint64_t)rw.member * R.Nt + t;
     X.e_mp[o] = (double)hi + (double)lo;
-    X.e_bound[o] = bsum * rel + (C + ks + 2.0) * 0x1p-140;
+    X.e_bound[o] = bsum * rel + (C + ks + 10.0) * 0x1p-140;
 }
 
 // ---------------------------------------------------------------- decide
@@ -574,6 +504,32 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     }
     __syncthreads();
     if (threadIdx.x < 3 && s_n[threadIdx.x]) atomicAdd(&X.counts[threadIdx.x], s_n[threadIdx.x]);
+    // Nothing left for the exact passes: finish the generation here -- the
+    // bookkeeping of contract_kernel's trial pass (generation index, minimum
+    // and stop test); the fitness of an interval-accepted member lies above
+    // the stop fitness, so its midpoint decides the stop test exactly.  Runs
+    // that track statistics keep the exact pass, which forms them.
+    if (threadIdx.x == 0) {
+        const bool idle = s_n[2] == 0 && !(R.flags & kTrackStats);
+        R.exact_idle = idle ? 1 : 0;
+        if (idle) {
+            const uint64_t ii = R.ii + 1;
+            if (ii + 2 <= R.N) {
+                const volatile double* f = R.fit_old;
+                double mn = f[0];
+                for (uint32_t m = 1; m < P; ++m) mn = f[m] < mn ? f[m] : mn;
+                R.ii = ii;
+                if (mn <= R.stop) {
+                    R.generation = ii;
+                    R.done = 1;
+                }
+            } else {
+                R.ii = ii;
+                R.generation = R.N - 2;
+                R.done = 1;
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------------ host

@@ -31,7 +31,6 @@ constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
 constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
-constexpr int kDigitizeThreads = 512;
 constexpr int kDecideThreads = 512;
 constexpr uint32_t kDecideMaxTau = 2048;  // timeslices whose 1/sigma is kept in shared memory
 // dynamic shared memory of split_contract_kernel for S sides: K digits
@@ -83,13 +82,80 @@ struct SplitRow {
 // partial sums of one CTA: [kRowTile][kTauTile] of (hi, lo, bound, 0)
 constexpr uint64_t kPartialBlock = (uint64_t)kRowTile * kTauTile;
 
-__global__ void digitize_kernel(RunDev* runs, SplitRun* split, const Work* work, int all_members);
 __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
                                       const SplitRow* rows, float4* partial, int* status);
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows,
                                      const float4* partial);
 __global__ void split_decide_kernel(RunDev* runs, SplitRun* split);
-constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 256);
+constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
+
+// ---- digit slicing of one value (shared by trial_kernel and the host)
+// exponent field of |v| (unbiased), or -2000 for zero / subnormal
+__device__ __forceinline__ int exp_of(double v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    const int ef = (int)(b >> 52);
+    return ef == 0 ? -2000 : ef - 1023;
+}
+
+// fixed-point fraction floor(|v| * 2^(42-e)) for a scale 2^e > |v|
+__device__ __forceinline__ uint64_t frac42(double v, int e) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    const int ef = (int)(b >> 52);
+    if (ef == 0) return 0;  // zero or subnormal: below every scale used here
+    const uint64_t mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int shift = 10 + e - (ef - 1023);
+    return shift >= 64 ? 0 : (mant >> shift);
+}
+
+__device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
+    const uint32_t f = __float_as_uint((float)d);  // exact: d < 128
+    return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
+}
+
+// The digit planes of one trial (both sides, genes in `x` at side stride
+// `side_stride`) by the calling CTA, a warp per 32-gene chunk: the chunk's
+// scale exponent (max over both sides), six 7-bit digits per gene, and the
+// trial's maximum exponent.  `s_max` is shared scratch of one int per warp.
+__device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_stride, uint32_t S, uint32_t M,
+                                               uint16_t* xdig, uint64_t plane_stride, int16_t* xexp,
+                                               int16_t* xexp_max, int* s_max) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
+    const uint32_t C = M / kChunk;
+    int wmax = -2000;
+    for (uint32_t c = warp; c < C; c += nw) {
+        const uint32_t j = c * kChunk + lane;
+        double v[2] = {0.0, 0.0};
+        int e = -2000;
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s)
+            if (s < S) {
+                v[s] = x[s * side_stride + j];
+                e = max(e, exp_of(v[s]));
+            }
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s) {
+            if (s >= S) break;
+            const uint64_t f = frac42(v[s], e);
+            const bool neg = v[s] < 0.0;
+#pragma unroll
+            for (int b = 0; b < kDigits; ++b) {
+                const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
+                xdig[((uint64_t)b * S + s) * plane_stride + j] = bf16_digit(d, neg);
+            }
+        }
+        if (lane == 0) xexp[c] = (int16_t)e;
+        wmax = max(wmax, e);
+    }
+    if (lane == 0) s_max[warp] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = -2000;
+        for (uint32_t k = 0; k < nw; ++k) m = max(m, s_max[k]);
+        *xexp_max = (int16_t)m;
+    }
+}
 
 // host-side digit decomposition of one value for a given scale exponent
 void digits_of(double v, int e, uint16_t out[kDigits]);

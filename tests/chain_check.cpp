@@ -1,5 +1,7 @@
 // CPU check of the blocked exact FMA-chain arithmetic (deac_chain.cuh):
-// host_fma_chain must equal the plain sequential fma chain bit for bit on
+// host_fma_chain and host_group_fma_chain (the sequential walk of the
+// device's group form, term shifts included) must equal the plain
+// sequential fma chain bit for bit on
 // random and adversarial inputs (ties, sign changes, cancellation,
 // subnormal, huge and zero terms).  Prints "ok <cases> <plain-steps>" or the
 // first mismatch and exits 1.
@@ -73,6 +75,14 @@ int main(int argc, char** argv) {
         if (kind == 5 && rng() % 2) start = -std::ldexp(1.0, (int)(rng() % 10));
         double ref = start;
         for (uint64_t k = 0; k < n; ++k) ref = std::fma(x[k], w[k], ref);
+        for (uint64_t sb : {2048ull, 61ull}) {
+            const double got = deac::host_group_fma_chain(x.data(), w.data(), n, start, sb);
+            if (bits(got) != bits(ref) && !(std::isnan(got) && std::isnan(ref))) {
+                std::printf("group mismatch case %d kind %d n %llu sb %llu: %.17g vs %.17g\n", c, kind,
+                            (unsigned long long)n, (unsigned long long)sb, got, ref);
+                return 1;
+            }
+        }
         for (uint64_t block : {256ull, 37ull}) {
             uint64_t plain = 0;
             const double got = deac::host_fma_chain(x.data(), w.data(), n, start, block, &plain);
