@@ -243,10 +243,120 @@ inline double host_fma_chain(const double* x, const double* w, uint64_t n, doubl
     return acc;
 }
 
+// One pass over the steps [k0, len) of a super-block from the state
+// (A0, ea) (positive), with the steps' terms cached relative to ea: predict
+// where the running sum crosses into higher binades (from the prefix of the
+// integer parts), sum the rounded integer steps of each predicted binade --
+// twice, for either parity of the binade's first state, since the ties to
+// even make the sum depend on it -- chain the binades with the crossing
+// steps run as plain fma, and verify every step's range condition.  Returns
+// the position up to which the chain is done, with the state there in *acc;
+// the caller continues from it.  This is the sequential statement of the
+// device pass in group_fma_chain.
+inline uint64_t host_predicted_pass(const double* x, const double* w, const uint64_t* tp, uint64_t k0,
+                                    uint64_t len, uint64_t A0, int ea, double* acc) {
+    using namespace chain_detail;
+    const uint64_t n = len - k0;
+    for (uint64_t i = 0; i < n; ++i)
+        if (unpack(tp[k0 + i]).flags & (kNeg | kBad)) return k0;  // not a positive run: no prediction
+    std::vector<uint32_t> cross(n), seg(n);
+    std::vector<int> ds(n), dk(n);
+    // predicted binade (relative to ea) of the state before each step and of
+    // the step's exact sum
+    uint64_t prefix = A0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const Term t = unpack(tp[k0 + i]);
+        const uint64_t T = prefix + t.F + ((t.flags & kGtZero) ? 1u : 0u);
+        const int bs = 64 - __builtin_clzll(prefix), bt = 64 - __builtin_clzll(T);
+        ds[i] = bs - 53 > 0 ? bs - 53 : 0;
+        dk[i] = bt - 53 > 0 ? bt - 53 : 0;
+        cross[i] = dk[i] > ds[i];
+        prefix += t.F;
+    }
+    // per segment (the steps between crossings, in the grid of their binade)
+    // and per parity p0 of its first state: the exclusive prefix P_p0 of the
+    // rounded integer steps, and the inclusive one
+    std::vector<uint64_t> cpos;
+    std::vector<int> cbin;
+    std::vector<int64_t> P0(n), P1(n), I0(n), I1(n);
+    std::vector<uint64_t> Fs(n);
+    uint32_t cnt = 0;
+    int64_t r0 = 0, r1 = 0;
+    uint32_t ma = 1, mb = 0;  // parity map from the segment start
+    for (uint64_t i = 0; i < n; ++i) {
+        if (cross[i]) {
+            cpos.push_back(k0 + i);
+            cbin.push_back(dk[i]);
+            ++cnt;
+            r0 = r1 = 0;
+            ma = 1;
+            mb = 0;
+            seg[i] = cnt;
+            P0[i] = P1[i] = I0[i] = I1[i] = 0;
+            continue;
+        }
+        Term t = unpack(tp[k0 + i]);
+        shift_term(t, ds[i]);
+        Fs[i] = t.F;
+        seg[i] = cnt;
+        P0[i] = r0;
+        P1[i] = r1;
+        for (uint32_t p0 = 0; p0 < 2; ++p0) {
+            const uint32_t par = (ma & p0) ^ mb;
+            const uint64_t mag = t.F + ((t.flags & kGtHalf) ? 1u : 0u) + ((t.flags & kTie) ? (par ^ (uint32_t)(t.F & 1u)) : 0u);
+            (p0 ? r1 : r0) += (int64_t)mag;
+        }
+        if (t.flags & kTie) {
+            ma = 0;
+            mb = 0;
+        } else {
+            mb ^= parity_flip(t);
+        }
+        I0[i] = r0;
+        I1[i] = r1;
+    }
+    // chain the segments
+    const uint32_t nseg = cnt + 1;
+    std::vector<uint64_t> Astart(nseg);
+    uint64_t fail = len;  // first segment start whose state is not the predicted one
+    double fail_acc = 0.0;
+    double a = state_join(0, A0, ea);
+    for (uint32_t m = 0; m < nseg; ++m) {
+        const int j = m == 0 ? 0 : cbin[m - 1];
+        const uint64_t start = m == 0 ? k0 : cpos[m - 1] + 1;
+        const uint64_t end = m < cnt ? cpos[m] : len;  // exclusive
+        uint32_t ng;
+        uint64_t A;
+        int e;
+        if (!state_ok(a) || (state_split(a, ng, A, e), ng != 0 || e != ea + j)) {
+            fail = start;
+            fail_acc = a;
+            break;
+        }
+        Astart[m] = A;
+        const int64_t Q = end > start ? ((A & 1u) ? I1[end - 1 - k0] : I0[end - 1 - k0]) : 0;
+        a = state_join(0, A + (uint64_t)Q, e);
+        if (m < cnt) a = std::fma(x[cpos[m]], w[cpos[m]], a);
+    }
+    // verify the steps before the first mismatch
+    for (uint64_t i = 0; i < n && k0 + i < fail; ++i) {
+        if (cross[i]) continue;
+        const uint64_t As = Astart[seg[i]];
+        const uint64_t A = As + (uint64_t)((As & 1u) ? P1[i] : P0[i]);
+        if (A + Fs[i] > kTwo53 - 1 || A < kTwo52 || A >= kTwo53) {
+            const int j = seg[i] == 0 ? 0 : cbin[seg[i] - 1];
+            *acc = state_join(0, A, ea + j);  // the state before this step
+            return k0 + i;
+        }
+    }
+    *acc = fail < len ? fail_acc : a;
+    return fail;
+}
+
 // Host form of group_fma_chain: the same super-blocks, plain first steps,
 // rounds and term shifts, with the scans walked sequentially.
 inline double host_group_fma_chain(const double* x, const double* w, uint64_t n, double acc, uint64_t SB,
-                                   uint64_t* rounds_out = nullptr) {
+                                   uint64_t* rounds_out = nullptr, bool predict = true) {
     using namespace chain_detail;
     uint64_t rounds = 0;
     std::vector<uint64_t> tp(SB);
@@ -264,6 +374,33 @@ inline double host_group_fma_chain(const double* x, const double* w, uint64_t n,
         int ea;
         state_split(acc, neg, A0, ea);
         for (uint64_t s = 0; s < len; ++s) tp[s] = s >= k0 ? pack(term(x[base + s], w[base + s], ea, neg)) : 0ull;
+        if (neg == 0 && predict) {
+            double a2;
+            const uint64_t done = host_predicted_pass(x + base, w + base, tp.data(), k0, len, A0, ea, &a2);
+            if (done > k0) {
+                acc = a2;
+                k0 = done;
+                if (k0 >= len) continue;
+                uint32_t neg2;
+                uint64_t A2;
+                int ea2;
+                state_split(acc, neg2, A2, ea2);
+                if (!state_ok(acc)) {
+                    acc = std::fma(x[base + k0], w[base + k0], acc);
+                    ++k0;
+                    while (k0 < len && !state_ok(acc)) {
+                        acc = std::fma(x[base + k0], w[base + k0], acc);
+                        ++k0;
+                    }
+                    if (k0 >= len) continue;
+                    state_split(acc, neg2, A2, ea2);
+                }
+                for (uint64_t s = k0; s < len; ++s) tp[s] = pack(term(x[base + s], w[base + s], ea2, neg2));
+                neg = neg2;
+                A0 = A2;
+                ea = ea2;
+            }
+        }
         for (;;) {
             ++rounds;
             uint64_t A = A0, bad = len;
@@ -309,11 +446,24 @@ inline double host_group_fma_chain(const double* x, const double* w, uint64_t n,
 
 #ifdef __CUDACC__
 // Scratch of one warp group running group_fma_chain (shared memory).
+constexpr uint32_t kMaxCross = 64;  // binade crossings one predicted pass handles
 struct ChainScratch {
     uint32_t map_a[8], map_b[8];  // per-warp parity maps
     long long sum[8];             // per-warp integer sums
     uint32_t bad[8];              // per-warp first invalid step
     unsigned long long a_bad;     // running integer at the first invalid step
+    // predicted pass
+    uint32_t cnt[8];              // per-warp crossing counts
+    long long sum1[8];            // per-warp sums for the other start parity
+    uint32_t flag[8];             // per-warp "not a positive run"
+    uint32_t cpos[kMaxCross];     // position of each crossing step
+    int32_t cbin[kMaxCross];      // binade (relative) after it
+    long long segq[2][kMaxCross + 1];          // per segment and start parity: its integer sum
+    unsigned long long astart[kMaxCross + 1];  // state of each segment's first step
+    uint8_t first_cross[256];     // per thread: its first step is a crossing
+    unsigned long long fail_state;
+    uint32_t fail_pos;
+    int32_t fail_bin;
 };
 
 namespace chain_detail {
@@ -324,6 +474,317 @@ __device__ __forceinline__ void group_bar(int id, int threads) {
 
 }  // namespace chain_detail
 
+namespace chain_detail {
+
+// segmented-scan elements: c crossings in the range; after the last one (or
+// from the range start) the parity map (a, b) resp. the sums (s0, s1)
+struct SegMap {
+    uint32_t c, a, b;
+};
+struct SegSum {
+    uint32_t c;
+    long long s0, s1;
+};
+__device__ __forceinline__ SegMap seg_combine(const SegMap& L, const SegMap& R) {
+    if (R.c) return SegMap{L.c + R.c, R.a, R.b};
+    return SegMap{L.c, L.a & R.a, (R.a & L.b) ^ R.b};
+}
+__device__ __forceinline__ SegSum seg_combine(const SegSum& L, const SegSum& R) {
+    if (R.c) return SegSum{L.c + R.c, R.s0, R.s1};
+    return SegSum{L.c, L.s0 + R.s0, L.s1 + R.s1};
+}
+
+// Exclusive group scan of a per-thread aggregate: warp shuffles, then the
+// warps' totals through shared memory.  `tot` receives the group total.
+template <int W>
+__device__ __forceinline__ SegMap group_scan(SegMap v, uint32_t lane, uint32_t wg, int bar_id, ChainScratch& sc,
+                                             SegMap& tot) {
+    SegMap inc = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const SegMap u{__shfl_up_sync(0xffffffffu, inc.c, o), __shfl_up_sync(0xffffffffu, inc.a, o),
+                       __shfl_up_sync(0xffffffffu, inc.b, o)};
+        if (lane >= o) inc = seg_combine(u, inc);
+    }
+    SegMap ex{__shfl_up_sync(0xffffffffu, inc.c, 1), __shfl_up_sync(0xffffffffu, inc.a, 1),
+              __shfl_up_sync(0xffffffffu, inc.b, 1)};
+    if (lane == 0) ex = SegMap{0u, 1u, 0u};
+    if (lane == 31) {
+        sc.cnt[wg] = inc.c;
+        sc.map_a[wg] = inc.a;
+        sc.map_b[wg] = inc.b;
+    }
+    group_bar(bar_id, W * 32);
+    SegMap before{0u, 1u, 0u}, all{0u, 1u, 0u};
+    for (uint32_t k = 0; k < (uint32_t)W; ++k) {
+        const SegMap t{sc.cnt[k], sc.map_a[k], sc.map_b[k]};
+        if (k < wg) before = seg_combine(before, t);
+        all = seg_combine(all, t);
+    }
+    group_bar(bar_id, W * 32);
+    tot = all;
+    return seg_combine(before, ex);
+}
+template <int W>
+__device__ __forceinline__ SegSum group_scan(SegSum v, uint32_t lane, uint32_t wg, int bar_id, ChainScratch& sc) {
+    SegSum inc = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const SegSum u{__shfl_up_sync(0xffffffffu, inc.c, o), __shfl_up_sync(0xffffffffu, inc.s0, o),
+                       __shfl_up_sync(0xffffffffu, inc.s1, o)};
+        if (lane >= o) inc = seg_combine(u, inc);
+    }
+    SegSum ex{__shfl_up_sync(0xffffffffu, inc.c, 1), __shfl_up_sync(0xffffffffu, inc.s0, 1),
+              __shfl_up_sync(0xffffffffu, inc.s1, 1)};
+    if (lane == 0) ex = SegSum{0u, 0, 0};
+    if (lane == 31) {
+        sc.cnt[wg] = inc.c;
+        sc.sum[wg] = inc.s0;
+        sc.sum1[wg] = inc.s1;
+    }
+    group_bar(bar_id, W * 32);
+    SegSum before{0u, 0, 0};
+    for (uint32_t k = 0; k < wg; ++k) before = seg_combine(before, SegSum{sc.cnt[k], sc.sum[k], sc.sum1[k]});
+    group_bar(bar_id, W * 32);
+    return seg_combine(before, ex);
+}
+
+// binade (relative to the pass's grid) of an integer multiple of the grid
+__device__ __forceinline__ int rel_binade(uint64_t v) {
+    const int b = 64 - __clzll((long long)v);
+    return b - 53 > 0 ? b - 53 : 0;
+}
+
+}  // namespace chain_detail
+
+// The predicted pass of host_predicted_pass, by the W warps of a group, each
+// thread over its E cached terms tp (steps tg*E + i of the super-block, the
+// ones before k0 and from len on are zero).  Returns the position reached
+// and the state there in acc (uniform over the group).
+template <int W, int E>
+__device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const double* w, const uint64_t (&tp)[E],
+                                                          uint32_t k0, uint32_t len, uint64_t A0, int ea,
+                                                          double& acc, uint32_t tg, int bar_id, ChainScratch& sc) {
+    using namespace chain_detail;
+    constexpr uint32_t NT = W * 32;
+    static_assert(NT <= sizeof(ChainScratch::first_cross) && W <= 8, "group larger than its scratch");
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    const uint32_t lane = tg & 31u, wg = tg >> 5, my0 = tg * E;
+    // --- prefix of the integer parts; is the run all positive and moderate?
+    // (each thread's part below 2^52 keeps every prefix below 2^61)
+    long long fsum = 0;
+    uint32_t badf = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < E; ++i) {
+        const Term t = unpack(tp[i]);
+        fsum += (long long)t.F;
+        badf |= t.flags & (kNeg | kBad);
+    }
+    badf |= fsum >= (1ll << 52) ? 1u : 0u;
+    long long finc = fsum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, finc, o);
+        if (lane >= o) finc += v;
+    }
+    const uint32_t wbad = __any_sync(0xffffffffu, badf != 0);
+    if (lane == 31) {
+        sc.sum[wg] = finc;
+        sc.flag[wg] = wbad;
+    }
+    group_bar(bar_id, NT);
+    long long fbefore = 0;
+    uint32_t anybad = 0;
+    for (uint32_t k = 0; k < (uint32_t)W; ++k) {
+        if (k < wg) fbefore += sc.sum[k];
+        anybad |= sc.flag[k];
+    }
+    group_bar(bar_id, NT);
+    if (anybad) return k0;
+    const uint64_t pstart = A0 + (uint64_t)(fbefore + finc - fsum);
+
+    // --- crossings (a step whose exact sum lies in a higher binade than its
+    // state) and the parity maps of the segments between them
+    uint32_t cross_bits = 0;
+    SegMap magg{0u, 1u, 0u};
+    {
+        uint64_t prefix = pstart;
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            Term t = unpack(tp[i]);
+            const uint32_t s = my0 + i;
+            const uint64_t T = prefix + t.F + ((t.flags & kGtZero) ? 1u : 0u);
+            const int ds = rel_binade(prefix), dk = rel_binade(T);
+            const bool cr = s >= k0 && s < len && dk > ds;
+            cross_bits |= (cr ? 1u : 0u) << i;
+            if (cr) {
+                magg = seg_combine(magg, SegMap{1u, 1u, 0u});
+            } else {
+                shift_term(t, ds);
+                magg = seg_combine(magg, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
+            }
+            prefix += unpack(tp[i]).F;
+        }
+    }
+    sc.first_cross[tg] = (uint8_t)(cross_bits & 1u);
+    for (uint32_t m = tg; m <= kMaxCross; m += NT) {  // empty segments sum to zero
+        sc.segq[0][m] = 0;
+        sc.segq[1][m] = 0;
+    }
+    SegMap mtot;
+    const SegMap mex = group_scan<W>(magg, lane, wg, bar_id, sc, mtot);
+    const uint32_t ncross = mtot.c;
+    if (ncross > kMaxCross) return k0;
+
+    // the integer steps of a segment for start parities 0 and 1, given the
+    // parity map from the segment's start
+    auto steps = [&](Term t, const SegMap& m, long long& q0, long long& q1) {
+        const uint64_t base = t.F + ((t.flags & kGtHalf) ? 1u : 0u);
+        const uint32_t par0 = m.b, par1 = m.a ^ m.b;
+        q0 = (long long)(base + ((t.flags & kTie) ? (par0 ^ (uint32_t)(t.F & 1u)) : 0u));
+        q1 = (long long)(base + ((t.flags & kTie) ? (par1 ^ (uint32_t)(t.F & 1u)) : 0u));
+    };
+    auto next_map = [&](const SegMap& m, const Term& t) {
+        return seg_combine(m, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
+    };
+    SegSum sagg{0u, 0, 0};
+    {
+        uint64_t prefix = pstart;
+        SegMap run = mex;
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            Term t = unpack(tp[i]);
+            const int ds = rel_binade(prefix);
+            prefix += t.F;
+            if ((cross_bits >> i) & 1u) {
+                sagg = seg_combine(sagg, SegSum{1u, 0, 0});
+                run = seg_combine(run, SegMap{1u, 1u, 0u});
+            } else {
+                shift_term(t, ds);
+                long long q0, q1;
+                steps(t, run, q0, q1);
+                sagg = seg_combine(sagg, SegSum{0u, q0, q1});
+                run = next_map(run, t);
+            }
+        }
+    }
+    const SegSum sex = group_scan<W>(sagg, lane, wg, bar_id, sc);
+    // crossing positions and binades; each segment's sums at its last step
+    {
+        uint64_t prefix = pstart;
+        SegMap runm = mex;
+        SegSum runs = sex;
+        const bool next_thread_cross = tg + 1 < NT ? sc.first_cross[tg + 1] != 0 : false;
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            Term t = unpack(tp[i]);
+            const uint32_t s = my0 + i;
+            const uint64_t T = prefix + t.F + ((t.flags & kGtZero) ? 1u : 0u);
+            const int ds = rel_binade(prefix), dk = rel_binade(T);
+            prefix += t.F;
+            if ((cross_bits >> i) & 1u) {
+                runs = seg_combine(runs, SegSum{1u, 0, 0});
+                runm = seg_combine(runm, SegMap{1u, 1u, 0u});
+                sc.cpos[runs.c - 1] = s;
+                sc.cbin[runs.c - 1] = dk;
+            } else {
+                shift_term(t, ds);
+                long long q0, q1;
+                steps(t, runm, q0, q1);
+                runs = seg_combine(runs, SegSum{0u, q0, q1});
+                runm = next_map(runm, t);
+                const bool next_cross = i + 1 < E ? ((cross_bits >> (i + 1)) & 1u) != 0 : next_thread_cross;
+                if (s >= k0 && s < len && (s + 1 == len || next_cross)) {
+                    sc.segq[0][runs.c] = runs.s0;
+                    sc.segq[1][runs.c] = runs.s1;
+                }
+            }
+        }
+    }
+    group_bar(bar_id, NT);
+
+    // --- chain the segments (every thread, on the same values)
+    double a = state_join(0, A0, ea);
+    uint32_t fail = len;
+    double fail_acc = 0.0;
+    for (uint32_t m = 0; m <= ncross; ++m) {
+        const int j = m == 0 ? 0 : sc.cbin[m - 1];
+        const uint32_t start = m == 0 ? k0 : sc.cpos[m - 1] + 1;
+        const uint32_t end = m < ncross ? sc.cpos[m] : len;
+        uint32_t ng;
+        uint64_t A;
+        int e;
+        bool ok = state_ok(a);
+        if (ok) {
+            state_split(a, ng, A, e);
+            ok = ng == 0 && e == ea + j;
+        }
+        if (!ok) {
+            fail = start;
+            fail_acc = a;
+            break;
+        }
+        if (tg == 0) sc.astart[m] = A;
+        const long long Q = end > start ? sc.segq[A & 1u][m] : 0;
+        a = state_join(0, A + (uint64_t)Q, e);
+        if (m < ncross) a = fma(x[sc.cpos[m]], w[sc.cpos[m]], a);
+    }
+    group_bar(bar_id, NT);
+
+    // --- verify every step before the first mismatch
+    uint32_t first_bad = kNone;
+    uint64_t bad_state = 0;
+    int bad_bin = 0;
+    {
+        uint64_t prefix = pstart;
+        SegMap runm = mex;
+        SegSum runs = sex;
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            Term t = unpack(tp[i]);
+            const uint32_t s = my0 + i;
+            const int ds = rel_binade(prefix);
+            prefix += t.F;
+            if ((cross_bits >> i) & 1u) {
+                runs = seg_combine(runs, SegSum{1u, 0, 0});
+                runm = seg_combine(runm, SegMap{1u, 1u, 0u});
+                continue;
+            }
+            shift_term(t, ds);
+            if (first_bad == kNone && s >= k0 && s < len && s < fail) {
+                const uint64_t As = sc.astart[runs.c];
+                const uint64_t A = As + (uint64_t)((As & 1u) ? runs.s1 : runs.s0);
+                if (A < kTwo52 || A >= kTwo53 || A + t.F > kTwo53 - 1) {
+                    first_bad = s;
+                    bad_state = A;
+                    bad_bin = runs.c == 0 ? 0 : sc.cbin[runs.c - 1];
+                }
+            }
+            long long q0, q1;
+            steps(t, runm, q0, q1);
+            runs = seg_combine(runs, SegSum{0u, q0, q1});
+            runm = next_map(runm, t);
+        }
+    }
+    const uint32_t wmin = __reduce_min_sync(0xffffffffu, first_bad);
+    if (lane == 0) sc.bad[wg] = wmin;
+    group_bar(bar_id, NT);
+    uint32_t bad = kNone;
+    for (uint32_t k = 0; k < (uint32_t)W; ++k) bad = sc.bad[k] < bad ? sc.bad[k] : bad;
+    if (bad != kNone && first_bad == bad) {
+        sc.fail_state = bad_state;
+        sc.fail_bin = bad_bin;
+    }
+    group_bar(bar_id, NT);
+    if (bad != kNone) {
+        acc = state_join(0, sc.fail_state, ea + sc.fail_bin);
+        group_bar(bar_id, NT);  // the scratch is reused next
+        return bad;
+    }
+    acc = fail < len ? fail_acc : a;
+    return fail;
+}
+
 // CTA-cooperative form: the W warps starting at warp `w0` evaluate the chain
 // over x[0..n), w[0..n) from `acc`; every thread of the group returns the
 // result.  Steps are split into super-blocks of W*32*E, each thread owning E
@@ -331,7 +792,7 @@ __device__ __forceinline__ void group_bar(int id, int threads) {
 // the whole super-block at once, and a binade change (a new round) shifts the
 // thread's cached terms instead of decoding them again.  Synchronises the
 // group with named barrier `bar_id` (not 0).
-template <int W, int E>
+template <int W, int E, bool kPredict = true>
 __device__ __forceinline__ double group_fma_chain(const double* x, const double* w, uint32_t n, double acc,
                                                   uint32_t w0, int bar_id, ChainScratch& sc) {
     using namespace chain_detail;
@@ -358,6 +819,42 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
         for (uint32_t i = 0; i < E; ++i) {
             const uint32_t s = my0 + i;
             tp[i] = (s >= k0 && s < len) ? pack(term(x[base + s], w[base + s], ea, neg)) : 0ull;
+        }
+        if (kPredict && neg == 0) {
+            // one pass over every binade of a positive run
+            double a2;
+            const uint32_t done = group_predicted_pass<W, E>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc);
+            if (done > k0) {
+                acc = a2;
+                k0 = done;
+                if (k0 >= len) continue;
+                while (k0 < len && !state_ok(acc)) {
+                    acc = fma(x[base + k0], w[base + k0], acc);
+                    ++k0;
+                }
+                if (k0 >= len) continue;
+                uint32_t neg2;
+                uint64_t A2;
+                int ea2;
+                state_split(acc, neg2, A2, ea2);
+                const bool shift = neg2 == neg && ea2 >= ea;
+#pragma unroll
+                for (uint32_t i = 0; i < E; ++i) {
+                    const uint32_t s = my0 + i;
+                    Term t = unpack(tp[i]);
+                    if (s < k0 || s >= len) {
+                        tp[i] = 0ull;
+                    } else if (shift && !(t.flags & kBad)) {
+                        shift_term(t, ea2 - ea);
+                        tp[i] = pack(t);
+                    } else {
+                        tp[i] = pack(term(x[base + s], w[base + s], ea2, neg2));
+                    }
+                }
+                neg = neg2;
+                A0 = A2;
+                ea = ea2;
+            }
         }
         for (;;) {
             // --- parity maps: par' = (a & par) ^ b; steps before k0 are identity

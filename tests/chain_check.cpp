@@ -26,7 +26,7 @@ int main(int argc, char** argv) {
     std::uniform_real_distribution<double> U(0.0, 1.0);
     uint64_t plain_total = 0, steps_total = 0;
     for (int c = 0; c < cases; ++c) {
-        const int kind = c % 8;
+        const int kind = c % 9;
         const uint64_t n = 1 + rng() % (kind == 0 ? 8192 : 1200);
         std::vector<double> x(n), w(n);
         for (uint64_t k = 0; k < n; ++k) {
@@ -63,6 +63,10 @@ int main(int argc, char** argv) {
                     a = (double)(rng() % 5);
                     b = rng() % 2 ? 0.5 : 1.5;
                     break;
+                case 8:  // positive, few significant bits: ties inside predicted binades
+                    a = std::ldexp((double)(rng() % 64 + 1), (int)(rng() % 8) - 4);
+                    b = std::ldexp((double)(rng() % 16 + 1), (int)(rng() % 6) - 3);
+                    break;
                 default:  // generic random doubles of random sign and scale
                     a = (U(rng) - 0.5) * std::ldexp(1.0, (int)(rng() % 60) - 30);
                     b = (U(rng) - 0.25) * std::ldexp(1.0, (int)(rng() % 60) - 30);
@@ -75,7 +79,7 @@ int main(int argc, char** argv) {
         if (kind == 5 && rng() % 2) start = -std::ldexp(1.0, (int)(rng() % 10));
         double ref = start;
         for (uint64_t k = 0; k < n; ++k) ref = std::fma(x[k], w[k], ref);
-        for (uint64_t sb : {2048ull, 61ull}) {
+        for (uint64_t sb : {2048ull, 61ull, 4096ull}) {
             const double got = deac::host_group_fma_chain(x.data(), w.data(), n, start, sb);
             if (bits(got) != bits(ref) && !(std::isnan(got) && std::isnan(ref))) {
                 std::printf("group mismatch case %d kind %d n %llu sb %llu: %.17g vs %.17g\n", c, kind,

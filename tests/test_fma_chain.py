@@ -53,6 +53,9 @@ def _chains(kind, n, count, rng):
             a = rng.integers(0, 5, n).astype(float)
             b = np.where(rng.random(n) < 0.5, 0.5, 1.5)
             start[c] = 2.0 ** 53 - float(rng.integers(0, 64))
+        elif kind == 8:  # positive, few significant bits: ties inside predicted binades
+            a = np.ldexp(rng.integers(1, 65, n).astype(float), rng.integers(-4, 4, n))
+            b = np.ldexp(rng.integers(1, 17, n).astype(float), rng.integers(-3, 3, n))
         else:  # random sign and scale
             a = (u - 0.5) * np.ldexp(1.0, rng.integers(-30, 30, n))
             b = (v - 0.25) * np.ldexp(1.0, rng.integers(-30, 30, n))
@@ -69,7 +72,7 @@ def test_warp_chain_matches_sequential_fma(engine, n):
     fn.restype = ctypes.c_int
     fn.argtypes = [dp, dp, ctypes.c_uint64, dp, ctypes.c_uint32, dp, dp]
     rng = np.random.default_rng(n)
-    for kind in range(8):
+    for kind in range(9):
         x, w, start = _chains(kind, n, 48, rng)
         fast = np.zeros(len(start))
         plain = np.zeros(len(start))
