@@ -353,10 +353,12 @@ def engine_arm(args, world, rank, local):
     split.enable_timing(False)
     split.close()
     # CTAs of the split contraction: one tile (64 rows x 128 timeslices) whose
-    # M/32 chunks are spread over about one CTA per SM
+    # M/32 chunks are spread over the SMs the normalisation row sums (one CTA
+    # per trial, beside it) leave free
     chunks = M // 32
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    per = -(-chunks // min(max(1, sms), chunks))
+    free = sms - min(RUNS_PER_GPU * P, sms // 2)
+    per = -(-chunks // min(max(1, free), chunks))
     split_ctas = -(-chunks // per)
     per_gen_us = {k: ms_k / G * 1e3 for k, (ms_k, n) in kt.items() if n}
     dominant = max(per_gen_us, key=per_gen_us.get)
@@ -367,8 +369,8 @@ def engine_arm(args, world, rank, local):
                                              "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
     tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
-    names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "digitize_kernel",
-             3: "split_contract_kernel", 4: "split_combine_kernel+split_decide_kernel"}
+    names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
+             3: "split_contract_kernel", 4: "split_combine_kernel+split_decide_kernel+scale_kernel"}
     roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs

@@ -447,20 +447,21 @@ inline double host_group_fma_chain(const double* x, const double* w, uint64_t n,
 #ifdef __CUDACC__
 // Scratch of one warp group running group_fma_chain (shared memory).
 constexpr uint32_t kMaxCross = 64;  // binade crossings one predicted pass handles
+constexpr uint32_t kChainMaxWarps = 16;
 struct ChainScratch {
-    uint32_t map_a[8], map_b[8];  // per-warp parity maps
-    long long sum[8];             // per-warp integer sums
-    uint32_t bad[8];              // per-warp first invalid step
+    uint32_t map_a[kChainMaxWarps], map_b[kChainMaxWarps];  // per-warp parity maps
+    long long sum[kChainMaxWarps];                          // per-warp integer sums
+    uint32_t bad[kChainMaxWarps];                           // per-warp first invalid step
     unsigned long long a_bad;     // running integer at the first invalid step
     // predicted pass
-    uint32_t cnt[8];              // per-warp crossing counts
-    long long sum1[8];            // per-warp sums for the other start parity
-    uint32_t flag[8];             // per-warp "not a positive run"
+    uint32_t cnt[kChainMaxWarps];   // per-warp crossing counts
+    long long sum1[kChainMaxWarps]; // per-warp sums for the other start parity
+    uint32_t flag[kChainMaxWarps];  // per-warp "not a positive run"
     uint32_t cpos[kMaxCross];     // position of each crossing step
     int32_t cbin[kMaxCross];      // binade (relative) after it
     long long segq[2][kMaxCross + 1];          // per segment and start parity: its integer sum
     unsigned long long astart[kMaxCross + 1];  // state of each segment's first step
-    uint8_t first_cross[256];     // per thread: its first step is a crossing
+    uint8_t first_cross[kChainMaxWarps * 32];  // per thread: its first step is a crossing
     unsigned long long fail_state;
     uint32_t fail_pos;
     int32_t fail_bin;
@@ -562,12 +563,14 @@ __device__ __forceinline__ int rel_binade(uint64_t v) {
 // ones before k0 and from len on are zero).  Returns the position reached
 // and the state there in acc (uniform over the group).
 template <int W, int E>
-__device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const double* w, const uint64_t (&tp)[E],
+__device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const double* w, uint64_t (&tp)[E],
                                                           uint32_t k0, uint32_t len, uint64_t A0, int ea,
-                                                          double& acc, uint32_t tg, int bar_id, ChainScratch& sc) {
+                                                          double& acc, uint32_t tg, int bar_id, ChainScratch& sc,
+                                                          bool& rewritten) {
     using namespace chain_detail;
+    rewritten = false;
     constexpr uint32_t NT = W * 32;
-    static_assert(NT <= sizeof(ChainScratch::first_cross) && W <= 8, "group larger than its scratch");
+    static_assert(W <= (int)kChainMaxWarps, "group larger than its scratch");
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     const uint32_t lane = tg & 31u, wg = tg >> 5, my0 = tg * E;
     // --- prefix of the integer parts; is the run all positive and moderate?
@@ -605,7 +608,11 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
 
     // --- crossings (a step whose exact sum lies in a higher binade than its
     // state) and the parity maps of the segments between them
+    // From here on tp[i] holds the step's term in the grid of its predicted
+    // binade (a crossing step keeps its binade after the crossing in cbin_of)
+    rewritten = true;
     uint32_t cross_bits = 0;
+    int cbin_of[E];
     SegMap magg{0u, 1u, 0u};
     {
         uint64_t prefix = pstart;
@@ -617,13 +624,16 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
             const int ds = rel_binade(prefix), dk = rel_binade(T);
             const bool cr = s >= k0 && s < len && dk > ds;
             cross_bits |= (cr ? 1u : 0u) << i;
+            cbin_of[i] = dk;
+            prefix += t.F;
             if (cr) {
                 magg = seg_combine(magg, SegMap{1u, 1u, 0u});
+                tp[i] = 0ull;
             } else {
                 shift_term(t, ds);
+                tp[i] = pack(t);
                 magg = seg_combine(magg, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
             }
-            prefix += unpack(tp[i]).F;
         }
     }
     sc.first_cross[tg] = (uint8_t)(cross_bits & 1u);
@@ -649,18 +659,14 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     };
     SegSum sagg{0u, 0, 0};
     {
-        uint64_t prefix = pstart;
         SegMap run = mex;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
-            Term t = unpack(tp[i]);
-            const int ds = rel_binade(prefix);
-            prefix += t.F;
+            const Term t = unpack(tp[i]);
             if ((cross_bits >> i) & 1u) {
                 sagg = seg_combine(sagg, SegSum{1u, 0, 0});
                 run = seg_combine(run, SegMap{1u, 1u, 0u});
             } else {
-                shift_term(t, ds);
                 long long q0, q1;
                 steps(t, run, q0, q1);
                 sagg = seg_combine(sagg, SegSum{0u, q0, q1});
@@ -671,24 +677,19 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     const SegSum sex = group_scan<W>(sagg, lane, wg, bar_id, sc);
     // crossing positions and binades; each segment's sums at its last step
     {
-        uint64_t prefix = pstart;
         SegMap runm = mex;
         SegSum runs = sex;
         const bool next_thread_cross = tg + 1 < NT ? sc.first_cross[tg + 1] != 0 : false;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
-            Term t = unpack(tp[i]);
+            const Term t = unpack(tp[i]);
             const uint32_t s = my0 + i;
-            const uint64_t T = prefix + t.F + ((t.flags & kGtZero) ? 1u : 0u);
-            const int ds = rel_binade(prefix), dk = rel_binade(T);
-            prefix += t.F;
             if ((cross_bits >> i) & 1u) {
                 runs = seg_combine(runs, SegSum{1u, 0, 0});
                 runm = seg_combine(runm, SegMap{1u, 1u, 0u});
                 sc.cpos[runs.c - 1] = s;
-                sc.cbin[runs.c - 1] = dk;
+                sc.cbin[runs.c - 1] = cbin_of[i];
             } else {
-                shift_term(t, ds);
                 long long q0, q1;
                 steps(t, runm, q0, q1);
                 runs = seg_combine(runs, SegSum{0u, q0, q1});
@@ -736,21 +737,17 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     uint64_t bad_state = 0;
     int bad_bin = 0;
     {
-        uint64_t prefix = pstart;
         SegMap runm = mex;
         SegSum runs = sex;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
-            Term t = unpack(tp[i]);
+            const Term t = unpack(tp[i]);
             const uint32_t s = my0 + i;
-            const int ds = rel_binade(prefix);
-            prefix += t.F;
             if ((cross_bits >> i) & 1u) {
                 runs = seg_combine(runs, SegSum{1u, 0, 0});
                 runm = seg_combine(runm, SegMap{1u, 1u, 0u});
                 continue;
             }
-            shift_term(t, ds);
             if (first_bad == kNone && s >= k0 && s < len && s < fail) {
                 const uint64_t As = sc.astart[runs.c];
                 const uint64_t A = As + (uint64_t)((As & 1u) ? runs.s1 : runs.s0);
@@ -794,7 +791,8 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
 // group with named barrier `bar_id` (not 0).
 template <int W, int E, bool kPredict = true>
 __device__ __forceinline__ double group_fma_chain(const double* x, const double* w, uint32_t n, double acc,
-                                                  uint32_t w0, int bar_id, ChainScratch& sc) {
+                                                  uint32_t w0, int bar_id, ChainScratch& sc,
+                                                  uint32_t early_steps = 32) {
     using namespace chain_detail;
     constexpr uint32_t NT = W * 32, SB = NT * E;
     constexpr uint32_t kNone = 0xFFFFFFFFu;
@@ -803,7 +801,7 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
         const uint32_t len = n - base < SB ? n - base : SB;
         uint32_t k0 = 0;
         // the first steps change binade every few steps: run them plainly
-        const uint32_t early = base == 0 ? (len < 32u ? len : 32u) : 0u;
+        const uint32_t early = base == 0 ? (len < early_steps ? len : early_steps) : 0u;
         while (k0 < early || (k0 < len && !state_ok(acc))) {
             acc = fma(x[base + k0], w[base + k0], acc);
             ++k0;
@@ -823,8 +821,10 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
         if (kPredict && neg == 0) {
             // one pass over every binade of a positive run
             double a2;
-            const uint32_t done = group_predicted_pass<W, E>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc);
-            if (done > k0) {
+            bool rewritten;
+            const uint32_t done =
+                group_predicted_pass<W, E>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc, rewritten);
+            if (done > k0 || rewritten) {
                 acc = a2;
                 k0 = done;
                 if (k0 >= len) continue;
@@ -837,19 +837,11 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
                 uint64_t A2;
                 int ea2;
                 state_split(acc, neg2, A2, ea2);
-                const bool shift = neg2 == neg && ea2 >= ea;
+                // the pass left terms of several grids: decode the rest again
 #pragma unroll
                 for (uint32_t i = 0; i < E; ++i) {
                     const uint32_t s = my0 + i;
-                    Term t = unpack(tp[i]);
-                    if (s < k0 || s >= len) {
-                        tp[i] = 0ull;
-                    } else if (shift && !(t.flags & kBad)) {
-                        shift_term(t, ea2 - ea);
-                        tp[i] = pack(t);
-                    } else {
-                        tp[i] = pack(term(x[base + s], w[base + s], ea2, neg2));
-                    }
+                    tp[i] = (s >= k0 && s < len) ? pack(term(x[base + s], w[base + s], ea2, neg2)) : 0ull;
                 }
                 neg = neg2;
                 A0 = A2;

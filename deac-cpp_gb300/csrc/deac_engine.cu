@@ -135,9 +135,16 @@ struct deac_batch {
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
-    // passes), 2 unused, 3 split contraction, 4 combine + decisions
+    // passes), 2 normalisation row sums, 3 split contraction, 4 combine + decisions (+ scaling)
     bool timing = false;
     cudaEvent_t ev[8] = {};
+    // split engine, --normalize runs: the normalisation row sums run on a
+    // second stream beside the tensor-core contraction (forked and joined
+    // with events, also inside the captured graphs)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    deac::Work* d_norm_work = nullptr;
+    uint32_t n_norm_ctas = 0;
     double kernel_ms[5] = {};
     uint64_t kernel_launches[5] = {};
 };
@@ -175,12 +182,30 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
         return mark(1);
     }
+    // the normalisation row sums of --normalize runs: forked beside the
+    // tensor-core contraction (in line when timing kernels one by one)
+    const bool fork = b->n_norm_ctas && !timed;
+    if (b->n_norm_ctas) {
+        cudaStream_t ns = s;
+        if (fork) {
+            CUDA_TRY(cudaEventRecord(b->ev_fork, s));
+            CUDA_TRY(cudaStreamWaitEvent(b->side_stream, b->ev_fork, 0));
+            ns = b->side_stream;
+        }
+        deac::norm_kernel<<<b->n_norm_ctas, deac::kNormThreads, deac::kNormSmemBytes, ns>>>(b->d_runs,
+                                                                                         b->d_norm_work);
+        if (fork) CUDA_TRY(cudaEventRecord(b->ev_join, b->side_stream));
+        if ((rc = mark(2))) return rc;
+    }
     deac::split_contract_kernel<<<b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
         b->d_runs, b->d_split, b->d_tiles, b->d_split_work, b->d_rows, b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
     deac::split_combine_kernel<<<b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s>>>(
         b->d_runs, b->d_split, b->d_tiles, b->d_rows, b->d_partial);
+    if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     deac::split_decide_kernel<<<(uint32_t)b->runs.size(), deac::kDecideThreads, 0, s>>>(b->d_runs, b->d_split);
+    if (b->n_norm_ctas)
+        deac::scale_kernel<<<b->n_trial_ctas, 512, 0, s>>>(b->d_runs, b->d_trial_work);
     if ((rc = mark(4))) return rc;
     launch_contract(b, s, deac::kModeParents);
     launch_contract(b, s, deac::kModeTrials);
@@ -397,6 +422,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
         const uint64_t o_cnt = sa.take(3 * 8);
+        const uint64_t o_rcp = sa.take(P * 8), o_nb = sa.take(P), o_ie = sa.take(Nt * 8);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
@@ -416,6 +442,12 @@ int upload_run(deac_batch* b, RunHost& r) {
         x.t_lo = reinterpret_cast<double*>(sb + o_tl);
         x.t_hi = reinterpret_cast<double*>(sb + o_th);
         x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
+        {
+            std::vector<double> ie(Nt);
+            for (uint64_t t = 0; t < Nt; ++t) ie[t] = 1.0 / r.err[t];
+            CUDA_TRY(cudaMemcpy(sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
+            x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
+        }
         d.changed = x.changed;
         d.xdig = x.xdig;
         d.xexp = x.xexp;
@@ -423,6 +455,10 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.recheck = x.recheck;
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;
+        d.recip = reinterpret_cast<double*>(sb + o_rcp);
+        d.norm_buf = reinterpret_cast<uint8_t*>(sb + o_nb);
+        // with --normalize the trials stay raw until the decisions
+        if (r.cfg.normalize) d.flags |= deac::kDeferNorm;
     }
     // host copies are no longer needed
     std::vector<uint64_t>().swap(r.rng_table);
@@ -508,6 +544,9 @@ int deac_batch_create(int device, void* cuda_stream, int32_t engine, deac_batch*
         b->own_stream = true;
     }
     CUDA_TRY(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
     for (auto& e : b->ev) CUDA_TRY(cudaEventCreate(&e));
     *out = b.release();
     return DEAC_OK;
@@ -597,6 +636,22 @@ int deac_batch_setup(deac_batch* b) {
                                   (int)b->contract_smem_bytes));
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        // one CTA per trial of every --normalize run
+        std::vector<deac::Work> nw;
+        for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+            const RunHost& r = *b->runs[ri];
+            if (!(r.dev.flags & deac::kDeferNorm)) continue;
+            for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
+        }
+        b->n_norm_ctas = (uint32_t)nw.size();
+        if (!nw.empty()) {
+            CUDA_TRY(cudaFuncSetAttribute(deac::norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)deac::kNormSmemBytes));
+            CUDA_TRY(cudaMalloc(&b->d_norm_work, nw.size() * sizeof(deac::Work)));
+            CUDA_TRY(cudaMemcpy(b->d_norm_work, nw.data(), nw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+        }
+    }
     CUDA_TRY(cudaMalloc(&b->d_trial_work, tw.size() * sizeof(deac::Work)));
     CUDA_TRY(cudaMalloc(&b->d_contract_work, cw.size() * sizeof(deac::Work)));
     CUDA_TRY(cudaMemcpy(b->d_trial_work, tw.data(), tw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
@@ -640,7 +695,13 @@ int deac_batch_setup(deac_batch* b) {
         // memory and all of TMEM)
         int sms = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-        const uint64_t want = std::max<uint64_t>(1, (uint64_t)sms / tiles.size());
+        // the normalisation row sums of --normalize runs run beside this
+        // kernel: leave them their SMs (up to half)
+        uint64_t norm_ctas = 0;
+        for (auto& r : b->runs)
+            if (r->cfg.normalize) norm_ctas += r->P;
+        const uint64_t free_sms = (uint64_t)sms - std::min<uint64_t>(norm_ctas, (uint64_t)sms / 2);
+        const uint64_t want = std::max<uint64_t>(1, free_sms / tiles.size());
         std::vector<deac::SplitWork> work;
         uint32_t blocks = 0;
         for (uint32_t t = 0; t < tiles.size(); ++t) {
@@ -922,6 +983,10 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_contract_work);
     for (auto& e : b->ev)
         if (e) cudaEventDestroy(e);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    cudaFree(b->d_norm_work);
+    if (b->side_stream) cudaStreamDestroy(b->side_stream);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;

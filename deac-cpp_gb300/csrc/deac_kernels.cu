@@ -311,7 +311,9 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         __syncthreads();
     }
 
-    if (normalize) {
+    // split engine, kDeferNorm: the trial stays raw here (norm_kernel and
+    // scale_kernel normalise it after the decisions)
+    if (normalize && (init_mode || !(R.flags & kDeferNorm))) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
         if (chain_warp) {
@@ -348,13 +350,107 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         __syncthreads();
     }
 
-    // split engine: flag the trial and slice a changed one into BF16 digits
-    // for the tensor-core contraction
+    // split engine: flag the trial (norm_kernel completes the flag of a
+    // kDeferNorm run) and slice it into BF16 digits for the tensor cores
     if (!init_mode && R.changed) {
         if (threadIdx.x == 0) R.changed[i] = trial_changed ? 1 : 0;
-        if (trial_changed)
-            digitize_trial(in_smem ? trial_s : dst, in_smem ? (uint64_t)M : PM, S, M, R.xdig + (uint64_t)i * M, PM,
-                           R.xexp + (uint64_t)i * (M / kChunk), R.xexp_max + i, s_digit_max);
+        digitize_trial(in_smem ? trial_s : dst, in_smem ? (uint64_t)M : PM, S, M, R.xdig + (uint64_t)i * M, PM,
+                       R.xexp + (uint64_t)i * (M / kChunk), R.xexp_max + i, s_digit_max);
+    }
+}
+
+// ---------------------------------------------------------------- norm
+// Split engine, kDeferNorm runs: one CTA per raw trial forms the exact
+// normalisation row sums (warps 0-7 the positive side, 8-15 the negative
+// side, staged kNormStage genes at a time in shared memory), then
+// norm = gemv_pair(...) and 1/norm exactly as trial_kernel does, and sets
+// the trial's `changed` flag (a mutated gene or a scale other than 1).
+__global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const Work* work) {
+    __shared__ ChainScratch s_chain[2];
+    __shared__ double s_sum[2];
+    extern __shared__ __align__(16) double norm_s[];  // per side: [kNormStage] genes, [kNormStage] weights
+    const Work wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    if (R.done) return;
+    const uint32_t i = wk.index;
+    const uint32_t P = R.P, M = R.M, S = R.S;
+    const uint64_t PM = (uint64_t)P * M;
+    const uint32_t buf = 1u - R.cur[i];
+    const uint32_t side = (threadIdx.x >> 5) / kChainWarps;
+    const double* x = R.pop + ((uint64_t)buf * S + side) * PM + (uint64_t)i * M;
+    const double* wts = side == 0 ? R.norm_pos : R.norm_neg;
+    double* s_x = norm_s + (uint64_t)side * 2 * kNormStage;
+    double* s_w = s_x + kNormStage;
+    const uint32_t tg = threadIdx.x - side * kChainWarps * 32;
+    double sum = 0.0;
+    for (uint32_t k0 = 0; k0 < M; k0 += kNormStage) {
+        const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
+        __syncthreads();
+        if (side < S) {
+            // all of this thread's loads in flight at once
+            constexpr uint32_t U = kNormStage / (kChainWarps * 32);
+            double vx[U], vw[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t k = tg + u * kChainWarps * 32;
+                vx[u] = k < len ? x[k0 + k] : 0.0;
+                vw[u] = k < len ? wts[k0 + k] : 0.0;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t k = tg + u * kChainWarps * 32;
+                if (k < len) {
+                    s_x[k] = vx[u];
+                    s_w[k] = vw[u];
+                }
+            }
+        }
+        __syncthreads();
+        if (side < S)
+            sum = group_fma_chain<kChainWarps, kChainSteps>(s_x, s_w, len, sum, side * kChainWarps, 1 + (int)side,
+                                                            s_chain[side], k0 == 0 ? 32u : 0u);
+    }
+    if (tg == 0 && side < S) s_sum[side] = sum;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
+    const double recip = 1.0 / norm;
+    R.recip[i] = recip;
+    if (recip != 1.0) R.changed[i] = 1;
+}
+
+// ---------------------------------------------------------------- scale
+// Split engine, kDeferNorm runs: normalise the trials whose genes the
+// generation keeps (accepted) or still needs (the exact passes): every gene
+// times 1/norm, as trial_kernel does.  One CTA per trial.
+__global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* work) {
+    const Work wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    if (!(R.flags & kDeferNorm)) return;
+    const uint32_t i = wk.index;
+    const uint32_t b = R.norm_buf[i];
+    if (b == 0xFFu) return;
+    const uint32_t M = R.M, S = R.S;
+    const uint64_t PM = (uint64_t)R.P * M;
+    const double recip = R.recip[i];
+    // eight genes in flight per thread
+    constexpr uint32_t U = 8;
+    for (uint64_t q0 = threadIdx.x; q0 < (uint64_t)S * M; q0 += (uint64_t)U * blockDim.x) {
+        double* g[U];
+        double v[U];
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u) {
+            const uint64_t q = q0 + (uint64_t)u * blockDim.x;
+            g[u] = nullptr;
+            if (q < (uint64_t)S * M) {
+                const uint32_t s = (uint32_t)(q / M);
+                g[u] = R.pop + ((uint64_t)b * S + s) * PM + (uint64_t)i * M + (q - (uint64_t)s * M);
+                v[u] = *g[u];
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < U; ++u)
+            if (g[u]) *g[u] = v[u] * recip;
     }
 }
 

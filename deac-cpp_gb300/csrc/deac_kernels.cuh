@@ -42,6 +42,7 @@ enum : uint32_t {
     kSignedWeights = 1u << 4,
     kTrackStats = 1u << 5,
     kTrace = 1u << 6,
+    kDeferNorm = 1u << 7,  // split engine: normalisation applied after the decisions
 };
 
 // Per-run descriptor, resident in device memory.
@@ -87,9 +88,13 @@ struct RunDev {
     const uint8_t* recheck;  // [P] decision left to the exact FP64 value
     double* f_lo;            // [P] interval holding the parent's exact fitness
     double* f_hi;
-    uint16_t* xdig;          // [6][S][P][M] digit planes of the changed trials
+    uint16_t* xdig;          // [6][S][P][M] digit planes of the trials
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int16_t* xexp_max;       // [P]
+    // split engine with --normalize (kDeferNorm): the trials stay raw until
+    // the decisions; norm_kernel forms each trial's exact reciprocal norm
+    double* recip;           // [P] 1/norm of each trial
+    uint8_t* norm_buf;       // [P] buffer of a trial to normalise now, 0xFF none
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
@@ -158,6 +163,15 @@ enum ContractMode : int {
 };
 
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
+// split engine, kDeferNorm runs: the exact normalisation row sums of one raw
+// trial per CTA (both sides), the reciprocal norm and the final `changed`
+// flag; and the normalisation of the trials the decisions keep (one CTA per
+// trial)
+constexpr int kNormThreads = 2 * kChainWarps * 32;
+constexpr uint32_t kNormStage = kChainWarps * 32 * kChainSteps;  // steps staged in shared memory at a time
+constexpr uint32_t kNormSmemBytes = 2 * 2 * kNormStage * sizeof(double);  // dynamic shared memory of norm_kernel
+__global__ void norm_kernel(RunDev* runs, const Work* work);
+__global__ void scale_kernel(RunDev* runs, const Work* work);
 __global__ void contract_kernel(RunDev* runs, const Work* work, int mode);
 
 }  // namespace deac

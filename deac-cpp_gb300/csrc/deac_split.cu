@@ -156,8 +156,10 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     if (tid == 0) s_live = *reinterpret_cast<volatile int*>(status) != 0 ? -1 : 0;
     __syncthreads();
     if (s_live == 0 && tid < tile.rows) {
+        // every trial of a running run is sliced (whether it changed is known
+        // only after the normalisation of kDeferNorm runs)
         const SplitRow rw = rows[tile.first_row + tid];
-        if (!runs[rw.run].done && split[rw.run].changed[rw.member]) atomicOr(&s_live, 1);
+        if (!runs[rw.run].done) atomicOr(&s_live, 1);
     }
     __syncthreads();
     if (s_live <= 0) return;
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     const RunDev& R = runs[rw.run];
     SplitRun& X = split[rw.run];
     const uint32_t t = tile.tau0 + tl;
-    if (R.done || t >= R.Nt || !X.changed[rw.member]) return;
+    if (R.done || t >= R.Nt) return;
     const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
     const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
     // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
@@ -426,7 +428,6 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
 // are flagged for the exact FP64 evaluation (contract_kernel, recheck mode).
 __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* runs, SplitRun* split) {
     __shared__ unsigned long long s_n[3];
-    __shared__ double s_inv_err[kDecideMaxTau];
     RunDev& R = runs[blockIdx.x];
     if (R.done) return;
     SplitRun& X = split[blockIdx.x];
@@ -434,16 +435,16 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     const bool force_exact = (R.flags & kTrackStats) != 0;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
     if (threadIdx.x < 3) s_n[threadIdx.x] = 0;
-    // 1/sigma once per timeslice (a relative error of 2^-53, covered below)
-    const bool inv_ok = Nt <= kDecideMaxTau;
-    if (inv_ok)
-        for (uint32_t t = threadIdx.x; t < Nt; t += blockDim.x) s_inv_err[t] = 1.0 / R.err[t];
+    // 1/sigma of each timeslice, formed once per run (a relative error of
+    // 2^-53, covered below)
+    const double* inv_err = X.inv_err;
     __syncthreads();
     for (uint32_t i = warp; i < P; i += nw) {
         const bool changed = X.changed[i] != 0;
         if (!changed) {
             if (lane == 0) {
                 // the trial is the parent: the same fitness, and ties accept
+                if (R.flags & kDeferNorm) R.norm_buf[i] = 0xFFu;
                 X.recheck[i] = 0;
                 X.t_lo[i] = X.f_lo[i];
                 X.t_hi[i] = X.f_hi[i];
@@ -460,27 +461,60 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
         // chi^2 of the estimate and a bound on its distance from the value
         // the FP64 engine computes (any summation order: the rounding term
         // covers n-term sums)
-        double chi = 0.0, dchi = 0.0;
-        for (uint32_t t = lane; t < Nt; t += 32) {
-            const uint64_t o = (uint64_t)i * Nt + t;
-            const double ie = inv_ok ? s_inv_err[t] : 1.0 / R.err[t];
-            // r and dr carry up to three roundings of 2^-53 each
-            const double r = (R.isf[t] - X.e_mp[o]) * ie;
-            const double dr = X.e_bound[o] * ie * (1.0 + 0x1.0p-50) + fabs(r) * 0x1.0p-51;
-            chi = fma(r, r, chi);
-            dchi += (2.0 * fabs(r) + dr) * dr;
+        // kDeferNorm: the estimate is of the raw trial; the kept trial is
+        // RN(gene / norm) per gene.  Scaled estimate and bound: the raw bound
+        // twice over (its FP64-chain term counts normalised genes, whose
+        // scale exponents can exceed the raw ones times 1/norm by a factor
+        // two), 0.001 of it more for the per-gene roundings (at most
+        // 2^-47 B while the raw bound is at least 2^-33 B), and 2^-51 |E|
+        // for the product's rounding.
+        const bool defer = (R.flags & kDeferNorm) != 0;
+        const double rc = defer ? R.recip[i] : 1.0;
+        // chi^2 in FP64; its error bound in FP32 rounded upward (every term
+        // is non-negative, so each rounding up keeps an upper bound)
+        double chi = 0.0;
+        float dchi = 0.0f;
+        constexpr uint32_t U = 4;  // timeslices per lane in flight
+        for (uint32_t t0 = lane; t0 < Nt; t0 += 32 * U) {
+            double em[U], eb0[U], f[U], ie[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t t = t0 + 32 * u;
+                const uint64_t o = (uint64_t)i * Nt + t;
+                const bool ok = t < Nt;
+                em[u] = ok ? X.e_mp[o] : 0.0;
+                eb0[u] = ok ? X.e_bound[o] : 0.0;
+                f[u] = ok ? R.isf[t] : 0.0;
+                ie[u] = ok ? inv_err[t] : 0.0;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const double e = defer ? em[u] * rc : em[u];
+                // r carries up to three roundings of 2^-53 each
+                const double r = (f[u] - e) * ie[u];
+                chi = fma(r, r, chi);
+                const float ar = __double2float_ru(fabs(r));
+                const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, __double2float_ru(eb0[u])),
+                                                             __double2float_ru(fabs(rc))),
+                                                   __fmul_ru(__double2float_ru(fabs(e)), 0x1.0p-51f))
+                                       : __double2float_ru(eb0[u]);
+                const float dr = __fadd_ru(__fmul_ru(__fmul_ru(eb, __double2float_ru(ie[u])), 1.0f + 0x1.0p-20f),
+                                           __fmul_ru(ar, 0x1.0p-51f));
+                dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
+            }
         }
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
-            dchi += __shfl_xor_sync(0xffffffffu, dchi, o);
+            dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
         }
         if (lane != 0) continue;
         X.recheck[i] = 0;
         chi /= (double)Nt;
-        dchi = dchi / (double)Nt * (1.0 + 0x1.0p-40) + chi * (double)(Nt + 8) * 0x1.0p-52;
-        const double lo = chi - dchi, hi = chi + dchi;
+        const double dchi_d = (double)dchi / (double)Nt * (1.0 + 0x1.0p-40) + chi * (double)(Nt + 8) * 0x1.0p-52;
+        const double lo = chi - dchi_d, hi = chi + dchi_d;
         X.t_lo[i] = lo;
         X.t_hi[i] = hi;
+        if (defer) R.norm_buf[i] = 0xFFu;
         if (lo > X.f_hi[i]) {  // certainly worse: reject
             atomicAdd(&s_n[1], 1ull);
             continue;
@@ -496,9 +530,11 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
                 R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
             }
             R.cur[i] = (uint8_t)(1u - R.cur[i]);
+            if (defer) R.norm_buf[i] = R.cur[i];  // the kept trial, now the parent
             atomicAdd(&s_n[1], 1ull);
             continue;
         }
+        if (defer) R.norm_buf[i] = (uint8_t)(1u - R.cur[i]);  // the exact passes read it
         X.recheck[i] = 1;  // settle with the exact FP64 value
         atomicAdd(&s_n[2], 1ull);
     }
@@ -509,21 +545,29 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     // and stop test); the fitness of an interval-accepted member lies above
     // the stop fitness, so its midpoint decides the stop test exactly.  Runs
     // that track statistics keep the exact pass, which forms them.
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
         const bool idle = s_n[2] == 0 && !(R.flags & kTrackStats);
-        R.exact_idle = idle ? 1 : 0;
+        if (lane == 0) R.exact_idle = idle ? 1 : 0;
         if (idle) {
             const uint64_t ii = R.ii + 1;
             if (ii + 2 <= R.N) {
+                // the minimum fitness, by a warp (the minimum of finite
+                // values does not depend on the order)
                 const volatile double* f = R.fit_old;
                 double mn = f[0];
-                for (uint32_t m = 1; m < P; ++m) mn = f[m] < mn ? f[m] : mn;
-                R.ii = ii;
-                if (mn <= R.stop) {
-                    R.generation = ii;
-                    R.done = 1;
+                for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double v = __shfl_xor_sync(0xffffffffu, mn, o);
+                    mn = v < mn ? v : mn;
                 }
-            } else {
+                if (lane == 0) {
+                    R.ii = ii;
+                    if (mn <= R.stop) {
+                        R.generation = ii;
+                        R.done = 1;
+                    }
+                }
+            } else if (lane == 0) {
                 R.ii = ii;
                 R.generation = R.N - 2;
                 R.done = 1;

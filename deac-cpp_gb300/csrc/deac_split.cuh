@@ -32,7 +32,6 @@ constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
 constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
 constexpr int kDecideThreads = 512;
-constexpr uint32_t kDecideMaxTau = 2048;  // timeslices whose 1/sigma is kept in shared memory
 // dynamic shared memory of split_contract_kernel for S sides: K digits
 // [6][S] x (128 x 32), trial digits [6][S] x (64 x 32), the two bound
 // operands (128 x 16, 64 x 16) and the double-float accumulators 64 x 128
@@ -59,6 +58,7 @@ struct SplitRun {
     double* t_hi;
     unsigned long long* counts;  // [3]: trials equal to the parent, settled by
                                  // the interval, settled by the exact FP64 value
+    const double* inv_err;  // [Nt] 1/sigma, rounded once
 };
 
 // One output tile: up to 64 (run, member) rows sharing one K, x 128

@@ -201,8 +201,9 @@ int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]);
 /* Device time of the kernels launched since timing was enabled, per kernel
  * kind, measured with CUDA events on the batch stream (ms): 0 trial kernel,
  * 1 contraction kernel (plain generation or the split engine's exact
- * passes), 2 unused (the trial kernel slices the split engine's digits),
- * 3 tensor-core contraction, 4 partial-sum combine and interval decisions.
+ * passes), 2 normalisation row sums of the split engine's --normalize
+ * runs, 3 tensor-core contraction, 4 partial-sum combine, interval decisions
+ * and the normalisation of the kept trials.
  * While timing is enabled, generations are launched one by one instead of
  * as CUDA graphs. */
 int deac_batch_enable_timing(deac_batch* b, int32_t enable);
