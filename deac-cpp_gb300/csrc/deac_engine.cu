@@ -82,6 +82,7 @@ struct KernelMatrix {
     double* k_pos = nullptr;
     double* k_neg = nullptr;
     uint16_t* kdig = nullptr;   // [kDigits][S][Nt][M]
+    bool nonneg = false;        // every entry >= 0
     int16_t* kexp = nullptr;    // [Nt][M/kChunk]
     int16_t* kexp_max = nullptr;  // [Nt]
     uint32_t group = 0;         // index of the runs sharing it (split tiles)
@@ -283,6 +284,10 @@ int upload_run(deac_batch* b, RunHost& r) {
             CUDA_TRY(cudaMalloc(&km.k_neg, Nt * M * sizeof(double)));
             CUDA_TRY(cudaMemcpy(km.k_neg, m.k_neg.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
         }
+        km.nonneg = true;
+        for (double v : m.k_pos) km.nonneg = km.nonneg && v >= 0.0;
+        if (S == 2)
+            for (double v : m.k_neg) km.nonneg = km.nonneg && v >= 0.0;
         if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
             // digit planes of K: one scale per (timeslice, 32-gene chunk)
             // shared by both sides, six 7-bit digits per value
@@ -457,8 +462,10 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.f_hi = x.f_hi;
         d.recip = reinterpret_cast<double*>(sb + o_rcp);
         d.norm_buf = reinterpret_cast<uint8_t*>(sb + o_nb);
+        CUDA_TRY(cudaMemset(d.norm_buf, 0xFF, P));  // no trial to normalise yet
         // with --normalize the trials stay raw until the decisions
         if (r.cfg.normalize) d.flags |= deac::kDeferNorm;
+        if (it->second.nonneg && !r.cfg.allow_negative_weight) d.flags |= deac::kNonNegProducts;
     }
     // host copies are no longer needed
     std::vector<uint64_t>().swap(r.rng_table);
@@ -710,6 +717,7 @@ int deac_batch_setup(deac_batch* b) {
             tiles[t].block0 = blocks;
             for (uint32_t c0 = 0; c0 < C; c0 += per) work.push_back({t, c0, std::min(C, c0 + per), blocks++});
             tiles[t].nsplit = blocks - tiles[t].block0;
+            tiles[t].per = per;
         }
         b->n_tiles = (uint32_t)tiles.size();
         b->n_split_ctas = (uint32_t)work.size();

@@ -424,11 +424,19 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // generation keeps (accepted) or still needs (the exact passes): every gene
 // times 1/norm, as trial_kernel does.  One CTA per trial.
 __global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* work) {
+    __shared__ uint32_t s_buf;
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
     if (!(R.flags & kDeferNorm)) return;
     const uint32_t i = wk.index;
-    const uint32_t b = R.norm_buf[i];
+    // the request is consumed: later launches (a finished run's included,
+    // whose decide_kernel no longer runs) find none
+    if (threadIdx.x == 0) {
+        s_buf = R.norm_buf[i];
+        R.norm_buf[i] = 0xFFu;
+    }
+    __syncthreads();
+    const uint32_t b = s_buf;
     if (b == 0xFFu) return;
     const uint32_t M = R.M, S = R.S;
     const uint64_t PM = (uint64_t)R.P * M;

@@ -43,6 +43,7 @@ enum : uint32_t {
     kTrackStats = 1u << 5,
     kTrace = 1u << 6,
     kDeferNorm = 1u << 7,  // split engine: normalisation applied after the decisions
+    kNonNegProducts = 1u << 8,  // every gene x kernel product is >= 0 (unsigned genes, K >= 0)
 };
 
 // Per-run descriptor, resident in device memory.

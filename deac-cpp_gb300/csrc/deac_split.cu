@@ -12,8 +12,8 @@ namespace deac {
 
 namespace {
 
-constexpr int kKept = kDigits;            // groups 0..5 kept
-constexpr uint32_t kTmemCols = 512;       // 6 groups x 64 rows + bound x 64 rows = 448 used
+constexpr int kKept = kDigits;            // digit-pair groups a+b = 0..6 kept
+constexpr uint32_t kTmemCols = 512;       // 7 groups x 64 rows + bound x 64 rows = 512
 constexpr uint32_t kBoundCol = kKept * kRowTile;
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier waits: 2 s
 constexpr int kStatusWait = 1;             // status: a tensor-core completion wait gave up
@@ -172,7 +172,6 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     uint8_t* sB = sA + kDigits * S * a_tile;
     uint8_t* sAb = sB + kDigits * S * b_tile;
     uint8_t* sBb = sAb + kTauTile * 16 * 2;
-    float2* acc = reinterpret_cast<float2*>(sBb + kRowTile * 16 * 2);  // [row][tau]
 
     // zero the rank-1 bound operands once (only k = 0 is written per chunk)
     for (uint32_t e = tid; e < (kTauTile + kRowTile) * 16; e += blockDim.x)
@@ -253,7 +252,10 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     const uint32_t quarter = warp & 3u, half = warp >> 2;
     const uint32_t tl = quarter * 32 + lane;  // timeslice within the tile
     const uint32_t r0 = half * 32;            // first of this thread's 32 rows
-    for (uint32_t r = 0; r < 32; ++r) acc[(r0 + r) * kTauTile + tl] = make_float2(0.0f, 0.0f);
+    // double-float accumulators of this thread's (timeslice, row) outputs
+    float acc_hi[32], acc_lo[32];
+#pragma unroll
+    for (uint32_t r = 0; r < 32; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
 
     stage(wk.c0);
     __syncthreads();  // s_kmax / s_xmax
@@ -298,9 +300,9 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         // the staging buffers are free again: load the next chunk meanwhile
         if (c + 1 < wk.c1) stage(c + 1);
 
-        // --- fold the six exact group sums of this chunk into the accumulators
+        // --- fold the seven exact group sums of this chunk into the accumulators
         const int ek = s_ek[tl];
-#pragma unroll 1
+#pragma unroll
         for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
             uint32_t d[kKept][8];
 #pragma unroll
@@ -309,8 +311,8 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const uint32_t r = r0 + j8 + j;
-                // sum_g D_g 2^(7(5-g)) as a double-float: every term is exact
-                float sh = __uint_as_float(d[0][j]) * 0x1p35f, sl = 0.0f;
+                // sum_g D_g 2^(7(6-g)) as a double-float: every term is exact
+                float sh = __uint_as_float(d[0][j]) * exp2_int(7 * (kKept - 1)), sl = 0.0f;
 #pragma unroll
                 for (int g = 1; g < kKept; ++g) {
                     float e;
@@ -319,17 +321,15 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
                 }
                 float hi, lo;
                 fast_two_sum(sh, sl, hi, lo);
-                // weight of the lowest kept group: 2^(e_x + e_K - 49)
+                // weight of the lowest kept group: 2^(e_x + e_K - 56)
                 const int k = s_ex[r] + ek - 7 * (kKept + 1);
-                if (k > 60) {  // beyond any sane data: make the estimate unusable
+                if (k > 50) {  // beyond any sane data: make the estimate unusable
                     hi = __int_as_float(0x7fc00000);
                     lo = 0.0f;
                 } else {
                     scale_pow2(hi, lo, k);
                 }
-                float2 a = acc[r * kTauTile + tl];
-                dw_add(a.x, a.y, hi, lo);
-                acc[r * kTauTile + tl] = a;
+                dw_add(acc_hi[j8 + j], acc_lo[j8 + j], hi, lo);
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -347,14 +347,16 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     if (ok) {
         // partial sums and the bound accumulator sum_c 2^(e_x-max_x + e_K-max_K)
         float4* out = partial + (uint64_t)wk.block * kPartialBlock;
+#pragma unroll
         for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
             uint32_t d[8];
             tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+#pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const uint32_t r = r0 + j8 + j;
-                const float2 a = acc[r * kTauTile + tl];
-                out[(uint64_t)r * kTauTile + tl] = make_float4(a.x, a.y, __uint_as_float(d[j]), 0.0f);
+                out[(uint64_t)r * kTauTile + tl] =
+                    make_float4(acc_hi[j8 + j], acc_lo[j8 + j], __uint_as_float(d[j]), 0.0f);
             }
         }
     }
@@ -413,13 +415,30 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
     // below 2^-23 per addition), terms under 2^-126 dropped
     const double bsum = ldexp(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
-    // |estimate - FP64 chain| <= B * (digits 2^-33 + FP64 chain M 2^-47 +
-    // digit-group sums 2^-37 + double-float additions (C + nsplit + 10) 2^-40
-    // + final FP64 sum 2^-46), plus what underflowed in FP32
-    const double rel = 0x1p-33 + M * 0x1p-47 + 0x1p-37 + (C + ks + 10.0) * 0x1p-40 + 0x1p-46;
+    // Error of the estimate against the FP64 chain value, in parts:
+    //  digits: dropped digit pairs and remainders, 2^-45.9 2^(e_x+e_K) per
+    //    product, 64 products a chunk:                     2^-39 B
+    //  digit-group sums in FP32 (TwoSum cascade of seven exact terms):
+    //    30 u^2 times the chunk's |terms| <= 64 2^(e_x+e_K):  2^-37 B
+    //  double-float additions, 3 u^2 |partial| each, along the longest
+    //    path (a split's chunks, then the combine):  depth 3 u^2 |sum|
+    //  the FP64 chains themselves, 2^-53 per step of |partial sum|, and
+    //    the final FP64 sum.
+    // |sum| is at most 64 B in general; when every product is >= 0 the
+    // partial sums are at most the value itself, bounded by E' below.
+    const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
+    const double e = (double)hi + (double)lo;
+    const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
+    double eb;
+    if (R.flags & kNonNegProducts) {
+        const double Ep = (fabs(e) + bsum * gen * 1.01) * (1.0 + 0x1p-40);
+        eb = bsum * 0x1p-39 + Ep * ((M + 1.0) * 0x1p-53 + 0x1p-43 + depth * 3.0 * 0x1p-48 + 0x1p-51);
+    } else {
+        eb = bsum * (gen + M * 0x1p-47 + 0x1p-46);
+    }
     const uint64_t o = (uint64_t)rw.member * R.Nt + t;
-    X.e_mp[o] = (double)hi + (double)lo;
-    X.e_bound[o] = bsum * rel + (C + ks + 10.0) * 0x1p-140;
+    X.e_mp[o] = e;
+    X.e_bound[o] = eb * (1.0 + 0x1p-40) + (C + ks + 10.0) * 0x1p-140;
 }
 
 // ---------------------------------------------------------------- decide
@@ -588,7 +607,7 @@ void digits_of(double v, int e, uint16_t out[kDigits]) {
             uint64_t bits;
             std::memcpy(&bits, &m, 8);
             const uint64_t mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-            const int shift = 10 + e - ef;
+            const int shift = (52 - kDigitBits) + e - ef;
             f = shift >= 64 ? 0 : (mant >> shift);
         }
     }

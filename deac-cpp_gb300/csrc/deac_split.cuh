@@ -3,16 +3,16 @@
 //
 // E[i,t] = sum_k x[i,k] K[t,k] (both sides) is evaluated from exact BF16
 // digit slices:  every value v of a 32-gene chunk is written as
-//     v = sign * 2^e * sum_{b=0..5} d_b 2^(-7(b+1)) + r,   0 <= d_b <= 127,
+//     v = sign * 2^e * sum_{b=0..6} d_b 2^(-7(b+1)) + r,   0 <= d_b <= 127,
 // with one power-of-two scale 2^e per (row, chunk) shared by both sides
-// (|r| < 2^(e-42)).  Digit products d_a d'_b < 2^14 and a group of equal
-// weight (a+b = g, g <= 5) summed over 32 genes x 2 sides is < 2^23, so the
-// tensor core's FP32 accumulation of each group is exact.  Per chunk the six
-// group sums are combined into a double-float (FP32 pair) value, scaled by
-// 2^(e_x + e_K - 49) and added to double-float accumulators; CTAs split the
-// chunks of a tile and a combine kernel adds their partial sums.  What is
-// dropped -- remainders and digit pairs with a+b > 5 -- is below
-// 2^-39.2 * 2^(e_x+e_K) per product, and the bound's chunk sums
+// (|r| < 2^(e-49)).  Digit products d_a d'_b < 2^14 and a group of equal
+// weight (a+b = g, g <= 6) summed over 32 genes x 2 sides is < 2^23, so the
+// tensor core's FP32 accumulation of each group is exact.  Per chunk the
+// seven group sums are combined into a double-float (FP32 pair) value,
+// scaled by 2^(e_x + e_K - 56) and added to double-float accumulators; CTAs
+// split the chunks of a tile and a combine kernel adds their partial sums.
+// What is dropped -- remainders and digit pairs with a+b > 6 -- is below
+// 2^-45.9 * 2^(e_x+e_K) per product, and the bound's chunk sums
 // B = sum_c 2^(e_x+e_K) are accumulated by one extra rank-1 MMA per chunk.
 // With the rounding bounds of the double-float steps and of the FP64 chain
 // itself this gives an interval that contains the value the plain FP64
@@ -26,18 +26,19 @@
 
 namespace deac {
 
-constexpr int kDigits = 6;         // 7-bit digits per value (42 bits)
+constexpr int kDigits = 7;         // 7-bit digits per value (49 bits)
+constexpr int kDigitBits = 7 * kDigits;
 constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
 constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
 constexpr int kDecideThreads = 512;
 // dynamic shared memory of split_contract_kernel for S sides: K digits
-// [6][S] x (128 x 32), trial digits [6][S] x (64 x 32), the two bound
-// operands (128 x 16, 64 x 16) and the double-float accumulators 64 x 128
+// [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and the two bound
+// operands (128 x 16, 64 x 16)
 constexpr uint32_t split_smem_bytes(uint32_t S) {
     return (uint32_t)kDigits * S * (kTauTile * kChunk * 2) + (uint32_t)kDigits * S * (kRowTile * kChunk * 2) +
-           (kTauTile + kRowTile) * 16 * 2 + kRowTile * kTauTile * 8;
+           (kTauTile + kRowTile) * 16 * 2;
 }
 
 // Split-engine buffers of one run (device pointers).
@@ -71,6 +72,7 @@ struct SplitTile {
     uint32_t run0;       // a run of the tile (for the shared K pointers)
     uint32_t nsplit;
     uint32_t block0;
+    uint32_t per;        // chunks of its longest split
 };
 // One CTA of split_contract_kernel: chunks [c0, c1) of a tile.
 struct SplitWork {
@@ -97,13 +99,13 @@ __device__ __forceinline__ int exp_of(double v) {
     return ef == 0 ? -2000 : ef - 1023;
 }
 
-// fixed-point fraction floor(|v| * 2^(42-e)) for a scale 2^e > |v|
-__device__ __forceinline__ uint64_t frac42(double v, int e) {
+// fixed-point fraction floor(|v| * 2^(49-e)) for a scale 2^e > |v|
+__device__ __forceinline__ uint64_t frac_digits(double v, int e) {
     const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
     const int ef = (int)(b >> 52);
     if (ef == 0) return 0;  // zero or subnormal: below every scale used here
     const uint64_t mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int shift = 10 + e - (ef - 1023);
+    const int shift = (52 - kDigitBits) + e - (ef - 1023);
     return shift >= 64 ? 0 : (mant >> shift);
 }
 
@@ -137,7 +139,7 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_st
 #pragma unroll
         for (uint32_t s = 0; s < 2; ++s) {
             if (s >= S) break;
-            const uint64_t f = frac42(v[s], e);
+            const uint64_t f = frac_digits(v[s], e);
             const bool neg = v[s] < 0.0;
 #pragma unroll
             for (int b = 0; b < kDigits; ++b) {
