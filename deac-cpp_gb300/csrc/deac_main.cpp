@@ -10,6 +10,7 @@
 //   --bosonic                                    one-sided genome (bdsf)
 //   --allow_negative_spectral_weight             ALLOW_NEGATIVE_SPECTRAL_WEIGHT
 //   --device N                                   CUDA device
+//   --engine plain|split                         evaluation engine (same results)
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -69,6 +70,7 @@ const std::vector<Option>& options() {
         {"", "--bosonic", "One-sided genome with the bosonic detailed-balance kernel (spectra_type bdsf).", "false", true},
         {"", "--allow_negative_spectral_weight", "Do not take the absolute value of mutant genes.", "false", true},
         {"", "--device", "CUDA device to run on.", "0", false},
+        {"", "--engine", "Evaluation engine: plain (FP64 throughout) or split (tensor-core contraction with exact FP64 decisions; genome_size a multiple of 32, no moment terms).", "plain", false},
     };
     return o;
 }
@@ -326,6 +328,9 @@ int main(int argc, char** argv) {
     cfg.stop_minimum_fitness = get_double(args, "--stop_minimum_fitness", 1.0);
     cfg.track_stats = args.has("--track_stats") ? 1 : 0;
     const int device = (int)get_ulong(args, "--device", 0);
+    const std::string engine_name = args.has("--engine") ? args.values.at("--engine") : "plain";
+    if (engine_name != "plain" && engine_name != "split") fail_with_error("--engine must be plain or split");
+    const int32_t engine = engine_name == "split" ? DEAC_ENGINE_SPLIT_BF16 : DEAC_ENGINE_PLAIN_FP64;
 
     const fs::path save_directory(args.has("--save_directory") ? args.values.at("--save_directory") : "./deacresults");
     std::error_code ec;
@@ -352,7 +357,7 @@ int main(int argc, char** argv) {
     if (cfg.first_moment >= 0.0) std::cout << "WARNING: setting first_moment_error to 1.0." << std::endl;
 
     deac_batch* batch = nullptr;
-    int rc = deac_batch_create(device, nullptr, DEAC_ENGINE_PLAIN_FP64, &batch);
+    int rc = deac_batch_create(device, nullptr, engine, &batch);
     if (rc == DEAC_OK) rc = deac_batch_add_run(batch, &cfg, tau, isf, err, nt, frequency.data(), frequency.size(), nullptr);
     if (rc == DEAC_OK) rc = deac_batch_run(batch);
     deac_run_result res{};
