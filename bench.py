@@ -227,8 +227,8 @@ def reference_arm(args, world, rank):
 # Algorithmic work per launch of each kernel kind of the split engine
 # (deac_batch_kernel_time kinds), for the roofline of the dominant one.
 BYTES_PER_TRIAL_GENE = 4 * 8 + 2 * 32 + 2 * 8 + 8  # parent+3 donors, PRNG state in/out, gene out twice, weight
-BYTES_PER_DIGITIZED_GENE = 8 + 6 * 2                # gene in, six BF16 digits out
-KEPT_DIGIT_PAIRS = 21                               # digit pairs a+b <= 5 of six 7-bit digits
+BYTES_PER_NORM_GENE = 8 + 8                         # raw gene and its weight in
+KEPT_DIGIT_PAIRS = 28                               # digit pairs a+b <= 6 of seven 7-bit digits
 
 
 def kernel_roofline(kind, launch_s, peaks, split_ctas):
@@ -239,9 +239,10 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
         achieved = work / launch_s / 1e9
         name = "trial_kernel"
     elif kind == 2:
-        work, unit, bound, peak = genes * BYTES_PER_DIGITIZED_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
+        # exact normalisation row sums: each trial's raw genes and the weights
+        work, unit, bound, peak = genes * BYTES_PER_NORM_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "digitize_kernel"
+        name = "norm_kernel"
     elif kind == 3:
         work = 2.0 * rows * NT * M * S * KEPT_DIGIT_PAIRS
         unit, bound, peak = "TFLOP/s", "tensor", peaks["bf16_tflops"]
@@ -252,7 +253,7 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
         unit, bound, peak = "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
         name = "split_combine_kernel+split_decide_kernel"
-    else:
+    else:  # kind 1
         work = 2.0 * 2 * rows * NT * M  # FP64 FMA chains, were every trial re-evaluated
         unit, bound, peak = "TFLOP/s", "fp64", 1.196
         achieved = work / launch_s / 1e12
@@ -367,7 +368,7 @@ def engine_arm(args, world, rank, local):
     roof = kernel_roofline(dominant, ms_d / n_d / 1e3, peaks, split_ctas)
     roof["peak_source"] = peaks["source"] + (" burst figure" if roof["bound"] != "fp64" else
                                              "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
-    tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_traffic.json"
+    tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
     names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
              3: "split_contract_kernel", 4: "split_combine_kernel+split_decide_kernel+scale_kernel"}
