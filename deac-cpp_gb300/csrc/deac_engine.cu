@@ -176,8 +176,12 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     };
     if (timed) CUDA_TRY(cudaEventRecord(b->ev[0], s));
     int rc;
-    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
-                                                                                        init_mode, b->smem_doubles);
+    if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode)
+        deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
+            b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
+    else
+        deac::trial_raw_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
+            b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
@@ -638,6 +642,8 @@ int deac_batch_setup(deac_batch* b) {
     b->trial_smem_bytes = trial_doubles * sizeof(double);
     b->contract_smem_bytes = contract_bytes;
     CUDA_TRY(cudaFuncSetAttribute(deac::trial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
+    CUDA_TRY(cudaFuncSetAttribute(deac::trial_raw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
     CUDA_TRY(cudaFuncSetAttribute(deac::contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)b->contract_smem_bytes));

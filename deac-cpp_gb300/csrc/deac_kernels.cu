@@ -132,8 +132,8 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
 // the row sum being formed (normalisation, first or third moment), when the
 // batch's capacity `smem_doubles` allows; otherwise the chains read global
 // memory (still k-ascending).
-__global__ void __launch_bounds__(kTrialThreads)
-trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
+template <bool kRowSums>
+__device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     extern __shared__ __align__(16) double trial_s[];
     __shared__ double s_cr[2], s_fw[2], s_sum[4];
     __shared__ uint64_t s_thr[2];
@@ -157,7 +157,8 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     const uint64_t base = (uint64_t)i * (1ull + SM);
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const bool normalize = (R.flags & kNormalize) != 0;
+    // without row sums (the split engine's generations) the trial stays raw
+    const bool normalize = kRowSums && (R.flags & kNormalize) != 0;
 
     // weights of one row sum, staged next to the genes when they fit
     auto weights = [&](const double* wp, const double* wn, const double*& tp, const double*& tn) {
@@ -174,7 +175,8 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         }
     };
     const double *norm_p = nullptr, *norm_n = nullptr;
-    if (normalize) weights(R.norm_pos, R.norm_neg, norm_p, norm_n);
+    const bool row_sums_here = normalize && (init_mode || !(R.flags & kDeferNorm));
+    if (row_sums_here) weights(R.norm_pos, R.norm_neg, norm_p, norm_n);
 
     if (!init_mode && threadIdx.x == 0) {
         // jDE (deac_gpu.cu:584-606): CR(+) on slot 0, F(+) slot 1,
@@ -253,13 +255,15 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
             const uint32_t j0 = c * kGeneChunk;
             const uint32_t len = min(kGeneChunk, M - j0);
             const uint32_t items = S * len;
-            for (uint32_t e0 = wid; e0 < items; e0 += 2 * nt) {
-                uint64_t st[2][4];
-                double a[2], b[2], cc[2], x[2];
-                uint32_t sd[2], jj[2];
-                bool ok[2];
+            // items in flight per thread: more where no row-sum code takes registers
+            constexpr int H = kRowSums ? 2 : 3;
+            for (uint32_t e0 = wid; e0 < items; e0 += H * nt) {
+                uint64_t st[H][4];
+                double a[H], b[H], cc[H], x[H];
+                uint32_t sd[H], jj[H];
+                bool ok[H];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
+                for (int h = 0; h < H; ++h) {
                     const uint32_t e = e0 + (uint32_t)h * nt;
                     ok[h] = e < items;
                     const uint32_t ee = ok[h] ? e : e0;
@@ -277,7 +281,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
                     x[h] = px[off];
                 }
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
+                for (int h = 0; h < H; ++h) {
                     if (!ok[h]) continue;
                     const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
                     store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
@@ -313,7 +317,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 
     // split engine, kDeferNorm: the trial stays raw here (norm_kernel and
     // scale_kernel normalise it after the decisions)
-    if (normalize && (init_mode || !(R.flags & kDeferNorm))) {
+    if (row_sums_here) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
         if (chain_warp) {
@@ -335,7 +339,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     }
 
     // moment row sums with alpha = 1 (deac.cpp:1418-1477)
-    for (int which = 0; which < 2; ++which) {
+    for (int which = 0; which < (kRowSums ? 2 : 0); ++which) {
         const uint32_t flag = which == 0 ? kFirstMoment : kThirdMoment;
         if (!(R.flags & flag)) continue;
         const double *tp, *tn;
@@ -357,6 +361,15 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
         digitize_trial(in_smem ? trial_s : dst, in_smem ? (uint64_t)M : PM, S, M, R.xdig + (uint64_t)i * M, PM,
                        R.xexp + (uint64_t)i * (M / kChunk), R.xexp_max + i, s_digit_max);
     }
+}
+
+__global__ void __launch_bounds__(kTrialThreads)
+trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
+    trial_body<true>(runs, work, init_mode, smem_doubles);
+}
+__global__ void __launch_bounds__(kTrialThreads)
+trial_raw_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
+    trial_body<false>(runs, work, init_mode, smem_doubles);
 }
 
 // ---------------------------------------------------------------- norm

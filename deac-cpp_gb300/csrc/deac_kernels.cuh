@@ -163,7 +163,11 @@ enum ContractMode : int {
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
 };
 
+// trial_kernel forms the normalisation and moment row sums (the plain
+// engine, and every engine's initial population); trial_raw_kernel leaves the
+// trial raw (the split engine's generations)
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
+__global__ void trial_raw_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
 // split engine, kDeferNorm runs: the exact normalisation row sums of one raw
 // trial per CTA (both sides), the reciprocal norm and the final `changed`
 // flag; and the normalisation of the trials the decisions keep (one CTA per
