@@ -415,7 +415,9 @@ def engine_arm(args, world, rank, local):
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
-        "gpu_launches": 6 * G * args.steps,  # trial, tensor contraction, combine, decide, 2 exact passes
+        # per generation: jDE, trial parts, normalisation row sums, tensor
+        # contraction, combine, decide, scale, 2 exact passes
+        "gpu_launches": 9 * G * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

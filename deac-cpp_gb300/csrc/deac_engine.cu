@@ -146,6 +146,10 @@ struct deac_batch {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     deac::Work* d_norm_work = nullptr;
     uint32_t n_norm_ctas = 0;
+    // split engine: the raw trials in parts (trial_part_kernel)
+    deac::Work* d_part_work = nullptr;
+    uint32_t n_part_ctas = 0;
+    size_t part_smem_bytes = 0;
     double kernel_ms[5] = {};
     uint64_t kernel_launches[5] = {};
 };
@@ -176,12 +180,14 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     };
     if (timed) CUDA_TRY(cudaEventRecord(b->ev[0], s));
     int rc;
-    if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode)
+    if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
         deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
             b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
-    else
-        deac::trial_raw_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
-            b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
+    } else {
+        deac::jde_kernel<<<(b->n_trial_ctas + 127) / 128, 128, 0, s>>>(b->d_runs, b->d_trial_work, b->n_trial_ctas);
+        deac::trial_part_kernel<<<b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s>>>(b->d_runs,
+                                                                                               b->d_part_work);
+    }
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
@@ -426,7 +432,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t C = M / deac::kChunk;
         Arena sa;
         const uint64_t o_xd = sa.take((uint64_t)deac::kDigits * S * P * M * 2);
-        const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 2);
+        const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 4), o_mu = sa.take(P * 3 * 4);
         const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
@@ -438,7 +444,8 @@ int upload_run(deac_batch* b, RunHost& r) {
         deac::SplitRun& x = r.split;
         x.xdig = reinterpret_cast<uint16_t*>(sb + o_xd);
         x.xexp = reinterpret_cast<int16_t*>(sb + o_xe);
-        x.xexp_max = reinterpret_cast<int16_t*>(sb + o_xm);
+        x.xexp_max = reinterpret_cast<int32_t*>(sb + o_xm);
+        CUDA_TRY(cudaMemset(x.xexp_max, 0x80, P * 4));  // below every exponent: no trial sliced yet
         x.kdig = it->second.kdig;
         x.kexp = it->second.kexp;
         x.kexp_max = it->second.kexp_max;
@@ -461,6 +468,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.xdig = x.xdig;
         d.xexp = x.xexp;
         d.xexp_max = x.xexp_max;
+        d.mutants = reinterpret_cast<uint32_t*>(sb + o_mu);
         d.recheck = x.recheck;
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;
@@ -643,8 +651,7 @@ int deac_batch_setup(deac_batch* b) {
     b->contract_smem_bytes = contract_bytes;
     CUDA_TRY(cudaFuncSetAttribute(deac::trial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
-    CUDA_TRY(cudaFuncSetAttribute(deac::trial_raw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
+
     CUDA_TRY(cudaFuncSetAttribute(deac::contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)b->contract_smem_bytes));
     b->n_trial_ctas = (uint32_t)tw.size();
@@ -657,6 +664,19 @@ int deac_batch_setup(deac_batch* b) {
             if (!(r.dev.flags & deac::kDeferNorm)) continue;
             for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
         }
+        std::vector<deac::Work> pw;
+        uint32_t smax = 1;
+        for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+            const RunHost& r = *b->runs[ri];
+            const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
+            smax = std::max<uint32_t>(smax, (uint32_t)r.S);
+            for (uint32_t i = 0; i < r.dev.P; ++i)
+                for (uint32_t q = 0; q < parts; ++q) pw.push_back({ri, (q << 20) | i});
+        }
+        b->n_part_ctas = (uint32_t)pw.size();
+        b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
+        CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::Work)));
+        CUDA_TRY(cudaMemcpy(b->d_part_work, pw.data(), pw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
         b->n_norm_ctas = (uint32_t)nw.size();
         if (!nw.empty()) {
             CUDA_TRY(cudaFuncSetAttribute(deac::norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1000,6 +1020,7 @@ int deac_batch_destroy(deac_batch* b) {
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
     cudaFree(b->d_norm_work);
+    cudaFree(b->d_part_work);
     if (b->side_stream) cudaStreamDestroy(b->side_stream);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->own_stream) cudaStreamDestroy(b->stream);

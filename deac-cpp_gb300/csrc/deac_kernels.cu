@@ -132,14 +132,56 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
 // the row sum being formed (normalisation, first or third moment), when the
 // batch's capacity `smem_doubles` allows; otherwise the chains read global
 // memory (still k-ascending).
-template <bool kRowSums>
+// jDE of member i (deac_gpu.cu:584-606): CR(+) on slot 0, F(+) slot 1,
+// CR(-) slot 2, F(-) slot 3; then the mutant indices on slot 0
+// (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.  Stores
+// the new CR and F and the four slots' states; returns CR, F and the indices.
+__device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[2], double fw_new[2],
+                                           uint32_t mut[3]) {
+    const uint32_t P = R.P, M = R.M, S = R.S;
+    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
+    uint64_t st[4];
+    load_state(R, base, st);
+    for (uint32_t s = 0; s < S; ++s) {
+        uint64_t* cur = st;
+        uint64_t tmp[4];
+        if (s == 1) {
+            load_state(R, base + 2, tmp);
+            cur = tmp;
+        }
+        const double cr_old = R.cr[s * P + i];
+        const double cr = draw(cur) < R.tau_cr ? draw(cur) : cr_old;
+        if (s == 1) store_state(R, base + 2, tmp);
+        cr_new[s] = cr;
+        R.cr[(uint64_t)S * P + s * P + i] = cr;
+
+        uint64_t fs[4];
+        const uint64_t fslot = base + (s == 0 ? 1 : 3);
+        load_state(R, fslot, fs);
+        const double fw_old = R.fw[s * P + i];
+        const double fw = draw(fs) < R.tau_f ? 2.0 * draw(fs) : fw_old;
+        store_state(R, fslot, fs);
+        fw_new[s] = fw;
+        R.fw[(uint64_t)S * P + s * P + i] = fw;
+    }
+    // rejection sampling as in the reference; P >= 4 is enforced on the
+    // host, so every loop has an admissible outcome
+    uint64_t r0 = i, r1 = i, r2 = i;
+    while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+    while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+    while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
+    store_state(R, base, st);
+    mut[0] = (uint32_t)r0;
+    mut[1] = (uint32_t)r1;
+    mut[2] = (uint32_t)r2;
+}
+
 __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     extern __shared__ __align__(16) double trial_s[];
     __shared__ double s_cr[2], s_fw[2], s_sum[4];
     __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
     __shared__ ChainScratch s_chain[2];
-    __shared__ int s_digit_max[kTrialThreads / 32];
 
     const Work w = work[blockIdx.x];
     RunDev& R = runs[w.run];
@@ -157,8 +199,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     const uint64_t base = (uint64_t)i * (1ull + SM);
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    // without row sums (the split engine's generations) the trial stays raw
-    const bool normalize = kRowSums && (R.flags & kNormalize) != 0;
+    const bool normalize = (R.flags & kNormalize) != 0;
 
     // weights of one row sum, staged next to the genes when they fit
     auto weights = [&](const double* wp, const double* wn, const double*& tp, const double*& tn) {
@@ -179,48 +220,16 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     if (row_sums_here) weights(R.norm_pos, R.norm_neg, norm_p, norm_n);
 
     if (!init_mode && threadIdx.x == 0) {
-        // jDE (deac_gpu.cu:584-606): CR(+) on slot 0, F(+) slot 1,
-        // CR(-) slot 2, F(-) slot 3; then mutant indices on slot 0
-        // (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.
-        uint64_t st[4];
-        load_state(R, base, st);
+        double cr[2], fw[2];
+        jde_member(R, i, cr, fw, s_mut);
         for (uint32_t s = 0; s < S; ++s) {
-            uint64_t* cur = st;
-            uint64_t tmp[4];
-            if (s == 1) {
-                load_state(R, base + 2, tmp);
-                cur = tmp;
-            }
-            const double cr_old = R.cr[s * P + i];
-            const double cr = draw(cur) < R.tau_cr ? draw(cur) : cr_old;
-            if (s == 1) store_state(R, base + 2, tmp);
-            s_cr[s] = cr;
-            s_thr[s] = crossover_threshold(cr);
-            R.cr[(uint64_t)S * P + s * P + i] = cr;
-
-            uint64_t fs[4];
-            const uint64_t fslot = base + (s == 0 ? 1 : 3);
-            load_state(R, fslot, fs);
-            const double fw_old = R.fw[s * P + i];
-            const double fw = draw(fs) < R.tau_f ? 2.0 * draw(fs) : fw_old;
-            store_state(R, fslot, fs);
-            s_fw[s] = fw;
-            R.fw[(uint64_t)S * P + s * P + i] = fw;
+            s_cr[s] = cr[s];
+            s_thr[s] = crossover_threshold(cr[s]);
+            s_fw[s] = fw[s];
         }
-        // rejection sampling as in the reference; P >= 4 is enforced on
-        // the host, so every loop has an admissible outcome
-        uint64_t r0 = i, r1 = i, r2 = i;
-        while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-        while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-        while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-        store_state(R, base, st);
-        s_mut[0] = (uint32_t)r0;
-        s_mut[1] = (uint32_t)r1;
-        s_mut[2] = (uint32_t)r2;
     }
     __syncthreads();
 
-    bool trial_changed = false;  // uniform over the CTA
     const double* gene_pos = in_smem ? trial_s : dst;
     const double* gene_neg = in_smem ? trial_s + M : dst + PM;
     // row-sum chains (normalisation and moments): warps 0-7 the positive
@@ -255,8 +264,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
             const uint32_t j0 = c * kGeneChunk;
             const uint32_t len = min(kGeneChunk, M - j0);
             const uint32_t items = S * len;
-            // items in flight per thread: more where no row-sum code takes registers
-            constexpr int H = kRowSums ? 2 : 3;
+            constexpr int H = 2;  // genes in flight per thread
             for (uint32_t e0 = wid; e0 < items; e0 += H * nt) {
                 uint64_t st[H][4];
                 double a[H], b[H], cc[H], x[H];
@@ -305,8 +313,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
             dst[PM] = z;
             if (in_smem) trial_s[M] = z;
         }
-        // the split engine skips the evaluation of a trial equal to its parent
-        trial_changed = __syncthreads_or(mutated) != 0;
+        __syncthreads();
     } else if (in_smem) {
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
@@ -327,7 +334,6 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
         __syncthreads();
         const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
         const double recip = 1.0 / norm;
-        trial_changed = trial_changed || recip != 1.0;
         for (uint64_t q = threadIdx.x; q < SM; q += blockDim.x) {
             const uint32_t s = (uint32_t)(q / M);
             const uint64_t g = (uint64_t)s * PM + (q - (uint64_t)s * M);
@@ -339,7 +345,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     }
 
     // moment row sums with alpha = 1 (deac.cpp:1418-1477)
-    for (int which = 0; which < (kRowSums ? 2 : 0); ++which) {
+    for (int which = 0; which < 2; ++which) {
         const uint32_t flag = which == 0 ? kFirstMoment : kThirdMoment;
         if (!(R.flags & flag)) continue;
         const double *tp, *tn;
@@ -354,22 +360,113 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
         __syncthreads();
     }
 
-    // split engine: flag the trial (norm_kernel completes the flag of a
-    // kDeferNorm run) and slice it into BF16 digits for the tensor cores
-    if (!init_mode && R.changed) {
-        if (threadIdx.x == 0) R.changed[i] = trial_changed ? 1 : 0;
-        digitize_trial(in_smem ? trial_s : dst, in_smem ? (uint64_t)M : PM, S, M, R.xdig + (uint64_t)i * M, PM,
-                       R.xexp + (uint64_t)i * (M / kChunk), R.xexp_max + i, s_digit_max);
-    }
 }
 
 __global__ void __launch_bounds__(kTrialThreads)
 trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
-    trial_body<true>(runs, work, init_mode, smem_doubles);
+    trial_body(runs, work, init_mode, smem_doubles);
 }
-__global__ void __launch_bounds__(kTrialThreads)
-trial_raw_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
-    trial_body<false>(runs, work, init_mode, smem_doubles);
+
+// --------------------------------------------------------------- split trials
+// Split engine: jDE and the mutant indices of every member, one thread each
+// (work = the trial work list).
+__global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work, uint32_t n) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const Work w = work[k];
+    RunDev& R = runs[w.run];
+    if (R.done) return;
+    double cr[2], fw[2];
+    uint32_t mut[3];
+    jde_member(R, w.index, cr, fw, mut);
+    for (int q = 0; q < 3; ++q) R.mutants[3 * w.index + q] = mut[q];
+}
+
+// Split engine: the raw trial of member i, genes [part*kTrialPart, ...) of
+// both sides, per CTA -- the crossover draw and DE/rand/1 mutation of each
+// gene as in trial_kernel, then the part's BF16 digit slices.  Sets the
+// trial's `changed` flag when a gene mutated and raises its maximum chunk
+// exponent (split_decide_kernel resets both after use).
+__global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev* runs, const Work* work) {
+    extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
+    __shared__ double s_fw[2];
+    __shared__ uint64_t s_thr[2];
+    __shared__ int s_digit_max[kTrialPartThreads / 32];
+    const Work wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    if (R.done) return;
+    const uint32_t i = wk.index & 0xFFFFFu, part = wk.index >> 20;
+    const uint32_t P = R.P, M = R.M, S = R.S;
+    const uint64_t PM = (uint64_t)P * M;
+    const uint32_t j0 = part * kTrialPart;
+    const uint32_t len = M - j0 < kTrialPart ? M - j0 : kTrialPart;
+    const uint32_t parent_buf = R.cur[i];
+    double* dst = R.pop + ((uint64_t)(1u - parent_buf) * S) * PM + (uint64_t)i * M;
+    if (threadIdx.x < S) {
+        const double cr = R.cr[(uint64_t)S * P + threadIdx.x * P + i];
+        s_thr[threadIdx.x] = crossover_threshold(cr);
+        s_fw[threadIdx.x] = R.fw[(uint64_t)S * P + threadIdx.x * P + i];
+    }
+    __syncthreads();
+    const uint32_t r0 = R.mutants[3 * i], r1 = R.mutants[3 * i + 1], r2 = R.mutants[3 * i + 2];
+    const uint64_t buf = (uint64_t)S * PM;
+    const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
+    const double* pb = R.pop + (uint64_t)R.cur[r1] * buf + (uint64_t)r1 * M;
+    const double* pc = R.pop + (uint64_t)R.cur[r2] * buf + (uint64_t)r2 * M;
+    const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
+    const bool keep_sign = (R.flags & kSignedWeights) != 0;
+    const uint64_t n = R.n_states;
+    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
+    const uint32_t items = S * len;
+    bool mutated = false;
+    constexpr int H = 3;  // genes in flight per thread (128 registers, no spills)
+    for (uint32_t e0 = threadIdx.x; e0 < items; e0 += H * blockDim.x) {
+        uint64_t st[H][4];
+        double a[H], b[H], cc[H], x[H];
+        uint32_t sd[H], jj[H];
+        bool ok[H];
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            const uint32_t e = e0 + (uint32_t)h * blockDim.x;
+            ok[h] = e < items;
+            const uint32_t ee = ok[h] ? e : e0;
+            sd[h] = ee / len;
+            jj[h] = j0 + (ee - sd[h] * len);
+            const uint64_t slot = base + 1 + (uint64_t)sd[h] * M + jj[h];
+            st[h][0] = R.rng[slot];
+            st[h][1] = R.rng[n + slot];
+            st[h][2] = R.rng[2 * n + slot];
+            st[h][3] = R.rng[3 * n + slot];
+            const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
+            a[h] = pa[off];
+            b[h] = pb[off];
+            cc[h] = pc[off];
+            x[h] = px[off];
+        }
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            if (!ok[h]) continue;
+            const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
+            store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
+            double v = x[h];
+            if (mutate) {
+                v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
+                if (!keep_sign) v = fabs(v);
+                mutated = true;
+            }
+            dst[(uint64_t)sd[h] * PM + jj[h]] = v;
+            part_s[(uint64_t)sd[h] * len + (jj[h] - j0)] = v;
+        }
+    }
+    __syncthreads();
+    if (S == 2 && j0 == 0 && threadIdx.x == 0) {
+        // gpu_match_population_zero (deac_gpu.cu:541-549)
+        dst[PM] = part_s[0];
+        part_s[len] = part_s[0];
+    }
+    if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;
+    digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * M + j0, PM,
+                   R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk, R.xexp_max + i, s_digit_max);
 }
 
 // ---------------------------------------------------------------- norm

@@ -89,9 +89,10 @@ struct RunDev {
     const uint8_t* recheck;  // [P] decision left to the exact FP64 value
     double* f_lo;            // [P] interval holding the parent's exact fitness
     double* f_hi;
-    uint16_t* xdig;          // [6][S][P][M] digit planes of the trials
+    uint16_t* xdig;          // [7][S][P][M] digit planes of the trials
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
-    int16_t* xexp_max;       // [P]
+    int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
+    uint32_t* mutants;       // [P][3] mutant indices of this generation
     // split engine with --normalize (kDeferNorm): the trials stay raw until
     // the decisions; norm_kernel forms each trial's exact reciprocal norm
     double* recip;           // [P] 1/norm of each trial
@@ -163,11 +164,14 @@ enum ContractMode : int {
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
 };
 
-// trial_kernel forms the normalisation and moment row sums (the plain
-// engine, and every engine's initial population); trial_raw_kernel leaves the
-// trial raw (the split engine's generations)
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
-__global__ void trial_raw_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
+// split engine generations: jDE of every member (one thread each), then the
+// raw trials in parts of kTrialPart genes per side (work index =
+// part << 20 | member), each with its BF16 digit slices
+constexpr uint32_t kTrialPart = 1024;
+constexpr int kTrialPartThreads = 256;
+__global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
+__global__ void trial_part_kernel(RunDev* runs, const Work* work);
 // split engine, kDeferNorm runs: the exact normalisation row sums of one raw
 // trial per CTA (both sides), the reciprocal norm and the final `changed`
 // flag; and the normalisation of the trials the decisions keep (one CTA per

@@ -559,6 +559,11 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     }
     __syncthreads();
     if (threadIdx.x < 3 && s_n[threadIdx.x]) atomicAdd(&X.counts[threadIdx.x], s_n[threadIdx.x]);
+    // the next generation's trial parts set the flags and raise the maxima anew
+    for (uint32_t m = threadIdx.x; m < P; m += blockDim.x) {
+        X.changed[m] = 0;
+        X.xexp_max[m] = (int32_t)0x80808080;
+    }
     // Nothing left for the exact passes: finish the generation here -- the
     // bookkeeping of contract_kernel's trial pass (generation index, minimum
     // and stop test); the fitness of an interval-accepted member lies above

@@ -48,7 +48,7 @@ struct SplitRun {
     const uint16_t* kdig;  // [kDigits][S][Nt][M] digits of K (shared)
     const int16_t* kexp;   // [Nt][M/kChunk]
     const int16_t* kexp_max;  // [Nt] max over chunks
-    int16_t* xexp_max;   // [P] max over chunks
+    int32_t* xexp_max;   // [P] max over chunks
     double* e_mp;        // [P][Nt] split estimate of the model ISF
     double* e_bound;     // [P][Nt] bound on |estimate - FP64 chain value|
     uint8_t* changed;    // [P] trial differs from its parent
@@ -114,13 +114,14 @@ __device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
     return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
 }
 
-// The digit planes of one trial (both sides, genes in `x` at side stride
-// `side_stride`) by the calling CTA, a warp per 32-gene chunk: the chunk's
-// scale exponent (max over both sides), six 7-bit digits per gene, and the
-// trial's maximum exponent.  `s_max` is shared scratch of one int per warp.
+// The digit planes of M genes of one trial (both sides, genes in `x` at side
+// stride `side_stride`) by the calling CTA, a warp per 32-gene chunk: the
+// chunk's scale exponent (max over both sides), seven 7-bit digits per gene,
+// and the maximum exponent raised into *xexp_max.  `s_max` is shared scratch
+// of one int per warp.
 __device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_stride, uint32_t S, uint32_t M,
                                                uint16_t* xdig, uint64_t plane_stride, int16_t* xexp,
-                                               int16_t* xexp_max, int* s_max) {
+                                               int32_t* xexp_max, int* s_max) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
     const uint32_t C = M / kChunk;
     int wmax = -2000;
@@ -155,7 +156,7 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_st
     if (threadIdx.x == 0) {
         int m = -2000;
         for (uint32_t k = 0; k < nw; ++k) m = max(m, s_max[k]);
-        *xexp_max = (int16_t)m;
+        atomicMax(xexp_max, m);
     }
 }
 
