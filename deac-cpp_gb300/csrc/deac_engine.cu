@@ -156,9 +156,28 @@ struct deac_batch {
 
 namespace {
 
-void launch_contract(deac_batch* b, cudaStream_t s, int mode) {
-    deac::contract_kernel<<<b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s>>>(
-        b->d_runs, b->d_contract_work, mode);
+// A launch that may start while the previous kernel on the stream is still
+// running (`early`: programmatic stream serialisation); the kernel's first
+// statement, grid_dependency_wait(), holds it until that kernel is done.
+template <typename... Params, typename... Args>
+void launch(void (*kernel)(Params...), uint32_t grid, uint32_t block, size_t smem, cudaStream_t s, bool early,
+            Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = early ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
+void launch_contract(deac_batch* b, cudaStream_t s, int mode, bool early = false) {
+    launch(deac::contract_kernel, b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s, early,
+           b->d_runs, static_cast<const deac::Work*>(b->d_contract_work), mode);
 }
 
 // One generation of every run: two launches for the plain engine; for the
@@ -179,14 +198,18 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         return DEAC_OK;
     };
     if (timed) CUDA_TRY(cudaEventRecord(b->ev[0], s));
+    // split engine generations: kernels whose only predecessor is the
+    // previous launch on `s` are scheduled early (not when timed one by one)
+    const bool early = !timed;
     int rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
         deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
             b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
     } else {
-        deac::jde_kernel<<<(b->n_trial_ctas + 127) / 128, 128, 0, s>>>(b->d_runs, b->d_trial_work, b->n_trial_ctas);
-        deac::trial_part_kernel<<<b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s>>>(b->d_runs,
-                                                                                               b->d_part_work);
+        launch(deac::jde_kernel, (b->n_trial_ctas + 127) / 128, 128, 0, s, early, b->d_runs,
+               static_cast<const deac::Work*>(b->d_trial_work), b->n_trial_ctas);
+        launch(deac::trial_part_kernel, b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early,
+               b->d_runs, static_cast<const deac::Work*>(b->d_part_work));
     }
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
@@ -208,18 +231,22 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         if (fork) CUDA_TRY(cudaEventRecord(b->ev_join, b->side_stream));
         if ((rc = mark(2))) return rc;
     }
-    deac::split_contract_kernel<<<b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s>>>(
-        b->d_runs, b->d_split, b->d_tiles, b->d_split_work, b->d_rows, b->d_partial, b->d_status);
+    launch(deac::split_contract_kernel, b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s, early,
+           b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
+           static_cast<const deac::SplitWork*>(b->d_split_work), static_cast<const deac::SplitRow*>(b->d_rows),
+           b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
-    deac::split_combine_kernel<<<b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s>>>(
-        b->d_runs, b->d_split, b->d_tiles, b->d_rows, b->d_partial);
+    launch(deac::split_combine_kernel, b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s, early, b->d_runs,
+           b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
+           static_cast<const float4*>(b->d_partial));
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     deac::split_decide_kernel<<<(uint32_t)b->runs.size(), deac::kDecideThreads, 0, s>>>(b->d_runs, b->d_split);
     if (b->n_norm_ctas)
-        deac::scale_kernel<<<b->n_trial_ctas, 512, 0, s>>>(b->d_runs, b->d_trial_work);
+        launch(deac::scale_kernel, b->n_trial_ctas, 512, 0, s, early, b->d_runs,
+               static_cast<const deac::Work*>(b->d_trial_work));
     if ((rc = mark(4))) return rc;
-    launch_contract(b, s, deac::kModeParents);
-    launch_contract(b, s, deac::kModeTrials);
+    launch_contract(b, s, deac::kModeParents, early);
+    launch_contract(b, s, deac::kModeTrials, early);
     return mark(1);
 }
 

@@ -14,14 +14,6 @@ namespace {
 
 constexpr int kTreeSlots = 1024;   // GPU_BLOCK_SIZE of the reference reductions
 
-__device__ __forceinline__ void load_state(const RunDev& R, uint64_t slot, uint64_t s[4]) {
-    const uint64_t n = R.n_states;
-    s[0] = R.rng[slot];
-    s[1] = R.rng[n + slot];
-    s[2] = R.rng[2 * n + slot];
-    s[3] = R.rng[3 * n + slot];
-}
-
 __device__ __forceinline__ void store_state(const RunDev& R, uint64_t slot, const uint64_t s[4]) {
     const uint64_t n = R.n_states;
     R.rng[slot] = s[0];
@@ -140,37 +132,46 @@ __device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[
                                            uint32_t mut[3]) {
     const uint32_t P = R.P, M = R.M, S = R.S;
     const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
-    uint64_t st[4];
-    load_state(R, base, st);
-    for (uint32_t s = 0; s < S; ++s) {
-        uint64_t* cur = st;
-        uint64_t tmp[4];
-        if (s == 1) {
-            load_state(R, base + 2, tmp);
-            cur = tmp;
-        }
-        const double cr_old = R.cr[s * P + i];
-        const double cr = draw(cur) < R.tau_cr ? draw(cur) : cr_old;
-        if (s == 1) store_state(R, base + 2, tmp);
-        cr_new[s] = cr;
-        R.cr[(uint64_t)S * P + s * P + i] = cr;
-
-        uint64_t fs[4];
-        const uint64_t fslot = base + (s == 0 ? 1 : 3);
-        load_state(R, fslot, fs);
-        const double fw_old = R.fw[s * P + i];
-        const double fw = draw(fs) < R.tau_f ? 2.0 * draw(fs) : fw_old;
-        store_state(R, fslot, fs);
-        fw_new[s] = fw;
-        R.fw[(uint64_t)S * P + s * P + i] = fw;
+    const uint64_t n = R.n_states;
+    const uint64_t* rng = R.rng;
+    // every load is issued before the first store: slot base (CR of side 0,
+    // then the mutant indices), base+1 (F of side 0), base+2 / base+3 (CR / F
+    // of side 1); the stores below overlap none of them
+    uint64_t st[4][4];
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q)
+#pragma unroll
+        for (uint32_t w = 0; w < 4; ++w) st[q][w] = (q < 2 * S) ? rng[w * n + base + q] : 0ull;
+    double cr_old[2], fw_old[2];
+#pragma unroll
+    for (uint32_t s = 0; s < 2; ++s) {
+        cr_old[s] = s < S ? R.cr[s * P + i] : 0.0;
+        fw_old[s] = s < S ? R.fw[s * P + i] : 0.0;
     }
+    const double tau_cr = R.tau_cr, tau_f = R.tau_f;
+    auto side = [&](uint32_t s, uint64_t (&cs)[4], uint64_t (&fs)[4]) {
+        const double cr = draw(cs) < tau_cr ? draw(cs) : cr_old[s];
+        const double fw = draw(fs) < tau_f ? 2.0 * draw(fs) : fw_old[s];
+        cr_new[s] = cr;
+        fw_new[s] = fw;
+    };
+    side(0, st[0], st[1]);
+    if (S == 2) side(1, st[2], st[3]);
     // rejection sampling as in the reference; P >= 4 is enforced on the
     // host, so every loop has an admissible outcome
     uint64_t r0 = i, r1 = i, r2 = i;
-    while (r0 == i) r0 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-    while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-    while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0], st[1], st[2], st[3]) % P;
-    store_state(R, base, st);
+    while (r0 == i) r0 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
+    while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
+    while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
+#pragma unroll
+    for (uint32_t s = 0; s < 2; ++s)
+        if (s < S) {
+            R.cr[(uint64_t)S * P + s * P + i] = cr_new[s];
+            R.fw[(uint64_t)S * P + s * P + i] = fw_new[s];
+        }
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q)
+        if (q < 2 * S) store_state(R, base + q, st[q]);
     mut[0] = (uint32_t)r0;
     mut[1] = (uint32_t)r1;
     mut[2] = (uint32_t)r2;
@@ -178,7 +179,7 @@ __device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[
 
 __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     extern __shared__ __align__(16) double trial_s[];
-    __shared__ double s_cr[2], s_fw[2], s_sum[4];
+    __shared__ double s_fw[2], s_sum[4];
     __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
     __shared__ ChainScratch s_chain[2];
@@ -222,11 +223,12 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     if (!init_mode && threadIdx.x == 0) {
         double cr[2], fw[2];
         jde_member(R, i, cr, fw, s_mut);
-        for (uint32_t s = 0; s < S; ++s) {
-            s_cr[s] = cr[s];
-            s_thr[s] = crossover_threshold(cr[s]);
-            s_fw[s] = fw[s];
-        }
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s)
+            if (s < S) {
+                s_thr[s] = crossover_threshold(cr[s]);
+                s_fw[s] = fw[s];
+            }
     }
     __syncthreads();
 
@@ -371,6 +373,7 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 // Split engine: jDE and the mutant indices of every member, one thread each
 // (work = the trial work list).
 __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work, uint32_t n) {
+    grid_dependency_wait();
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const Work w = work[k];
@@ -388,6 +391,7 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
 // trial's `changed` flag when a gene mutated and raises its maximum chunk
 // exponent (split_decide_kernel resets both after use).
 __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev* runs, const Work* work) {
+    grid_dependency_wait();
     extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
     __shared__ double s_fw[2];
     __shared__ uint64_t s_thr[2];
@@ -476,6 +480,7 @@ __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev
 // norm = gemv_pair(...) and 1/norm exactly as trial_kernel does, and sets
 // the trial's `changed` flag (a mutated gene or a scale other than 1).
 __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const Work* work) {
+    grid_dependency_wait();
     __shared__ ChainScratch s_chain[2];
     __shared__ double s_sum[2];
     extern __shared__ __align__(16) double norm_s[];  // per side: [kNormStage] genes, [kNormStage] weights
@@ -534,6 +539,7 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // generation keeps (accepted) or still needs (the exact passes): every gene
 // times 1/norm, as trial_kernel does.  One CTA per trial.
 __global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* work) {
+    grid_dependency_wait();
     __shared__ uint32_t s_buf;
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
@@ -578,6 +584,7 @@ __global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* wo
 // row stride chunk+2), reused by the finishing CTA as 4 x 1024 reduction
 // slots.
 __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int mode) {
+    grid_dependency_wait();
     extern __shared__ __align__(16) double dyn[];
     __shared__ int s_last, s_any;
 

@@ -164,6 +164,17 @@ enum ContractMode : int {
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
 };
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialisation attribute may be scheduled while its predecessor on
+// the stream still runs.  Every generation kernel calls this first: it blocks
+// until the predecessor grid has completed with its memory visible, then
+// lets the next grid be scheduled (which waits here in turn, so at most two
+// grids overlap).  Without the attribute both instructions return at once.
+__device__ __forceinline__ void grid_dependency_wait() {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
 // split engine generations: jDE of every member (one thread each), then the
 // raw trials in parts of kTrialPart genes per side (work index =

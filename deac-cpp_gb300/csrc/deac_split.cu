@@ -134,6 +134,7 @@ __device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
 __global__ void __launch_bounds__(kSplitThreads, 1)
 split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
                       const SplitRow* rows, float4* partial, int* status) {
+    grid_dependency_wait();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t s_tmem;
     __shared__ __align__(8) uint64_t s_bar;
@@ -373,6 +374,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
 // a fixed order and turned into the estimate and its error bound.
 __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
                                                             const SplitRow* rows, const float4* partial) {
+    grid_dependency_wait();
     __shared__ float4 s_part[8][32];
     const SplitTile tile = tiles[blockIdx.x / kCombineCtasPerTile];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -446,6 +448,7 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
 // then the selection decisions that the interval settles.  Undecided members
 // are flagged for the exact FP64 evaluation (contract_kernel, recheck mode).
 __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* runs, SplitRun* split) {
+    grid_dependency_wait();
     __shared__ unsigned long long s_n[3];
     RunDev& R = runs[blockIdx.x];
     if (R.done) return;
