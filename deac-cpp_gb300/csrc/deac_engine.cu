@@ -11,6 +11,8 @@
 // The stop test runs on the device, so the host never synchronises inside
 // a block -- the reference does a D2H copy and ~10 stream syncs per
 // generation (deac.cpp:1140-1147 and the deac_wait calls of 1168-1574).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,7 +83,7 @@ struct Arena {
 struct KernelMatrix {
     double* k_pos = nullptr;
     double* k_neg = nullptr;
-    uint16_t* kdig = nullptr;   // [kDigits][S][Nt][M]
+    uint16_t* kdig = nullptr;   // tiled digit planes (rows = timeslices)
     bool nonneg = false;        // every entry >= 0
     int16_t* kexp = nullptr;    // [Nt][M/kChunk]
     int16_t* kexp_max = nullptr;  // [Nt]
@@ -131,6 +133,8 @@ struct deac_batch {
     deac::SplitRun* d_split = nullptr;
     deac::SplitTile* d_tiles = nullptr;
     deac::SplitWork* d_split_work = nullptr;
+    std::vector<uint16_t*> group_xdig;      // trial digit planes per kernel-matrix group
+    CUtensorMap* d_maps = nullptr;          // per group: K planes, trial planes
     deac::SplitRow* d_rows = nullptr;
     float4* d_partial = nullptr;       // partial sums of the split contraction CTAs
     uint32_t n_tiles = 0, n_split_ctas = 0;
@@ -234,7 +238,7 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     launch(deac::split_contract_kernel, b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s, early,
            b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
            static_cast<const deac::SplitWork*>(b->d_split_work), static_cast<const deac::SplitRow*>(b->d_rows),
-           b->d_partial, b->d_status);
+           static_cast<const CUtensorMap*>(b->d_maps), b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
     launch(deac::split_combine_kernel, b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s, early, b->d_runs,
            b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
@@ -327,7 +331,8 @@ int upload_run(deac_batch* b, RunHost& r) {
             for (double v : m.k_neg) km.nonneg = km.nonneg && v >= 0.0;
         if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
             // digit planes of K: one scale per (timeslice, 32-gene chunk)
-            // shared by both sides, six 7-bit digits per value
+            // shared by both sides, seven 7-bit digits per value, tiled as
+            // [plane][unit of 8 genes][timeslice][8]
             const uint64_t C = M / deac::kChunk;
             std::vector<uint16_t> kdig((uint64_t)deac::kDigits * S * Nt * M);
             std::vector<int16_t> kexp(Nt * C), kmax(Nt, -1000);
@@ -347,7 +352,7 @@ int upload_run(deac_batch* b, RunHost& r) {
                             uint16_t dg[deac::kDigits];
                             deac::digits_of((sd ? m.k_neg : m.k_pos)[t * M + j], e, dg);
                             for (int d = 0; d < deac::kDigits; ++d)
-                                kdig[(((uint64_t)d * S + sd) * Nt + t) * M + j] = dg[d];
+                                kdig[((((uint64_t)d * S + sd) * (M / 8) + j / 8) * Nt + t) * 8 + (j & 7)] = dg[d];
                         }
                 }
             CUDA_TRY(cudaMalloc(&km.kdig, kdig.size() * 2));
@@ -458,7 +463,6 @@ int upload_run(deac_batch* b, RunHost& r) {
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
         const uint64_t C = M / deac::kChunk;
         Arena sa;
-        const uint64_t o_xd = sa.take((uint64_t)deac::kDigits * S * P * M * 2);
         const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 4), o_mu = sa.take(P * 3 * 4);
         const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
@@ -469,7 +473,6 @@ int upload_run(deac_batch* b, RunHost& r) {
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
         deac::SplitRun& x = r.split;
-        x.xdig = reinterpret_cast<uint16_t*>(sb + o_xd);
         x.xexp = reinterpret_cast<int16_t*>(sb + o_xe);
         x.xexp_max = reinterpret_cast<int32_t*>(sb + o_xm);
         CUDA_TRY(cudaMemset(x.xexp_max, 0x80, P * 4));  // below every exponent: no trial sliced yet
@@ -492,7 +495,6 @@ int upload_run(deac_batch* b, RunHost& r) {
             x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
         }
         d.changed = x.changed;
-        d.xdig = x.xdig;
         d.xexp = x.xexp;
         d.xexp_max = x.xexp_max;
         d.mutants = reinterpret_cast<uint32_t*>(sb + o_mu);
@@ -528,6 +530,79 @@ int build_graph(deac_batch* b) {
     cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(DEAC_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    return DEAC_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Split engine: the trial digit planes of every group of runs that share a
+// kernel matrix, one tiled buffer per group with the members of its runs as
+// consecutive rows (the row order of the split tiles), and the two TMA
+// tensor maps per group that split_contract_kernel loads its chunks with.
+int make_group_planes(deac_batch* b) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return fail(DEAC_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const uint32_t ng = (uint32_t)b->kcache.size();
+    std::vector<const KernelMatrix*> kms(ng, nullptr);
+    for (auto& kv : b->kcache) kms[kv.second.group] = &kv.second;
+    std::vector<CUtensorMap> maps(2 * ng);
+    b->group_xdig.assign(ng, nullptr);
+    for (uint32_t g = 0; g < ng; ++g) {
+        uint64_t R = 0, M = 0, Nt = 0;
+        int S = 1;
+        for (auto& rp : b->runs)
+            if (rp->kgroup == g) {
+                R += rp->P;
+                M = rp->M;
+                Nt = rp->Nt;
+                S = rp->S;
+            }
+        if (R == 0) continue;
+        const uint64_t planes = (uint64_t)deac::kDigits * S, units = M / 8;
+        CUDA_TRY(cudaMalloc(&b->group_xdig[g], planes * units * R * 8 * 2));
+        CUDA_TRY(cudaMemset(b->group_xdig[g], 0, planes * units * R * 8 * 2));
+        uint64_t row = 0;
+        for (auto& rp : b->runs)
+            if (rp->kgroup == g) {
+                uint16_t* x = b->group_xdig[g] + row * 8;
+                rp->split.xdig = x;
+                rp->split.xdig_unit = R * 8;
+                rp->split.xdig_plane = M * R;
+                rp->dev.xdig = x;
+                rp->dev.xdig_unit = R * 8;
+                rp->dev.xdig_plane = M * R;
+                row += rp->P;
+            }
+        // dims: 8 genes, rows, units of 8 genes, planes; box: one chunk of
+        // one tile (128 timeslices resp. 64 trial rows) of every plane
+        auto make = [&](CUtensorMap* m, void* base, uint64_t rows, uint32_t box_rows) -> int {
+            const cuuint64_t dims[4] = {8, rows, units, planes};
+            const cuuint64_t strides[3] = {16, rows * 16, units * rows * 16};
+            const cuuint32_t box[4] = {8, box_rows, deac::kChunk / 8, (cuuint32_t)planes};
+            const cuuint32_t estr[4] = {1, 1, 1, 1};
+            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(DEAC_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+            return DEAC_OK;
+        };
+        int rc = make(&maps[2 * g], kms[g]->kdig, Nt, deac::kTauTile);
+        if (rc) return rc;
+        rc = make(&maps[2 * g + 1], b->group_xdig[g], R, deac::kRowTile);
+        if (rc) return rc;
+    }
+    CUDA_TRY(cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)));
+    CUDA_TRY(cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
     return DEAC_OK;
 }
 
@@ -716,6 +791,10 @@ int deac_batch_setup(deac_batch* b) {
     CUDA_TRY(cudaMalloc(&b->d_contract_work, cw.size() * sizeof(deac::Work)));
     CUDA_TRY(cudaMemcpy(b->d_trial_work, tw.data(), tw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b->d_contract_work, cw.data(), cw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        int rc = make_group_planes(b);
+        if (rc) return rc;
+    }
     std::vector<deac::RunDev> descs;
     for (auto& r : b->runs) descs.push_back(r->dev);
     CUDA_TRY(cudaMalloc(&b->d_runs, descs.size() * sizeof(deac::RunDev)));
@@ -744,7 +823,7 @@ int deac_batch_setup(deac_batch* b) {
             for (size_t r0 = 0; r0 < grp.size(); r0 += deac::kRowTile) {
                 const uint32_t nrow = (uint32_t)std::min<size_t>(deac::kRowTile, grp.size() - r0);
                 for (uint32_t t0 = 0; t0 < nt; t0 += deac::kTauTile) {
-                    tiles.push_back({t0, (uint32_t)(rows.size() + r0), nrow, grp[r0].run, 0, 0});
+                    tiles.push_back({t0, (uint32_t)(rows.size() + r0), nrow, grp[r0].run, 0, 0, 0, g, (uint32_t)r0});
                     tile_chunks.push_back(chunks);
                 }
             }
@@ -1036,6 +1115,8 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_split);
     cudaFree(b->d_tiles);
     cudaFree(b->d_split_work);
+    for (uint16_t* x : b->group_xdig) cudaFree(x);
+    cudaFree(b->d_maps);
     cudaFree(b->d_partial);
     cudaFree(b->d_rows);
     cudaFree(b->d_status);

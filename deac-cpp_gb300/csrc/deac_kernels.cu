@@ -469,7 +469,8 @@ __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev
         part_s[len] = part_s[0];
     }
     if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;
-    digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * M + j0, PM,
+    digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * 8 + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_plane,
+                   R.xdig_unit,
                    R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk, R.xexp_max + i, s_digit_max);
 }
 

@@ -89,7 +89,9 @@ struct RunDev {
     const uint8_t* recheck;  // [P] decision left to the exact FP64 value
     double* f_lo;            // [P] interval holding the parent's exact fitness
     double* f_hi;
-    uint16_t* xdig;          // [7][S][P][M] digit planes of the trials
+    uint16_t* xdig;          // tiled digit planes of the trials (member 0's row)
+    uint64_t xdig_unit;      // elements between units of 8 genes
+    uint64_t xdig_plane;     // elements between planes
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
     uint32_t* mutants;       // [P][3] mutant indices of this generation

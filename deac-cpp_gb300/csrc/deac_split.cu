@@ -76,8 +76,49 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
                  : "r"(taddr));
 }
 
-__device__ __forceinline__ void cp16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+// one 4-D tiled TMA load into shared memory, completing on `bar` (tensor map
+// in global memory, coordinates innermost first)
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// more bytes to come in the current phase, without an arrival
+__device__ __forceinline__ void mbar_add_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// The digit-pair MMAs of one chunk (one thread): group g accumulates every
+// pair a+b = g of trial digit a and K digit g-a, both sides, two K steps of
+// 16 genes.  Descriptors are the planes' base descriptors plus constant
+// offsets (addresses in 16-byte units; the 14-bit field never carries).
+template <int S>
+__device__ __forceinline__ void issue_chunk_mmas(uint32_t tmem, uint64_t dA, uint64_t dB, uint32_t idesc) {
+    constexpr uint32_t a_plane = kTauTile * kChunk * 2 / 16, b_plane = kRowTile * kChunk * 2 / 16;
+    constexpr uint32_t a_step = 2 * kTauTile, b_step = 2 * kRowTile;  // two units of 8 genes
+#pragma unroll
+    for (int g = 0; g < kDigits; ++g)
+#pragma unroll
+        for (int a = 0; a <= g; ++a)
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int ks = 0; ks < kChunk / 16; ++ks) {
+                    const uint64_t da = dA + (uint64_t)(((g - a) * S + s) * a_plane + ks * a_step);
+                    const uint64_t db = dB + (uint64_t)((a * S + s) * b_plane + ks * b_step);
+                    mma_bf16(tmem + g * kRowTile, da, db, idesc, (a | s | ks) ? 1u : 0u);
+                }
 }
 
 // Error-free transformations in FP32 (IEEE round-to-nearest; the file is
@@ -133,11 +174,11 @@ __device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
 // (hi, lo, bound) for the combine kernel.
 __global__ void __launch_bounds__(kSplitThreads, 1)
 split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
-                      const SplitRow* rows, float4* partial, int* status) {
-    grid_dependency_wait();
+                      const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t s_tmem;
-    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(8) uint64_t s_bar;   // MMA completion
+    __shared__ __align__(8) uint64_t s_full;  // the chunk's digit planes have landed
     __shared__ int s_ek[kTauTile], s_kmax[kTauTile];
     __shared__ int s_ex[kRowTile], s_xmax[kRowTile];
     __shared__ int s_live;
@@ -151,60 +192,35 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     const uint32_t C = M / kChunk;
     const uint32_t tau0 = tile.tau0;
 
-    // is any row of the tile a changed trial of a running run?  (Nothing is
-    // done either after a failed wait in an earlier launch, until the host
-    // has seen the status; one thread reads it so the CTA agrees.)
-    if (tid == 0) s_live = *reinterpret_cast<volatile int*>(status) != 0 ? -1 : 0;
-    __syncthreads();
-    if (s_live == 0 && tid < tile.rows) {
-        // every trial of a running run is sliced (whether it changed is known
-        // only after the normalisation of kDeferNorm runs)
-        const SplitRow rw = rows[tile.first_row + tid];
-        if (!runs[rw.run].done) atomicOr(&s_live, 1);
-    }
-    __syncthreads();
-    if (s_live <= 0) return;
-
-    // shared memory: K digits [6][S] x (128 x 32), trial digits [6][S] x
-    // (64 x 32), bound operands (128 x 16) and (64 x 16), accumulators
+    // shared memory: K digits [7S planes] x (128 x 32), trial digits [7S]
+    // x (64 x 32), each plane [unit][row][8 genes] as the TMA box lands
+    // (core matrices 8 rows = 128 bytes apart, units one row block apart),
+    // and the bound operands (128 x 16) and (64 x 16)
     const uint32_t a_tile = kTauTile * kChunk * 2;  // 8 KB
     const uint32_t b_tile = kRowTile * kChunk * 2;  // 4 KB
     uint8_t* sA = smem;
     uint8_t* sB = sA + kDigits * S * a_tile;
     uint8_t* sAb = sB + kDigits * S * b_tile;
     uint8_t* sBb = sAb + kTauTile * 16 * 2;
+    const uint32_t stage_bytes = (uint32_t)kDigits * S * (a_tile + b_tile);
+    const CUtensorMap* map_k = maps + 2 * tile.group;
+    const CUtensorMap* map_x = maps + 2 * tile.group + 1;
 
     // zero the rank-1 bound operands once (only k = 0 is written per chunk)
     for (uint32_t e = tid; e < (kTauTile + kRowTile) * 16; e += blockDim.x)
         reinterpret_cast<uint16_t*>(sAb)[e] = 0;
 
-    // staging roles: K digits -> (timeslice row, two 16-byte units);
-    // trial digits -> (trial row, one unit)
-    const uint32_t a_row = tid >> 1, a_u0 = (tid & 1u) * 2;
-    const bool a_ok = tau0 + a_row < Nt;
-    const uint16_t* a_src = X0.kdig + (uint64_t)(tau0 + (a_ok ? a_row : 0)) * M;
-    const uint64_t a_plane = (uint64_t)Nt * M;
-    const uint32_t b_row = tid >> 2, b_u = tid & 3u;
-    const bool b_ok = b_row < tile.rows;
-    const uint16_t* b_src = nullptr;
-    uint64_t b_plane = 0;
-    if (b_ok) {
-        const SplitRow rw = rows[tile.first_row + b_row];
-        b_plane = (uint64_t)runs[rw.run].P * M;
-        b_src = split[rw.run].xdig + (uint64_t)rw.member * M;
-    }
+    // one thread loads a chunk's planes of both operands: two TMA boxes
+    // (timeslices beyond Nt and rows beyond the group read as zero)
+    const uint32_t a_bytes = (uint32_t)kDigits * S * a_tile, b_bytes = (uint32_t)kDigits * S * b_tile;
+    auto load_k = [&](uint32_t c) { tma_load_4d(sA, map_k, 0, (int)tau0, (int)(c * (kChunk / 8)), 0, &s_full); };
+    auto load_x = [&](uint32_t c) {
+        tma_load_4d(sB, map_x, 0, (int)tile.grow0, (int)(c * (kChunk / 8)), 0, &s_full);
+    };
     auto stage = [&](uint32_t c) {
-        const uint32_t g0 = c * kChunk;
-        for (uint32_t q = 0; q < (uint32_t)kDigits * S; ++q) {
-            if (a_ok) {
-                uint8_t* dst = sA + q * a_tile;
-                const uint16_t* src = a_src + q * a_plane + g0;
-                cp16(dst + canon(a_row, a_u0 * 8, kChunk), src + a_u0 * 8);
-                cp16(dst + canon(a_row, a_u0 * 8 + 8, kChunk), src + a_u0 * 8 + 8);
-            }
-            if (b_ok) cp16(sB + q * b_tile + canon(b_row, b_u * 8, kChunk), b_src + q * b_plane + g0 + b_u * 8);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        mbar_expect_tx(&s_full, stage_bytes);
+        load_k(c);
+        load_x(c);
     };
     // chunk exponents and the bound operands 2^(e - max) at k = 0
     auto scales = [&](uint32_t c) {
@@ -237,9 +253,39 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_full)));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        // K is constant: its first chunk loads while the trial kernel ends
+        mbar_add_tx(&s_full, a_bytes);
+        load_k(wk.c0);
     }
     if (tid < kTauTile) s_kmax[tid] = (tau0 + tid < Nt) ? X0.kexp_max[tau0 + tid] : 0;
+
+    // everything below reads what the trial kernel wrote
+    grid_dependency_wait();
+    // is any row of the tile a changed trial of a running run?  (Nothing is
+    // done either after a failed wait in an earlier launch, until the host
+    // has seen the status; one thread reads it so the CTA agrees.)
+    if (tid == 0) s_live = *reinterpret_cast<volatile int*>(status) != 0 ? -1 : 0;
+    __syncthreads();
+    if (s_live == 0 && tid < tile.rows) {
+        // every trial of a running run is sliced (whether it changed is known
+        // only after the normalisation of kDeferNorm runs)
+        const SplitRow rw = rows[tile.first_row + tid];
+        if (!runs[rw.run].done) atomicOr(&s_live, 1);
+    }
+    __syncthreads();
+    if (s_live <= 0) {
+        // nothing to do: let the K load land, then release TMEM
+        if (tid == 0) mbar_arrive(&s_full);
+        if (tid == 0) mbar_wait(&s_full, 0);
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();
+        if (warp == 0)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(s_tmem), "r"(kTmemCols));
+        return;
+    }
     if (tid >= kTauTile && tid < kTauTile + kRowTile) {
         const uint32_t r = tid - kTauTile;
         int m = 0;
@@ -258,10 +304,12 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
 #pragma unroll
     for (uint32_t r = 0; r < 32; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
 
-    stage(wk.c0);
     __syncthreads();  // s_kmax / s_xmax
+    if (tid == 0) {
+        mbar_expect_tx(&s_full, b_bytes);
+        load_x(wk.c0);
+    }
     scales(wk.c0);
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
@@ -273,22 +321,16 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     bool ok = true;
     for (uint32_t c = wk.c0; c < wk.c1; ++c) {
         const uint32_t it = c - wk.c0;
+        // the chunk's planes (one thread waits; the CTA agrees on the outcome)
+        ok = __syncthreads_and(tid == 0 ? mbar_wait(&s_full, it & 1u) : true) != 0;
+        if (!ok) break;
         // --- MMAs (one thread): group g accumulates every digit pair a+b=g
         if (tid == 0) {
-            const uint32_t lbo = 128, sbo = (kChunk / 8) * 128;
-            for (uint32_t g = 0; g < (uint32_t)kKept; ++g) {
-                uint32_t first = 1;
-                for (uint32_t a = 0; a <= g; ++a) {
-                    const uint32_t bq = g - a;  // K digit index
-                    for (uint32_t s = 0; s < S; ++s)
-                        for (uint32_t ks = 0; ks < kChunk / 16; ++ks) {
-                            const uint64_t da = smem_desc(smem_u32(sA + (bq * S + s) * a_tile) + ks * 256, lbo, sbo);
-                            const uint64_t db = smem_desc(smem_u32(sB + (a * S + s) * b_tile) + ks * 256, lbo, sbo);
-                            mma_bf16(tmem + g * kRowTile, da, db, idesc, first ? 0u : 1u);
-                            first = 0;
-                        }
-                }
-            }
+            // K-adjacent core matrices one unit apart, row blocks 128 bytes
+            const uint64_t dA = smem_desc(smem_u32(sA), kTauTile * 16, 128);
+            const uint64_t dB = smem_desc(smem_u32(sB), kRowTile * 16, 128);
+            if (S == 2) issue_chunk_mmas<2>(tmem, dA, dB, idesc);
+            else issue_chunk_mmas<1>(tmem, dA, dB, idesc);
             const uint64_t dab = smem_desc(smem_u32(sAb), 128, 256);
             const uint64_t dbb = smem_desc(smem_u32(sBb), 128, 256);
             mma_bf16(tmem + kBoundCol, dab, dbb, idesc, it > 0 ? 1u : 0u);
@@ -299,7 +341,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         if (!ok) break;
         // the staging buffers are free again: load the next chunk meanwhile
-        if (c + 1 < wk.c1) stage(c + 1);
+        if (tid == 0 && c + 1 < wk.c1) stage(c + 1);
 
         // --- fold the seven exact group sums of this chunk into the accumulators
         const int ek = s_ek[tl];
@@ -337,7 +379,6 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         __syncthreads();  // every read of s_ek/s_ex and of TMEM is done
         if (c + 1 < wk.c1) {
             scales(c + 1);
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n");

@@ -18,7 +18,18 @@
 // itself this gives an interval that contains the value the plain FP64
 // engine computes, so selection decisions made from it are the FP64
 // decisions (deac_kernels.cuh, contract_kernel).
+//
+// Digit planes are stored pre-tiled for the tensor memory accelerator: plane
+// q = digit*S + side, then units of 8 genes, then rows, then the 8 genes
+// (16 bytes), i.e. element (q, row, gene j) at
+//     ((q * M/8 + j/8) * rows + row) * 8 + j%8.
+// One 4-D TMA box {8 genes, 128 or 64 rows, 4 units, 7S planes} then lands in
+// shared memory as [plane][unit][row][8]: the canonical K-major no-swizzle
+// operand layout with 16-byte rows, core matrices 8 rows apart (128 bytes)
+// and units one row-block apart.
 #pragma once
+
+#include <cuda.h>
 
 #include <cstdint>
 
@@ -43,9 +54,12 @@ constexpr uint32_t split_smem_bytes(uint32_t S) {
 
 // Split-engine buffers of one run (device pointers).
 struct SplitRun {
-    uint16_t* xdig;      // [kDigits][S][P][M] BF16 digits of the trial genes
+    uint16_t* xdig;      // BF16 digits of the trial genes: member 0's row of the
+                         // tiled planes of all runs sharing K (rows R)
+    uint64_t xdig_unit;  // elements between units of 8 genes (R * 8)
+    uint64_t xdig_plane; // elements between planes (M * R)
     int16_t* xexp;       // [P][M/kChunk] chunk scale exponents of the trial
-    const uint16_t* kdig;  // [kDigits][S][Nt][M] digits of K (shared)
+    const uint16_t* kdig;  // tiled digit planes of K, rows = timeslices (shared)
     const int16_t* kexp;   // [Nt][M/kChunk]
     const int16_t* kexp_max;  // [Nt] max over chunks
     int32_t* xexp_max;   // [P] max over chunks
@@ -73,6 +87,8 @@ struct SplitTile {
     uint32_t nsplit;
     uint32_t block0;
     uint32_t per;        // chunks of its longest split
+    uint32_t group;      // runs sharing K: index of its tensor maps
+    uint32_t grow0;      // first row within the group's trial digit planes
 };
 // One CTA of split_contract_kernel: chunks [c0, c1) of a tile.
 struct SplitWork {
@@ -84,8 +100,10 @@ struct SplitRow {
 // partial sums of one CTA: [kRowTile][kTauTile] of (hi, lo, bound, 0)
 constexpr uint64_t kPartialBlock = (uint64_t)kRowTile * kTauTile;
 
+// tensor maps per group: [2g] the K digit planes (box 128 timeslice rows),
+// [2g+1] the trial digit planes (box 64 rows)
 __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
-                                      const SplitRow* rows, float4* partial, int* status);
+                                      const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status);
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows,
                                      const float4* partial);
 __global__ void split_decide_kernel(RunDev* runs, SplitRun* split);
@@ -117,11 +135,12 @@ __device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
 // The digit planes of M genes of one trial (both sides, genes in `x` at side
 // stride `side_stride`) by the calling CTA, a warp per 32-gene chunk: the
 // chunk's scale exponent (max over both sides), seven 7-bit digits per gene,
-// and the maximum exponent raised into *xexp_max.  `s_max` is shared scratch
-// of one int per warp.
+// and the maximum exponent raised into *xexp_max.  `xdig` points at the
+// trial's row in the tiled planes at its first gene's unit.  `s_max` is
+// shared scratch of one int per warp.
 __device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_stride, uint32_t S, uint32_t M,
-                                               uint16_t* xdig, uint64_t plane_stride, int16_t* xexp,
-                                               int32_t* xexp_max, int* s_max) {
+                                               uint16_t* xdig, uint64_t plane_stride, uint64_t unit_stride,
+                                               int16_t* xexp, int32_t* xexp_max, int* s_max) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
     const uint32_t C = M / kChunk;
     int wmax = -2000;
@@ -145,7 +164,7 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_st
 #pragma unroll
             for (int b = 0; b < kDigits; ++b) {
                 const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
-                xdig[((uint64_t)b * S + s) * plane_stride + j] = bf16_digit(d, neg);
+                xdig[((uint64_t)b * S + s) * plane_stride + (j >> 3) * unit_stride + (j & 7u)] = bf16_digit(d, neg);
             }
         }
         if (lane == 0) xexp[c] = (int16_t)e;
