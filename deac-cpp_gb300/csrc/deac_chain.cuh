@@ -465,6 +465,12 @@ struct ChainScratch {
     unsigned long long fail_state;
     uint32_t fail_pos;
     int32_t fail_bin;
+    // results of the group's one-thread sequential parts
+    double early_acc;      // state after the plain first steps
+    uint32_t early_k0;     // steps done plainly
+    double pass_acc;       // state where the predicted pass stopped
+    uint32_t pass_fail;    // position where the chaining of the segments stopped
+    uint32_t pass_ranged;  // every chained segment ended inside its binade
 };
 
 namespace chain_detail {
@@ -558,11 +564,19 @@ __device__ __forceinline__ int rel_binade(uint64_t v) {
 
 }  // namespace chain_detail
 
+// Position of step k in x and w: the plain order, or (kSwz) one super-block
+// stored step-major per thread -- step t*E + i at i*(W*32) + t -- so that the
+// group's threads read their E steps from consecutive addresses.
+template <int W, int E, bool kSwz>
+__device__ __forceinline__ uint32_t chain_slot(uint32_t k) {
+    return kSwz ? (k % (uint32_t)E) * (uint32_t)(W * 32) + k / (uint32_t)E : k;
+}
+
 // The predicted pass of host_predicted_pass, by the W warps of a group, each
 // thread over its E cached terms tp (steps tg*E + i of the super-block, the
 // ones before k0 and from len on are zero).  Returns the position reached
 // and the state there in acc (uniform over the group).
-template <int W, int E>
+template <int W, int E, bool kSwz>
 __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const double* w, uint64_t (&tp)[E],
                                                           uint32_t k0, uint32_t len, uint64_t A0, int ea,
                                                           double& acc, uint32_t tg, int bar_id, ChainScratch& sc,
@@ -704,33 +718,51 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     }
     group_bar(bar_id, NT);
 
-    // --- chain the segments (every thread, on the same values)
-    double a = state_join(0, A0, ea);
-    uint32_t fail = len;
-    double fail_acc = 0.0;
-    for (uint32_t m = 0; m <= ncross; ++m) {
-        const int j = m == 0 ? 0 : sc.cbin[m - 1];
-        const uint32_t start = m == 0 ? k0 : sc.cpos[m - 1] + 1;
-        const uint32_t end = m < ncross ? sc.cpos[m] : len;
-        uint32_t ng;
-        uint64_t A;
-        int e;
-        bool ok = state_ok(a);
-        if (ok) {
-            state_split(a, ng, A, e);
-            ok = ng == 0 && e == ea + j;
+    // --- chain the segments (one thread; the others read the outcome).  A
+    // positive run only grows, and each step adds at least its integer part,
+    // so a segment whose end state stays below 2^53 had every step inside its
+    // binade; only a segment that reaches it needs the step-wise check below.
+    if (tg == 0) {
+        double a = state_join(0, A0, ea);
+        uint32_t fail = len;
+        double fail_acc = 0.0;
+        uint32_t ranged = 1u;
+        for (uint32_t m = 0; m <= ncross; ++m) {
+            const int j = m == 0 ? 0 : sc.cbin[m - 1];
+            const uint32_t start = m == 0 ? k0 : sc.cpos[m - 1] + 1;
+            const uint32_t end = m < ncross ? sc.cpos[m] : len;
+            uint32_t ng;
+            uint64_t A;
+            int e;
+            bool ok = state_ok(a);
+            if (ok) {
+                state_split(a, ng, A, e);
+                ok = ng == 0 && e == ea + j;
+            }
+            if (!ok) {
+                fail = start;
+                fail_acc = a;
+                break;
+            }
+            sc.astart[m] = A;
+            const long long Q = end > start ? sc.segq[A & 1u][m] : 0;
+            if (A + (uint64_t)Q > kTwo53 - 1) ranged = 0u;
+            a = state_join(0, A + (uint64_t)Q, e);
+            if (m < ncross) {
+                const uint32_t q = chain_slot<W, E, kSwz>(sc.cpos[m]);
+                a = fma(x[q], w[q], a);
+            }
         }
-        if (!ok) {
-            fail = start;
-            fail_acc = a;
-            break;
-        }
-        if (tg == 0) sc.astart[m] = A;
-        const long long Q = end > start ? sc.segq[A & 1u][m] : 0;
-        a = state_join(0, A + (uint64_t)Q, e);
-        if (m < ncross) a = fma(x[sc.cpos[m]], w[sc.cpos[m]], a);
+        sc.pass_acc = fail < len ? fail_acc : a;
+        sc.pass_fail = fail;
+        sc.pass_ranged = ranged;
     }
     group_bar(bar_id, NT);
+    const uint32_t fail = sc.pass_fail;
+    if (sc.pass_ranged) {
+        acc = sc.pass_acc;
+        return fail;
+    }
 
     // --- verify every step before the first mismatch
     uint32_t first_bad = kNone;
@@ -778,7 +810,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         group_bar(bar_id, NT);  // the scratch is reused next
         return bad;
     }
-    acc = fail < len ? fail_acc : a;
+    acc = sc.pass_acc;
     return fail;
 }
 
@@ -788,8 +820,9 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
 // consecutive steps; a round scans the parity maps and the integer steps of
 // the whole super-block at once, and a binade change (a new round) shifts the
 // thread's cached terms instead of decoding them again.  Synchronises the
-// group with named barrier `bar_id` (not 0).
-template <int W, int E, bool kPredict = true>
+// group with named barrier `bar_id` (not 0).  With kSwz, x and w hold one
+// super-block (n <= W*32*E) in the order of chain_slot.
+template <int W, int E, bool kPredict = true, bool kSwz = false>
 __device__ __forceinline__ double group_fma_chain(const double* x, const double* w, uint32_t n, double acc,
                                                   uint32_t w0, int bar_id, ChainScratch& sc,
                                                   uint32_t early_steps = 32) {
@@ -797,16 +830,31 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
     constexpr uint32_t NT = W * 32, SB = NT * E;
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     const uint32_t tg = threadIdx.x - w0 * 32, lane = tg & 31u, wg = tg >> 5;
+    auto xs = [&](uint32_t k) { return x[chain_slot<W, E, kSwz>(k)]; };
+    auto ws = [&](uint32_t k) { return w[chain_slot<W, E, kSwz>(k)]; };
     for (uint32_t base = 0; base < n; base += SB) {
         const uint32_t len = n - base < SB ? n - base : SB;
         uint32_t k0 = 0;
-        // the first steps change binade every few steps: run them plainly
+        // the first steps change binade every few steps: one thread runs
+        // them plainly
         const uint32_t early = base == 0 ? (len < early_steps ? len : early_steps) : 0u;
-        while (k0 < early || (k0 < len && !state_ok(acc))) {
-            acc = fma(x[base + k0], w[base + k0], acc);
-            ++k0;
+        if (early > 0 || !state_ok(acc)) {
+            if (tg == 0) {
+                while (k0 < early || (k0 < len && !state_ok(acc))) {
+                    acc = fma(xs(base + k0), ws(base + k0), acc);
+                    ++k0;
+                }
+                sc.early_acc = acc;
+                sc.early_k0 = k0;
+            }
+            group_bar(bar_id, NT);
+            acc = sc.early_acc;
+            k0 = sc.early_k0;
+            if (k0 >= len) {
+                group_bar(bar_id, NT);  // every thread has read the scratch
+                continue;
+            }
         }
-        if (k0 >= len) continue;
         uint32_t neg;
         uint64_t A0;
         int ea;
@@ -816,20 +864,20 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
             const uint32_t s = my0 + i;
-            tp[i] = (s >= k0 && s < len) ? pack(term(x[base + s], w[base + s], ea, neg)) : 0ull;
+            tp[i] = (s >= k0 && s < len) ? pack(term(xs(base + s), ws(base + s), ea, neg)) : 0ull;
         }
         if (kPredict && neg == 0) {
             // one pass over every binade of a positive run
             double a2;
             bool rewritten;
             const uint32_t done =
-                group_predicted_pass<W, E>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc, rewritten);
+                group_predicted_pass<W, E, kSwz>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc, rewritten);
             if (done > k0 || rewritten) {
                 acc = a2;
                 k0 = done;
                 if (k0 >= len) continue;
                 while (k0 < len && !state_ok(acc)) {
-                    acc = fma(x[base + k0], w[base + k0], acc);
+                    acc = fma(xs(base + k0), ws(base + k0), acc);
                     ++k0;
                 }
                 if (k0 >= len) continue;
@@ -841,7 +889,7 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
 #pragma unroll
                 for (uint32_t i = 0; i < E; ++i) {
                     const uint32_t s = my0 + i;
-                    tp[i] = (s >= k0 && s < len) ? pack(term(x[base + s], w[base + s], ea2, neg2)) : 0ull;
+                    tp[i] = (s >= k0 && s < len) ? pack(term(xs(base + s), ws(base + s), ea2, neg2)) : 0ull;
                 }
                 neg = neg2;
                 A0 = A2;
@@ -949,10 +997,10 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
             if (first_bad == bad) sc.a_bad = A_at_bad;
             group_bar(bar_id, NT);
             acc = state_join(neg, (uint64_t)sc.a_bad, ea);
-            acc = fma(x[base + bad], w[base + bad], acc);
+            acc = fma(xs(base + bad), ws(base + bad), acc);
             k0 = bad + 1;
             while (k0 < len && !state_ok(acc)) {
-                acc = fma(x[base + k0], w[base + k0], acc);
+                acc = fma(xs(base + k0), ws(base + k0), acc);
                 ++k0;
             }
             group_bar(bar_id, NT);  // every thread has read the scratch
@@ -972,7 +1020,7 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
                     shift_term(t, ea2 - ea);
                     tp[i] = pack(t);
                 } else {
-                    tp[i] = pack(term(x[base + s], w[base + s], ea2, neg2));
+                    tp[i] = pack(term(xs(base + s), ws(base + s), ea2, neg2));
                 }
             }
             neg = neg2;

@@ -503,28 +503,41 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
         const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
         __syncthreads();
         if (side < S) {
-            // all of this thread's loads in flight at once
-            constexpr uint32_t U = kNormStage / (kChainWarps * 32);
-            double vx[U], vw[U];
+            // this thread's steps tg*E .. tg*E+E-1 of the stage, all loads in
+            // flight at once, stored step-major (chain_slot order) so that
+            // the chain's threads read them without bank conflicts
+            constexpr uint32_t E = kChainSteps, NT = kChainWarps * 32;
+            double vx[E], vw[E];
+            const uint32_t k = tg * E;
+            if (k + E <= len) {
+                const double2* px = reinterpret_cast<const double2*>(x + k0 + k);
+                const double2* pw = reinterpret_cast<const double2*>(wts + k0 + k);
 #pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t k = tg + u * kChainWarps * 32;
-                vx[u] = k < len ? x[k0 + k] : 0.0;
-                vw[u] = k < len ? wts[k0 + k] : 0.0;
+                for (uint32_t u = 0; u < E / 2; ++u) {
+                    const double2 a = px[u], b = pw[u];
+                    vx[2 * u] = a.x;
+                    vx[2 * u + 1] = a.y;
+                    vw[2 * u] = b.x;
+                    vw[2 * u + 1] = b.y;
+                }
+            } else {
+#pragma unroll
+                for (uint32_t u = 0; u < E; ++u) {
+                    vx[u] = k + u < len ? x[k0 + k + u] : 0.0;
+                    vw[u] = k + u < len ? wts[k0 + k + u] : 0.0;
+                }
             }
 #pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t k = tg + u * kChainWarps * 32;
-                if (k < len) {
-                    s_x[k] = vx[u];
-                    s_w[k] = vw[u];
-                }
+            for (uint32_t u = 0; u < E; ++u) {
+                s_x[u * NT + tg] = vx[u];
+                s_w[u * NT + tg] = vw[u];
             }
         }
         __syncthreads();
         if (side < S)
-            sum = group_fma_chain<kChainWarps, kChainSteps>(s_x, s_w, len, sum, side * kChainWarps, 1 + (int)side,
-                                                            s_chain[side], k0 == 0 ? 32u : 0u);
+            sum = group_fma_chain<kChainWarps, kChainSteps, true, true>(s_x, s_w, len, sum, side * kChainWarps,
+                                                                        1 + (int)side, s_chain[side],
+                                                                        k0 == 0 ? 32u : 0u);
     }
     if (tg == 0 && side < S) s_sum[side] = sum;
     __syncthreads();
