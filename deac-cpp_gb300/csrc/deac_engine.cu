@@ -16,9 +16,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <string>
@@ -68,6 +70,14 @@ constexpr uint64_t kTrialSmemCapDoubles = 25600;  // 200 KB: trial genes + one r
 constexpr uint64_t kTailSlotsBytes = 4 * 1024 * 8;  // reduction slots of the finishing CTA
 
 uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+// smallest float >= |v| (infinity beyond the float range)
+float float_up(double v) {
+    v = std::fabs(v);
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
 
 struct Arena {
     uint64_t size = 0;
@@ -468,7 +478,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
         const uint64_t o_cnt = sa.take(3 * 8);
-        const uint64_t o_rcp = sa.take(P * 8), o_nb = sa.take(P), o_ie = sa.take(Nt * 8);
+        const uint64_t o_rcp = sa.take(P * 8), o_nb = sa.take(P), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
@@ -489,10 +499,20 @@ int upload_run(deac_batch* b, RunHost& r) {
         x.t_hi = reinterpret_cast<double*>(sb + o_th);
         x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
         {
+            // 1/sigma as the decisions use it, and float upper bounds for
+            // their error bounds
             std::vector<double> ie(Nt);
-            for (uint64_t t = 0; t < Nt; ++t) ie[t] = 1.0 / r.err[t];
+            std::vector<float> ief(Nt);
+            for (uint64_t t = 0; t < Nt; ++t) {
+                ie[t] = 1.0 / r.err[t];
+                ief[t] = float_up(ie[t]);
+            }
             CUDA_TRY(cudaMemcpy(sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(sb + o_ief, ief.data(), Nt * 4, cudaMemcpyHostToDevice));
             x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
+            x.inv_err_up = reinterpret_cast<const float*>(sb + o_ief);
+            x.inv_nt = 1.0 / (double)Nt;
+            x.inv_nt_up = float_up(x.inv_nt);
         }
         d.changed = x.changed;
         d.xexp = x.xexp;

@@ -145,6 +145,18 @@ __device__ __forceinline__ void dw_add(float& ah, float& al, float bh, float bl)
     fast_two_sum(vh, vl, ah, al);
 }
 
+// A float upper bound of |x| from integer operations alone (the FP64 pipe is
+// the scarce one): the leading 24 bits of |x| truncated, plus one unit in the
+// last place; 2^-126 below the float normal range, infinity above it (and
+// for NaN, which the FP64 part of the decision rejects on its own).
+__device__ __forceinline__ float f32_up(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    const int e = (int)(b >> 52) - 1023 + 127;
+    if (e >= 255) return __uint_as_float(0x7f800000u);
+    if (e <= 0) return 0x1p-126f;
+    return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
+}
+
 __device__ __forceinline__ float exp2_int(int n) {  // 2^n for -126 <= n <= 127
     return __uint_as_float((uint32_t)(n + 127) << 23);
 }
@@ -491,6 +503,7 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
 __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* runs, SplitRun* split) {
     grid_dependency_wait();
     __shared__ unsigned long long s_n[3];
+    __shared__ double s_fit[kDecideMaxMembers];
     RunDev& R = runs[blockIdx.x];
     if (R.done) return;
     SplitRun& X = split[blockIdx.x];
@@ -501,6 +514,9 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     // 1/sigma of each timeslice, formed once per run (a relative error of
     // 2^-53, covered below)
     const double* inv_err = X.inv_err;
+    const float* inv_err_up = X.inv_err_up;
+    // each member's fitness after the decision (the minimum below)
+    for (uint32_t m = threadIdx.x; m < P && m < kDecideMaxMembers; m += blockDim.x) s_fit[m] = R.fit_old[m];
     __syncthreads();
     for (uint32_t i = warp; i < P; i += nw) {
         const bool changed = X.changed[i] != 0;
@@ -533,13 +549,17 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
         // for the product's rounding.
         const bool defer = (R.flags & kDeferNorm) != 0;
         const double rc = defer ? R.recip[i] : 1.0;
-        // chi^2 in FP64; its error bound in FP32 rounded upward (every term
-        // is non-negative, so each rounding up keeps an upper bound)
-        double chi = 0.0;
+        const float rc_up = f32_up(rc);
+        // chi^2 in FP64 (four timeslices per lane in flight, one sum each);
+        // its error bound in FP32 rounded upward (every term is
+        // non-negative, so each rounding up keeps an upper bound), the FP32
+        // operands taken as upper bounds by integer operations
+        double chi4[4] = {0.0, 0.0, 0.0, 0.0};
         float dchi = 0.0f;
         constexpr uint32_t U = 4;  // timeslices per lane in flight
         for (uint32_t t0 = lane; t0 < Nt; t0 += 32 * U) {
             double em[U], eb0[U], f[U], ie[U];
+            float ief[U];
 #pragma unroll
             for (uint32_t u = 0; u < U; ++u) {
                 const uint32_t t = t0 + 32 * u;
@@ -549,31 +569,34 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
                 eb0[u] = ok ? X.e_bound[o] : 0.0;
                 f[u] = ok ? R.isf[t] : 0.0;
                 ie[u] = ok ? inv_err[t] : 0.0;
+                ief[u] = ok ? inv_err_up[t] : 0.0f;
             }
 #pragma unroll
             for (uint32_t u = 0; u < U; ++u) {
                 const double e = defer ? em[u] * rc : em[u];
                 // r carries up to three roundings of 2^-53 each
                 const double r = (f[u] - e) * ie[u];
-                chi = fma(r, r, chi);
-                const float ar = __double2float_ru(fabs(r));
-                const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, __double2float_ru(eb0[u])),
-                                                             __double2float_ru(fabs(rc))),
-                                                   __fmul_ru(__double2float_ru(fabs(e)), 0x1.0p-51f))
-                                       : __double2float_ru(eb0[u]);
-                const float dr = __fadd_ru(__fmul_ru(__fmul_ru(eb, __double2float_ru(ie[u])), 1.0f + 0x1.0p-20f),
+                chi4[u] = fma(r, r, chi4[u]);
+                const float ar = f32_up(r);
+                const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up(eb0[u])), rc_up),
+                                                   __fmul_ru(f32_up(e), 0x1.0p-51f))
+                                       : f32_up(eb0[u]);
+                const float dr = __fadd_ru(__fmul_ru(__fmul_ru(eb, ief[u]), 1.0f + 0x1.0p-20f),
                                            __fmul_ru(ar, 0x1.0p-51f));
                 dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
             }
         }
+        double chi = (chi4[0] + chi4[1]) + (chi4[2] + chi4[3]);
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
             dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
         }
         if (lane != 0) continue;
         X.recheck[i] = 0;
-        chi /= (double)Nt;
-        const double dchi_d = (double)dchi / (double)Nt * (1.0 + 0x1.0p-40) + chi * (double)(Nt + 8) * 0x1.0p-52;
+        // /Nt as a product with 1/Nt rounded once: two roundings where a
+        // quotient has one, covered by two more units of the slack below
+        chi *= X.inv_nt;
+        const double dchi_d = (double)__fmul_ru(dchi, X.inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
         const double lo = chi - dchi_d, hi = chi + dchi_d;
         X.t_lo[i] = lo;
         X.t_hi[i] = hi;
@@ -588,6 +611,7 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
             X.f_lo[i] = lo;
             X.f_hi[i] = hi;
             R.fit_old[i] = 0.5 * (lo + hi);
+            if (i < kDecideMaxMembers) s_fit[i] = 0.5 * (lo + hi);
             for (uint32_t s = 0; s < S; ++s) {
                 R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
                 R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
@@ -621,9 +645,15 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
             if (ii + 2 <= R.N) {
                 // the minimum fitness, by a warp (the minimum of finite
                 // values does not depend on the order)
-                const volatile double* f = R.fit_old;
-                double mn = f[0];
-                for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
+                double mn;
+                if (P <= kDecideMaxMembers) {
+                    mn = s_fit[0];
+                    for (uint32_t m = lane; m < P; m += 32) mn = s_fit[m] < mn ? s_fit[m] : mn;
+                } else {
+                    const volatile double* f = R.fit_old;
+                    mn = f[0];
+                    for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
+                }
                 for (int o = 16; o > 0; o >>= 1) {
                     const double v = __shfl_xor_sync(0xffffffffu, mn, o);
                     mn = v < mn ? v : mn;

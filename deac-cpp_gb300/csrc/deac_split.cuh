@@ -44,6 +44,7 @@ constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
 constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
 constexpr int kDecideThreads = 512;
+constexpr uint32_t kDecideMaxMembers = 128;  // fitness values kept in shared memory
 // dynamic shared memory of split_contract_kernel for S sides: K digits
 // [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and the two bound
 // operands (128 x 16, 64 x 16)
@@ -74,6 +75,9 @@ struct SplitRun {
     unsigned long long* counts;  // [3]: trials equal to the parent, settled by
                                  // the interval, settled by the exact FP64 value
     const double* inv_err;  // [Nt] 1/sigma, rounded once
+    const float* inv_err_up;  // [Nt] float upper bounds of inv_err
+    double inv_nt;            // 1/Nt, rounded once
+    float inv_nt_up;          // a float upper bound of 1/Nt
 };
 
 // One output tile: up to 64 (run, member) rows sharing one K, x 128
