@@ -257,8 +257,12 @@ inline uint64_t host_predicted_pass(const double* x, const double* w, const uint
                                     uint64_t len, uint64_t A0, int ea, double* acc) {
     using namespace chain_detail;
     const uint64_t n = len - k0;
-    for (uint64_t i = 0; i < n; ++i)
+    uint64_t ftot = 0;
+    for (uint64_t i = 0; i < n; ++i) {
         if (unpack(tp[k0 + i]).flags & (kNeg | kBad)) return k0;  // not a positive run: no prediction
+        ftot += unpack(tp[k0 + i]).F;  // each below 2^54: the total is checked before it can overflow
+        if (ftot >= (1ull << 60)) return k0;  // every prefix stays below 2^61
+    }
     std::vector<uint32_t> cross(n), seg(n);
     std::vector<int> ds(n), dk(n);
     // predicted binade (relative to ea) of the state before each step and of
@@ -447,6 +451,7 @@ inline double host_group_fma_chain(const double* x, const double* w, uint64_t n,
 #ifdef __CUDACC__
 // Scratch of one warp group running group_fma_chain (shared memory).
 constexpr uint32_t kMaxCross = 64;  // binade crossings one predicted pass handles
+constexpr int kMaxPredictedPasses = 4;  // per super-block, before the rounds take over
 constexpr uint32_t kChainMaxWarps = 16;
 struct ChainScratch {
     uint32_t map_a[kChainMaxWarps], map_b[kChainMaxWarps];  // per-warp parity maps
@@ -574,21 +579,54 @@ __device__ __forceinline__ uint32_t chain_slot(uint32_t k) {
 
 // The predicted pass of host_predicted_pass, by the W warps of a group, each
 // thread over its E cached terms tp (steps tg*E + i of the super-block, the
-// ones before k0 and from len on are zero).  Returns the position reached
-// and the state there in acc (uniform over the group).
+// ones before k0 and from len_all on are zero).  It covers the steps before
+// the first one whose term it cannot place: a negative term, or one beyond
+// the grid (at least 2^54 units: a sure binade change, `at_bad` when the pass
+// stops there).  Returns the position reached and the state there in acc
+// (uniform over the group).
 template <int W, int E, bool kSwz>
 __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const double* w, uint64_t (&tp)[E],
-                                                          uint32_t k0, uint32_t len, uint64_t A0, int ea,
+                                                          uint32_t k0, uint32_t len_all, uint64_t A0, int ea,
                                                           double& acc, uint32_t tg, int bar_id, ChainScratch& sc,
-                                                          bool& rewritten) {
+                                                          bool& rewritten, bool& at_bad) {
     using namespace chain_detail;
     rewritten = false;
+    at_bad = false;
+    acc = state_join(0, A0, ea);
     constexpr uint32_t NT = W * 32;
     static_assert(W <= (int)kChainMaxWarps, "group larger than its scratch");
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     const uint32_t lane = tg & 31u, wg = tg >> 5, my0 = tg * E;
+    // --- the first unplaceable step (position * 2 + 1 when negative)
+    uint32_t key = kNone;
+#pragma unroll
+    for (uint32_t i = 0; i < E; ++i) {
+        const uint32_t f = unpack(tp[i]).flags;
+        if (key == kNone && (f & (kNeg | kBad))) key = ((my0 + i) << 1) | ((f & kNeg) ? 1u : 0u);
+    }
+    key = __reduce_min_sync(0xffffffffu, key);
+    if (lane == 0) sc.bad[wg] = key;
+    group_bar(bar_id, NT);
+    for (uint32_t k = 0; k < (uint32_t)W; ++k) key = sc.bad[k] < key ? sc.bad[k] : key;
+    const uint32_t len = key == kNone ? len_all : key >> 1;
+    const bool stop_bad = key != kNone && !(key & 1u);
+    if (len <= k0) {
+        at_bad = stop_bad;
+        group_bar(bar_id, NT);  // the scratch is reused next
+        return k0;
+    }
+    if (key != kNone) {
+        // the steps from the unplaceable one on are not this pass's
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i)
+            if (my0 + i >= len) tp[i] = 0ull;
+        rewritten = true;
+    }
     // --- prefix of the integer parts; is the run all positive and moderate?
-    // (each thread's part below 2^52 keeps every prefix below 2^61)
+    // Every F is below 2^54, so a thread's part is below 2^57 and a warp's
+    // below 2^62 (no overflow); warp totals below 2^57 keep every prefix of
+    // the group below 2^61.  (A run that grows several-fold within a few
+    // steps -- the first steps of a peak -- stays predictable.)
     long long fsum = 0;
     uint32_t badf = 0;
 #pragma unroll
@@ -597,7 +635,6 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         fsum += (long long)t.F;
         badf |= t.flags & (kNeg | kBad);
     }
-    badf |= fsum >= (1ll << 52) ? 1u : 0u;
     long long finc = fsum;
 #pragma unroll
     for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -607,7 +644,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     const uint32_t wbad = __any_sync(0xffffffffu, badf != 0);
     if (lane == 31) {
         sc.sum[wg] = finc;
-        sc.flag[wg] = wbad;
+        sc.flag[wg] = wbad | (finc >= (1ll << 57) ? 1u : 0u);
     }
     group_bar(bar_id, NT);
     long long fbefore = 0;
@@ -761,6 +798,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     const uint32_t fail = sc.pass_fail;
     if (sc.pass_ranged) {
         acc = sc.pass_acc;
+        at_bad = stop_bad && fail == len;
         return fail;
     }
 
@@ -811,6 +849,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         return bad;
     }
     acc = sc.pass_acc;
+    at_bad = stop_bad && fail == len;
     return fail;
 }
 
@@ -866,36 +905,34 @@ __device__ __forceinline__ double group_fma_chain(const double* x, const double*
             const uint32_t s = my0 + i;
             tp[i] = (s >= k0 && s < len) ? pack(term(xs(base + s), ws(base + s), ea, neg)) : 0ull;
         }
-        if (kPredict && neg == 0) {
-            // one pass over every binade of a positive run
+        // predicted passes over the binades of a positive run, each up to
+        // the next term beyond its grid (run plainly: a sure binade change)
+        for (int pass = 0; kPredict && neg == 0 && pass < kMaxPredictedPasses; ++pass) {
             double a2;
-            bool rewritten;
-            const uint32_t done =
-                group_predicted_pass<W, E, kSwz>(x + base, w + base, tp, k0, len, A0, ea, a2, tg, bar_id, sc, rewritten);
-            if (done > k0 || rewritten) {
-                acc = a2;
-                k0 = done;
-                if (k0 >= len) continue;
-                while (k0 < len && !state_ok(acc)) {
-                    acc = fma(xs(base + k0), ws(base + k0), acc);
-                    ++k0;
-                }
-                if (k0 >= len) continue;
-                uint32_t neg2;
-                uint64_t A2;
-                int ea2;
-                state_split(acc, neg2, A2, ea2);
-                // the pass left terms of several grids: decode the rest again
+            bool rewritten, at_bad;
+            const uint32_t done = group_predicted_pass<W, E, kSwz>(x + base, w + base, tp, k0, len, A0, ea, a2, tg,
+                                                                   bar_id, sc, rewritten, at_bad);
+            if (!(done > k0 || rewritten || at_bad)) break;  // no progress: the rounds below
+            acc = a2;
+            k0 = done;
+            if (at_bad) {
+                acc = fma(xs(base + k0), ws(base + k0), acc);
+                ++k0;
+            }
+            while (k0 < len && !state_ok(acc)) {
+                acc = fma(xs(base + k0), ws(base + k0), acc);
+                ++k0;
+            }
+            if (k0 >= len) break;
+            // the pass left terms of several grids: decode the rest again
+            state_split(acc, neg, A0, ea);
 #pragma unroll
-                for (uint32_t i = 0; i < E; ++i) {
-                    const uint32_t s = my0 + i;
-                    tp[i] = (s >= k0 && s < len) ? pack(term(xs(base + s), ws(base + s), ea2, neg2)) : 0ull;
-                }
-                neg = neg2;
-                A0 = A2;
-                ea = ea2;
+            for (uint32_t i = 0; i < E; ++i) {
+                const uint32_t s = my0 + i;
+                tp[i] = (s >= k0 && s < len) ? pack(term(xs(base + s), ws(base + s), ea, neg)) : 0ull;
             }
         }
+        if (k0 >= len) continue;
         for (;;) {
             // --- parity maps: par' = (a & par) ^ b; steps before k0 are identity
             uint32_t pa = 1u, pb = 0u;

@@ -250,7 +250,9 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
            static_cast<const deac::SplitWork*>(b->d_split_work), static_cast<const deac::SplitRow*>(b->d_rows),
            static_cast<const CUtensorMap*>(b->d_maps), b->d_partial, b->d_status);
     if ((rc = mark(3))) return rc;
-    launch(deac::split_combine_kernel, b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s, early, b->d_runs,
+    // not scheduled early: its waiting CTAs would hold the SMs that the
+    // normalisation row sums need
+    launch(deac::split_combine_kernel, b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s, early && !fork, b->d_runs,
            b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
            static_cast<const float4*>(b->d_partial));
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
