@@ -439,6 +439,7 @@ int upload_run(deac_batch* b, RunHost& r) {
     d.contract_ctas = member_tiles * tau_tiles;
     d.N = N;
     d.tau_cr = r.cfg.self_adapting_crossover_probability;
+    d.p_magic = ~0ull / P;
     d.tau_f = r.cfg.self_adapting_differential_weight_probability;
     d.alpha = 1.0 / m.zeroth_moment;
     d.stop = r.cfg.stop_minimum_fitness;

@@ -128,15 +128,27 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
 // CR(-) slot 2, F(-) slot 3; then the mutant indices on slot 0
 // (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.  Stores
 // the new CR and F and the four slots' states; returns CR, F and the indices.
+// x % P for the 64-bit draws of the mutant indices: q = floor(x * m / 2^64)
+// with m = floor((2^64 - 1) / P) is at most two below floor(x / P), so two
+// corrections give the exact remainder (no 64-bit division routine).
+__device__ __forceinline__ uint64_t mod_p(uint64_t x, uint64_t P, uint64_t m) {
+    uint64_t r = x - __umul64hi(x, m) * P;
+    if (r >= P) r -= P;
+    if (r >= P) r -= P;
+    return r;
+}
+
+// jDE of member i (the self-adaptation of CR and F per side, then three
+// distinct mutant indices by rejection sampling) from RNG slots base ..
+// base+2S-1: slot base (CR of side 0, then the mutant indices), base+1 (F of
+// side 0), base+2 / base+3 (CR / F of side 1).  Every load is issued before
+// the first store; the stores overlap none of them.
 __device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[2], double fw_new[2],
                                            uint32_t mut[3]) {
     const uint32_t P = R.P, M = R.M, S = R.S;
     const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
     const uint64_t n = R.n_states;
     const uint64_t* rng = R.rng;
-    // every load is issued before the first store: slot base (CR of side 0,
-    // then the mutant indices), base+1 (F of side 0), base+2 / base+3 (CR / F
-    // of side 1); the stores below overlap none of them
     uint64_t st[4][4];
 #pragma unroll
     for (uint32_t q = 0; q < 4; ++q)
@@ -160,9 +172,10 @@ __device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[
     // rejection sampling as in the reference; P >= 4 is enforced on the
     // host, so every loop has an admissible outcome
     uint64_t r0 = i, r1 = i, r2 = i;
-    while (r0 == i) r0 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
-    while (r1 == i || r1 == r0) r1 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
-    while (r2 == i || r2 == r0 || r2 == r1) r2 = xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]) % P;
+    const uint64_t pm = R.p_magic;
+    while (r0 == i) r0 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
+    while (r1 == i || r1 == r0) r1 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
+    while (r2 == i || r2 == r0 || r2 == r1) r2 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
 #pragma unroll
     for (uint32_t s = 0; s < 2; ++s)
         if (s < S) {

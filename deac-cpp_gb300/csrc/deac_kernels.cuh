@@ -56,6 +56,7 @@ struct RunDev {
     uint32_t chunk;          // genes per shared-memory stage of contract_kernel
     uint64_t N;              // number_of_generations
     double tau_cr, tau_f;    // self-adaptation probabilities
+    uint64_t p_magic;        // floor((2^64 - 1) / P): x % P without a 64-bit division
     double alpha;            // 1 / F(0), the normalisation scale
     double stop;             // stop_minimum_fitness
     double first_target, third_target, third_error;
