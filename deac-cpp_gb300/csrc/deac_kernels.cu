@@ -567,42 +567,41 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // times 1/norm, as trial_kernel does.  One CTA per trial.
 __global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* work) {
     grid_dependency_wait();
-    __shared__ uint32_t s_buf;
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
     if (!(R.flags & kDeferNorm)) return;
     const uint32_t i = wk.index;
-    // the request is consumed: later launches (a finished run's included,
-    // whose decide_kernel no longer runs) find none
-    if (threadIdx.x == 0) {
-        s_buf = R.norm_buf[i];
-        R.norm_buf[i] = 0xFFu;
-    }
-    __syncthreads();
-    const uint32_t b = s_buf;
+    // every thread reads the request and the factor (one round trip)
+    const uint32_t b = R.norm_buf[i];
+    const double recip = R.recip[i];
     if (b == 0xFFu) return;
     const uint32_t M = R.M, S = R.S;
     const uint64_t PM = (uint64_t)R.P * M;
-    const double recip = R.recip[i];
-    // eight genes in flight per thread
+    // pairs of genes (M is a multiple of the 32-gene chunk), sixteen genes
+    // in flight per thread
+    const uint32_t half = M / 2, pairs = S * half;
     constexpr uint32_t U = 8;
-    for (uint64_t q0 = threadIdx.x; q0 < (uint64_t)S * M; q0 += (uint64_t)U * blockDim.x) {
-        double* g[U];
-        double v[U];
+    for (uint32_t q0 = threadIdx.x; q0 < pairs; q0 += U * blockDim.x) {
+        double2* g[U];
+        double2 v[U];
 #pragma unroll
         for (uint32_t u = 0; u < U; ++u) {
-            const uint64_t q = q0 + (uint64_t)u * blockDim.x;
+            const uint32_t q = q0 + u * blockDim.x;
             g[u] = nullptr;
-            if (q < (uint64_t)S * M) {
-                const uint32_t s = (uint32_t)(q / M);
-                g[u] = R.pop + ((uint64_t)b * S + s) * PM + (uint64_t)i * M + (q - (uint64_t)s * M);
+            if (q < pairs) {
+                const uint32_t s = q / half;
+                g[u] = reinterpret_cast<double2*>(R.pop + ((uint64_t)b * S + s) * PM + (uint64_t)i * M) + (q - s * half);
                 v[u] = *g[u];
             }
         }
 #pragma unroll
         for (uint32_t u = 0; u < U; ++u)
-            if (g[u]) *g[u] = v[u] * recip;
+            if (g[u]) *g[u] = make_double2(v[u].x * recip, v[u].y * recip);
     }
+    // the request is consumed: later launches (a finished run's included,
+    // whose decide kernel no longer runs) find none
+    __syncthreads();
+    if (threadIdx.x == 0) R.norm_buf[i] = 0xFFu;
 }
 
 // ------------------------------------------------------------- contract
