@@ -46,6 +46,7 @@ struct Term {
     uint32_t flags;    // kGtHalf | kTie | kGtZero | kNeg | kBad
 };
 constexpr uint32_t kGtHalf = 1u, kTie = 2u, kGtZero = 4u, kNeg = 8u, kBad = 16u;
+constexpr uint32_t kBig = 32u;  // with kBad: finite, but 2^54 or more on this grid
 
 // A term packed in one word (F < 2^54 in the low bits, the flags above) to
 // keep the per-thread caches of the group form in registers.
@@ -126,7 +127,7 @@ __host__ __device__ __forceinline__ Term term(double x, double w, int ea, uint32
     uint32_t half = 0, sticky = 0;
     if (sh >= 0) {
         if (sh >= 54 || hi != 0 || (lo >> (54 - sh)) != 0) {
-            t.flags = kBad;  // |v| >= 2^54: leaves the binade for sure
+            t.flags = kBad | kBig;  // |v| >= 2^54: leaves the binade for sure
             return t;
         }
         t.F = lo << sh;
@@ -145,7 +146,7 @@ __host__ __device__ __forceinline__ Term term(double x, double w, int ea, uint32
                 fh = 0;
             }
             if (fh != 0 || (fl >> 54) != 0) {
-                t.flags = kBad;
+                t.flags = kBad | kBig;
                 return t;
             }
             t.F = fl;
@@ -569,6 +570,13 @@ __device__ __forceinline__ int rel_binade(uint64_t v) {
 
 }  // namespace chain_detail
 
+// A term decoded on the grid 2^e of a positive state, out of line: the
+// predicted pass calls it only for the rare terms beyond its start grid, and
+// one copy keeps the unrolled loops small.
+static __device__ __noinline__ uint64_t packed_term(double x, double w, int e) {
+    return chain_detail::pack(chain_detail::term(x, w, e, 0));
+}
+
 // Position of step k in x and w: the plain order, or (kSwz) one super-block
 // stored step-major per thread -- step t*E + i at i*(W*32) + t -- so that the
 // group's threads read their E steps from consecutive addresses.
@@ -597,71 +605,97 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     static_assert(W <= (int)kChainMaxWarps, "group larger than its scratch");
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     const uint32_t lane = tg & 31u, wg = tg >> 5, my0 = tg * E;
-    // --- the first unplaceable step (position * 2 + 1 when negative)
-    uint32_t key = kNone;
+    // A term beyond the start grid (kBig: a state that grows several-fold
+    // within the super-block, a peak after small first steps) is placed on a
+    // grid 2^kCoarse coarser -- its F there, times 2^kCoarse, stands in for
+    // the prefix -- and decoded again on its predicted binade's grid below.
+    // A first attempt keeps such terms; if the prefixes outgrow their budget
+    // a second one ends the pass at the first of them.
+    constexpr int kCoarse = 8;
+    uint32_t len = len_all;
+    bool stop_bad = false;
+    uint64_t pstart = 0;
+    for (int attempt = 0;; ++attempt) {
+        // --- the first unplaceable step (position * 2 + 1 when negative)
+        uint32_t key = kNone;
 #pragma unroll
-    for (uint32_t i = 0; i < E; ++i) {
-        const uint32_t f = unpack(tp[i]).flags;
-        if (key == kNone && (f & (kNeg | kBad))) key = ((my0 + i) << 1) | ((f & kNeg) ? 1u : 0u);
+        for (uint32_t i = 0; i < E; ++i) {
+            const uint32_t s = my0 + i;
+            Term t = unpack(tp[i]);
+            if (key != kNone || s < k0 || s >= len_all) continue;
+            if (attempt == 0 && (t.flags & kBig)) {
+                const uint32_t q = chain_slot<W, E, kSwz>(s);
+                t = unpack(packed_term(x[q], w[q], ea + kCoarse));
+                if (!(t.flags & (kNeg | kBad)) && t.F < (1ull << (57 - kCoarse))) {
+                    tp[i] = pack(Term{t.F, kBad | kBig});  // F on the coarse grid
+                    continue;
+                }
+            }
+            if (t.flags & (kNeg | kBad)) key = (s << 1) | ((t.flags & kNeg) ? 1u : 0u);
+        }
+        key = __reduce_min_sync(0xffffffffu, key);
+        if (lane == 0) sc.bad[wg] = key;
+        group_bar(bar_id, NT);
+        for (uint32_t k = 0; k < (uint32_t)W; ++k) key = sc.bad[k] < key ? sc.bad[k] : key;
+        len = key == kNone ? len_all : key >> 1;
+        stop_bad = key != kNone && !(key & 1u);
+        if (len <= k0) {
+            at_bad = stop_bad;
+            group_bar(bar_id, NT);  // the scratch is reused next
+            return k0;
+        }
+        // --- prefix of the integer parts up to len.  Every F below len is
+        // under 2^57 (coarse ones scaled), a thread's part is clamped there
+        // and a warp's stays below 2^62; warp totals below 2^57 keep every
+        // prefix of the group below 2^61.
+        long long fsum = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            const Term t = unpack(tp[i]);
+            if (my0 + i < len) fsum += (long long)((t.flags & kBig) ? t.F << kCoarse : t.F);
+        }
+        fsum = fsum < (1ll << 57) ? fsum : (1ll << 57);
+        long long finc = fsum;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const long long v = __shfl_up_sync(0xffffffffu, finc, o);
+            if (lane >= o) finc += v;
+        }
+        if (lane == 31) {
+            sc.sum[wg] = finc;
+            sc.flag[wg] = finc >= (1ll << 57) ? 1u : 0u;
+        }
+        group_bar(bar_id, NT);
+        long long fbefore = 0;
+        uint32_t anybad = 0;
+        for (uint32_t k = 0; k < (uint32_t)W; ++k) {
+            if (k < wg) fbefore += sc.sum[k];
+            anybad |= sc.flag[k];
+        }
+        group_bar(bar_id, NT);
+        if (!anybad) {
+            pstart = A0 + (uint64_t)(fbefore + finc - fsum);
+            break;
+        }
+        if (attempt == 1) return k0;
+        // the second attempt: decode the coarse terms on the start grid again
+        // (beyond it: they end the pass)
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i)
+            if (unpack(tp[i]).flags & kBig) tp[i] = pack(Term{0ull, kBad | kBig});
     }
-    key = __reduce_min_sync(0xffffffffu, key);
-    if (lane == 0) sc.bad[wg] = key;
-    group_bar(bar_id, NT);
-    for (uint32_t k = 0; k < (uint32_t)W; ++k) key = sc.bad[k] < key ? sc.bad[k] : key;
-    const uint32_t len = key == kNone ? len_all : key >> 1;
-    const bool stop_bad = key != kNone && !(key & 1u);
-    if (len <= k0) {
-        at_bad = stop_bad;
-        group_bar(bar_id, NT);  // the scratch is reused next
-        return k0;
-    }
-    if (key != kNone) {
+    rewritten = true;
+    if (len < len_all) {
         // the steps from the unplaceable one on are not this pass's
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i)
             if (my0 + i >= len) tp[i] = 0ull;
-        rewritten = true;
     }
-    // --- prefix of the integer parts; is the run all positive and moderate?
-    // Every F is below 2^54, so a thread's part is below 2^57 and a warp's
-    // below 2^62 (no overflow); warp totals below 2^57 keep every prefix of
-    // the group below 2^61.  (A run that grows several-fold within a few
-    // steps -- the first steps of a peak -- stays predictable.)
-    long long fsum = 0;
-    uint32_t badf = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < E; ++i) {
-        const Term t = unpack(tp[i]);
-        fsum += (long long)t.F;
-        badf |= t.flags & (kNeg | kBad);
-    }
-    long long finc = fsum;
-#pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        const long long v = __shfl_up_sync(0xffffffffu, finc, o);
-        if (lane >= o) finc += v;
-    }
-    const uint32_t wbad = __any_sync(0xffffffffu, badf != 0);
-    if (lane == 31) {
-        sc.sum[wg] = finc;
-        sc.flag[wg] = wbad | (finc >= (1ll << 57) ? 1u : 0u);
-    }
-    group_bar(bar_id, NT);
-    long long fbefore = 0;
-    uint32_t anybad = 0;
-    for (uint32_t k = 0; k < (uint32_t)W; ++k) {
-        if (k < wg) fbefore += sc.sum[k];
-        anybad |= sc.flag[k];
-    }
-    group_bar(bar_id, NT);
-    if (anybad) return k0;
-    const uint64_t pstart = A0 + (uint64_t)(fbefore + finc - fsum);
 
     // --- crossings (a step whose exact sum lies in a higher binade than its
     // state) and the parity maps of the segments between them
     // From here on tp[i] holds the step's term in the grid of its predicted
     // binade (a crossing step keeps its binade after the crossing in cbin_of)
-    rewritten = true;
     uint32_t cross_bits = 0;
     int cbin_of[E];
     SegMap magg{0u, 1u, 0u};
@@ -671,17 +705,28 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         for (uint32_t i = 0; i < E; ++i) {
             Term t = unpack(tp[i]);
             const uint32_t s = my0 + i;
-            const uint64_t T = prefix + t.F + ((t.flags & kGtZero) ? 1u : 0u);
+            const bool big = (t.flags & kBig) != 0;
+            const uint64_t F = big ? t.F << kCoarse : t.F;
+            const uint64_t T = prefix + F + ((t.flags & kGtZero) ? 1u : 0u);
             const int ds = rel_binade(prefix), dk = rel_binade(T);
-            const bool cr = s >= k0 && s < len && dk > ds;
+            bool cr = s >= k0 && s < len && dk > ds;
+            bool on_grid = false;  // t already on the grid of binade ds
+            if (big && !cr && s >= k0 && s < len) {
+                // the coarse term on its own step's grid (a step still beyond
+                // it certainly changes binade: a crossing, run plainly)
+                const uint32_t q = chain_slot<W, E, kSwz>(s);
+                t = unpack(packed_term(x[q], w[q], ea + ds));
+                if (t.flags & (kNeg | kBad)) cr = true;
+                on_grid = true;
+            }
             cross_bits |= (cr ? 1u : 0u) << i;
             cbin_of[i] = dk;
-            prefix += t.F;
+            prefix += F;
             if (cr) {
                 magg = seg_combine(magg, SegMap{1u, 1u, 0u});
                 tp[i] = 0ull;
             } else {
-                shift_term(t, ds);
+                if (!on_grid) shift_term(t, ds);
                 tp[i] = pack(t);
                 magg = seg_combine(magg, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
             }

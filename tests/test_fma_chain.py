@@ -56,6 +56,15 @@ def _chains(kind, n, count, rng):
         elif kind == 8:  # positive, few significant bits: ties inside predicted binades
             a = np.ldexp(rng.integers(1, 65, n).astype(float), rng.integers(-4, 4, n))
             b = np.ldexp(rng.integers(1, 17, n).astype(float), rng.integers(-3, 3, n))
+        elif kind == 9:  # a peak after tiny first steps: terms far beyond the first states' grid
+            centre, width = rng.uniform(n / 8, n / 2), max(2.0, n / 16)
+            a = np.exp(-((k - centre) / width) ** 2) * (1.0 + 0.3 * u)
+            b = np.full(n, 0.125)
+        elif kind == 10:  # positive with rare spikes of 2^10 .. 2^60
+            a = u.copy()
+            spikes = rng.random(n) < 0.01
+            a[spikes] *= np.ldexp(1.0, rng.integers(10, 61, int(spikes.sum())))
+            b = np.full(n, 0.125)
         else:  # random sign and scale
             a = (u - 0.5) * np.ldexp(1.0, rng.integers(-30, 30, n))
             b = (v - 0.25) * np.ldexp(1.0, rng.integers(-30, 30, n))
@@ -72,7 +81,7 @@ def test_warp_chain_matches_sequential_fma(engine, n):
     fn.restype = ctypes.c_int
     fn.argtypes = [dp, dp, ctypes.c_uint64, dp, ctypes.c_uint32, dp, dp]
     rng = np.random.default_rng(n)
-    for kind in range(9):
+    for kind in range(11):
         x, w, start = _chains(kind, n, 48, rng)
         fast = np.zeros(len(start))
         plain = np.zeros(len(start))
