@@ -472,6 +472,7 @@ struct ChainScratch {
     uint32_t fail_pos;
     int32_t fail_bin;
     // results of the group's one-thread sequential parts
+    uint32_t grow[kChainMaxWarps];  // per warp: a term too large for the unit prefix
     double early_acc;      // state after the plain first steps
     uint32_t early_k0;     // steps done plainly
     double pass_acc;       // state where the predicted pass stopped
@@ -563,8 +564,8 @@ __device__ __forceinline__ SegSum group_scan(SegSum v, uint32_t lane, uint32_t w
 }
 
 // binade (relative to the pass's grid) of an integer multiple of the grid
-__device__ __forceinline__ int rel_binade(uint64_t v) {
-    const int b = 64 - __clzll((long long)v);
+__device__ __forceinline__ int rel_binade(uint64_t v, int c = 0) {  // v in units of 2^c of the grid
+    const int b = 64 - __clzll((long long)v) + c;
     return b - 53 > 0 ? b - 53 : 0;
 }
 
@@ -605,38 +606,60 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     static_assert(W <= (int)kChainMaxWarps, "group larger than its scratch");
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     const uint32_t lane = tg & 31u, wg = tg >> 5, my0 = tg * E;
-    // A term beyond the start grid (kBig: a state that grows several-fold
-    // within the super-block, a peak after small first steps) is placed on a
-    // grid 2^kCoarse coarser -- its F there, times 2^kCoarse, stands in for
+    // The prefix predicts binades only, in units of 2^c of the start grid
+    // (its error near a binade edge is caught by the checks below).  A term
+    // beyond the start grid (kBig: a state that grows several-fold within
+    // the super-block, a peak after small first steps) is placed on the grid
+    // 2^(c + kCoarse) -- its F there, times 2^kCoarse, stands in for it in
     // the prefix -- and decoded again on its predicted binade's grid below.
-    // A first attempt keeps such terms; if the prefixes outgrow their budget
-    // a second one ends the pass at the first of them.
-    constexpr int kCoarse = 8;
+    // Attempts: units 1, then 2^16 when the prefixes outgrow their budget
+    // (a growth beyond 2^8, or one term beyond it), then the old rule: the
+    // pass ends at the first term beyond the start grid.
+    constexpr int kCoarse = 8, kUnitStep = 16;
     uint32_t len = len_all;
     bool stop_bad = false;
     uint64_t pstart = 0;
+    int c = 0;  // prefix units 2^c
     for (int attempt = 0;; ++attempt) {
+        c = attempt == 1 ? kUnitStep : 0;
         // --- the first unplaceable step (position * 2 + 1 when negative)
-        uint32_t key = kNone;
+        uint32_t key = kNone, grow = 0;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
             const uint32_t s = my0 + i;
             Term t = unpack(tp[i]);
             if (key != kNone || s < k0 || s >= len_all) continue;
-            if (attempt == 0 && (t.flags & kBig)) {
+            if (attempt < 2 && (t.flags & kBig)) {
                 const uint32_t q = chain_slot<W, E, kSwz>(s);
-                t = unpack(packed_term(x[q], w[q], ea + kCoarse));
+                t = unpack(packed_term(x[q], w[q], ea + c + kCoarse));
                 if (!(t.flags & (kNeg | kBad)) && t.F < (1ull << (57 - kCoarse))) {
                     tp[i] = pack(Term{t.F, kBad | kBig});  // F on the coarse grid
                     continue;
                 }
+                if (attempt == 0 && !(t.flags & kNeg) && (!(t.flags & kBad) || (t.flags & kBig))) {
+                    grow = 1u;  // beyond the unit prefix's budget: coarser units
+                    continue;
+                }
+                key = (s << 1) | ((t.flags & kNeg) ? 1u : 0u);  // beyond the coarse budget too
+                continue;
             }
             if (t.flags & (kNeg | kBad)) key = (s << 1) | ((t.flags & kNeg) ? 1u : 0u);
         }
         key = __reduce_min_sync(0xffffffffu, key);
-        if (lane == 0) sc.bad[wg] = key;
+        grow = __any_sync(0xffffffffu, grow != 0);
+        if (lane == 0) {
+            sc.bad[wg] = key;
+            sc.grow[wg] = grow;
+        }
         group_bar(bar_id, NT);
-        for (uint32_t k = 0; k < (uint32_t)W; ++k) key = sc.bad[k] < key ? sc.bad[k] : key;
+        for (uint32_t k = 0; k < (uint32_t)W; ++k) {
+            key = sc.bad[k] < key ? sc.bad[k] : key;
+            grow |= sc.grow[k];
+        }
+        if (attempt == 0 && grow) {
+            group_bar(bar_id, NT);  // the scratch is reused next
+            continue;               // straight to the coarser units
+        }
         len = key == kNone ? len_all : key >> 1;
         stop_bad = key != kNone && !(key & 1u);
         if (len <= k0) {
@@ -652,7 +675,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
             const Term t = unpack(tp[i]);
-            if (my0 + i < len) fsum += (long long)((t.flags & kBig) ? t.F << kCoarse : t.F);
+            if (my0 + i < len) fsum += (long long)((t.flags & kBig) ? t.F << kCoarse : t.F >> c);
         }
         fsum = fsum < (1ll << 57) ? fsum : (1ll << 57);
         long long finc = fsum;
@@ -674,15 +697,16 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         }
         group_bar(bar_id, NT);
         if (!anybad) {
-            pstart = A0 + (uint64_t)(fbefore + finc - fsum);
+            pstart = (A0 >> c) + (uint64_t)(fbefore + finc - fsum);
             break;
         }
-        if (attempt == 1) return k0;
-        // the second attempt: decode the coarse terms on the start grid again
-        // (beyond it: they end the pass)
+        if (attempt == 2) return k0;
+        if (attempt == 1) {
+            // the last attempt: terms beyond the start grid end the pass
 #pragma unroll
-        for (uint32_t i = 0; i < E; ++i)
-            if (unpack(tp[i]).flags & kBig) tp[i] = pack(Term{0ull, kBad | kBig});
+            for (uint32_t i = 0; i < E; ++i)
+                if (unpack(tp[i]).flags & kBig) tp[i] = pack(Term{0ull, kBad | kBig});
+        }
     }
     rewritten = true;
     if (len < len_all) {
@@ -706,9 +730,9 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
             Term t = unpack(tp[i]);
             const uint32_t s = my0 + i;
             const bool big = (t.flags & kBig) != 0;
-            const uint64_t F = big ? t.F << kCoarse : t.F;
-            const uint64_t T = prefix + F + ((t.flags & kGtZero) ? 1u : 0u);
-            const int ds = rel_binade(prefix), dk = rel_binade(T);
+            const uint64_t F = big ? t.F << kCoarse : t.F >> c;
+            const uint64_t T = prefix + F + ((c == 0 && (t.flags & kGtZero)) ? 1u : 0u);
+            const int ds = rel_binade(prefix, c), dk = rel_binade(T, c);
             bool cr = s >= k0 && s < len && dk > ds;
             bool on_grid = false;  // t already on the grid of binade ds
             if (big && !cr && s >= k0 && s < len) {
