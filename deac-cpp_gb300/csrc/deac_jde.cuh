@@ -1,0 +1,89 @@
+// deac_jde.cuh -- the jDE step of one member (self-adaptation of CR and F per
+// side, then three distinct mutant indices by rejection sampling), shared by
+// the trial kernels and by the split engine's decisions, which draw the next
+// generation's jDE as soon as a run's selections are final.
+//
+// RNG slots of member i (base = i * (1 + S*M), word-major table of n states):
+// base (CR of side 0, then the mutant indices), base+1 (F of side 0),
+// base+2 / base+3 (CR / F of side 1) -- deac_gpu.cu's per-member states.
+#pragma once
+
+#include <cstdint>
+
+#include "deac_kernels.cuh"
+#include "deac_rng.cuh"
+
+namespace deac {
+
+__device__ __forceinline__ double jde_draw_unit(uint64_t (&s)[4]) { return to_unit(xoshiro_next(s[0], s[1], s[2], s[3])); }
+
+// x % P for the 64-bit draws of the mutant indices: q = floor(x * m / 2^64)
+// with m = floor((2^64 - 1) / P) is at most two below floor(x / P), so two
+// corrections give the exact remainder (no 64-bit division routine).
+__device__ __forceinline__ uint64_t mod_p(uint64_t x, uint64_t P, uint64_t m) {
+    uint64_t r = x - __umul64hi(x, m) * P;
+    if (r >= P) r -= P;
+    if (r >= P) r -= P;
+    return r;
+}
+
+// the jDE slots of member i (every load at once)
+__device__ __forceinline__ void jde_load(const RunDev& R, uint32_t i, uint64_t (&st)[4][4]) {
+    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)R.S * R.M);
+    const uint64_t n = R.n_states;
+    const uint64_t* rng = R.rng;
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q)
+#pragma unroll
+        for (uint32_t w = 0; w < 4; ++w) st[q][w] = (q < 2 * R.S) ? rng[w * n + base + q] : 0ull;
+}
+
+// the draws of member i from its slots st (advanced in place) and its
+// current CR / F
+__device__ __forceinline__ void jde_draw(const RunDev& R, uint32_t i, uint64_t (&st)[4][4], const double cr_old[2],
+                                         const double fw_old[2], double cr_new[2], double fw_new[2], uint32_t mut[3]) {
+    const uint32_t P = R.P;
+    const double tau_cr = R.tau_cr, tau_f = R.tau_f;
+    auto side = [&](uint32_t s, uint64_t (&cs)[4], uint64_t (&fs)[4]) {
+        const double cr = jde_draw_unit(cs) < tau_cr ? jde_draw_unit(cs) : cr_old[s];
+        const double fw = jde_draw_unit(fs) < tau_f ? 2.0 * jde_draw_unit(fs) : fw_old[s];
+        cr_new[s] = cr;
+        fw_new[s] = fw;
+    };
+    side(0, st[0], st[1]);
+    if (R.S == 2) side(1, st[2], st[3]);
+    // rejection sampling as in the reference; P >= 4 is enforced on the
+    // host, so every loop has an admissible outcome
+    uint64_t r0 = i, r1 = i, r2 = i;
+    const uint64_t pm = R.p_magic;
+    while (r0 == i) r0 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
+    while (r1 == i || r1 == r0) r1 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
+    while (r2 == i || r2 == r0 || r2 == r1) r2 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
+    mut[0] = (uint32_t)r0;
+    mut[1] = (uint32_t)r1;
+    mut[2] = (uint32_t)r2;
+}
+
+// store the outcome: the new CR / F (upper halves of cr / fw), the advanced
+// slots and, when `mutants` is set, the indices
+__device__ __forceinline__ void jde_store(RunDev& R, uint32_t i, const uint64_t (&st)[4][4], const double cr_new[2],
+                                          const double fw_new[2], const uint32_t mut[3], bool mutants) {
+    const uint32_t P = R.P, S = R.S;
+    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * R.M);
+    const uint64_t n = R.n_states;
+#pragma unroll
+    for (uint32_t s = 0; s < 2; ++s)
+        if (s < S) {
+            R.cr[(uint64_t)S * P + s * P + i] = cr_new[s];
+            R.fw[(uint64_t)S * P + s * P + i] = fw_new[s];
+        }
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q)
+        if (q < 2 * S)
+#pragma unroll
+            for (uint32_t w = 0; w < 4; ++w) R.rng[w * n + base + q] = st[q][w];
+    if (mutants)
+        for (uint32_t q = 0; q < 3; ++q) R.mutants[3 * i + q] = mut[q];
+}
+
+}  // namespace deac

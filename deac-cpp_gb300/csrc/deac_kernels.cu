@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "deac_chain.cuh"
+#include "deac_jde.cuh"
 #include "deac_kernels.cuh"
 #include "deac_rng.cuh"
 #include "deac_split.cuh"
@@ -22,9 +23,6 @@ __device__ __forceinline__ void store_state(const RunDev& R, uint64_t slot, cons
     R.rng[3 * n + slot] = s[3];
 }
 
-__device__ __forceinline__ double draw(uint64_t s[4]) {
-    return to_unit(xoshiro_next(s[0], s[1], s[2], s[3]));
-}
 
 // Integer form of the crossover test  (x >> 11) * 2^-53 < cr
 // (deac_gpu.cu:641): with m = x >> 11 < 2^53 and X = cr * 2^53 (exact),
@@ -128,66 +126,19 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
 // CR(-) slot 2, F(-) slot 3; then the mutant indices on slot 0
 // (deac_gpu.cu:608-633), the launch order of deac.cpp:1168-1219.  Stores
 // the new CR and F and the four slots' states; returns CR, F and the indices.
-// x % P for the 64-bit draws of the mutant indices: q = floor(x * m / 2^64)
-// with m = floor((2^64 - 1) / P) is at most two below floor(x / P), so two
-// corrections give the exact remainder (no 64-bit division routine).
-__device__ __forceinline__ uint64_t mod_p(uint64_t x, uint64_t P, uint64_t m) {
-    uint64_t r = x - __umul64hi(x, m) * P;
-    if (r >= P) r -= P;
-    if (r >= P) r -= P;
-    return r;
-}
-
-// jDE of member i (the self-adaptation of CR and F per side, then three
-// distinct mutant indices by rejection sampling) from RNG slots base ..
-// base+2S-1: slot base (CR of side 0, then the mutant indices), base+1 (F of
-// side 0), base+2 / base+3 (CR / F of side 1).  Every load is issued before
-// the first store; the stores overlap none of them.
+// jDE of member i with every result stored (deac_jde.cuh)
 __device__ __forceinline__ void jde_member(RunDev& R, uint32_t i, double cr_new[2], double fw_new[2],
                                            uint32_t mut[3]) {
-    const uint32_t P = R.P, M = R.M, S = R.S;
-    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
-    const uint64_t n = R.n_states;
-    const uint64_t* rng = R.rng;
     uint64_t st[4][4];
-#pragma unroll
-    for (uint32_t q = 0; q < 4; ++q)
-#pragma unroll
-        for (uint32_t w = 0; w < 4; ++w) st[q][w] = (q < 2 * S) ? rng[w * n + base + q] : 0ull;
+    jde_load(R, i, st);
     double cr_old[2], fw_old[2];
 #pragma unroll
     for (uint32_t s = 0; s < 2; ++s) {
-        cr_old[s] = s < S ? R.cr[s * P + i] : 0.0;
-        fw_old[s] = s < S ? R.fw[s * P + i] : 0.0;
+        cr_old[s] = s < R.S ? R.cr[s * R.P + i] : 0.0;
+        fw_old[s] = s < R.S ? R.fw[s * R.P + i] : 0.0;
     }
-    const double tau_cr = R.tau_cr, tau_f = R.tau_f;
-    auto side = [&](uint32_t s, uint64_t (&cs)[4], uint64_t (&fs)[4]) {
-        const double cr = draw(cs) < tau_cr ? draw(cs) : cr_old[s];
-        const double fw = draw(fs) < tau_f ? 2.0 * draw(fs) : fw_old[s];
-        cr_new[s] = cr;
-        fw_new[s] = fw;
-    };
-    side(0, st[0], st[1]);
-    if (S == 2) side(1, st[2], st[3]);
-    // rejection sampling as in the reference; P >= 4 is enforced on the
-    // host, so every loop has an admissible outcome
-    uint64_t r0 = i, r1 = i, r2 = i;
-    const uint64_t pm = R.p_magic;
-    while (r0 == i) r0 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
-    while (r1 == i || r1 == r0) r1 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
-    while (r2 == i || r2 == r0 || r2 == r1) r2 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
-#pragma unroll
-    for (uint32_t s = 0; s < 2; ++s)
-        if (s < S) {
-            R.cr[(uint64_t)S * P + s * P + i] = cr_new[s];
-            R.fw[(uint64_t)S * P + s * P + i] = fw_new[s];
-        }
-#pragma unroll
-    for (uint32_t q = 0; q < 4; ++q)
-        if (q < 2 * S) store_state(R, base + q, st[q]);
-    mut[0] = (uint32_t)r0;
-    mut[1] = (uint32_t)r1;
-    mut[2] = (uint32_t)r2;
+    jde_draw(R, i, st, cr_old, fw_old, cr_new, fw_new, mut);
+    jde_store(R, i, st, cr_new, fw_new, mut, false);
 }
 
 __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
@@ -391,7 +342,7 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
     if (k >= n) return;
     const Work w = work[k];
     RunDev& R = runs[w.run];
-    if (R.done) return;
+    if (R.done || R.jde_ready) return;  // the decisions drew it already
     double cr[2], fw[2];
     uint32_t mut[3];
     jde_member(R, w.index, cr, fw, mut);

@@ -96,6 +96,7 @@ struct RunDev {
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
     uint32_t* mutants;       // [P][3] mutant indices of this generation
+    int32_t jde_ready;       // split engine: the decisions drew the next generation's jDE
     // split engine with --normalize (kDeferNorm): the trials stay raw until
     // the decisions; norm_kernel forms each trial's exact reciprocal norm
     double* recip;           // [P] 1/norm of each trial

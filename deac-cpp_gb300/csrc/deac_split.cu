@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "deac_jde.cuh"
 #include "deac_split.cuh"
 
 namespace deac {
@@ -504,8 +505,13 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     grid_dependency_wait();
     __shared__ unsigned long long s_n[3];
     __shared__ double s_fit[kDecideMaxMembers];
+    __shared__ int s_jde;
     RunDev& R = runs[blockIdx.x];
     if (R.done) return;
+    // the next generation's jDE slots of this thread's member, loaded now
+    // (drawn below once the selections are final)
+    uint64_t jst[4][4];
+    if (threadIdx.x < R.P) jde_load(R, threadIdx.x, jst);
     SplitRun& X = split[blockIdx.x];
     const uint32_t P = R.P, Nt = R.Nt, S = R.S;
     const bool force_exact = (R.flags & kTrackStats) != 0;
@@ -639,7 +645,10 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
     // that track statistics keep the exact pass, which forms them.
     if (warp == 0) {
         const bool idle = s_n[2] == 0 && !(R.flags & kTrackStats);
-        if (lane == 0) R.exact_idle = idle ? 1 : 0;
+        if (lane == 0) {
+            R.exact_idle = idle ? 1 : 0;
+            s_jde = (idle && P <= blockDim.x) ? 1 : 0;  // a thread per member
+        }
         if (idle) {
             const uint64_t ii = R.ii + 1;
             if (ii + 2 <= R.N) {
@@ -671,6 +680,23 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
                 R.done = 1;
             }
         }
+    }
+    // Every selection final (no exact pass follows): draw the next
+    // generation's jDE here, one thread per member, from the slots loaded
+    // above and the CR / F the selections kept; jde_kernel then skips the run.
+    __syncthreads();
+    if (threadIdx.x == 0) R.jde_ready = s_jde;
+    if (s_jde && threadIdx.x < P) {
+        const uint32_t m = threadIdx.x;
+        double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
+        uint32_t mut[3];
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s) {
+            cr_old[s] = s < S ? R.cr[s * P + m] : 0.0;
+            fw_old[s] = s < S ? R.fw[s * P + m] : 0.0;
+        }
+        jde_draw(R, m, jst, cr_old, fw_old, cr_new, fw_new, mut);
+        jde_store(R, m, jst, cr_new, fw_new, mut, true);
     }
 }
 
