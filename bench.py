@@ -252,7 +252,7 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
         work = 16.0 * rows * NT * split_ctas + rows * NT * 16  # partial sums in, estimate + bound out
         unit, bound, peak = "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "split_combine_kernel+split_decide_kernel"
+        name = "split_combine_kernel+split_select_kernel"
     else:  # kind 1
         work = 2.0 * 2 * rows * NT * M  # FP64 FMA chains, were every trial re-evaluated
         unit, bound, peak = "TFLOP/s", "fp64", 1.196
@@ -371,7 +371,7 @@ def engine_arm(args, world, rank, local):
     tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
     names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
-             3: "split_contract_kernel", 4: "split_combine_kernel+split_decide_kernel+scale_kernel"}
+             3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
     roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs
@@ -416,8 +416,8 @@ def engine_arm(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         # per generation: jDE, trial parts, normalisation row sums, tensor
-        # contraction, combine, decide, scale, 2 exact passes
-        "gpu_launches": 9 * G * args.steps,
+        # contraction, combine, selection, 2 exact passes
+        "gpu_launches": 8 * G * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

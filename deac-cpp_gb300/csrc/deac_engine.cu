@@ -256,10 +256,8 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
            b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
            static_cast<const float4*>(b->d_partial));
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
-    deac::split_decide_kernel<<<(uint32_t)b->runs.size(), deac::kDecideThreads, 0, s>>>(b->d_runs, b->d_split);
-    if (b->n_norm_ctas)
-        launch(deac::scale_kernel, b->n_trial_ctas, 512, 0, s, early, b->d_runs,
-               static_cast<const deac::Work*>(b->d_trial_work));
+    deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
+                                                                               b->d_trial_work);
     if ((rc = mark(4))) return rc;
     launch_contract(b, s, deac::kModeParents, early);
     launch_contract(b, s, deac::kModeTrials, early);
@@ -480,8 +478,8 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
-        const uint64_t o_cnt = sa.take(3 * 8);
-        const uint64_t o_rcp = sa.take(P * 8), o_nb = sa.take(P), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
+        const uint64_t o_cnt = sa.take(3 * 8), o_jd = sa.take(P);
+        const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
@@ -521,12 +519,11 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.xexp = x.xexp;
         d.xexp_max = x.xexp_max;
         d.mutants = reinterpret_cast<uint32_t*>(sb + o_mu);
+        d.jde_done = reinterpret_cast<uint8_t*>(sb + o_jd);  // zero: jde_kernel draws every member
         d.recheck = x.recheck;
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;
         d.recip = reinterpret_cast<double*>(sb + o_rcp);
-        d.norm_buf = reinterpret_cast<uint8_t*>(sb + o_nb);
-        CUDA_TRY(cudaMemset(d.norm_buf, 0xFF, P));  // no trial to normalise yet
         // with --normalize the trials stay raw until the decisions
         if (r.cfg.normalize) d.flags |= deac::kDeferNorm;
         if (it->second.nonneg && !r.cfg.allow_negative_weight) d.flags |= deac::kNonNegProducts;

@@ -288,8 +288,8 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
         __syncthreads();
     }
 
-    // split engine, kDeferNorm: the trial stays raw here (norm_kernel and
-    // scale_kernel normalise it after the decisions)
+    // split engine, kDeferNorm: the trial stays raw here (norm_kernel forms
+    // its norm; split_select_kernel normalises it after the decision)
     if (row_sums_here) {
         // normalisation row sum and reciprocal scale
         // (deac_gpu.cu:345-374 with alpha = 1/F(0), then 406-415)
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
     if (k >= n) return;
     const Work w = work[k];
     RunDev& R = runs[w.run];
-    if (R.done || R.jde_ready) return;  // the decisions drew it already
+    if (R.done || R.jde_done[w.index]) return;  // the selection drew it already
     double cr[2], fw[2];
     uint32_t mut[3];
     jde_member(R, w.index, cr, fw, mut);
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
 // both sides, per CTA -- the crossover draw and DE/rand/1 mutation of each
 // gene as in trial_kernel, then the part's BF16 digit slices.  Sets the
 // trial's `changed` flag when a gene mutated and raises its maximum chunk
-// exponent (split_decide_kernel resets both after use).
+// exponent (split_select_kernel resets both after use).
 __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev* runs, const Work* work) {
     grid_dependency_wait();
     extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
@@ -510,49 +510,6 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
     const double recip = 1.0 / norm;
     R.recip[i] = recip;
     if (recip != 1.0) R.changed[i] = 1;
-}
-
-// ---------------------------------------------------------------- scale
-// Split engine, kDeferNorm runs: normalise the trials whose genes the
-// generation keeps (accepted) or still needs (the exact passes): every gene
-// times 1/norm, as trial_kernel does.  One CTA per trial.
-__global__ void __launch_bounds__(512) scale_kernel(RunDev* runs, const Work* work) {
-    grid_dependency_wait();
-    const Work wk = work[blockIdx.x];
-    RunDev& R = runs[wk.run];
-    if (!(R.flags & kDeferNorm)) return;
-    const uint32_t i = wk.index;
-    // every thread reads the request and the factor (one round trip)
-    const uint32_t b = R.norm_buf[i];
-    const double recip = R.recip[i];
-    if (b == 0xFFu) return;
-    const uint32_t M = R.M, S = R.S;
-    const uint64_t PM = (uint64_t)R.P * M;
-    // pairs of genes (M is a multiple of the 32-gene chunk), sixteen genes
-    // in flight per thread
-    const uint32_t half = M / 2, pairs = S * half;
-    constexpr uint32_t U = 8;
-    for (uint32_t q0 = threadIdx.x; q0 < pairs; q0 += U * blockDim.x) {
-        double2* g[U];
-        double2 v[U];
-#pragma unroll
-        for (uint32_t u = 0; u < U; ++u) {
-            const uint32_t q = q0 + u * blockDim.x;
-            g[u] = nullptr;
-            if (q < pairs) {
-                const uint32_t s = q / half;
-                g[u] = reinterpret_cast<double2*>(R.pop + ((uint64_t)b * S + s) * PM + (uint64_t)i * M) + (q - s * half);
-                v[u] = *g[u];
-            }
-        }
-#pragma unroll
-        for (uint32_t u = 0; u < U; ++u)
-            if (g[u]) *g[u] = make_double2(v[u].x * recip, v[u].y * recip);
-    }
-    // the request is consumed: later launches (a finished run's included,
-    // whose decide kernel no longer runs) find none
-    __syncthreads();
-    if (threadIdx.x == 0) R.norm_buf[i] = 0xFFu;
 }
 
 // ------------------------------------------------------------- contract

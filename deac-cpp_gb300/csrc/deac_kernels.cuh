@@ -96,18 +96,17 @@ struct RunDev {
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
     uint32_t* mutants;       // [P][3] mutant indices of this generation
-    int32_t jde_ready;       // split engine: the decisions drew the next generation's jDE
+    uint8_t* jde_done;       // [P] split engine: the selection drew the member's next jDE
     // split engine with --normalize (kDeferNorm): the trials stay raw until
     // the decisions; norm_kernel forms each trial's exact reciprocal norm
     double* recip;           // [P] 1/norm of each trial
-    uint8_t* norm_buf;       // [P] buffer of a trial to normalise now, 0xFF none
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
     uint32_t ticket;         // CTAs of contract_kernel done this launch
     int32_t done;
     int32_t exact_idle;      // split engine: this generation needs no exact pass
-                             // (set by split_decide_kernel, which then also did
+                             // (set by split_select_kernel, which then also did
                              // the generation's bookkeeping)
 };
 
@@ -189,13 +188,11 @@ __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const Work* work);
 // split engine, kDeferNorm runs: the exact normalisation row sums of one raw
 // trial per CTA (both sides), the reciprocal norm and the final `changed`
-// flag; and the normalisation of the trials the decisions keep (one CTA per
-// trial)
+// flag
 constexpr int kNormThreads = 2 * kChainWarps * 32;
 constexpr uint32_t kNormStage = kChainWarps * 32 * kChainSteps;  // steps staged in shared memory at a time
 constexpr uint32_t kNormSmemBytes = 2 * 2 * kNormStage * sizeof(double);  // dynamic shared memory of norm_kernel
 __global__ void norm_kernel(RunDev* runs, const Work* work);
-__global__ void scale_kernel(RunDev* runs, const Work* work);
 __global__ void contract_kernel(RunDev* runs, const Work* work, int mode);
 
 }  // namespace deac

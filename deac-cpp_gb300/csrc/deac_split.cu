@@ -497,52 +497,48 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     X.e_bound[o] = eb * (1.0 + 0x1p-40) + (C + ks + 10.0) * 0x1p-140;
 }
 
-// ---------------------------------------------------------------- decide
-// One CTA per run, a warp per member: the estimate's chi^2 and its interval,
-// then the selection decisions that the interval settles.  Undecided members
-// are flagged for the exact FP64 evaluation (contract_kernel, recheck mode).
-__global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* runs, SplitRun* split) {
+// ---------------------------------------------------------------- select
+// One CTA per member: the estimate's chi^2 and its interval, the selection
+// decision the interval settles (undecided members are flagged for the exact
+// FP64 evaluation, contract_kernel's recheck mode), the normalisation of the
+// trial the run keeps or still needs (kDeferNorm), and the next generation's
+// jDE of the member once its selection is final.  The run's last CTA does
+// the generation's bookkeeping when no member needs the exact pass.
+__global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* runs, SplitRun* split,
+                                                                     const Work* work) {
     grid_dependency_wait();
-    __shared__ unsigned long long s_n[3];
-    __shared__ double s_fit[kDecideMaxMembers];
-    __shared__ int s_jde;
-    RunDev& R = runs[blockIdx.x];
+    __shared__ double s_chi[kSelectThreads / 32];
+    __shared__ float s_dchi[kSelectThreads / 32];
+    __shared__ int s_outcome, s_last;
+    enum { kReject = 0, kAccept = 1, kRecheck = 2, kSame = 3 };
+    const Work wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    SplitRun& X = split[wk.run];
     if (R.done) return;
-    // the next generation's jDE slots of this thread's member, loaded now
-    // (drawn below once the selections are final)
-    uint64_t jst[4][4];
-    if (threadIdx.x < R.P) jde_load(R, threadIdx.x, jst);
-    SplitRun& X = split[blockIdx.x];
-    const uint32_t P = R.P, Nt = R.Nt, S = R.S;
+    const uint32_t i = wk.index;
+    const uint32_t P = R.P, Nt = R.Nt, S = R.S, M = R.M;
+    const bool defer = (R.flags & kDeferNorm) != 0;
     const bool force_exact = (R.flags & kTrackStats) != 0;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
-    if (threadIdx.x < 3) s_n[threadIdx.x] = 0;
-    // 1/sigma of each timeslice, formed once per run (a relative error of
-    // 2^-53, covered below)
-    const double* inv_err = X.inv_err;
-    const float* inv_err_up = X.inv_err_up;
-    // each member's fitness after the decision (the minimum below)
-    for (uint32_t m = threadIdx.x; m < P && m < kDecideMaxMembers; m += blockDim.x) s_fit[m] = R.fit_old[m];
-    __syncthreads();
-    for (uint32_t i = warp; i < P; i += nw) {
-        const bool changed = X.changed[i] != 0;
-        if (!changed) {
-            if (lane == 0) {
-                // the trial is the parent: the same fitness, and ties accept
-                if (R.flags & kDeferNorm) R.norm_buf[i] = 0xFFu;
-                X.recheck[i] = 0;
-                X.t_lo[i] = X.f_lo[i];
-                X.t_hi[i] = X.f_hi[i];
-                R.fit_new[i] = X.f_lo[i];
-                for (uint32_t s = 0; s < S; ++s) {
-                    R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
-                    R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
-                }
-                R.cur[i] = (uint8_t)(1u - R.cur[i]);
-                atomicAdd(&s_n[0], 1ull);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    // the member's jDE slots for the next generation, loaded now
+    uint64_t jst[4][4];
+    if (tid == 0) jde_load(R, i, jst);
+    const bool changed = X.changed[i] != 0;
+    if (!changed) {
+        if (tid == 0) {
+            // the trial is the parent: the same fitness, and ties accept
+            X.recheck[i] = 0;
+            X.t_lo[i] = X.f_lo[i];
+            X.t_hi[i] = X.f_hi[i];
+            R.fit_new[i] = X.f_lo[i];
+            for (uint32_t s = 0; s < S; ++s) {
+                R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
+                R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
             }
-            continue;
+            R.cur[i] = (uint8_t)(1u - R.cur[i]);
+            s_outcome = kSame;
         }
+    } else {
         // chi^2 of the estimate and a bound on its distance from the value
         // the FP64 engine computes (any summation order: the rounding term
         // covers n-term sums)
@@ -553,150 +549,166 @@ __global__ void __launch_bounds__(kDecideThreads) split_decide_kernel(RunDev* ru
         // two), 0.001 of it more for the per-gene roundings (at most
         // 2^-47 B while the raw bound is at least 2^-33 B), and 2^-51 |E|
         // for the product's rounding.
-        const bool defer = (R.flags & kDeferNorm) != 0;
         const double rc = defer ? R.recip[i] : 1.0;
         const float rc_up = f32_up(rc);
-        // chi^2 in FP64 (four timeslices per lane in flight, one sum each);
-        // its error bound in FP32 rounded upward (every term is
-        // non-negative, so each rounding up keeps an upper bound), the FP32
-        // operands taken as upper bounds by integer operations
-        double chi4[4] = {0.0, 0.0, 0.0, 0.0};
+        // chi^2 in FP64; its error bound in FP32 rounded upward (every term
+        // is non-negative, so each rounding up keeps an upper bound), the
+        // FP32 operands taken as upper bounds by integer operations
+        double chi = 0.0;
         float dchi = 0.0f;
-        constexpr uint32_t U = 4;  // timeslices per lane in flight
-        for (uint32_t t0 = lane; t0 < Nt; t0 += 32 * U) {
-            double em[U], eb0[U], f[U], ie[U];
-            float ief[U];
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t t = t0 + 32 * u;
-                const uint64_t o = (uint64_t)i * Nt + t;
-                const bool ok = t < Nt;
-                em[u] = ok ? X.e_mp[o] : 0.0;
-                eb0[u] = ok ? X.e_bound[o] : 0.0;
-                f[u] = ok ? R.isf[t] : 0.0;
-                ie[u] = ok ? inv_err[t] : 0.0;
-                ief[u] = ok ? inv_err_up[t] : 0.0f;
-            }
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const double e = defer ? em[u] * rc : em[u];
-                // r carries up to three roundings of 2^-53 each
-                const double r = (f[u] - e) * ie[u];
-                chi4[u] = fma(r, r, chi4[u]);
-                const float ar = f32_up(r);
-                const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up(eb0[u])), rc_up),
-                                                   __fmul_ru(f32_up(e), 0x1.0p-51f))
-                                       : f32_up(eb0[u]);
-                const float dr = __fadd_ru(__fmul_ru(__fmul_ru(eb, ief[u]), 1.0f + 0x1.0p-20f),
-                                           __fmul_ru(ar, 0x1.0p-51f));
-                dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
-            }
+        for (uint32_t t = tid; t < Nt; t += kSelectThreads) {
+            const uint64_t o = (uint64_t)i * Nt + t;
+            const double em = X.e_mp[o], eb0 = X.e_bound[o], f = R.isf[t], ie = X.inv_err[t];
+            const float ief = X.inv_err_up[t];
+            const double e = defer ? em * rc : em;
+            // r carries up to three roundings of 2^-53 each
+            const double r = (f - e) * ie;
+            chi = fma(r, r, chi);
+            const float ar = f32_up(r);
+            const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up(eb0)), rc_up),
+                                               __fmul_ru(f32_up(e), 0x1.0p-51f))
+                                   : f32_up(eb0);
+            const float dr =
+                __fadd_ru(__fmul_ru(__fmul_ru(eb, ief), 1.0f + 0x1.0p-20f), __fmul_ru(ar, 0x1.0p-51f));
+            dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
         }
-        double chi = (chi4[0] + chi4[1]) + (chi4[2] + chi4[3]);
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
             dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
         }
-        if (lane != 0) continue;
-        X.recheck[i] = 0;
-        // /Nt as a product with 1/Nt rounded once: two roundings where a
-        // quotient has one, covered by two more units of the slack below
-        chi *= X.inv_nt;
-        const double dchi_d = (double)__fmul_ru(dchi, X.inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
-        const double lo = chi - dchi_d, hi = chi + dchi_d;
-        X.t_lo[i] = lo;
-        X.t_hi[i] = hi;
-        if (defer) R.norm_buf[i] = 0xFFu;
-        if (lo > X.f_hi[i]) {  // certainly worse: reject
-            atomicAdd(&s_n[1], 1ull);
-            continue;
+        if (lane == 0) {
+            s_chi[warp] = chi;
+            s_dchi[warp] = dchi;
         }
-        const bool certain_accept = hi <= X.f_lo[i];
-        if (certain_accept && !force_exact && lo > R.stop) {
-            // certainly no worse: accept with the interval as its fitness
-            X.f_lo[i] = lo;
-            X.f_hi[i] = hi;
-            R.fit_old[i] = 0.5 * (lo + hi);
-            if (i < kDecideMaxMembers) s_fit[i] = 0.5 * (lo + hi);
-            for (uint32_t s = 0; s < S; ++s) {
-                R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
-                R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
+        __syncthreads();
+        if (tid == 0) {
+            chi = 0.0;
+            dchi = 0.0f;
+            for (uint32_t w = 0; w < kSelectThreads / 32; ++w) {
+                chi += s_chi[w];
+                dchi = __fadd_ru(dchi, s_dchi[w]);
             }
-            R.cur[i] = (uint8_t)(1u - R.cur[i]);
-            if (defer) R.norm_buf[i] = R.cur[i];  // the kept trial, now the parent
-            atomicAdd(&s_n[1], 1ull);
-            continue;
+            X.recheck[i] = 0;
+            // /Nt as a product with 1/Nt rounded once: two roundings where a
+            // quotient has one, covered by two more units of the slack below
+            chi *= X.inv_nt;
+            const double dchi_d = (double)__fmul_ru(dchi, X.inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
+            const double lo = chi - dchi_d, hi = chi + dchi_d;
+            X.t_lo[i] = lo;
+            X.t_hi[i] = hi;
+            int outcome;
+            if (lo > X.f_hi[i]) {  // certainly worse: reject
+                outcome = kReject;
+            } else if (hi <= X.f_lo[i] && !force_exact && lo > R.stop) {
+                // certainly no worse: accept with the interval as its fitness
+                X.f_lo[i] = lo;
+                X.f_hi[i] = hi;
+                R.fit_old[i] = 0.5 * (lo + hi);
+                for (uint32_t s = 0; s < S; ++s) {
+                    R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
+                    R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
+                }
+                R.cur[i] = (uint8_t)(1u - R.cur[i]);
+                outcome = kAccept;
+            } else {
+                X.recheck[i] = 1;  // settle with the exact FP64 value
+                outcome = kRecheck;
+            }
+            s_outcome = outcome;
         }
-        if (defer) R.norm_buf[i] = (uint8_t)(1u - R.cur[i]);  // the exact passes read it
-        X.recheck[i] = 1;  // settle with the exact FP64 value
-        atomicAdd(&s_n[2], 1ull);
     }
     __syncthreads();
-    if (threadIdx.x < 3 && s_n[threadIdx.x]) atomicAdd(&X.counts[threadIdx.x], s_n[threadIdx.x]);
-    // the next generation's trial parts set the flags and raise the maxima anew
-    for (uint32_t m = threadIdx.x; m < P; m += blockDim.x) {
-        X.changed[m] = 0;
-        X.xexp_max[m] = (int32_t)0x80808080;
-    }
-    // Nothing left for the exact passes: finish the generation here -- the
-    // bookkeeping of contract_kernel's trial pass (generation index, minimum
-    // and stop test); the fitness of an interval-accepted member lies above
-    // the stop fitness, so its midpoint decides the stop test exactly.  Runs
-    // that track statistics keep the exact pass, which forms them.
-    if (warp == 0) {
-        const bool idle = s_n[2] == 0 && !(R.flags & kTrackStats);
-        if (lane == 0) {
-            R.exact_idle = idle ? 1 : 0;
-            s_jde = (idle && P <= blockDim.x) ? 1 : 0;  // a thread per member
+    const int outcome = s_outcome;
+    // kDeferNorm: normalise the trial the run keeps (now the parent) or
+    // still needs (the exact passes read it): every gene times 1/norm, as
+    // trial_kernel does (M is a multiple of the 32-gene chunk: gene pairs).
+    // Warps 1.. do it (all loads in flight at once for M = 4096) while
+    // warp 0 draws the jDE.
+    if (defer && (outcome == kAccept || outcome == kRecheck) && warp != 0) {
+        const uint32_t b = outcome == kAccept ? R.cur[i] : 1u - R.cur[i];
+        const double recip = R.recip[i];
+        const uint64_t PM = (uint64_t)P * M;
+        const uint32_t half = M / 2, pairs = S * half;
+        constexpr uint32_t NS = kSelectThreads - 32, U = 9;
+        double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)b * S * PM + (uint64_t)i * M);
+        // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
+        auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
+        for (uint32_t q0 = tid - 32; q0 < pairs; q0 += U * NS) {
+            double2 v[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) v[u] = *at(q);
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) *at(q) = make_double2(v[u].x * recip, v[u].y * recip);
+            }
         }
-        if (idle) {
-            const uint64_t ii = R.ii + 1;
-            if (ii + 2 <= R.N) {
-                // the minimum fitness, by a warp (the minimum of finite
-                // values does not depend on the order)
-                double mn;
-                if (P <= kDecideMaxMembers) {
-                    mn = s_fit[0];
-                    for (uint32_t m = lane; m < P; m += 32) mn = s_fit[m] < mn ? s_fit[m] : mn;
-                } else {
-                    const volatile double* f = R.fit_old;
-                    mn = f[0];
-                    for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
-                }
-                for (int o = 16; o > 0; o >>= 1) {
-                    const double v = __shfl_xor_sync(0xffffffffu, mn, o);
-                    mn = v < mn ? v : mn;
-                }
-                if (lane == 0) {
-                    R.ii = ii;
-                    if (mn <= R.stop) {
-                        R.generation = ii;
-                        R.done = 1;
-                    }
-                }
-            } else if (lane == 0) {
-                R.ii = ii;
-                R.generation = R.N - 2;
+    }
+    if (tid == 0) {
+        // the next generation's jDE once the selection is final (the exact
+        // passes leave the member alone); jde_kernel draws the others
+        if (outcome != kRecheck) {
+            double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
+            uint32_t mut[3];
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s) {
+                cr_old[s] = s < S ? R.cr[s * P + i] : 0.0;
+                fw_old[s] = s < S ? R.fw[s * P + i] : 0.0;
+            }
+            jde_draw(R, i, jst, cr_old, fw_old, cr_new, fw_new, mut);
+            jde_store(R, i, jst, cr_new, fw_new, mut, true);
+        }
+        R.jde_done[i] = outcome != kRecheck ? 1 : 0;
+        // the next generation's trial parts set the flag and raise the maximum
+        X.changed[i] = 0;
+        X.xexp_max[i] = (int32_t)0x80808080;
+        atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
+        if (outcome == kRecheck) atomicAdd(&X.sel_recheck, 1u);
+        __threadfence();
+        s_last = atomicAdd(&X.sel_ticket, 1u) == P - 1;
+    }
+    __syncthreads();
+    if (!s_last || warp != 0) return;
+    // The run's last member: with nothing left for the exact passes, finish
+    // the generation here -- the bookkeeping of contract_kernel's trial pass
+    // (generation index, minimum and stop test); the fitness of an
+    // interval-accepted member lies above the stop fitness, so its midpoint
+    // decides the stop test exactly.  Runs that track statistics keep the
+    // exact pass, which forms them.
+    __threadfence();
+    const volatile uint32_t* vr = &X.sel_recheck;
+    const bool idle = *vr == 0 && !force_exact;
+    if (lane == 0) {
+        R.exact_idle = idle ? 1 : 0;
+        X.sel_recheck = 0;
+        X.sel_ticket = 0;
+    }
+    if (!idle) return;
+    const uint64_t ii = R.ii + 1;
+    if (ii + 2 <= R.N) {
+        // the minimum fitness (the minimum of finite values does not depend
+        // on the order)
+        const volatile double* f = R.fit_old;
+        double mn = f[0];
+        for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double v = __shfl_xor_sync(0xffffffffu, mn, o);
+            mn = v < mn ? v : mn;
+        }
+        if (lane == 0) {
+            R.ii = ii;
+            if (mn <= R.stop) {
+                R.generation = ii;
                 R.done = 1;
             }
         }
-    }
-    // Every selection final (no exact pass follows): draw the next
-    // generation's jDE here, one thread per member, from the slots loaded
-    // above and the CR / F the selections kept; jde_kernel then skips the run.
-    __syncthreads();
-    if (threadIdx.x == 0) R.jde_ready = s_jde;
-    if (s_jde && threadIdx.x < P) {
-        const uint32_t m = threadIdx.x;
-        double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
-        uint32_t mut[3];
-#pragma unroll
-        for (uint32_t s = 0; s < 2; ++s) {
-            cr_old[s] = s < S ? R.cr[s * P + m] : 0.0;
-            fw_old[s] = s < S ? R.fw[s * P + m] : 0.0;
-        }
-        jde_draw(R, m, jst, cr_old, fw_old, cr_new, fw_new, mut);
-        jde_store(R, m, jst, cr_new, fw_new, mut, true);
+    } else if (lane == 0) {
+        R.ii = ii;
+        R.generation = R.N - 2;
+        R.done = 1;
     }
 }
 

@@ -43,8 +43,7 @@ constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
 constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
-constexpr int kDecideThreads = 512;
-constexpr uint32_t kDecideMaxMembers = 128;  // fitness values kept in shared memory
+constexpr int kSelectThreads = 512;
 // dynamic shared memory of split_contract_kernel for S sides: K digits
 // [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and the two bound
 // operands (128 x 16, 64 x 16)
@@ -74,6 +73,8 @@ struct SplitRun {
     double* t_hi;
     unsigned long long* counts;  // [3]: trials equal to the parent, settled by
                                  // the interval, settled by the exact FP64 value
+    uint32_t sel_ticket;         // members through split_select_kernel this generation
+    uint32_t sel_recheck;        // of them left for the exact pass
     const double* inv_err;  // [Nt] 1/sigma, rounded once
     const float* inv_err_up;  // [Nt] float upper bounds of inv_err
     double inv_nt;            // 1/Nt, rounded once
@@ -110,7 +111,7 @@ __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const Split
                                       const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status);
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows,
                                      const float4* partial);
-__global__ void split_decide_kernel(RunDev* runs, SplitRun* split);
+__global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* work);
 constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
 
 // ---- digit slicing of one value (shared by trial_kernel and the host)
