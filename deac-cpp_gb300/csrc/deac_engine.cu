@@ -484,6 +484,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
         deac::SplitRun& x = r.split;
+        x.sel_min_bits = ~0ull;  // no member tallied yet
         x.xexp = reinterpret_cast<int16_t*>(sb + o_xe);
         x.xexp_max = reinterpret_cast<int32_t*>(sb + o_xm);
         CUDA_TRY(cudaMemset(x.xexp_max, 0x80, P * 4));  // below every exponent: no trial sliced yet

@@ -619,6 +619,16 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     }
     __syncthreads();
     const int outcome = s_outcome;
+    if (tid == 0) {
+        // the run's tallies: the members' fitness minimum (non-negative
+        // doubles order as their bit patterns), the outcome counts and the
+        // members left for the exact pass; then the ticket
+        atomicMin(&X.sel_min_bits, (unsigned long long)__double_as_longlong(R.fit_old[i]));
+        atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
+        if (outcome == kRecheck) atomicAdd(&X.sel_recheck, 1u);
+        __threadfence();
+        s_last = atomicAdd(&X.sel_ticket, 1u) == P - 1;
+    }
     // kDeferNorm: normalise the trial the run keeps (now the parent) or
     // still needs (the exact passes read it): every gene times 1/norm, as
     // trial_kernel does (M is a multiple of the 32-gene chunk: gene pairs).
@@ -665,47 +675,33 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         // the next generation's trial parts set the flag and raise the maximum
         X.changed[i] = 0;
         X.xexp_max[i] = (int32_t)0x80808080;
-        atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
-        if (outcome == kRecheck) atomicAdd(&X.sel_recheck, 1u);
-        __threadfence();
-        s_last = atomicAdd(&X.sel_ticket, 1u) == P - 1;
     }
     __syncthreads();
-    if (!s_last || warp != 0) return;
+    if (!s_last || warp != 1) return;
     // The run's last member: with nothing left for the exact passes, finish
     // the generation here -- the bookkeeping of contract_kernel's trial pass
     // (generation index, minimum and stop test); the fitness of an
     // interval-accepted member lies above the stop fitness, so its midpoint
     // decides the stop test exactly.  Runs that track statistics keep the
     // exact pass, which forms them.
+    if (lane != 0) return;
     __threadfence();
-    const volatile uint32_t* vr = &X.sel_recheck;
-    const bool idle = *vr == 0 && !force_exact;
-    if (lane == 0) {
-        R.exact_idle = idle ? 1 : 0;
-        X.sel_recheck = 0;
-        X.sel_ticket = 0;
-    }
+    const uint32_t nre = *reinterpret_cast<volatile uint32_t*>(&X.sel_recheck);
+    const double mn = __longlong_as_double((long long)*reinterpret_cast<volatile unsigned long long*>(&X.sel_min_bits));
+    X.sel_recheck = 0;
+    X.sel_ticket = 0;
+    X.sel_min_bits = ~0ull;
+    const bool idle = nre == 0 && !force_exact;
+    R.exact_idle = idle ? 1 : 0;
     if (!idle) return;
     const uint64_t ii = R.ii + 1;
     if (ii + 2 <= R.N) {
-        // the minimum fitness (the minimum of finite values does not depend
-        // on the order)
-        const volatile double* f = R.fit_old;
-        double mn = f[0];
-        for (uint32_t m = lane; m < P; m += 32) mn = f[m] < mn ? f[m] : mn;
-        for (int o = 16; o > 0; o >>= 1) {
-            const double v = __shfl_xor_sync(0xffffffffu, mn, o);
-            mn = v < mn ? v : mn;
+        R.ii = ii;
+        if (mn <= R.stop) {
+            R.generation = ii;
+            R.done = 1;
         }
-        if (lane == 0) {
-            R.ii = ii;
-            if (mn <= R.stop) {
-                R.generation = ii;
-                R.done = 1;
-            }
-        }
-    } else if (lane == 0) {
+    } else {
         R.ii = ii;
         R.generation = R.N - 2;
         R.done = 1;

@@ -75,6 +75,7 @@ struct SplitRun {
                                  // the interval, settled by the exact FP64 value
     uint32_t sel_ticket;         // members through split_select_kernel this generation
     uint32_t sel_recheck;        // of them left for the exact pass
+    unsigned long long sel_min_bits;  // their fitness minimum (bits; all ones: none yet)
     const double* inv_err;  // [Nt] 1/sigma, rounded once
     const float* inv_err_up;  // [Nt] float upper bounds of inv_err
     double inv_nt;            // 1/Nt, rounded once
