@@ -439,6 +439,13 @@ int upload_run(deac_batch* b, RunHost& r) {
     d.tau_cr = r.cfg.self_adapting_crossover_probability;
     d.p_magic = ~0ull / P;
     d.tau_f = r.cfg.self_adapting_differential_weight_probability;
+    auto thr = [](double tau) -> uint64_t {  // m < thr  <=>  m 2^-53 < tau for m < 2^53
+        if (!(tau > 0.0)) return 0;
+        if (tau >= 1.0) return 1ull << 53;
+        return (uint64_t)std::ceil(tau * 0x1.0p53);
+    };
+    d.tau_cr_thr = thr(d.tau_cr);
+    d.tau_f_thr = thr(d.tau_f);
     d.alpha = 1.0 / m.zeroth_moment;
     d.stop = r.cfg.stop_minimum_fitness;
     d.first_target = r.cfg.first_moment;

@@ -15,8 +15,6 @@
 
 namespace deac {
 
-__device__ __forceinline__ double jde_draw_unit(uint64_t (&s)[4]) { return to_unit(xoshiro_next(s[0], s[1], s[2], s[3])); }
-
 // x % P for the 64-bit draws of the mutant indices: q = floor(x * m / 2^64)
 // with m = floor((2^64 - 1) / P) is at most two below floor(x / P), so two
 // corrections give the exact remainder (no 64-bit division routine).
@@ -43,12 +41,13 @@ __device__ __forceinline__ void jde_load(const RunDev& R, uint32_t i, uint64_t (
 __device__ __forceinline__ void jde_draw(const RunDev& R, uint32_t i, uint64_t (&st)[4][4], const double cr_old[2],
                                          const double fw_old[2], double cr_new[2], double fw_new[2], uint32_t mut[3]) {
     const uint32_t P = R.P;
-    const double tau_cr = R.tau_cr, tau_f = R.tau_f;
+    // draw < tau  <=>  (x >> 11) < ceil(tau 2^53) (draw = (x >> 11) 2^-53
+    // exactly): integer tests, a conversion only for a new value
+    const uint64_t thr_cr = R.tau_cr_thr, thr_f = R.tau_f_thr;
+    auto bits = [](uint64_t (&st)[4]) { return xoshiro_next(st[0], st[1], st[2], st[3]) >> 11; };
     auto side = [&](uint32_t s, uint64_t (&cs)[4], uint64_t (&fs)[4]) {
-        const double cr = jde_draw_unit(cs) < tau_cr ? jde_draw_unit(cs) : cr_old[s];
-        const double fw = jde_draw_unit(fs) < tau_f ? 2.0 * jde_draw_unit(fs) : fw_old[s];
-        cr_new[s] = cr;
-        fw_new[s] = fw;
+        cr_new[s] = bits(cs) < thr_cr ? (double)bits(cs) * 0x1.0p-53 : cr_old[s];
+        fw_new[s] = bits(fs) < thr_f ? (double)bits(fs) * 0x1.0p-52 : fw_old[s];  // 2 * draw
     };
     side(0, st[0], st[1]);
     if (R.S == 2) side(1, st[2], st[3]);

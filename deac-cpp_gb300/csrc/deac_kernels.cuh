@@ -57,6 +57,7 @@ struct RunDev {
     uint64_t N;              // number_of_generations
     double tau_cr, tau_f;    // self-adaptation probabilities
     uint64_t p_magic;        // floor((2^64 - 1) / P): x % P without a 64-bit division
+    uint64_t tau_cr_thr, tau_f_thr;  // ceil(tau 2^53): draw < tau as an integer test
     double alpha;            // 1 / F(0), the normalisation scale
     double stop;             // stop_minimum_fitness
     double first_target, third_target, third_error;

@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     grid_dependency_wait();
     __shared__ double s_chi[kSelectThreads / 32];
     __shared__ float s_dchi[kSelectThreads / 32];
-    __shared__ int s_outcome, s_last;
+    __shared__ int s_outcome;
     enum { kReject = 0, kAccept = 1, kRecheck = 2, kSame = 3 };
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
@@ -520,9 +520,18 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const bool defer = (R.flags & kDeferNorm) != 0;
     const bool force_exact = (R.flags & kTrackStats) != 0;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    constexpr uint32_t kJdeThread = 32;  // warp 1 draws the jDE; warp 0 keeps the run's tallies
     // the member's jDE slots for the next generation, loaded now
     uint64_t jst[4][4];
-    if (tid == 0) jde_load(R, i, jst);
+    if (tid == kJdeThread) jde_load(R, i, jst);
+    // this thread's first timeslice, loaded with the `changed` flag (one
+    // round trip; unused when the trial equals its parent)
+    const uint64_t o0 = (uint64_t)i * Nt + tid;
+    const bool t0_ok = tid < Nt;
+    const double em0 = t0_ok ? X.e_mp[o0] : 0.0, eb00 = t0_ok ? X.e_bound[o0] : 0.0;
+    const double f0 = t0_ok ? R.isf[tid] : 0.0, ie0 = t0_ok ? X.inv_err[tid] : 0.0;
+    const float ief0 = t0_ok ? X.inv_err_up[tid] : 0.0f;
+    const double rc = defer ? R.recip[i] : 1.0;
     const bool changed = X.changed[i] != 0;
     if (!changed) {
         if (tid == 0) {
@@ -549,17 +558,13 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         // two), 0.001 of it more for the per-gene roundings (at most
         // 2^-47 B while the raw bound is at least 2^-33 B), and 2^-51 |E|
         // for the product's rounding.
-        const double rc = defer ? R.recip[i] : 1.0;
         const float rc_up = f32_up(rc);
         // chi^2 in FP64; its error bound in FP32 rounded upward (every term
         // is non-negative, so each rounding up keeps an upper bound), the
         // FP32 operands taken as upper bounds by integer operations
         double chi = 0.0;
         float dchi = 0.0f;
-        for (uint32_t t = tid; t < Nt; t += kSelectThreads) {
-            const uint64_t o = (uint64_t)i * Nt + t;
-            const double em = X.e_mp[o], eb0 = X.e_bound[o], f = R.isf[t], ie = X.inv_err[t];
-            const float ief = X.inv_err_up[t];
+        auto term = [&](double em, double eb0, double f, double ie, float ief) {
             const double e = defer ? em * rc : em;
             // r carries up to three roundings of 2^-53 each
             const double r = (f - e) * ie;
@@ -571,6 +576,11 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             const float dr =
                 __fadd_ru(__fmul_ru(__fmul_ru(eb, ief), 1.0f + 0x1.0p-20f), __fmul_ru(ar, 0x1.0p-51f));
             dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
+        };
+        if (t0_ok) term(em0, eb00, f0, ie0, ief0);
+        for (uint32_t t = tid + kSelectThreads; t < Nt; t += kSelectThreads) {
+            const uint64_t o = (uint64_t)i * Nt + t;
+            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], X.inv_err_up[t]);
         }
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
@@ -627,37 +637,36 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
         if (outcome == kRecheck) atomicAdd(&X.sel_recheck, 1u);
         __threadfence();
-        s_last = atomicAdd(&X.sel_ticket, 1u) == P - 1;
-    }
-    // kDeferNorm: normalise the trial the run keeps (now the parent) or
-    // still needs (the exact passes read it): every gene times 1/norm, as
-    // trial_kernel does (M is a multiple of the 32-gene chunk: gene pairs).
-    // Warps 1.. do it (all loads in flight at once for M = 4096) while
-    // warp 0 draws the jDE.
-    if (defer && (outcome == kAccept || outcome == kRecheck) && warp != 0) {
-        const uint32_t b = outcome == kAccept ? R.cur[i] : 1u - R.cur[i];
-        const double recip = R.recip[i];
-        const uint64_t PM = (uint64_t)P * M;
-        const uint32_t half = M / 2, pairs = S * half;
-        constexpr uint32_t NS = kSelectThreads - 32, U = 9;
-        double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)b * S * PM + (uint64_t)i * M);
-        // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
-        auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
-        for (uint32_t q0 = tid - 32; q0 < pairs; q0 += U * NS) {
-            double2 v[U];
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t q = q0 + u * NS;
-                if (q < pairs) v[u] = *at(q);
-            }
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t q = q0 + u * NS;
-                if (q < pairs) *at(q) = make_double2(v[u].x * recip, v[u].y * recip);
+        if (atomicAdd(&X.sel_ticket, 1u) == P - 1) {
+            // The run's last member: with nothing left for the exact
+            // passes, finish the generation here -- the bookkeeping of
+            // contract_kernel's trial pass (generation index, minimum and
+            // stop test); the fitness of an interval-accepted member lies
+            // above the stop fitness, so its midpoint decides the stop test
+            // exactly.  Runs that track statistics keep the exact pass,
+            // which forms them.
+            __threadfence();
+            const uint32_t nre = *reinterpret_cast<volatile uint32_t*>(&X.sel_recheck);
+            const double mn =
+                __longlong_as_double((long long)*reinterpret_cast<volatile unsigned long long*>(&X.sel_min_bits));
+            X.sel_recheck = 0;
+            X.sel_ticket = 0;
+            X.sel_min_bits = ~0ull;
+            const bool idle = nre == 0 && !force_exact;
+            R.exact_idle = idle ? 1 : 0;
+            if (idle) {
+                const uint64_t ii = R.ii + 1;
+                R.ii = ii;
+                if (ii + 2 > R.N) {
+                    R.generation = R.N - 2;
+                    R.done = 1;
+                } else if (mn <= R.stop) {
+                    R.generation = ii;
+                    R.done = 1;
+                }
             }
         }
-    }
-    if (tid == 0) {
+    } else if (tid == kJdeThread) {
         // the next generation's jDE once the selection is final (the exact
         // passes leave the member alone); jde_kernel draws the others
         if (outcome != kRecheck) {
@@ -675,36 +684,31 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         // the next generation's trial parts set the flag and raise the maximum
         X.changed[i] = 0;
         X.xexp_max[i] = (int32_t)0x80808080;
-    }
-    __syncthreads();
-    if (!s_last || warp != 1) return;
-    // The run's last member: with nothing left for the exact passes, finish
-    // the generation here -- the bookkeeping of contract_kernel's trial pass
-    // (generation index, minimum and stop test); the fitness of an
-    // interval-accepted member lies above the stop fitness, so its midpoint
-    // decides the stop test exactly.  Runs that track statistics keep the
-    // exact pass, which forms them.
-    if (lane != 0) return;
-    __threadfence();
-    const uint32_t nre = *reinterpret_cast<volatile uint32_t*>(&X.sel_recheck);
-    const double mn = __longlong_as_double((long long)*reinterpret_cast<volatile unsigned long long*>(&X.sel_min_bits));
-    X.sel_recheck = 0;
-    X.sel_ticket = 0;
-    X.sel_min_bits = ~0ull;
-    const bool idle = nre == 0 && !force_exact;
-    R.exact_idle = idle ? 1 : 0;
-    if (!idle) return;
-    const uint64_t ii = R.ii + 1;
-    if (ii + 2 <= R.N) {
-        R.ii = ii;
-        if (mn <= R.stop) {
-            R.generation = ii;
-            R.done = 1;
+    } else if (warp >= 2 && defer && (outcome == kAccept || outcome == kRecheck)) {
+        // kDeferNorm: normalise the trial the run keeps (now the parent) or
+        // still needs (the exact passes read it): every gene times 1/norm,
+        // as trial_kernel does (M is a multiple of the 32-gene chunk: gene
+        // pairs), all loads in flight at once for M = 4096
+        const uint32_t b = outcome == kAccept ? R.cur[i] : 1u - R.cur[i];
+        const uint64_t PM = (uint64_t)P * M;
+        const uint32_t half = M / 2, pairs = S * half;
+        constexpr uint32_t NS = kSelectThreads - 64, U = 10;
+        double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)b * S * PM + (uint64_t)i * M);
+        // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
+        auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
+        for (uint32_t q0 = tid - 64; q0 < pairs; q0 += U * NS) {
+            double2 v[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) v[u] = *at(q);
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) *at(q) = make_double2(v[u].x * rc, v[u].y * rc);
+            }
         }
-    } else {
-        R.ii = ii;
-        R.generation = R.N - 2;
-        R.done = 1;
     }
 }
 
