@@ -226,7 +226,7 @@ def reference_arm(args, world, rank):
 
 # Algorithmic work per launch of each kernel kind of the split engine
 # (deac_batch_kernel_time kinds), for the roofline of the dominant one.
-BYTES_PER_TRIAL_GENE = 4 * 8 + 2 * 32 + 2 * 8 + 8  # parent+3 donors, PRNG state in/out, gene out twice, weight
+BYTES_PER_TRIAL_GENE = 4 * 8 + 2 * 32 + 8 + 7 * 2   # parent+3 donors, PRNG state in/out, gene out, 7 BF16 digits out
 BYTES_PER_NORM_GENE = 8 + 8                         # raw gene and its weight in
 KEPT_DIGIT_PAIRS = 28                               # digit pairs a+b <= 6 of seven 7-bit digits
 
@@ -237,7 +237,7 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
     if kind == 0:
         work, unit, bound, peak = genes * BYTES_PER_TRIAL_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "trial_kernel"
+        name = "trial_part_kernel+jde_kernel"
     elif kind == 2:
         # exact normalisation row sums: each trial's raw genes and the weights
         work, unit, bound, peak = genes * BYTES_PER_NORM_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
@@ -370,7 +370,7 @@ def engine_arm(args, world, rank, local):
                                              "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
     tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
-    names = {0: "trial_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
+    names = {0: "trial_part_kernel+jde_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
              3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
     roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
