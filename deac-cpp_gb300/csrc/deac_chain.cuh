@@ -122,8 +122,40 @@ __host__ __device__ __forceinline__ Term term(double x, double w, int ea, uint32
     const int ew = Ew ? (int)Ew - 1075 : -1074;
     const uint32_t neg = (uint32_t)((bx ^ bw) >> 63) ^ neg_acc;
     uint64_t hi, lo;
-    mul_wide(mx, mw, hi, lo);  // < 2^106
-    const int sh = ex + ew - ea;
+    mul_wide(mx, mw, hi, lo);  // P < 2^106, |v| = P / 2^r
+    const int r = ea - ex - ew;
+    if (r >= 51) {
+        // the usual case, without 128-bit variable shifts: h = floor(P / 2^42)
+        // (P < 2^106 fits), the bits below 2^42 only as a sticky flag; the
+        // half bit of |v| is bit r-1-42 >= 8 of h
+        const uint64_t h = (lo >> 42) | (hi << 22);
+        const uint32_t low = (lo << 22) != 0 ? 1u : 0u;
+        const int hb = r - 43;
+        uint64_t F;
+        uint32_t half, sticky;
+        if (hb < 63) {
+            F = h >> (hb + 1);
+            half = (uint32_t)(h >> hb) & 1u;
+            sticky = ((h << (64 - hb)) != 0 ? 1u : 0u) | low;
+        } else if (hb == 63) {
+            F = 0;
+            half = (uint32_t)(h >> 63);
+            sticky = ((h << 1) != 0 ? 1u : 0u) | low;
+        } else {
+            F = 0;
+            half = 0;
+            sticky = 1;  // 0 < |v| < 1/2 (P > 0)
+        }
+        if ((F >> 54) != 0) {
+            t.flags = kBad | kBig;
+            return t;
+        }
+        t.F = F;
+        t.flags = (half && sticky ? kGtHalf : 0u) | (half && !sticky ? kTie : 0u) | (half || sticky ? kGtZero : 0u) |
+                  (neg ? kNeg : 0u);
+        return t;
+    }
+    const int sh = -r;
     uint32_t half = 0, sticky = 0;
     if (sh >= 0) {
         if (sh >= 54 || hi != 0 || (lo >> (54 - sh)) != 0) {

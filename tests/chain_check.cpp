@@ -20,8 +20,66 @@ static uint64_t bits(double d) {
     return b;
 }
 
+// term() against its definition evaluated with 128-bit integers: |v| =
+// mx*mw / 2^(ea - ex - ew), F = floor(|v|), the fraction above / at / below
+// one half, a term of 2^54 or more (or non-finite) flagged kBad.
+static bool term_matches(double x, double w, int ea, uint32_t neg_acc) {
+    using namespace deac::chain_detail;
+    const Term t = term(x, w, ea, neg_acc);
+    const uint64_t bx = bits(x), bw = bits(w);
+    const int Ex = (int)((bx >> 52) & 0x7FF), Ew = (int)((bw >> 52) & 0x7FF);
+    if (Ex == 0x7FF || Ew == 0x7FF) return (t.flags & kBad) != 0;
+    const uint64_t mx = (bx & ((1ull << 52) - 1)) | (Ex ? (1ull << 52) : 0), mw = (bw & ((1ull << 52) - 1)) | (Ew ? (1ull << 52) : 0);
+    if (mx == 0 || mw == 0) return t.F == 0 && t.flags == 0;
+    const int ex = Ex ? Ex - 1075 : -1074, ew = Ew ? Ew - 1075 : -1074;
+    const unsigned __int128 P = (unsigned __int128)mx * mw;
+    const int r = ea - ex - ew;
+    unsigned __int128 F;
+    bool half = false, sticky = false;
+    if (r <= 0) {
+        if (-r >= 54 || (P >> (54 + r)) != 0) return (t.flags & kBad) != 0;
+        F = P << -r;
+    } else if (r >= 128) {
+        F = 0;
+        sticky = true;
+    } else {
+        F = P >> r;
+        half = ((P >> (r - 1)) & 1) != 0;
+        sticky = r > 1 && (P & ((((unsigned __int128)1) << (r - 1)) - 1)) != 0;
+    }
+    if ((F >> 54) != 0) return (t.flags & kBad) != 0;
+    const uint32_t neg = (uint32_t)((bx ^ bw) >> 63) ^ neg_acc;
+    const uint32_t flags = (half && sticky ? kGtHalf : 0u) | (half && !sticky ? kTie : 0u) |
+                           (half || sticky ? kGtZero : 0u) | (neg ? kNeg : 0u);
+    return t.F == (uint64_t)F && t.flags == flags;
+}
+
 int main(int argc, char** argv) {
     const int cases = argc > 1 ? std::atoi(argv[1]) : 4000;
+    {
+        // decoded terms: random significands, every exponent gap around the
+        // decoding paths, subnormal and power-of-two operands
+        std::mt19937_64 trng(777);
+        for (int k = 0; k < 400000; ++k) {
+            const uint64_t u = trng(), v = trng();
+            double x, w;
+            const int mode = k % 4;
+            uint64_t bx = (u & ((1ull << 52) - 1)) | ((uint64_t)(1 + trng() % 2046) << 52) | (u & (1ull << 63));
+            uint64_t bw = (v & ((1ull << 52) - 1)) | ((uint64_t)(1 + trng() % 2046) << 52);
+            if (mode == 1) bx &= ~((1ull << (trng() % 53)) - 1);  // few significant bits: exact halves
+            if (mode == 2) bw = (bw & ~((1ull << 52) - 1));         // power-of-two weight
+            if (mode == 3) bx &= (1ull << 52) - 1;                  // subnormal gene
+            std::memcpy(&x, &bx, 8);
+            std::memcpy(&w, &bw, 8);
+            const int Ex = (int)((bx >> 52) & 0x7FF), Ew = (int)((bw >> 52) & 0x7FF);
+            const int base = (Ex ? Ex - 1075 : -1074) + (Ew ? Ew - 1075 : -1074);
+            const int ea = base + (int)(trng() % 200) - 20;  // gaps r from -20 to 179
+            if (!term_matches(x, w, ea, (uint32_t)(trng() & 1))) {
+                std::printf("term mismatch x=%a w=%a ea=%d\n", x, w, ea);
+                return 1;
+            }
+        }
+    }
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     uint64_t plain_total = 0, steps_total = 0;
