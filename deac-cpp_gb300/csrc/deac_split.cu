@@ -308,14 +308,16 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         }
         s_xmax[r] = m;
     }
-    // this thread's TMEM lane (timeslice) and rows
-    const uint32_t quarter = warp & 3u, half = warp >> 2;
+    // this thread's TMEM lane (timeslice) and rows: warp w reads lane
+    // quarter w % 4 (a tcgen05.ld rule), row slice w / 4
+    constexpr uint32_t kRows = kRowTile / (kSplitThreads / 128);  // rows per thread
+    const uint32_t quarter = warp & 3u, slice = warp >> 2;
     const uint32_t tl = quarter * 32 + lane;  // timeslice within the tile
-    const uint32_t r0 = half * 32;            // first of this thread's 32 rows
+    const uint32_t r0 = slice * kRows;        // first of this thread's rows
     // double-float accumulators of this thread's (timeslice, row) outputs
-    float acc_hi[32], acc_lo[32];
+    float acc_hi[kRows], acc_lo[kRows];
 #pragma unroll
-    for (uint32_t r = 0; r < 32; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
+    for (uint32_t r = 0; r < kRows; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
 
     __syncthreads();  // s_kmax / s_xmax
     if (tid == 0) {
@@ -359,7 +361,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         // --- fold the seven exact group sums of this chunk into the accumulators
         const int ek = s_ek[tl];
 #pragma unroll
-        for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
+        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
             uint32_t d[kKept][8];
 #pragma unroll
             for (int g = 0; g < kKept; ++g) tmem_ld8(lane_base + g * kRowTile + r0 + j8, d[g]);
@@ -403,7 +405,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         // partial sums and the bound accumulator sum_c 2^(e_x-max_x + e_K-max_K)
         float4* out = partial + (uint64_t)wk.block * kPartialBlock;
 #pragma unroll
-        for (uint32_t j8 = 0; j8 < 32; j8 += 8) {
+        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
             uint32_t d[8];
             tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");

@@ -42,7 +42,7 @@ constexpr int kDigitBits = 7 * kDigits;
 constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // MMA N: trial rows
-constexpr int kSplitThreads = 256; // two warps per TMEM lane quarter
+constexpr int kSplitThreads = 512; // four warps per TMEM lane quarter, 16 rows each
 constexpr int kSelectThreads = 512;
 // dynamic shared memory of split_contract_kernel for S sides: K digits
 // [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and the two bound
