@@ -523,9 +523,20 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const bool force_exact = (R.flags & kTrackStats) != 0;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     constexpr uint32_t kJdeThread = 32;  // warp 1 draws the jDE; warp 0 keeps the run's tallies
-    // the member's jDE slots for the next generation, loaded now
+    // the member's jDE slots for the next generation and both halves of its
+    // CR / F (the parent's, the trial's), loaded now
     uint64_t jst[4][4];
-    if (tid == kJdeThread) jde_load(R, i, jst);
+    double cr2[2][2], fw2[2][2];  // [parent, trial][side]
+    if (tid == kJdeThread) {
+        jde_load(R, i, jst);
+#pragma unroll
+        for (uint32_t h = 0; h < 2; ++h)
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s) {
+                cr2[h][s] = s < S ? R.cr[(uint64_t)h * S * P + s * P + i] : 0.0;
+                fw2[h][s] = s < S ? R.fw[(uint64_t)h * S * P + s * P + i] : 0.0;
+            }
+    }
     // this thread's first timeslice, loaded with the `changed` flag (one
     // round trip; unused when the trial equals its parent)
     const uint64_t o0 = (uint64_t)i * Nt + tid;
@@ -593,13 +604,16 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             s_dchi[warp] = dchi;
         }
         __syncthreads();
-        if (tid == 0) {
-            chi = 0.0;
-            dchi = 0.0f;
-            for (uint32_t w = 0; w < kSelectThreads / 32; ++w) {
-                chi += s_chi[w];
-                dchi = __fadd_ru(dchi, s_dchi[w]);
+        if (warp == 0) {
+            // the warps' sums by a shuffle tree (any order: the bound covers it)
+            chi = lane < kSelectThreads / 32 ? s_chi[lane] : 0.0;
+            dchi = lane < kSelectThreads / 32 ? s_dchi[lane] : 0.0f;
+            for (int o = 8; o > 0; o >>= 1) {
+                chi += __shfl_xor_sync(0xffffffffu, chi, o);
+                dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
             }
+        }
+        if (tid == 0) {
             X.recheck[i] = 0;
             // /Nt as a product with 1/Nt rounded once: two roundings where a
             // quotient has one, covered by two more units of the slack below
@@ -674,10 +688,12 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         if (outcome != kRecheck) {
             double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
             uint32_t mut[3];
+            // the CR / F the selection kept: the trial's unless rejected
+            const uint32_t h = outcome == kReject ? 0u : 1u;
 #pragma unroll
             for (uint32_t s = 0; s < 2; ++s) {
-                cr_old[s] = s < S ? R.cr[s * P + i] : 0.0;
-                fw_old[s] = s < S ? R.fw[s * P + i] : 0.0;
+                cr_old[s] = h ? cr2[1][s] : cr2[0][s];
+                fw_old[s] = h ? fw2[1][s] : fw2[0][s];
             }
             jde_draw(R, i, jst, cr_old, fw_old, cr_new, fw_new, mut);
             jde_store(R, i, jst, cr_new, fw_new, mut, true);
