@@ -237,7 +237,7 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
     if kind == 0:
         work, unit, bound, peak = genes * BYTES_PER_TRIAL_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "trial_part_kernel+jde_kernel"
+        name = "trial_part_kernel"
     elif kind == 2:
         # exact normalisation row sums: each trial's raw genes and the weights
         work, unit, bound, peak = genes * BYTES_PER_NORM_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
@@ -370,7 +370,7 @@ def engine_arm(args, world, rank, local):
                                              "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
     tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
-    names = {0: "trial_part_kernel+jde_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
+    names = {0: "trial_part_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
              3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
     roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
@@ -415,9 +415,9 @@ def engine_arm(args, world, rank, local):
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
-        # per generation: jDE, trial parts, normalisation row sums, tensor
+        # per generation: trial parts, normalisation row sums, tensor
         # contraction, combine, selection, 2 exact passes
-        "gpu_launches": 8 * G * args.steps,
+        "gpu_launches": 7 * G * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

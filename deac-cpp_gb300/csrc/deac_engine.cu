@@ -220,14 +220,15 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
             b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
     } else {
-        launch(deac::jde_kernel, (b->n_trial_ctas + 127) / 128, 128, 0, s, early, b->d_runs,
-               static_cast<const deac::Work*>(b->d_trial_work), b->n_trial_ctas);
         launch(deac::trial_part_kernel, b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early,
                b->d_runs, static_cast<const deac::Work*>(b->d_part_work));
     }
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
         launch_contract(b, s, init_mode ? deac::kModeInit : deac::kModeGeneration);
+        if (init_mode && b->engine != DEAC_ENGINE_PLAIN_FP64)
+            deac::jde_kernel<<<(b->n_trial_ctas + 127) / 128, 128, 0, s>>>(
+                b->d_runs, static_cast<const deac::Work*>(b->d_trial_work), b->n_trial_ctas);
         return mark(1);
     }
     // the normalisation row sums of --normalize runs: forked beside the
@@ -485,7 +486,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
-        const uint64_t o_cnt = sa.take(3 * 8), o_jd = sa.take(P);
+        const uint64_t o_cnt = sa.take(3 * 8);
         const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
@@ -527,7 +528,6 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.xexp = x.xexp;
         d.xexp_max = x.xexp_max;
         d.mutants = reinterpret_cast<uint32_t*>(sb + o_mu);
-        d.jde_done = reinterpret_cast<uint8_t*>(sb + o_jd);  // zero: jde_kernel draws every member
         d.recheck = x.recheck;
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;

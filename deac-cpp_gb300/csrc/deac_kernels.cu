@@ -335,14 +335,15 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 
 // --------------------------------------------------------------- split trials
 // Split engine: jDE and the mutant indices of every member, one thread each
-// (work = the trial work list).
+// (work = the trial work list), once after the initial population; later
+// generations draw them where each member's selection becomes final
+// (split_select_kernel, or the exact trial pass of contract_kernel).
 __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work, uint32_t n) {
-    grid_dependency_wait();
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const Work w = work[k];
     RunDev& R = runs[w.run];
-    if (R.done || R.jde_done[w.index]) return;  // the selection drew it already
+    if (R.done) return;
     double cr[2], fw[2];
     uint32_t mut[3];
     jde_member(R, w.index, cr, fw, mut);
@@ -355,82 +356,109 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
 // trial's `changed` flag when a gene mutated and raises its maximum chunk
 // exponent (split_select_kernel resets both after use).
 __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev* runs, const Work* work) {
-    grid_dependency_wait();
     extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
     __shared__ double s_fw[2];
     __shared__ uint64_t s_thr[2];
+    __shared__ uint32_t s_mut[3];
+    __shared__ uint8_t s_cur[kTrialPartThreads];
     __shared__ int s_digit_max[kTrialPartThreads / 32];
+    // Before the wait only the static run description is read: the part's
+    // PRNG states (which the preceding exact pass leaves alone) are
+    // prefetched into L2 meanwhile.
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
-    if (R.done) return;
     const uint32_t i = wk.index & 0xFFFFFu, part = wk.index >> 20;
     const uint32_t P = R.P, M = R.M, S = R.S;
     const uint64_t PM = (uint64_t)P * M;
     const uint32_t j0 = part * kTrialPart;
     const uint32_t len = M - j0 < kTrialPart ? M - j0 : kTrialPart;
-    const uint32_t parent_buf = R.cur[i];
-    double* dst = R.pop + ((uint64_t)(1u - parent_buf) * S) * PM + (uint64_t)i * M;
+    const uint64_t n = R.n_states;
+    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
+    const uint64_t buf = (uint64_t)S * PM;
+    if (threadIdx.x < 4 * S)
+        prefetch_l2(R.rng + (threadIdx.x / S) * n + base + 1 + (uint64_t)(threadIdx.x % S) * M + j0, len,
+                    R.rng + 4 * n);
+    grid_dependency_wait();
+    if (R.done) return;
+    // one round trip: the member's CR / F and mutant indices, and the
+    // parent buffer of every member of the run (of the mutants on demand
+    // when the run has more members than the CTA has threads)
+    const bool table = P <= kTrialPartThreads;
+    if (table && threadIdx.x < P) s_cur[threadIdx.x] = R.cur[threadIdx.x];
     if (threadIdx.x < S) {
         const double cr = R.cr[(uint64_t)S * P + threadIdx.x * P + i];
         s_thr[threadIdx.x] = crossover_threshold(cr);
         s_fw[threadIdx.x] = R.fw[(uint64_t)S * P + threadIdx.x * P + i];
+    } else if (threadIdx.x >= 32 && threadIdx.x < 35) {
+        s_mut[threadIdx.x - 32] = R.mutants[3 * i + threadIdx.x - 32];
     }
     __syncthreads();
-    const uint32_t r0 = R.mutants[3 * i], r1 = R.mutants[3 * i + 1], r2 = R.mutants[3 * i + 2];
-    const uint64_t buf = (uint64_t)S * PM;
-    const double* pa = R.pop + (uint64_t)R.cur[r0] * buf + (uint64_t)r0 * M;
-    const double* pb = R.pop + (uint64_t)R.cur[r1] * buf + (uint64_t)r1 * M;
-    const double* pc = R.pop + (uint64_t)R.cur[r2] * buf + (uint64_t)r2 * M;
+    const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
+    auto cur = [&](uint32_t m) -> uint64_t { return table ? s_cur[m] : R.cur[m]; };
+    const uint32_t parent_buf = (uint32_t)cur(i);
+    double* dst = R.pop + ((uint64_t)(1u - parent_buf) * S) * PM + (uint64_t)i * M;
+    const double* pa = R.pop + cur(r0) * buf + (uint64_t)r0 * M;
+    const double* pb = R.pop + cur(r1) * buf + (uint64_t)r1 * M;
+    const double* pc = R.pop + cur(r2) * buf + (uint64_t)r2 * M;
     const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
+    if (S == 2 && threadIdx.x < 4) {
+        // the second side's rows, read after the first side's pass
+        const double* rows[4] = {pa, pb, pc, px};
+        prefetch_l2(rows[threadIdx.x] + PM + j0, len, R.pop + 2 * buf);
+    }
     const bool keep_sign = (R.flags & kSignedWeights) != 0;
-    const uint64_t n = R.n_states;
-    const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
-    const uint32_t items = S * len;
     bool mutated = false;
-    constexpr int H = 3;  // genes in flight per thread (128 registers, no spills)
-    for (uint32_t e0 = threadIdx.x; e0 < items; e0 += H * blockDim.x) {
-        uint64_t st[H][4];
-        double a[H], b[H], cc[H], x[H];
-        uint32_t sd[H], jj[H];
-        bool ok[H];
+    constexpr uint32_t H = 4;  // genes in flight per thread (one pass of a 1024-gene side)
+    for (uint32_t s = 0; s < S; ++s) {
+        uint64_t* st0 = R.rng + base + 1 + (uint64_t)s * M + j0;
+        const uint64_t off = (uint64_t)s * PM + j0;
+        const double *qa = pa + off, *qb = pb + off, *qc = pc + off, *qx = px + off;
+        double* qd = dst + off;
+        double* qs = part_s + s * len;
+        const uint64_t thr = s_thr[s];
+        const double fw = s_fw[s];
+        for (uint32_t j = threadIdx.x; j < len; j += H * blockDim.x) {
+            uint64_t st[H][4];
+            double a[H], b[H], c[H], x[H];
 #pragma unroll
-        for (int h = 0; h < H; ++h) {
-            const uint32_t e = e0 + (uint32_t)h * blockDim.x;
-            ok[h] = e < items;
-            const uint32_t ee = ok[h] ? e : e0;
-            sd[h] = ee / len;
-            jj[h] = j0 + (ee - sd[h] * len);
-            const uint64_t slot = base + 1 + (uint64_t)sd[h] * M + jj[h];
-            st[h][0] = R.rng[slot];
-            st[h][1] = R.rng[n + slot];
-            st[h][2] = R.rng[2 * n + slot];
-            st[h][3] = R.rng[3 * n + slot];
-            const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
-            a[h] = pa[off];
-            b[h] = pb[off];
-            cc[h] = pc[off];
-            x[h] = px[off];
-        }
-#pragma unroll
-        for (int h = 0; h < H; ++h) {
-            if (!ok[h]) continue;
-            const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
-            store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
-            double v = x[h];
-            if (mutate) {
-                v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
-                if (!keep_sign) v = fabs(v);
-                mutated = true;
+            for (uint32_t h = 0; h < H; ++h) {
+                const uint32_t jj = j + h * blockDim.x;
+                const uint32_t k = jj < len ? jj : j;
+                st[h][0] = st0[k];
+                st[h][1] = st0[n + k];
+                st[h][2] = st0[2 * n + k];
+                st[h][3] = st0[3 * n + k];
+                a[h] = qa[k];
+                b[h] = qb[k];
+                c[h] = qc[k];
+                x[h] = qx[k];
             }
-            dst[(uint64_t)sd[h] * PM + jj[h]] = v;
-            part_s[(uint64_t)sd[h] * len + (jj[h] - j0)] = v;
+#pragma unroll
+            for (uint32_t h = 0; h < H; ++h) {
+                const uint32_t jj = j + h * blockDim.x;
+                if (jj >= len) continue;
+                const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < thr;
+                uint64_t* so = st0 + jj;
+                so[0] = st[h][0];
+                so[n] = st[h][1];
+                so[2 * n] = st[h][2];
+                so[3 * n] = st[h][3];
+                double v = x[h];
+                if (mutate) {
+                    v = fma(fw, b[h] - c[h], a[h]);
+                    if (!keep_sign) v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
+                    mutated = true;
+                }
+                qd[jj] = v;
+                qs[part_slot(jj, s)] = v;
+            }
         }
     }
     __syncthreads();
     if (S == 2 && j0 == 0 && threadIdx.x == 0) {
         // gpu_match_population_zero (deac_gpu.cu:541-549)
-        dst[PM] = part_s[0];
-        part_s[len] = part_s[0];
+        dst[PM] = part_s[part_slot(0, 0)];
+        part_s[len + part_slot(0, 1)] = part_s[part_slot(0, 0)];
     }
     if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;
     digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * 8 + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_plane,
@@ -709,6 +737,17 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
         }
         ii += 1;
         __syncthreads();
+        if (mode == kModeTrials && threadIdx.x >= 32) {
+            // the next generation's jDE of the members settled here (the
+            // selection kernel drew the others), beside the statistics
+            for (uint32_t m = threadIdx.x - 32; m < P; m += blockDim.x - 32) {
+                if (!wanted(m)) continue;
+                double cr[2], fw[2];
+                uint32_t mut[3];
+                jde_member(R, m, cr, fw, mut);
+                for (int q = 0; q < 3; ++q) R.mutants[3 * m + q] = mut[q];
+            }
+        }
     }
 
     // top of the next generation (deac.cpp:1138-1166): statistics of the

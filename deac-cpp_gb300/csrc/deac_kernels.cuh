@@ -97,7 +97,6 @@ struct RunDev {
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
     uint32_t* mutants;       // [P][3] mutant indices of this generation
-    uint8_t* jde_done;       // [P] split engine: the selection drew the member's next jDE
     // split engine with --normalize (kDeferNorm): the trials stay raw until
     // the decisions; norm_kernel forms each trial's exact reciprocal norm
     double* recip;           // [P] 1/norm of each trial
@@ -179,10 +178,23 @@ __device__ __forceinline__ void grid_dependency_wait() {
     asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
+// Asynchronous L2 prefetch of the `count` elements at p, rounded out to the
+// 16-byte units a bulk copy addresses and clipped at `end` (one past the
+// buffer's last element), so that it never reaches beyond the buffer.
+template <typename T>
+__device__ __forceinline__ void prefetch_l2(const T* p, uint64_t count, const T* end) {
+    const uint64_t a = reinterpret_cast<uint64_t>(p) & ~15ull;
+    uint64_t e = (reinterpret_cast<uint64_t>(p + count) + 15u) & ~15ull;
+    const uint64_t lim = reinterpret_cast<uint64_t>(end) & ~15ull;
+    if (e > lim) e = lim;
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
+}
+
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
-// split engine generations: jDE of every member (one thread each), then the
-// raw trials in parts of kTrialPart genes per side (work index =
-// part << 20 | member), each with its BF16 digit slices
+// split engine: jDE of every member (one thread each) after the initial
+// population; each generation's raw trials in parts of kTrialPart genes per
+// side (work index = part << 20 | member), each with its BF16 digit slices
 constexpr uint32_t kTrialPart = 1024;
 constexpr int kTrialPartThreads = 256;
 __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);

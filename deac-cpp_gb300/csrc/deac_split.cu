@@ -684,7 +684,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         }
     } else if (tid == kJdeThread) {
         // the next generation's jDE once the selection is final (the exact
-        // passes leave the member alone); jde_kernel draws the others
+        // passes leave the member alone); the exact trial pass draws the others
         if (outcome != kRecheck) {
             double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
             uint32_t mut[3];
@@ -698,7 +698,6 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             jde_draw(R, i, jst, cr_old, fw_old, cr_new, fw_new, mut);
             jde_store(R, i, jst, cr_new, fw_new, mut, true);
         }
-        R.jde_done[i] = outcome != kRecheck ? 1 : 0;
         // the next generation's trial parts set the flag and raise the maximum
         X.changed[i] = 0;
         X.xexp_max[i] = (int32_t)0x80808080;

@@ -138,45 +138,86 @@ __device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
     return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
 }
 
-// The digit planes of M genes of one trial (both sides, genes in `x` at side
-// stride `side_stride`) by the calling CTA, a warp per 32-gene chunk: the
-// chunk's scale exponent (max over both sides), seven 7-bit digits per gene,
-// and the maximum exponent raised into *xexp_max.  `xdig` points at the
-// trial's row in the tiled planes at its first gene's unit.  `s_max` is
+// Position in shared memory of gene j (of a trial part) on side s, within
+// the side's row: the genes of each 8-gene unit permuted in pairs so that the
+// eight threads of a chunk in digitize_trial read their units' pairs from
+// eight distinct bank groups.
+__device__ __forceinline__ uint32_t part_slot(uint32_t j, uint32_t s) {
+    return j ^ ((((j >> 4) & 1u) << 2) | ((s & 1u) << 1));
+}
+
+// BF16 bits (in the upper half of the word) of the 7-bit digit of f at bit
+// `shift`, negated when sg = -1: (2^23 + d) - 2^23 in one exact FMA, which
+// gives +0 for d = 0 on either sign.
+__device__ __forceinline__ uint32_t digit_bits(uint64_t f, int shift, float sg) {
+    const uint32_t d = (uint32_t)(f >> shift) & 127u;
+    return __float_as_uint(__fmaf_rn(sg, __uint_as_float(0x4B000000u | d), -sg * 8388608.0f));
+}
+
+// The digit planes of the `len` genes (a multiple of kChunk) of one trial
+// part, both sides, read from shared memory `x` (side s at s * side_stride,
+// gene j at part_slot(j, s)) by the calling CTA (blockDim.x a multiple of
+// 32): eight threads per 32-gene chunk, each one 16-byte unit of 8 genes of
+// one side.  A chunk's scale exponent is the maximum over both sides; each
+// gene gets seven 7-bit digits, written as one 16-byte store per digit plane;
+// the part's maximum exponent is raised into *xexp_max.  `xdig` points at the
+// trial's row in the tiled planes at the part's first unit.  `s_max` is
 // shared scratch of one int per warp.
-__device__ __forceinline__ void digitize_trial(const double* x, uint64_t side_stride, uint32_t S, uint32_t M,
+__device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_stride, uint32_t S, uint32_t len,
                                                uint16_t* xdig, uint64_t plane_stride, uint64_t unit_stride,
                                                int16_t* xexp, int32_t* xexp_max, int* s_max) {
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
-    const uint32_t C = M / kChunk;
+    const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t s = (threadIdx.x >> 2) & 1u, uq = threadIdx.x & 3u;
+    const uint32_t C = len / kChunk, per_pass = blockDim.x >> 3;
+    const uint64_t digit_step = (uint64_t)S * plane_stride;  // from one digit plane to the next
     int wmax = -2000;
-    for (uint32_t c = warp; c < C; c += nw) {
-        const uint32_t j = c * kChunk + lane;
-        double v[2] = {0.0, 0.0};
+    for (uint32_t c0 = 0; c0 < C; c0 += per_pass) {
+        const uint32_t c = c0 + (threadIdx.x >> 3);
+        const bool live = c < C && s < S;
+        const uint32_t u = c * 4 + uq;  // this thread's unit within the part
+        double v[8];
         int e = -2000;
+        if (live) {
+            const double* row = x + s * side_stride + u * 8;
 #pragma unroll
-        for (uint32_t s = 0; s < 2; ++s)
-            if (s < S) {
-                v[s] = x[s * side_stride + j];
-                e = max(e, exp_of(v[s]));
+            for (uint32_t k = 0; k < 4; ++k) {
+                const double2 q = *reinterpret_cast<const double2*>(row + part_slot(u * 8 + 2 * k, s) - u * 8);
+                v[2 * k] = q.x;
+                v[2 * k + 1] = q.y;
             }
-        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-        e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
 #pragma unroll
-        for (uint32_t s = 0; s < 2; ++s) {
-            if (s >= S) break;
-            const uint64_t f = frac_digits(v[s], e);
-            const bool neg = v[s] < 0.0;
+            for (uint32_t k = 0; k < 8; ++k) e = max(e, exp_of(v[k]));
+        }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
+        if (live) {
+            uint64_t f[8];
+            float sg[8];
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                f[k] = frac_digits(v[k], e);
+                // the sign bit (integer test: FP64 compares share the narrow
+                // FP64 pipe); -0 and zero digits give +0 either way
+                sg[k] = __double_as_longlong(v[k]) < 0 ? -1.0f : 1.0f;
+            }
+            uint16_t* q = xdig + s * plane_stride + (uint64_t)u * unit_stride;
 #pragma unroll
             for (int b = 0; b < kDigits; ++b) {
-                const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
-                xdig[((uint64_t)b * S + s) * plane_stride + (j >> 3) * unit_stride + (j & 7u)] = bf16_digit(d, neg);
+                const int sh = 7 * (kDigits - 1 - b);
+                uint32_t w[4];
+#pragma unroll
+                for (uint32_t k = 0; k < 4; ++k)
+                    w[k] = __byte_perm(digit_bits(f[2 * k], sh, sg[2 * k]), digit_bits(f[2 * k + 1], sh, sg[2 * k + 1]),
+                                       0x7632);
+                *reinterpret_cast<uint4*>(q + b * digit_step) = make_uint4(w[0], w[1], w[2], w[3]);
             }
+            if ((threadIdx.x & 7u) == 0) xexp[c] = (int16_t)e;
         }
-        if (lane == 0) xexp[c] = (int16_t)e;
-        wmax = max(wmax, e);
+        if (c < C) wmax = max(wmax, e);
     }
-    if (lane == 0) s_max[warp] = wmax;
+    wmax = __reduce_max_sync(0xffffffffu, wmax);
+    if ((threadIdx.x & 31u) == 0) s_max[warp] = wmax;
     __syncthreads();
     if (threadIdx.x == 0) {
         int m = -2000;
