@@ -514,8 +514,11 @@ struct ChainScratch {
 
 namespace chain_detail {
 
+// The non-aligned barrier: the threads of a warp may arrive diverged (after
+// a branch taken by one thread, e.g. the group's one-thread sequential
+// parts); the aligned form (bar.sync) requires the warp to arrive converged.
 __device__ __forceinline__ void group_bar(int id, int threads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+    asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
 }  // namespace chain_detail

@@ -73,7 +73,7 @@ def _chains(kind, n, count, rng):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [1, 7, 256, 257, 4096, 5000])
+@pytest.mark.parametrize("n", [1, 7, 256, 257, 4096, 5000, 12288])
 def test_warp_chain_matches_sequential_fma(engine, n):
     lib = engine.load_library()
     fn = lib.deac_debug_fma_chains
