@@ -36,19 +36,30 @@ __device__ __forceinline__ void jde_load(const RunDev& R, uint32_t i, uint64_t (
         for (uint32_t w = 0; w < 4; ++w) st[q][w] = (q < 2 * R.S) ? rng[w * n + base + q] : 0ull;
 }
 
-// the draws of member i from its slots st (advanced in place) and its
-// current CR / F
-__device__ __forceinline__ void jde_draw(const RunDev& R, uint32_t i, uint64_t (&st)[4][4], const double cr_old[2],
-                                         const double fw_old[2], double cr_new[2], double fw_new[2], uint32_t mut[3]) {
+// Every draw of member i's jDE step from its slots st (advanced in place):
+// per side whether CR / F take a new value and that value, then the mutant
+// indices.  None of it depends on the current CR / F, so the draws can be
+// made before the selection that decides which CR / F the member keeps.
+struct JdeDraws {
+    double cr[2], fw[2];
+    bool cr_new[2], fw_new[2];
+    uint32_t mut[3];
+};
+
+__device__ __forceinline__ void jde_draws(const RunDev& R, uint32_t i, uint64_t (&st)[4][4], JdeDraws& d) {
     const uint32_t P = R.P;
     // draw < tau  <=>  (x >> 11) < ceil(tau 2^53) (draw = (x >> 11) 2^-53
     // exactly): integer tests, a conversion only for a new value
     const uint64_t thr_cr = R.tau_cr_thr, thr_f = R.tau_f_thr;
     auto bits = [](uint64_t (&st)[4]) { return xoshiro_next(st[0], st[1], st[2], st[3]) >> 11; };
     auto side = [&](uint32_t s, uint64_t (&cs)[4], uint64_t (&fs)[4]) {
-        cr_new[s] = bits(cs) < thr_cr ? (double)bits(cs) * 0x1.0p-53 : cr_old[s];
-        fw_new[s] = bits(fs) < thr_f ? (double)bits(fs) * 0x1.0p-52 : fw_old[s];  // 2 * draw
+        d.cr_new[s] = bits(cs) < thr_cr;
+        d.cr[s] = d.cr_new[s] ? (double)bits(cs) * 0x1.0p-53 : 0.0;
+        d.fw_new[s] = bits(fs) < thr_f;
+        d.fw[s] = d.fw_new[s] ? (double)bits(fs) * 0x1.0p-52 : 0.0;  // 2 * draw
     };
+    d.cr_new[1] = d.fw_new[1] = false;
+    d.cr[1] = d.fw[1] = 0.0;
     side(0, st[0], st[1]);
     if (R.S == 2) side(1, st[2], st[3]);
     // rejection sampling as in the reference; P >= 4 is enforced on the
@@ -58,9 +69,31 @@ __device__ __forceinline__ void jde_draw(const RunDev& R, uint32_t i, uint64_t (
     while (r0 == i) r0 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
     while (r1 == i || r1 == r0) r1 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
     while (r2 == i || r2 == r0 || r2 == r1) r2 = mod_p(xoshiro_next(st[0][0], st[0][1], st[0][2], st[0][3]), P, pm);
-    mut[0] = (uint32_t)r0;
-    mut[1] = (uint32_t)r1;
-    mut[2] = (uint32_t)r2;
+    d.mut[0] = (uint32_t)r0;
+    d.mut[1] = (uint32_t)r1;
+    d.mut[2] = (uint32_t)r2;
+}
+
+// the new CR / F from the draws and the CR / F the member keeps
+__device__ __forceinline__ void jde_apply(const JdeDraws& d, const double cr_old[2], const double fw_old[2],
+                                          double cr_new[2], double fw_new[2]) {
+#pragma unroll
+    for (uint32_t s = 0; s < 2; ++s) {
+        cr_new[s] = d.cr_new[s] ? d.cr[s] : cr_old[s];
+        fw_new[s] = d.fw_new[s] ? d.fw[s] : fw_old[s];
+    }
+}
+
+// the draws of member i from its slots st (advanced in place) and its
+// current CR / F
+__device__ __forceinline__ void jde_draw(const RunDev& R, uint32_t i, uint64_t (&st)[4][4], const double cr_old[2],
+                                         const double fw_old[2], double cr_new[2], double fw_new[2], uint32_t mut[3]) {
+    JdeDraws d;
+    jde_draws(R, i, st, d);
+    jde_apply(d, cr_old, fw_old, cr_new, fw_new);
+    mut[0] = d.mut[0];
+    mut[1] = d.mut[1];
+    mut[2] = d.mut[2];
 }
 
 // store the outcome: the new CR / F (upper halves of cr / fw), the advanced

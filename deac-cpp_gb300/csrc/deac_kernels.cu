@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
 // gene as in trial_kernel, then the part's BF16 digit slices.  Sets the
 // trial's `changed` flag when a gene mutated and raises its maximum chunk
 // exponent (split_select_kernel resets both after use).
-__global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev* runs, const Work* work) {
+__global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev* runs, const Work* work) {
     extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
     __shared__ double s_fw[2];
     __shared__ uint64_t s_thr[2];
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kTrialPartThreads, 2) trial_part_kernel(RunDev
     }
     const bool keep_sign = (R.flags & kSignedWeights) != 0;
     bool mutated = false;
-    constexpr uint32_t H = 4;  // genes in flight per thread (one pass of a 1024-gene side)
+    constexpr uint32_t H = 4;  // genes in flight per thread (one pass of a 512-gene side)
     for (uint32_t s = 0; s < S; ++s) {
         uint64_t* st0 = R.rng + base + 1 + (uint64_t)s * M + j0;
         const uint64_t off = (uint64_t)s * PM + j0;

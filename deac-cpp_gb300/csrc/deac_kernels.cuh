@@ -195,8 +195,8 @@ __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int 
 // split engine: jDE of every member (one thread each) after the initial
 // population; each generation's raw trials in parts of kTrialPart genes per
 // side (work index = part << 20 | member), each with its BF16 digit slices
-constexpr uint32_t kTrialPart = 1024;
-constexpr int kTrialPartThreads = 256;
+constexpr uint32_t kTrialPart = 512;
+constexpr int kTrialPartThreads = 128;
 __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const Work* work);
 // split engine, kDeferNorm runs: the exact normalisation row sums of one raw

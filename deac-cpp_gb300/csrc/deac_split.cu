@@ -500,17 +500,23 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
 }
 
 // ---------------------------------------------------------------- select
-// One CTA per member: the estimate's chi^2 and its interval, the selection
-// decision the interval settles (undecided members are flagged for the exact
-// FP64 evaluation, contract_kernel's recheck mode), the normalisation of the
-// trial the run keeps or still needs (kDeferNorm), and the next generation's
-// jDE of the member once its selection is final.  The run's last CTA does
-// the generation's bookkeeping when no member needs the exact pass.
+// One CTA per member, in two roles.  Warps 0-3 form the estimate's chi^2 and
+// its interval and make the selection decision the interval settles
+// (undecided members are flagged for the exact FP64 evaluation,
+// contract_kernel's recheck mode); thread 0 then keeps the run's tallies,
+// and the run's last CTA does the generation's bookkeeping when no member
+// needs the exact pass.  Warps 4-14 meanwhile normalise the raw trial of
+// kDeferNorm runs (needed when it is kept or rechecked; a rejected trial's
+// row is rewritten by the next generation's trial parts, so scaling it
+// regardless takes the scaling off the decision's path), and the last
+// warp's first thread draws the next generation's jDE, which it stores once
+// the decision is known.
 __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* runs, SplitRun* split,
                                                                      const Work* work) {
     grid_dependency_wait();
-    __shared__ double s_chi[kSelectThreads / 32];
-    __shared__ float s_dchi[kSelectThreads / 32];
+    constexpr uint32_t kChiWarps = 4, kChiThreads = kChiWarps * 32;
+    __shared__ double s_chi[kChiWarps];
+    __shared__ float s_dchi[kChiWarps];
     __shared__ int s_outcome;
     enum { kReject = 0, kAccept = 1, kRecheck = 2, kSame = 3 };
     const Work wk = work[blockIdx.x];
@@ -522,30 +528,93 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const bool defer = (R.flags & kDeferNorm) != 0;
     const bool force_exact = (R.flags & kTrackStats) != 0;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    constexpr uint32_t kJdeThread = 32;  // warp 1 draws the jDE; warp 0 keeps the run's tallies
-    // the member's jDE slots for the next generation and both halves of its
-    // CR / F (the parent's, the trial's), loaded now
-    uint64_t jst[4][4];
-    double cr2[2][2], fw2[2][2];  // [parent, trial][side]
-    if (tid == kJdeThread) {
-        jde_load(R, i, jst);
-#pragma unroll
-        for (uint32_t h = 0; h < 2; ++h)
-#pragma unroll
-            for (uint32_t s = 0; s < 2; ++s) {
-                cr2[h][s] = s < S ? R.cr[(uint64_t)h * S * P + s * P + i] : 0.0;
-                fw2[h][s] = s < S ? R.fw[(uint64_t)h * S * P + s * P + i] : 0.0;
-            }
-    }
-    // this thread's first timeslice, loaded with the `changed` flag (one
-    // round trip; unused when the trial equals its parent)
+    constexpr uint32_t kJdeThread = kSelectThreads - 32;
+    // read by every thread before thread 0 may change them, in one round
+    // trip with the chi^2 warps' first timeslice and the generation index
+    const uint32_t cur0 = R.cur[i];
+    const bool changed = X.changed[i] != 0;
+    const double rc = defer ? R.recip[i] : 1.0;
+    const bool t0_ok = tid < kChiThreads && tid < Nt;
     const uint64_t o0 = (uint64_t)i * Nt + tid;
-    const bool t0_ok = tid < Nt;
     const double em0 = t0_ok ? X.e_mp[o0] : 0.0, eb00 = t0_ok ? X.e_bound[o0] : 0.0;
     const double f0 = t0_ok ? R.isf[tid] : 0.0, ie0 = t0_ok ? X.inv_err[tid] : 0.0;
     const float ief0 = t0_ok ? X.inv_err_up[tid] : 0.0f;
-    const double rc = defer ? R.recip[i] : 1.0;
-    const bool changed = X.changed[i] != 0;
+    const uint64_t ii0 = tid == 0 ? R.ii : 0;  // changed only by the run's bookkeeping below
+    double fit_kept = tid == 0 ? R.fit_old[i] : 0.0;  // the member's fitness after the selection
+    __syncthreads();
+
+    if (warp == kJdeThread / 32) {
+        // the member's jDE slots and both halves of its CR / F (the
+        // parent's, the trial's); every draw is made now, the selection only
+        // picks the CR / F they apply to
+        uint64_t jst[4][4];
+        double cr2[2][2], fw2[2][2];  // [parent, trial][side]
+        JdeDraws jd;
+        if (tid == kJdeThread) {
+            jde_load(R, i, jst);
+#pragma unroll
+            for (uint32_t h = 0; h < 2; ++h)
+#pragma unroll
+                for (uint32_t s = 0; s < 2; ++s) {
+                    cr2[h][s] = s < S ? R.cr[(uint64_t)h * S * P + s * P + i] : 0.0;
+                    fw2[h][s] = s < S ? R.fw[(uint64_t)h * S * P + s * P + i] : 0.0;
+                }
+            jde_draws(R, i, jst, jd);
+        }
+        // the decision (warp 0 arrives once s_outcome is written)
+        asm volatile("barrier.sync 2, 64;" ::: "memory");
+        if (tid == kJdeThread) {
+            const int outcome = s_outcome;
+            // the next generation's jDE once the selection is final (the
+            // exact passes leave the member alone); the exact trial pass
+            // draws the others
+            if (outcome != kRecheck) {
+                double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
+                // the CR / F the selection kept: the trial's unless rejected
+                const uint32_t h = outcome == kReject ? 0u : 1u;
+#pragma unroll
+                for (uint32_t s = 0; s < 2; ++s) {
+                    cr_old[s] = h ? cr2[1][s] : cr2[0][s];
+                    fw_old[s] = h ? fw2[1][s] : fw2[0][s];
+                }
+                jde_apply(jd, cr_old, fw_old, cr_new, fw_new);
+                jde_store(R, i, jst, cr_new, fw_new, jd.mut, true);
+            }
+            // the next generation's trial parts set the flag and raise the maximum
+            X.changed[i] = 0;
+            X.xexp_max[i] = (int32_t)0x80808080;
+        }
+        return;
+    }
+    if (warp >= kChiWarps) {
+        if (defer && changed) {
+            // every gene of the trial (buffer 1 - cur) times 1/norm, as
+            // trial_kernel does (M is a multiple of the 32-gene chunk: gene
+            // pairs), all loads in flight at once for M = 4096
+            const uint64_t PM = (uint64_t)P * M;
+            const uint32_t half = M / 2, pairs = S * half;
+            constexpr uint32_t NS = kSelectThreads - kChiThreads - 32, U = 12;
+            double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)(1u - cur0) * S * PM + (uint64_t)i * M);
+            // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
+            auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
+            for (uint32_t q0 = tid - kChiThreads; q0 < pairs; q0 += U * NS) {
+                double2 v[U];
+#pragma unroll
+                for (uint32_t u = 0; u < U; ++u) {
+                    const uint32_t q = q0 + u * NS;
+                    if (q < pairs) v[u] = *at(q);
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < U; ++u) {
+                    const uint32_t q = q0 + u * NS;
+                    if (q < pairs) *at(q) = make_double2(v[u].x * rc, v[u].y * rc);
+                }
+            }
+        }
+        return;
+    }
+
+    // ---- warps 0-3: the decision
     if (!changed) {
         if (tid == 0) {
             // the trial is the parent: the same fitness, and ties accept
@@ -557,7 +626,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
                 R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
                 R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
             }
-            R.cur[i] = (uint8_t)(1u - R.cur[i]);
+            R.cur[i] = (uint8_t)(1u - cur0);
             s_outcome = kSame;
         }
     } else {
@@ -591,7 +660,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
         };
         if (t0_ok) term(em0, eb00, f0, ie0, ief0);
-        for (uint32_t t = tid + kSelectThreads; t < Nt; t += kSelectThreads) {
+        for (uint32_t t = tid + kChiThreads; t < Nt; t += kChiThreads) {
             const uint64_t o = (uint64_t)i * Nt + t;
             term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], X.inv_err_up[t]);
         }
@@ -603,17 +672,11 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             s_chi[warp] = chi;
             s_dchi[warp] = dchi;
         }
-        __syncthreads();
-        if (warp == 0) {
-            // the warps' sums by a shuffle tree (any order: the bound covers it)
-            chi = lane < kSelectThreads / 32 ? s_chi[lane] : 0.0;
-            dchi = lane < kSelectThreads / 32 ? s_dchi[lane] : 0.0f;
-            for (int o = 8; o > 0; o >>= 1) {
-                chi += __shfl_xor_sync(0xffffffffu, chi, o);
-                dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
-            }
-        }
+        asm volatile("barrier.sync 1, %0;" ::"r"(kChiThreads) : "memory");
         if (tid == 0) {
+            // the warps' sums (any order: the bound covers it)
+            chi = (s_chi[0] + s_chi[1]) + (s_chi[2] + s_chi[3]);
+            dchi = __fadd_ru(__fadd_ru(s_dchi[0], s_dchi[1]), __fadd_ru(s_dchi[2], s_dchi[3]));
             X.recheck[i] = 0;
             // /Nt as a product with 1/Nt rounded once: two roundings where a
             // quotient has one, covered by two more units of the slack below
@@ -629,12 +692,13 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
                 // certainly no worse: accept with the interval as its fitness
                 X.f_lo[i] = lo;
                 X.f_hi[i] = hi;
-                R.fit_old[i] = 0.5 * (lo + hi);
+                fit_kept = 0.5 * (lo + hi);
+                R.fit_old[i] = fit_kept;
                 for (uint32_t s = 0; s < S; ++s) {
                     R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
                     R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
                 }
-                R.cur[i] = (uint8_t)(1u - R.cur[i]);
+                R.cur[i] = (uint8_t)(1u - cur0);
                 outcome = kAccept;
             } else {
                 X.recheck[i] = 1;  // settle with the exact FP64 value
@@ -643,87 +707,45 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             s_outcome = outcome;
         }
     }
-    __syncthreads();
+    if (warp != 0) return;
+    __syncwarp();
+    // the decision to the jDE warp, without waiting for it
+    asm volatile("barrier.arrive 2, 64;" ::: "memory");
+    if (tid != 0) return;
     const int outcome = s_outcome;
-    if (tid == 0) {
-        // the run's tallies: the members' fitness minimum (non-negative
-        // doubles order as their bit patterns), the outcome counts and the
-        // members left for the exact pass; then the ticket
-        atomicMin(&X.sel_min_bits, (unsigned long long)__double_as_longlong(R.fit_old[i]));
-        atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
-        if (outcome == kRecheck) atomicAdd(&X.sel_recheck, 1u);
+    // the run's tallies: the members' fitness minimum (non-negative doubles
+    // order as their bit patterns) and the outcome counts; then the ticket,
+    // which counts the members through (low word) and those left for the
+    // exact pass (high word)
+    atomicMin(&X.sel_min_bits, (unsigned long long)__double_as_longlong(fit_kept));
+    atomicAdd(&X.counts[outcome == kSame ? 0 : outcome == kRecheck ? 2 : 1], 1ull);
+    const unsigned long long mine = 1ull + (outcome == kRecheck ? (1ull << 32) : 0ull);
+    __threadfence();
+    const unsigned long long before = atomicAdd(&X.sel_ticket, mine);
+    if ((uint32_t)before == P - 1) {
+        // The run's last member: with nothing left for the exact passes,
+        // finish the generation here -- the bookkeeping of contract_kernel's
+        // trial pass (generation index, minimum and stop test); the fitness
+        // of an interval-accepted member lies above the stop fitness, so its
+        // midpoint decides the stop test exactly.  Runs that track
+        // statistics keep the exact pass, which forms them.
+        const uint32_t nre = (uint32_t)((before + mine) >> 32);
         __threadfence();
-        if (atomicAdd(&X.sel_ticket, 1u) == P - 1) {
-            // The run's last member: with nothing left for the exact
-            // passes, finish the generation here -- the bookkeeping of
-            // contract_kernel's trial pass (generation index, minimum and
-            // stop test); the fitness of an interval-accepted member lies
-            // above the stop fitness, so its midpoint decides the stop test
-            // exactly.  Runs that track statistics keep the exact pass,
-            // which forms them.
-            __threadfence();
-            const uint32_t nre = *reinterpret_cast<volatile uint32_t*>(&X.sel_recheck);
-            const double mn =
-                __longlong_as_double((long long)*reinterpret_cast<volatile unsigned long long*>(&X.sel_min_bits));
-            X.sel_recheck = 0;
-            X.sel_ticket = 0;
-            X.sel_min_bits = ~0ull;
-            const bool idle = nre == 0 && !force_exact;
-            R.exact_idle = idle ? 1 : 0;
-            if (idle) {
-                const uint64_t ii = R.ii + 1;
-                R.ii = ii;
-                if (ii + 2 > R.N) {
-                    R.generation = R.N - 2;
-                    R.done = 1;
-                } else if (mn <= R.stop) {
-                    R.generation = ii;
-                    R.done = 1;
-                }
-            }
-        }
-    } else if (tid == kJdeThread) {
-        // the next generation's jDE once the selection is final (the exact
-        // passes leave the member alone); the exact trial pass draws the others
-        if (outcome != kRecheck) {
-            double cr_old[2], fw_old[2], cr_new[2], fw_new[2];
-            uint32_t mut[3];
-            // the CR / F the selection kept: the trial's unless rejected
-            const uint32_t h = outcome == kReject ? 0u : 1u;
-#pragma unroll
-            for (uint32_t s = 0; s < 2; ++s) {
-                cr_old[s] = h ? cr2[1][s] : cr2[0][s];
-                fw_old[s] = h ? fw2[1][s] : fw2[0][s];
-            }
-            jde_draw(R, i, jst, cr_old, fw_old, cr_new, fw_new, mut);
-            jde_store(R, i, jst, cr_new, fw_new, mut, true);
-        }
-        // the next generation's trial parts set the flag and raise the maximum
-        X.changed[i] = 0;
-        X.xexp_max[i] = (int32_t)0x80808080;
-    } else if (warp >= 2 && defer && (outcome == kAccept || outcome == kRecheck)) {
-        // kDeferNorm: normalise the trial the run keeps (now the parent) or
-        // still needs (the exact passes read it): every gene times 1/norm,
-        // as trial_kernel does (M is a multiple of the 32-gene chunk: gene
-        // pairs), all loads in flight at once for M = 4096
-        const uint32_t b = outcome == kAccept ? R.cur[i] : 1u - R.cur[i];
-        const uint64_t PM = (uint64_t)P * M;
-        const uint32_t half = M / 2, pairs = S * half;
-        constexpr uint32_t NS = kSelectThreads - 64, U = 10;
-        double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)b * S * PM + (uint64_t)i * M);
-        // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
-        auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
-        for (uint32_t q0 = tid - 64; q0 < pairs; q0 += U * NS) {
-            double2 v[U];
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t q = q0 + u * NS;
-                if (q < pairs) v[u] = *at(q);
-            }
-#pragma unroll
-            for (uint32_t u = 0; u < U; ++u) {
-                const uint32_t q = q0 + u * NS;
-                if (q < pairs) *at(q) = make_double2(v[u].x * rc, v[u].y * rc);
+        const double mn =
+            __longlong_as_double((long long)*reinterpret_cast<volatile unsigned long long*>(&X.sel_min_bits));
+        X.sel_ticket = 0;
+        X.sel_min_bits = ~0ull;
+        const bool idle = nre == 0 && !force_exact;
+        R.exact_idle = idle ? 1 : 0;
+        if (idle) {
+            const uint64_t ii = ii0 + 1;
+            R.ii = ii;
+            if (ii + 2 > R.N) {
+                R.generation = R.N - 2;
+                R.done = 1;
+            } else if (mn <= R.stop) {
+                R.generation = ii;
+                R.done = 1;
             }
         }
     }

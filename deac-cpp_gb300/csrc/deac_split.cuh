@@ -73,8 +73,8 @@ struct SplitRun {
     double* t_hi;
     unsigned long long* counts;  // [3]: trials equal to the parent, settled by
                                  // the interval, settled by the exact FP64 value
-    uint32_t sel_ticket;         // members through split_select_kernel this generation
-    uint32_t sel_recheck;        // of them left for the exact pass
+    unsigned long long sel_ticket;  // this generation: members through split_select_kernel (low
+                                    // word) and of them left for the exact pass (high word)
     unsigned long long sel_min_bits;  // their fitness minimum (bits; all ones: none yet)
     const double* inv_err;  // [Nt] 1/sigma, rounded once
     const float* inv_err_up;  // [Nt] float upper bounds of inv_err
