@@ -490,6 +490,8 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
     double* s_x = norm_s + (uint64_t)side * 2 * kNormStage;
     double* s_w = s_x + kNormStage;
     const uint32_t tg = threadIdx.x - side * kChainWarps * 32;
+    // the later stages' genes into L2 while the first stage's chain runs
+    if (tg == 0 && side < S && M > kNormStage) prefetch_l2(x + kNormStage, M - kNormStage, x + M);
     double sum = 0.0;
     for (uint32_t k0 = 0; k0 < M; k0 += kNormStage) {
         const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
