@@ -190,8 +190,9 @@ void launch(void (*kernel)(Params...), uint32_t grid, uint32_t block, size_t sme
 }
 
 void launch_contract(deac_batch* b, cudaStream_t s, int mode, bool early = false) {
-    launch(deac::contract_kernel, b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s, early,
-           b->d_runs, static_cast<const deac::Work*>(b->d_contract_work), mode);
+    const uint32_t grid = mode == deac::kModeRecheck ? 2 * b->n_contract_ctas : b->n_contract_ctas;
+    launch(deac::contract_kernel, grid, deac::kContractThreads, b->contract_smem_bytes, s, early, b->d_runs,
+           static_cast<const deac::Work*>(b->d_contract_work), mode);
 }
 
 // One generation of every run: two launches for the plain engine; for the
@@ -260,8 +261,7 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
                                                                                b->d_trial_work);
     if ((rc = mark(4))) return rc;
-    launch_contract(b, s, deac::kModeParents, early);
-    launch_contract(b, s, deac::kModeTrials, early);
+    launch_contract(b, s, deac::kModeRecheck, early);
     return mark(1);
 }
 
@@ -387,7 +387,7 @@ int upload_run(deac_batch* b, RunHost& r) {
     const uint64_t o_rng = a.take(4 * r.n_states * 8);
     const uint64_t o_cr = a.take(2ull * S * P * 8), o_fw = a.take(2ull * S * P * 8);
     const uint64_t o_fo = a.take(P * 8), o_fnw = a.take(P * 8);
-    const uint64_t o_E = a.take(P * Nt * 8), o_mom = a.take(2 * P * 8);
+    const uint64_t o_E = a.take(P * Nt * 8), o_E2 = a.take(P * Nt * 8), o_mom = a.take(2 * P * 8);
     const uint64_t o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
     const uint64_t o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
     CUDA_TRY(cudaMalloc(&r.arena, a.size));
@@ -475,6 +475,7 @@ int upload_run(deac_batch* b, RunHost& r) {
     d.fit_old = ptr(o_fo);
     d.fit_new = ptr(o_fnw);
     d.model_isf = ptr(o_E);
+    d.model_isf2 = ptr(o_E2);
     d.moments = ptr(o_mom);
     d.stats = ptr(o_stats);
     d.trace = ptr(o_trace);

@@ -362,9 +362,9 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     __shared__ uint32_t s_mut[3];
     __shared__ uint8_t s_cur[kTrialPartThreads];
     __shared__ int s_digit_max[kTrialPartThreads / 32];
-    // Before the wait only the static run description is read: the part's
-    // PRNG states (which the preceding exact pass leaves alone) are
-    // prefetched into L2 meanwhile.
+    // Before the wait only the static run description is read, and the
+    // part's PRNG states are prefetched into L2 meanwhile (a hint: their
+    // values are read after the wait).
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
     const uint32_t i = wk.index & 0xFFFFFu, part = wk.index >> 20;
@@ -552,19 +552,26 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     extern __shared__ __align__(16) double dyn[];
     __shared__ int s_last, s_any;
 
-    const Work w = work[blockIdx.x];
+    // kModeRecheck: the first half of the grid evaluates what kModeParents
+    // does, the second half what kModeTrials does
+    const bool both = mode == kModeRecheck;
+    const uint32_t half_n = both ? gridDim.x / 2 : gridDim.x;
+    const int pmode = both ? (blockIdx.x < half_n ? kModeParents : kModeTrials) : mode;  // this CTA's pass
+    const Work w = work[blockIdx.x % half_n];
     RunDev& R = runs[w.run];
     if (R.done && mode != kModeFinal) return;
-    if ((mode == kModeParents || mode == kModeTrials) && R.exact_idle) return;
+    if ((mode == kModeParents || mode == kModeTrials || both) && R.exact_idle) return;
     const bool init_mode = mode == kModeInit;
-    // members evaluated by this launch, and which of their two buffers
-    const bool use_parent = mode == kModeInit || mode == kModeParents || mode == kModeFinal;
-    auto wanted = [&](uint32_t m) -> bool {
-        if (mode == kModeGeneration || mode == kModeInit) return true;
-        if (mode == kModeTrials) return R.recheck[m] != 0;
+    // members evaluated by a pass, and which of their two buffers
+    auto parents_of = [](int pm) { return pm == kModeInit || pm == kModeParents || pm == kModeFinal; };
+    auto wanted_in = [&](int pm, uint32_t m) -> bool {
+        if (pm == kModeGeneration || pm == kModeInit) return true;
+        if (pm == kModeTrials) return R.recheck[m] != 0;
         const bool inexact = R.f_lo[m] != R.f_hi[m];
-        return mode == kModeFinal ? inexact : (R.recheck[m] != 0 && inexact);
+        return pm == kModeFinal ? inexact : (R.recheck[m] != 0 && inexact);
     };
+    const bool use_parent = parents_of(pmode);
+    auto wanted = [&](uint32_t m) -> bool { return wanted_in(pmode, m); };
     const uint32_t P = R.P, M = R.M, Nt = R.Nt, S = R.S;
     const uint32_t MT = R.member_tile, TT = R.tau_tile, CH = R.chunk;
     const uint64_t PM = (uint64_t)P * M;
@@ -658,14 +665,15 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     // the two gpu_matmul calls: C = 1*c_pos + 0*C, then C = 1*c_neg + 1*C
     double e = acc;
     if (S == 2) e = __shfl_xor_sync(0xffffffffu, acc, 16) + acc;
-    if (valid && side == 0) R.model_isf[(uint64_t)i * Nt + t] = e;
+    double* const model_out = both && pmode == kModeTrials ? R.model_isf2 : R.model_isf;
+    if (valid && side == 0) model_out[(uint64_t)i * Nt + t] = e;
 
     // the last CTA of this run finishes the generation
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t done_ctas = atomicAdd(&R.ticket, 1u) + 1u;
-        s_last = done_ctas == R.contract_ctas;
+        s_last = done_ctas == (both ? 2 * R.contract_ctas : R.contract_ctas);
     }
     __syncthreads();
     if (!s_last) return;
@@ -674,14 +682,18 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t lanes = Nt < kTreeSlots ? Nt : kTreeSlots;
     const uint32_t width = pow2_ceil(lanes);
-    double* fit_dst = use_parent ? R.fit_old : R.fit_new;
     double* sl = dyn + (uint64_t)warp * kTreeSlots;
 
     // reduced chi^2 (deac_gpu.cu:417-448) plus the moment terms
-    // (deac_gpu.cu:450-456; order of deac.cpp:1479-1499), a warp per member
-    const volatile double* E_all = R.model_isf;
+    // (deac_gpu.cu:450-456; order of deac.cpp:1479-1499), a warp per member;
+    // kModeRecheck: the parents' pass, then the trials'
+    for (int pass = 0; pass < (both ? 2 : 1); ++pass) {
+    const int fmode = both ? (pass == 0 ? kModeParents : kModeTrials) : mode;
+    const bool fit_parent = parents_of(fmode);
+    double* fit_dst = fit_parent ? R.fit_old : R.fit_new;
+    const volatile double* E_all = both && pass == 1 ? R.model_isf2 : R.model_isf;
     for (uint32_t m = warp; m < P; m += nwarps) {
-        if (!wanted(m)) continue;  // warp-uniform
+        if (!wanted_in(fmode, m)) continue;  // warp-uniform
         for (uint32_t s = lane; s < width; s += 32) {
             double v = 0.0;
             for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
@@ -709,11 +721,12 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
                 fit = fma(term, term, fit);
             }
             fit_dst[m] = fit;
-            if (use_parent && R.f_lo) R.f_lo[m] = R.f_hi[m] = fit;  // now exact
+            if (fit_parent && R.f_lo) R.f_lo[m] = R.f_hi[m] = fit;  // now exact
         }
         __syncwarp();
     }
     __syncthreads();
+    }
     if (mode == kModeParents || mode == kModeFinal) {
         if (threadIdx.x == 0) R.ticket = 0;
         return;  // no selection and no bookkeeping in these passes
@@ -723,8 +736,9 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
     if (!init_mode) {
         // greedy selection, ties accept (deac_gpu.cu:551-582); the split
         // engine's trial pass settles only the members the intervals left open
+        const int smode = both ? kModeTrials : mode;  // the members selected here
         for (uint32_t m = threadIdx.x; m < P; m += blockDim.x) {
-            if (!wanted(m)) continue;
+            if (!wanted_in(smode, m)) continue;
             const double fn = R.fit_new[m];
             if ((R.flags & kTrace) && ii < R.trace_cap) R.trace[ii * P + m] = fn;
             if (fn <= R.fit_old[m]) {
@@ -739,11 +753,11 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
         }
         ii += 1;
         __syncthreads();
-        if (mode == kModeTrials && threadIdx.x >= 32) {
+        if (smode == kModeTrials && threadIdx.x >= 32) {
             // the next generation's jDE of the members settled here (the
             // selection kernel drew the others), beside the statistics
             for (uint32_t m = threadIdx.x - 32; m < P; m += blockDim.x - 32) {
-                if (!wanted(m)) continue;
+                if (!wanted_in(smode, m)) continue;
                 double cr[2], fw[2];
                 uint32_t mut[3];
                 jde_member(R, m, cr, fw, mut);

@@ -82,6 +82,7 @@ struct RunDev {
     double* fit_old;         // [P]
     double* fit_new;         // [P]
     double* model_isf;       // [P][Nt]
+    double* model_isf2;      // [P][Nt] kModeRecheck: the trials' (model_isf holds the parents')
     double* moments;         // [P][2]: first, third
     double* stats;           // [mean|minimum|squared mean][N]
     double* trace;           // [trace_cap][P]
@@ -165,6 +166,8 @@ enum ContractMode : int {
     kModeParents = 2,     // split engine: exact fitness of undecided members' inexact parents
     kModeTrials = 3,      // split engine: exact fitness and selection of undecided trials, bookkeeping
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
+    kModeRecheck = 5,     // split engine, a grid of two halves: kModeParents, then kModeTrials,
+                          // one CTA finishing both
 };
 
 // Programmatic dependent launch: a kernel launched with the programmatic
