@@ -257,7 +257,7 @@ def kernel_roofline(kind, launch_s, peaks, split_ctas):
         work = 2.0 * 2 * rows * NT * M  # FP64 FMA chains, were every trial re-evaluated
         unit, bound, peak = "TFLOP/s", "fp64", 1.196
         achieved = work / launch_s / 1e12
-        name = "contract_kernel (exact passes)"
+        name = "contract_kernel (exact pass)"
     return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
             "kernel": name, "work_per_launch": work, "launch_us": launch_s * 1e6}
 
@@ -370,7 +370,7 @@ def engine_arm(args, world, rank, local):
                                              "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
     tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
     roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
-    names = {0: "trial_part_kernel", 1: "contract_kernel (exact passes)", 2: "norm_kernel",
+    names = {0: "trial_part_kernel", 1: "contract_kernel (exact pass)", 2: "norm_kernel",
              3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
     roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
 
@@ -416,8 +416,8 @@ def engine_arm(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         # per generation: trial parts, normalisation row sums, tensor
-        # contraction, combine, selection, 2 exact passes
-        "gpu_launches": 7 * G * args.steps,
+        # contraction, combine, selection, the exact pass
+        "gpu_launches": 6 * G * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
