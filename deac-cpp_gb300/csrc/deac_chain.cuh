@@ -542,6 +542,19 @@ __device__ __forceinline__ SegSum seg_combine(const SegSum& L, const SegSum& R) 
     if (R.c) return SegSum{L.c + R.c, R.s0, R.s1};
     return SegSum{L.c, L.s0 + R.s0, L.s1 + R.s1};
 }
+// Both at once: c crossings; after the last one (or from the range start)
+// the parity map (a, b) and the sums (s0, s1) of the steps for start
+// parities 0 and 1.  Composing L then R without a crossing in R, R's start
+// parity is L's map applied to L's start parity.
+struct SegAll {
+    uint32_t c, a, b;
+    long long s0, s1;
+};
+__device__ __forceinline__ SegAll seg_combine(const SegAll& L, const SegAll& R) {
+    if (R.c) return SegAll{L.c + R.c, R.a, R.b, R.s0, R.s1};
+    const uint32_t p0 = L.b, p1 = L.a ^ L.b;  // R's start parity for L's start parity 0, 1
+    return SegAll{L.c, L.a & R.a, (R.a & L.b) ^ R.b, L.s0 + (p0 ? R.s1 : R.s0), L.s1 + (p1 ? R.s1 : R.s0)};
+}
 
 // Exclusive group scan of a per-thread aggregate: warp shuffles, then the
 // warps' totals through shared memory.  `tot` receives the group total.
@@ -595,6 +608,41 @@ __device__ __forceinline__ SegSum group_scan(SegSum v, uint32_t lane, uint32_t w
     SegSum before{0u, 0, 0};
     for (uint32_t k = 0; k < wg; ++k) before = seg_combine(before, SegSum{sc.cnt[k], sc.sum[k], sc.sum1[k]});
     group_bar(bar_id, W * 32);
+    return seg_combine(before, ex);
+}
+
+template <int W>
+__device__ __forceinline__ SegAll group_scan(SegAll v, uint32_t lane, uint32_t wg, int bar_id, ChainScratch& sc,
+                                            uint32_t& total_c) {
+    SegAll inc = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const SegAll u{__shfl_up_sync(0xffffffffu, inc.c, o), __shfl_up_sync(0xffffffffu, inc.a, o),
+                       __shfl_up_sync(0xffffffffu, inc.b, o), __shfl_up_sync(0xffffffffu, inc.s0, o),
+                       __shfl_up_sync(0xffffffffu, inc.s1, o)};
+        if (lane >= o) inc = seg_combine(u, inc);
+    }
+    SegAll ex{__shfl_up_sync(0xffffffffu, inc.c, 1), __shfl_up_sync(0xffffffffu, inc.a, 1),
+              __shfl_up_sync(0xffffffffu, inc.b, 1), __shfl_up_sync(0xffffffffu, inc.s0, 1),
+              __shfl_up_sync(0xffffffffu, inc.s1, 1)};
+    if (lane == 0) ex = SegAll{0u, 1u, 0u, 0, 0};
+    if (lane == 31) {
+        sc.cnt[wg] = inc.c;
+        sc.map_a[wg] = inc.a;
+        sc.map_b[wg] = inc.b;
+        sc.sum[wg] = inc.s0;
+        sc.sum1[wg] = inc.s1;
+    }
+    group_bar(bar_id, W * 32);
+    SegAll before{0u, 1u, 0u, 0, 0};
+    uint32_t tc = 0;
+    for (uint32_t k = 0; k < (uint32_t)W; ++k) {
+        const uint32_t ck = sc.cnt[k];
+        if (k < wg) before = seg_combine(before, SegAll{ck, sc.map_a[k], sc.map_b[k], sc.sum[k], sc.sum1[k]});
+        tc += ck;
+    }
+    group_bar(bar_id, W * 32);
+    total_c = tc;
     return seg_combine(before, ex);
 }
 
@@ -757,7 +805,7 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     // binade (a crossing step keeps its binade after the crossing in cbin_of)
     uint32_t cross_bits = 0;
     int cbin_of[E];
-    SegMap magg{0u, 1u, 0u};
+    SegAll agg{0u, 1u, 0u, 0, 0};
     {
         uint64_t prefix = pstart;
 #pragma unroll
@@ -782,12 +830,17 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
             cbin_of[i] = dk;
             prefix += F;
             if (cr) {
-                magg = seg_combine(magg, SegMap{1u, 1u, 0u});
+                agg = seg_combine(agg, SegAll{1u, 1u, 0u, 0, 0});
                 tp[i] = 0ull;
             } else {
                 if (!on_grid) shift_term(t, ds);
                 tp[i] = pack(t);
-                magg = seg_combine(magg, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
+                // the step for entering parity 0 and 1, and its map
+                const long long b0 = (long long)(t.F + ((t.flags & kGtHalf) ? 1u : 0u));
+                const bool tie = (t.flags & kTie) != 0;
+                const long long f1 = (long long)(t.F & 1u);
+                agg = seg_combine(agg, tie ? SegAll{0u, 0u, 0u, b0 + f1, b0 + (f1 ^ 1)}
+                                           : SegAll{0u, 1u, parity_flip(t), b0, b0});
             }
         }
     }
@@ -796,10 +849,12 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         sc.segq[0][m] = 0;
         sc.segq[1][m] = 0;
     }
-    SegMap mtot;
-    const SegMap mex = group_scan<W>(magg, lane, wg, bar_id, sc, mtot);
-    const uint32_t ncross = mtot.c;
+    uint32_t ncross;
+    const SegAll ex = group_scan<W>(agg, lane, wg, bar_id, sc, ncross);
     if (ncross > kMaxCross) return k0;
+    // the map and the sums from the segment's start to this thread's first step
+    const SegMap mex{ex.c, ex.a, ex.b};
+    const SegSum sex{ex.c, ex.s0, ex.s1};
 
     // the integer steps of a segment for start parities 0 and 1, given the
     // parity map from the segment's start
@@ -812,24 +867,6 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     auto next_map = [&](const SegMap& m, const Term& t) {
         return seg_combine(m, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
     };
-    SegSum sagg{0u, 0, 0};
-    {
-        SegMap run = mex;
-#pragma unroll
-        for (uint32_t i = 0; i < E; ++i) {
-            const Term t = unpack(tp[i]);
-            if ((cross_bits >> i) & 1u) {
-                sagg = seg_combine(sagg, SegSum{1u, 0, 0});
-                run = seg_combine(run, SegMap{1u, 1u, 0u});
-            } else {
-                long long q0, q1;
-                steps(t, run, q0, q1);
-                sagg = seg_combine(sagg, SegSum{0u, q0, q1});
-                run = next_map(run, t);
-            }
-        }
-    }
-    const SegSum sex = group_scan<W>(sagg, lane, wg, bar_id, sc);
     // crossing positions and binades; each segment's sums at its last step
     {
         SegMap runm = mex;
