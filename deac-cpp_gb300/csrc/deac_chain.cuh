@@ -868,10 +868,11 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
         return seg_combine(m, (t.flags & kTie) ? SegMap{0u, 0u, 0u} : SegMap{0u, 1u, parity_flip(t)});
     };
     // crossing positions and binades; each segment's sums at its last step
-    {
+    // (only threads holding a crossing or a segment's last step write)
+    const bool next_thread_cross = tg + 1 < NT ? sc.first_cross[tg + 1] != 0 : false;
+    if (cross_bits != 0 || next_thread_cross || (len > my0 && len <= my0 + E)) {
         SegMap runm = mex;
         SegSum runs = sex;
-        const bool next_thread_cross = tg + 1 < NT ? sc.first_cross[tg + 1] != 0 : false;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
             const Term t = unpack(tp[i]);
