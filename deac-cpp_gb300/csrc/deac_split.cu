@@ -541,6 +541,19 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const float ief0 = t0_ok ? X.inv_err_up[tid] : 0.0f;
     const uint64_t ii0 = tid == 0 ? R.ii : 0;  // changed only by the run's bookkeeping below
     double fit_kept = tid == 0 ? R.fit_old[i] : 0.0;  // the member's fitness after the selection
+    // the decision's other operands (thread 0)
+    const double f_lo0 = tid == 0 ? X.f_lo[i] : 0.0, f_hi0 = tid == 0 ? X.f_hi[i] : 0.0;
+    const double inv_nt = tid == 0 ? X.inv_nt : 0.0, stop = tid == 0 ? R.stop : 0.0;
+    const float inv_nt_up = tid == 0 ? X.inv_nt_up : 0.0f;
+    double cr_t[2] = {0.0, 0.0}, fw_t[2] = {0.0, 0.0};  // the trial's CR / F, kept on acceptance
+    if (tid == 0) {
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s)
+            if (s < S) {
+                cr_t[s] = R.cr[(uint64_t)S * P + s * P + i];
+                fw_t[s] = R.fw[(uint64_t)S * P + s * P + i];
+            }
+    }
     __syncthreads();
 
     if (warp == kJdeThread / 32) {
@@ -619,13 +632,15 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         if (tid == 0) {
             // the trial is the parent: the same fitness, and ties accept
             X.recheck[i] = 0;
-            X.t_lo[i] = X.f_lo[i];
-            X.t_hi[i] = X.f_hi[i];
-            R.fit_new[i] = X.f_lo[i];
-            for (uint32_t s = 0; s < S; ++s) {
-                R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
-                R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
-            }
+            X.t_lo[i] = f_lo0;
+            X.t_hi[i] = f_hi0;
+            R.fit_new[i] = f_lo0;
+#pragma unroll
+            for (uint32_t s = 0; s < 2; ++s)
+                if (s < S) {
+                    R.cr[s * P + i] = cr_t[s];
+                    R.fw[s * P + i] = fw_t[s];
+                }
             R.cur[i] = (uint8_t)(1u - cur0);
             s_outcome = kSame;
         }
@@ -680,24 +695,26 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             X.recheck[i] = 0;
             // /Nt as a product with 1/Nt rounded once: two roundings where a
             // quotient has one, covered by two more units of the slack below
-            chi *= X.inv_nt;
-            const double dchi_d = (double)__fmul_ru(dchi, X.inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
+            chi *= inv_nt;
+            const double dchi_d = (double)__fmul_ru(dchi, inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
             const double lo = chi - dchi_d, hi = chi + dchi_d;
             X.t_lo[i] = lo;
             X.t_hi[i] = hi;
             int outcome;
-            if (lo > X.f_hi[i]) {  // certainly worse: reject
+            if (lo > f_hi0) {  // certainly worse: reject
                 outcome = kReject;
-            } else if (hi <= X.f_lo[i] && !force_exact && lo > R.stop) {
+            } else if (hi <= f_lo0 && !force_exact && lo > stop) {
                 // certainly no worse: accept with the interval as its fitness
                 X.f_lo[i] = lo;
                 X.f_hi[i] = hi;
                 fit_kept = 0.5 * (lo + hi);
                 R.fit_old[i] = fit_kept;
-                for (uint32_t s = 0; s < S; ++s) {
-                    R.cr[s * P + i] = R.cr[(uint64_t)S * P + s * P + i];
-                    R.fw[s * P + i] = R.fw[(uint64_t)S * P + s * P + i];
-                }
+#pragma unroll
+                for (uint32_t s = 0; s < 2; ++s)
+                    if (s < S) {
+                        R.cr[s * P + i] = cr_t[s];
+                        R.fw[s * P + i] = fw_t[s];
+                    }
                 R.cur[i] = (uint8_t)(1u - cur0);
                 outcome = kAccept;
             } else {
