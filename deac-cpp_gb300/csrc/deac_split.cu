@@ -505,12 +505,10 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
 // (undecided members are flagged for the exact FP64 evaluation,
 // contract_kernel's recheck mode); thread 0 then keeps the run's tallies,
 // and the run's last CTA does the generation's bookkeeping when no member
-// needs the exact pass.  Warps 4-14 meanwhile normalise the raw trial of
-// kDeferNorm runs (needed when it is kept or rechecked; a rejected trial's
-// row is rewritten by the next generation's trial parts, so scaling it
-// regardless takes the scaling off the decision's path), and the last
-// warp's first thread draws the next generation's jDE, which it stores once
-// the decision is known.
+// needs the exact pass.  Warps 4-14 meanwhile load the raw trial of
+// kDeferNorm runs and, once the decision is known, normalise it when it is
+// kept or rechecked; the last warp's first thread draws the next
+// generation's jDE, which it stores once the decision is known.
 __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* runs, SplitRun* split,
                                                                      const Work* work) {
     grid_dependency_wait();
@@ -600,26 +598,46 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         return;
     }
     if (warp >= kChiWarps) {
-        if (defer && changed) {
-            // every gene of the trial (buffer 1 - cur) times 1/norm, as
-            // trial_kernel does (M is a multiple of the 32-gene chunk: gene
-            // pairs), all loads in flight at once for M = 4096
-            const uint64_t PM = (uint64_t)P * M;
-            const uint32_t half = M / 2, pairs = S * half;
-            constexpr uint32_t NS = kSelectThreads - kChiThreads - 32, U = 12;
-            double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)(1u - cur0) * S * PM + (uint64_t)i * M);
-            // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
-            auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
-            for (uint32_t q0 = tid - kChiThreads; q0 < pairs; q0 += U * NS) {
-                double2 v[U];
+        // The trial (buffer 1 - cur) of kDeferNorm runs, kept or rechecked,
+        // normalised: every gene times 1/norm, as trial_kernel does.  Its
+        // genes are loaded while warps 0-3 decide (all loads of the first
+        // pass in flight at once: one pass for M = 4096); the FP64
+        // multiplies wait for the decision, which has the narrow FP64 pipe
+        // to itself meanwhile, and are skipped for a rejected trial.
+        const bool need = defer && changed;
+        const uint64_t PM = (uint64_t)P * M;
+        const uint32_t half = M / 2, pairs = S * half;  // M is a multiple of the 32-gene chunk: gene pairs
+        constexpr uint32_t NS = kSelectThreads - kChiThreads - 32, U = 12;
+        double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)(1u - cur0) * S * PM + (uint64_t)i * M);
+        // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
+        auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
+        const uint32_t q0 = tid - kChiThreads;
+        double2 v[U];
+        if (need) {
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) v[u] = *at(q);
+            }
+        }
+        // the decision (warp 0 arrives once s_outcome is written)
+        asm volatile("barrier.sync 3, %0;" ::"r"(NS + 32) : "memory");
+        const int outcome = s_outcome;
+        if (need && (outcome == kAccept || outcome == kRecheck)) {
+#pragma unroll
+            for (uint32_t u = 0; u < U; ++u) {
+                const uint32_t q = q0 + u * NS;
+                if (q < pairs) *at(q) = make_double2(v[u].x * rc, v[u].y * rc);
+            }
+            for (uint32_t qb = q0 + U * NS; qb < pairs; qb += U * NS) {
 #pragma unroll
                 for (uint32_t u = 0; u < U; ++u) {
-                    const uint32_t q = q0 + u * NS;
+                    const uint32_t q = qb + u * NS;
                     if (q < pairs) v[u] = *at(q);
                 }
 #pragma unroll
                 for (uint32_t u = 0; u < U; ++u) {
-                    const uint32_t q = q0 + u * NS;
+                    const uint32_t q = qb + u * NS;
                     if (q < pairs) *at(q) = make_double2(v[u].x * rc, v[u].y * rc);
                 }
             }
@@ -726,8 +744,9 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     }
     if (warp != 0) return;
     __syncwarp();
-    // the decision to the jDE warp, without waiting for it
+    // the decision to the jDE warp and the scaling warps, without waiting
     asm volatile("barrier.arrive 2, 64;" ::: "memory");
+    asm volatile("barrier.arrive 3, %0;" ::"r"(kSelectThreads - kChiThreads - 32 + 32) : "memory");
     if (tid != 0) return;
     const int outcome = s_outcome;
     // the run's tallies: the members' fitness minimum (non-negative doubles
