@@ -493,10 +493,12 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
     // the later stages' genes into L2 while the first stage's chain runs
     if (tg == 0 && side < S && M > kNormStage) prefetch_l2(x + kNormStage, M - kNormStage, x + M);
     double sum = 0.0;
-    for (uint32_t k0 = 0; k0 < M; k0 += kNormStage) {
+    // each side's group runs on its own: its staging and chain synchronise
+    // with the group's named barrier only
+    for (uint32_t k0 = 0; side < S && k0 < M; k0 += kNormStage) {
         const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
-        __syncthreads();
-        if (side < S) {
+        chain_detail::group_bar(1 + (int)side, kChainWarps * 32);  // the chain is done with the stage buffer
+        {
             // this thread's steps tg*E .. tg*E+E-1 of the stage, all loads in
             // flight at once, stored step-major (chain_slot order) so that
             // the chain's threads read them without bank conflicts
@@ -527,11 +529,9 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
                 s_w[u * NT + tg] = vw[u];
             }
         }
-        __syncthreads();
-        if (side < S)
-            sum = group_fma_chain<kChainWarps, kChainSteps, true, true>(s_x, s_w, len, sum, side * kChainWarps,
-                                                                        1 + (int)side, s_chain[side],
-                                                                        k0 == 0 ? 32u : 0u);
+        chain_detail::group_bar(1 + (int)side, kChainWarps * 32);
+        sum = group_fma_chain<kChainWarps, kChainSteps, true, true>(s_x, s_w, len, sum, side * kChainWarps,
+                                                                    1 + (int)side, s_chain[side], k0 == 0 ? 32u : 0u);
     }
     if (tg == 0 && side < S) s_sum[side] = sum;
     __syncthreads();
