@@ -548,7 +548,14 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // row stride chunk+2), reused by the finishing CTA as 4 x 1024 reduction
 // slots.
 __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int mode) {
-    grid_dependency_wait();
+    if (mode == kModeRecheck) {
+        // the next generation's trial parts read nothing before their own
+        // wait: let them be scheduled while the selection still runs
+        asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+        asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    } else {
+        grid_dependency_wait();
+    }
     extern __shared__ __align__(16) double dyn[];
     __shared__ int s_last, s_any;
 
