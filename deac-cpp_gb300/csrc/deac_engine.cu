@@ -23,6 +23,7 @@
 #include <limits>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -107,7 +108,7 @@ struct RunHost {
     int S = 2;
     deac::Model model;
     std::vector<double> pop0;            // [S][P][M] initial parents
-    std::vector<uint64_t> rng_table;     // 4 x n_states word-major
+    uint64_t rng_start[4] = {0, 0, 0, 0};  // generator state after the initial draws
     uint64_t n_states = 0;
     uint64_t trace_cap = 0;
     char* arena = nullptr;               // device allocation of this run
@@ -137,6 +138,12 @@ struct deac_batch {
     size_t trial_smem_bytes = 0;
     size_t contract_smem_bytes = 0;
     bool set_up = false;
+    // snapshot of every run's status, parent fitness and parent buffers,
+    // taken after the last launch (finalised: split-engine parents exact)
+    bool snapped = false;
+    std::vector<deac::RunDev> snap;
+    std::vector<std::vector<double>> snap_fit;
+    std::vector<std::vector<uint8_t>> snap_cur;
     cudaGraphExec_t graph = nullptr;
     std::vector<deac::RunDev> status;  // host mirror of d_runs
     // split engine
@@ -149,6 +156,7 @@ struct deac_batch {
     float4* d_partial = nullptr;       // partial sums of the split contraction CTAs
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
+    uint64_t* d_jpow = nullptr;         // jump_powers on the device
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
     // passes), 2 normalisation row sums, 3 split contraction, 4 combine + decisions (+ scaling)
     bool timing = false;
@@ -269,11 +277,29 @@ int launch_generation_timed(deac_batch* b) { return launch_generation(b, b->stre
 
 // Split engine: make every parent's fitness exact (the final argmin, the
 // reported minimum and the state fetches read them).
+// Make every split-engine parent's fitness exact and take the snapshot the
+// result and fetch calls read; nothing is done again until the next launch.
 int finalize_split(deac_batch* b) {
-    if (b->engine != DEAC_ENGINE_SPLIT_BF16) return DEAC_OK;
-    launch_contract(b, b->stream, deac::kModeFinal);
-    CUDA_TRY(cudaGetLastError());
+    if (b->snapped) return DEAC_OK;
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        launch_contract(b, b->stream, deac::kModeFinal);
+        CUDA_TRY(cudaGetLastError());
+    }
+    const size_t n = b->runs.size();
+    b->snap.resize(n);
+    b->snap_fit.resize(n);
+    b->snap_cur.resize(n);
+    CUDA_TRY(cudaMemcpyAsync(b->snap.data(), b->d_runs, n * sizeof(deac::RunDev), cudaMemcpyDeviceToHost,
+                             b->stream));
+    for (size_t r = 0; r < n; ++r) {
+        const deac::RunDev& d = b->runs[r]->dev;  // the host copy holds the same buffer addresses
+        b->snap_fit[r].resize(d.P);
+        b->snap_cur[r].resize(d.P);
+        CUDA_TRY(cudaMemcpyAsync(b->snap_fit[r].data(), d.fit_old, d.P * 8, cudaMemcpyDeviceToHost, b->stream));
+        CUDA_TRY(cudaMemcpyAsync(b->snap_cur[r].data(), d.cur, d.P, cudaMemcpyDeviceToHost, b->stream));
+    }
     CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->snapped = true;
     return DEAC_OK;
 }
 
@@ -288,6 +314,31 @@ std::string kernel_key(const RunHost& r) {
     put(r.tau.data(), r.tau.size() * sizeof(double));
     put(r.freq.data(), r.freq.size() * sizeof(double));
     return k;
+}
+
+// Bits of the largest jump count below n (at least one).
+uint32_t jump_bits(uint64_t n) {
+    uint32_t b = 1;
+    while (b < 64 && (1ull << b) < n) ++b;
+    return b;
+}
+
+// The matrices J^(2^b), b < bits, of the PRNG jump over GF(2) (1024 words
+// each), grown on demand and kept for the process: the same for every run.
+const std::vector<uint64_t>& jump_powers(uint32_t bits) {
+    static std::mutex mu;
+    static std::vector<uint64_t> tab;
+    std::lock_guard<std::mutex> lock(mu);
+    if (tab.empty()) {
+        tab.resize(1024);
+        deac::jump_matrix(tab.data());
+    }
+    while (tab.size() < (size_t)bits * 1024) {
+        const size_t k = tab.size();
+        tab.resize(k + 1024);
+        deac::gf2_matmul(tab.data() + k - 1024, tab.data() + k - 1024, tab.data() + k);
+    }
+    return tab;
 }
 
 // Host part of one run's set-up: constants, initial population, PRNG table.
@@ -311,14 +362,9 @@ void prepare_run(RunHost& r) {
     if (S == 2)
         for (uint64_t i = 0; i < P; ++i) r.pop0[P * M + i * M] = r.pop0[i * M];
     // per-gene states: state k = jump^k(generator after the initial draws)
-    // (deac.cpp:1114-1126), stored in this engine's member-major slots
+    // (deac.cpp:1114-1126), formed on the device by rng_table_kernel
     r.n_states = P * (1 + (uint64_t)S * M);
-    r.rng_table.assign(4 * r.n_states, 0);
-    for (uint64_t k = 0; k < r.n_states; ++k) {
-        const uint64_t slot = deac::rng_slot((uint32_t)P, (uint32_t)M, (uint32_t)S, k);
-        for (int w = 0; w < 4; ++w) r.rng_table[(uint64_t)w * r.n_states + slot] = g.s[w];
-        g.jump();
-    }
+    for (int w = 0; w < 4; ++w) r.rng_start[w] = g.s[w];
 }
 
 int upload_run(deac_batch* b, RunHost& r) {
@@ -345,33 +391,12 @@ int upload_run(deac_batch* b, RunHost& r) {
             // shared by both sides, seven 7-bit digits per value, tiled as
             // [plane][unit of 8 genes][timeslice][8]
             const uint64_t C = M / deac::kChunk;
-            std::vector<uint16_t> kdig((uint64_t)deac::kDigits * S * Nt * M);
-            std::vector<int16_t> kexp(Nt * C), kmax(Nt, -1000);
-            for (uint64_t t = 0; t < Nt; ++t)
-                for (uint64_t c = 0; c < C; ++c) {
-                    int e = -2000;
-                    for (int sd = 0; sd < S; ++sd)
-                        for (uint64_t j = c * deac::kChunk; j < (c + 1) * deac::kChunk; ++j) {
-                            const double v = (sd ? m.k_neg : m.k_pos)[t * M + j];
-                            if (v != 0.0 && std::isnormal(v)) e = std::max(e, std::ilogb(v));
-                        }
-                    e = e <= -1500 ? -1000 : e + 1;
-                    kexp[t * C + c] = (int16_t)e;
-                    kmax[t] = (int16_t)std::max<int>(kmax[t], e);
-                    for (int sd = 0; sd < S; ++sd)
-                        for (uint64_t j = c * deac::kChunk; j < (c + 1) * deac::kChunk; ++j) {
-                            uint16_t dg[deac::kDigits];
-                            deac::digits_of((sd ? m.k_neg : m.k_pos)[t * M + j], e, dg);
-                            for (int d = 0; d < deac::kDigits; ++d)
-                                kdig[((((uint64_t)d * S + sd) * (M / 8) + j / 8) * Nt + t) * 8 + (j & 7)] = dg[d];
-                        }
-                }
-            CUDA_TRY(cudaMalloc(&km.kdig, kdig.size() * 2));
-            CUDA_TRY(cudaMemcpy(km.kdig, kdig.data(), kdig.size() * 2, cudaMemcpyHostToDevice));
-            CUDA_TRY(cudaMalloc(&km.kexp, kexp.size() * 2));
-            CUDA_TRY(cudaMemcpy(km.kexp, kexp.data(), kexp.size() * 2, cudaMemcpyHostToDevice));
-            CUDA_TRY(cudaMalloc(&km.kexp_max, kmax.size() * 2));
-            CUDA_TRY(cudaMemcpy(km.kexp_max, kmax.data(), kmax.size() * 2, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMalloc(&km.kdig, (uint64_t)deac::kDigits * S * Nt * M * 2));
+            CUDA_TRY(cudaMalloc(&km.kexp, Nt * C * 2));
+            CUDA_TRY(cudaMalloc(&km.kexp_max, Nt * 2));
+            deac::k_digits_kernel<<<(unsigned)Nt, 256>>>(km.k_pos, S == 2 ? km.k_neg : nullptr, (uint32_t)Nt,
+                                                         (uint32_t)M, km.kdig, km.kexp, km.kexp_max);
+            CUDA_TRY(cudaGetLastError());
         }
         km.group = (uint32_t)b->kcache.size();
         it = b->kcache.emplace(key, km).first;
@@ -403,7 +428,15 @@ int upload_run(deac_batch* b, RunHost& r) {
         (rc = up(o_fn, m.first_neg)) || (rc = up(o_tp, m.third_pos)) || (rc = up(o_tn, m.third_neg)) ||
         (rc = up(o_pop, r.pop0)))
         return rc;
-    CUDA_TRY(cudaMemcpy(base + o_rng, r.rng_table.data(), r.rng_table.size() * 8, cudaMemcpyHostToDevice));
+    {
+        const uint32_t bits = jump_bits(r.n_states);
+        const uint64_t blocks = std::min<uint64_t>((r.n_states + 255) / 256, 4096);
+        deac::rng_table_kernel<<<(unsigned)blocks, 256>>>(reinterpret_cast<uint64_t*>(base + o_rng), r.n_states,
+                                                          b->d_jpow, bits, r.rng_start[0], r.rng_start[1],
+                                                          r.rng_start[2], r.rng_start[3], (uint32_t)P, (uint32_t)M,
+                                                          (uint32_t)S);
+        CUDA_TRY(cudaGetLastError());
+    }
     std::vector<double> crfw(2ull * S * P, 0.0);
     for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.crossover_probability;
     if ((rc = up(o_cr, crfw))) return rc;
@@ -538,7 +571,6 @@ int upload_run(deac_batch* b, RunHost& r) {
         if (it->second.nonneg && !r.cfg.allow_negative_weight) d.flags |= deac::kNonNegProducts;
     }
     // host copies are no longer needed
-    std::vector<uint64_t>().swap(r.rng_table);
     return DEAC_OK;
 }
 
@@ -760,6 +792,13 @@ int deac_batch_setup(deac_batch* b) {
             for (auto& th : pool) th.join();
         }
     }
+    {
+        uint32_t bits = 1;
+        for (auto& r : b->runs) bits = std::max(bits, jump_bits(r->n_states));
+        const std::vector<uint64_t>& jp = jump_powers(bits);
+        CUDA_TRY(cudaMalloc(&b->d_jpow, (size_t)bits * 1024 * 8));
+        CUDA_TRY(cudaMemcpy(b->d_jpow, jp.data(), (size_t)bits * 1024 * 8, cudaMemcpyHostToDevice));
+    }
     uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
@@ -906,6 +945,7 @@ int deac_batch_launch(deac_batch* b, uint64_t generations) {
     if (!b) return fail(DEAC_E_INVALID, "null batch");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
     if (b->timing) {
+        b->snapped = false;
         for (uint64_t g = 0; g < generations; ++g) {
             int rc = launch_generation_timed(b);
             if (rc) return rc;
@@ -915,6 +955,7 @@ int deac_batch_launch(deac_batch* b, uint64_t generations) {
     }
     int rc = build_graph(b);
     if (rc) return rc;
+    b->snapped = false;
     for (uint64_t g = 0; g < generations; g += kGraphBlock) CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
     return DEAC_OK;
 }
@@ -1015,11 +1056,7 @@ int deac_batch_result(deac_batch* b, uint32_t run, deac_run_result* out) {
     RunHost& r = *b->runs[run];
     int rc = finalize_split(b);
     if (rc) return rc;
-    deac::RunDev st;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
-    std::vector<double> fit(r.P);
-    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, r.P * 8, cudaMemcpyDeviceToHost));
-    summarize(r, st, fit, out);
+    summarize(r, b->snap[run], b->snap_fit[run], out);
     return DEAC_OK;
 }
 
@@ -1033,19 +1070,17 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
     // the bus (the reference copies the whole population, deac.cpp:1577-1590)
     int rc0 = finalize_split(b);
     if (rc0) return rc0;
-    deac::RunDev st;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
-    std::vector<double> fit(P);
-    std::vector<uint8_t> cur(P);
-    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, P * 8, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(cur.data(), st.cur, P, cudaMemcpyDeviceToHost));
+    const deac::RunDev& st = b->snap[run];
+    const std::vector<double>& fit = b->snap_fit[run];
+    const std::vector<uint8_t>& cur = b->snap_cur[run];
     deac_run_result res;
     summarize(r, st, fit, &res);
     const uint64_t best = res.best_index;
     std::vector<double> genes(S * M);
     for (uint64_t s = 0; s < S; ++s)
-        CUDA_TRY(cudaMemcpy(&genes[s * M], st.pop + ((uint64_t)cur[best] * S * P + s * P + best) * M, M * 8,
-                            cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpyAsync(&genes[s * M], st.pop + ((uint64_t)cur[best] * S * P + s * P + best) * M, M * 8,
+                                 cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     const uint64_t L = res.spectrum_length;
     std::vector<double> dsf(L), fr(L);
     deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes.data(), S == 2 ? &genes[M] : nullptr, dsf.data(),
@@ -1149,6 +1184,7 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_partial);
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
+    cudaFree(b->d_jpow);
     cudaFree(b->d_runs);
     cudaFree(b->d_trial_work);
     cudaFree(b->d_contract_work);

@@ -333,6 +333,26 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     trial_body(runs, work, init_mode, smem_doubles);
 }
 
+// ------------------------------------------------------------ PRNG table
+__global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow, uint32_t bits, uint64_t s0,
+                                 uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t v[4] = {s0, s1, s2, s3};
+        for (uint32_t b = 0; b < bits; ++b)
+            if ((k >> b) & 1u) {
+                uint64_t o[4];
+                gf2_matvec(jpow + (uint64_t)b * 1024, v, o);
+                v[0] = o[0];
+                v[1] = o[1];
+                v[2] = o[2];
+                v[3] = o[3];
+            }
+        const uint64_t slot = rng_slot(P, M, S, k);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) rng[(uint64_t)w * n + slot] = v[w];
+    }
+}
+
 // --------------------------------------------------------------- split trials
 // Split engine: jDE and the mutant indices of every member, one thread each
 // (work = the trial work list), once after the initial population; later

@@ -195,6 +195,11 @@ __device__ __forceinline__ void prefetch_l2(const T* p, uint64_t count, const T*
 }
 
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
+// the PRNG table of a run: state k = J^k s for the generator state s after
+// the initial draws, from the matrices J^(2^b) (jpow, 1024 words each), into
+// slot rng_slot(P, M, S, k) of the word-major table of n states
+__global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow, uint32_t bits, uint64_t s0,
+                                 uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S);
 // split engine: jDE of every member (one thread each) after the initial
 // population; each generation's raw trials in parts of kTrialPart genes per
 // side (work index = part << 20 | member), each with its BF16 digit slices

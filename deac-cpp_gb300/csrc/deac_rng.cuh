@@ -81,4 +81,37 @@ struct Xoshiro {
     }
 };
 
+// The jump as a linear map of the 256-bit state over GF(2): a 256 x 256
+// matrix stored as 256 columns of 4 words (column i = jump(e_i)).  J^k s,
+// the state k jumps on, is then a product of the matrices J^(2^b) of k's
+// set bits -- independent per k, where the jumps themselves form a chain.
+DEAC_HD void gf2_matvec(const uint64_t* cols, const uint64_t v[4], uint64_t out[4]) {
+    uint64_t a = 0, b = 0, c = 0, d = 0;
+    for (uint32_t i = 0; i < 256; ++i) {
+        const uint64_t m = 0ull - ((v[i >> 6] >> (i & 63u)) & 1ull);
+        a ^= cols[4 * i] & m;
+        b ^= cols[4 * i + 1] & m;
+        c ^= cols[4 * i + 2] & m;
+        d ^= cols[4 * i + 3] & m;
+    }
+    out[0] = a;
+    out[1] = b;
+    out[2] = c;
+    out[3] = d;
+}
+
+inline void jump_matrix(uint64_t cols[1024]) {
+    for (uint32_t i = 0; i < 256; ++i) {
+        Xoshiro x{{0, 0, 0, 0}};
+        x.s[i >> 6] = 1ull << (i & 63u);
+        x.jump();
+        for (int w = 0; w < 4; ++w) cols[4 * i + w] = x.s[w];
+    }
+}
+
+// C = A B (column j of C is A times column j of B)
+inline void gf2_matmul(const uint64_t* A, const uint64_t* B, uint64_t* C) {
+    for (uint32_t j = 0; j < 256; ++j) gf2_matvec(A, B + 4 * j, C + 4 * j);
+}
+
 }  // namespace deac

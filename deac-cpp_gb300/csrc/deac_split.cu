@@ -787,6 +787,43 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     }
 }
 
+// ------------------------------------------------------------ K digits
+__global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt, uint32_t M, uint16_t* kdig,
+                                int16_t* kexp, int16_t* kexp_max) {
+    __shared__ int s_max[8];
+    const uint32_t t = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t S = kn ? 2u : 1u, C = M / kChunk, nw = blockDim.x >> 5;
+    int wmax = -1000;
+    for (uint32_t c = warp; c < C; c += nw) {
+        const uint32_t j = c * kChunk + lane;
+        const double v0 = kp[(uint64_t)t * M + j], v1 = kn ? kn[(uint64_t)t * M + j] : 0.0;
+        // the exponents of the normal values (zeros, subnormals and
+        // non-finite values set no scale, as std::isnormal on the host)
+        auto ex = [](double v) { const int e = exp_of(v); return e > 1023 ? -2000 : e; };
+        int e = max(ex(v0), ex(v1));
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        e = e <= -1500 ? -1000 : e + 1;  // scale 2^e above every |v| of the chunk
+        for (uint32_t sd = 0; sd < S; ++sd) {
+            const double v = sd ? v1 : v0;
+            const uint64_t f = frac_digits(v, e);
+            const bool neg = v < 0.0;
+            for (int d = 0; d < kDigits; ++d) {
+                const uint32_t dg = (uint32_t)(f >> (7 * (kDigits - 1 - d))) & 127u;
+                kdig[((((uint64_t)d * S + sd) * (M / 8) + j / 8) * Nt + t) * 8 + (j & 7u)] = bf16_digit(dg, neg);
+            }
+        }
+        if (lane == 0) kexp[(uint64_t)t * C + c] = (int16_t)e;
+        wmax = max(wmax, e);
+    }
+    if (lane == 0) s_max[warp] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = -1000;
+        for (uint32_t k = 0; k < nw; ++k) m = max(m, s_max[k]);
+        kexp_max[t] = (int16_t)m;
+    }
+}
+
 // ------------------------------------------------------------------ host
 void digits_of(double v, int e, uint16_t out[kDigits]) {
     const double m = std::fabs(v);

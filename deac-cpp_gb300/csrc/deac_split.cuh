@@ -113,6 +113,13 @@ __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const Split
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows,
                                      const float4* partial);
 __global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* work);
+// The digit planes of K (kn null for one-sided K), one CTA per timeslice t:
+// per 32-gene chunk the scale exponent shared by both sides (kexp[t][c]),
+// seven 7-bit digits per value as BF16 in the tiled planes
+// [plane][unit of 8 genes][timeslice][8], and the timeslice's largest scale
+// exponent (kexp_max[t]); the same digits as digits_of on the host.
+__global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt, uint32_t M, uint16_t* kdig,
+                                int16_t* kexp, int16_t* kexp_max);
 constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
 
 // ---- digit slicing of one value (shared by trial_kernel and the host)

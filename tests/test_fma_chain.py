@@ -20,6 +20,17 @@ def test_host_chain_matches_sequential_fma(tmp_path):
     assert out.stdout.startswith("ok")
 
 
+def test_prng_table_jump_powers_match_the_jump_chain(tmp_path):
+    # the per-gene PRNG states come from GF(2) matrix powers of the jump
+    # (rng_table_kernel); on the host they must equal the chain of jumps
+    exe = tmp_path / "rng_jump_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(REPO / "deac-cpp_gb300" / "csrc"),
+                    str(REPO / "tests" / "rng_jump_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), "70000"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok")
+
+
 def _chains(kind, n, count, rng):
     x = np.empty((count, n))
     w = np.empty((count, n))
