@@ -383,9 +383,12 @@ def engine_arm(args, world, rank, local):
     h2d = 0
     for cfg, tau, isf, err, freq in configs:
         b2.add_run(cfg, tau, isf, err, freq)
+        # isf and its errors, the normalisation weights of both sides, the
+        # initial parents, CR and F (the PRNG table and K's digit planes
+        # are formed on the device)
         s = 2
-        h2d += 8 * (3 * NT + 2 * s * P * M + 4 * P * (1 + s * M) + 4 * s * P)
-    h2d += 8 * 2 * NT * M + 2 * 6 * 2 * NT * M  # shared kernel matrix and its digit planes
+        h2d += 8 * (2 * NT + s * M + s * P * M + 4 * s * P)
+    h2d += 8 * 2 * NT * M  # the shared kernel matrix
     b2.setup()
     d2h = 0
     for _ in range(args.steps):
