@@ -416,18 +416,31 @@ int upload_run(deac_batch* b, RunHost& r) {
     const uint64_t o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
     const uint64_t o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
     CUDA_TRY(cudaMalloc(&r.arena, a.size));
-    CUDA_TRY(cudaMemset(r.arena, 0, a.size));
     char* base = r.arena;
-    auto up = [&](uint64_t off, const std::vector<double>& v) -> int {
-        if (!v.empty()) CUDA_TRY(cudaMemcpy(base + off, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
-        return DEAC_OK;
+    // the arena's initial contents as one host image (zeros but for the
+    // inputs, the initial parents and CR / F), copied around the PRNG
+    // table, which rng_table_kernel forms on the device
+    std::vector<char> image(a.size, 0);
+    auto put = [&](uint64_t off, const std::vector<double>& v) {
+        if (!v.empty()) std::memcpy(image.data() + off, v.data(), v.size() * 8);
     };
-    int rc = DEAC_OK;
-    if ((rc = up(o_isf, r.isf)) || (rc = up(o_err, r.err)) || (rc = up(o_tw, m.tau_weight)) ||
-        (rc = up(o_np, m.norm_pos)) || (rc = up(o_nn, m.norm_neg)) || (rc = up(o_fp, m.first_pos)) ||
-        (rc = up(o_fn, m.first_neg)) || (rc = up(o_tp, m.third_pos)) || (rc = up(o_tn, m.third_neg)) ||
-        (rc = up(o_pop, r.pop0)))
-        return rc;
+    put(o_isf, r.isf);
+    put(o_err, r.err);
+    put(o_tw, m.tau_weight);
+    put(o_np, m.norm_pos);
+    put(o_nn, m.norm_neg);
+    put(o_fp, m.first_pos);
+    put(o_fn, m.first_neg);
+    put(o_tp, m.third_pos);
+    put(o_tn, m.third_neg);
+    put(o_pop, r.pop0);
+    std::vector<double> crfw(2ull * S * P, 0.0);
+    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.crossover_probability;
+    put(o_cr, crfw);
+    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
+    put(o_fw, crfw);
+    CUDA_TRY(cudaMemcpy(base, image.data(), o_rng, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(base + o_cr, image.data() + o_cr, a.size - o_cr, cudaMemcpyHostToDevice));
     {
         const uint32_t bits = jump_bits(r.n_states);
         const uint64_t blocks = std::min<uint64_t>((r.n_states + 255) / 256, 4096);
@@ -437,11 +450,6 @@ int upload_run(deac_batch* b, RunHost& r) {
                                                           (uint32_t)S);
         CUDA_TRY(cudaGetLastError());
     }
-    std::vector<double> crfw(2ull * S * P, 0.0);
-    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.crossover_probability;
-    if ((rc = up(o_cr, crfw))) return rc;
-    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
-    if ((rc = up(o_fw, crfw))) return rc;
 
     deac::RunDev& d = r.dev;
     d = deac::RunDev{};
