@@ -157,6 +157,7 @@ struct deac_batch {
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
+    double* h_genes = nullptr;          // pinned staging of a fetched member's genes
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
     // passes), 2 normalisation row sums, 3 split contraction, 4 combine + decisions (+ scaling)
     bool timing = false;
@@ -1084,14 +1085,19 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
     deac_run_result res;
     summarize(r, st, fit, &res);
     const uint64_t best = res.best_index;
-    std::vector<double> genes(S * M);
+    if (!b->h_genes) {
+        uint64_t most = 0;
+        for (auto& rp : b->runs) most = std::max<uint64_t>(most, (uint64_t)rp->S * rp->M);
+        CUDA_TRY(cudaMallocHost(&b->h_genes, most * 8));
+    }
+    double* const genes = b->h_genes;
     for (uint64_t s = 0; s < S; ++s)
         CUDA_TRY(cudaMemcpyAsync(&genes[s * M], st.pop + ((uint64_t)cur[best] * S * P + s * P + best) * M, M * 8,
                                  cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     const uint64_t L = res.spectrum_length;
     std::vector<double> dsf(L), fr(L);
-    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes.data(), S == 2 ? &genes[M] : nullptr, dsf.data(),
+    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes, S == 2 ? &genes[M] : nullptr, dsf.data(),
                         fr.data());
     if (best_dsf) std::memcpy(best_dsf, dsf.data(), L * 8);
     if (best_frequency) std::memcpy(best_frequency, fr.data(), L * 8);
@@ -1193,6 +1199,7 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
     cudaFree(b->d_jpow);
+    if (b->h_genes) cudaFreeHost(b->h_genes);
     cudaFree(b->d_runs);
     cudaFree(b->d_trial_work);
     cudaFree(b->d_contract_work);
