@@ -158,6 +158,10 @@ struct deac_batch {
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
     double* h_genes = nullptr;          // pinned staging of a fetched member's genes
+    uint32_t* d_fit_off = nullptr;      // snapshot_kernel: each run's first fitness slot (and the total)
+    uint64_t* d_snap = nullptr;         // snapshot_kernel output
+    uint64_t* h_snap = nullptr;         // its pinned host copy
+    size_t snap_bytes = 0;
     // timing: kernel kinds 0 trial, 1 contract (plain generation or exact
     // passes), 2 normalisation row sums, 3 split contraction, 4 combine + decisions (+ scaling)
     bool timing = false;
@@ -286,20 +290,38 @@ int finalize_split(deac_batch* b) {
         launch_contract(b, b->stream, deac::kModeFinal);
         CUDA_TRY(cudaGetLastError());
     }
+    // every run's descriptor, parent fitness and parent buffers packed on
+    // the device and read back in one copy
     const size_t n = b->runs.size();
+    if (!b->d_snap) {
+        std::vector<uint32_t> off(n + 1, 0);
+        for (size_t r = 0; r < n; ++r) off[r + 1] = off[r] + b->runs[r]->dev.P;
+        b->snap_bytes = n * sizeof(deac::RunDev) + (size_t)off[n] * 9;
+        CUDA_TRY(cudaMalloc(&b->d_fit_off, off.size() * 4));
+        CUDA_TRY(cudaMemcpy(b->d_fit_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_snap, b->snap_bytes));
+        CUDA_TRY(cudaMallocHost(&b->h_snap, b->snap_bytes));
+    }
+    deac::snapshot_kernel<<<(unsigned)n, 128, 0, b->stream>>>(b->d_runs, (uint32_t)n, b->d_fit_off, b->d_snap);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(b->h_snap, b->d_snap, b->snap_bytes, cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->snap.resize(n);
     b->snap_fit.resize(n);
     b->snap_cur.resize(n);
-    CUDA_TRY(cudaMemcpyAsync(b->snap.data(), b->d_runs, n * sizeof(deac::RunDev), cudaMemcpyDeviceToHost,
-                             b->stream));
+    std::memcpy(b->snap.data(), b->h_snap, n * sizeof(deac::RunDev));
+    const double* fit = reinterpret_cast<const double*>(reinterpret_cast<const char*>(b->h_snap) +
+                                                        n * sizeof(deac::RunDev));
+    size_t total = 0;
+    for (size_t r = 0; r < n; ++r) total += b->runs[r]->dev.P;
+    const uint8_t* cur = reinterpret_cast<const uint8_t*>(fit + total);
+    size_t o = 0;
     for (size_t r = 0; r < n; ++r) {
-        const deac::RunDev& d = b->runs[r]->dev;  // the host copy holds the same buffer addresses
-        b->snap_fit[r].resize(d.P);
-        b->snap_cur[r].resize(d.P);
-        CUDA_TRY(cudaMemcpyAsync(b->snap_fit[r].data(), d.fit_old, d.P * 8, cudaMemcpyDeviceToHost, b->stream));
-        CUDA_TRY(cudaMemcpyAsync(b->snap_cur[r].data(), d.cur, d.P, cudaMemcpyDeviceToHost, b->stream));
+        const uint32_t P = b->runs[r]->dev.P;
+        b->snap_fit[r].assign(fit + o, fit + o + P);
+        b->snap_cur[r].assign(cur + o, cur + o + P);
+        o += P;
     }
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->snapped = true;
     return DEAC_OK;
 }
@@ -1200,6 +1222,9 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_status);
     cudaFree(b->d_jpow);
     if (b->h_genes) cudaFreeHost(b->h_genes);
+    cudaFree(b->d_fit_off);
+    cudaFree(b->d_snap);
+    if (b->h_snap) cudaFreeHost(b->h_snap);
     cudaFree(b->d_runs);
     cudaFree(b->d_trial_work);
     cudaFree(b->d_contract_work);

@@ -333,6 +333,24 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
     trial_body(runs, work, init_mode, smem_doubles);
 }
 
+// -------------------------------------------------------------- snapshot
+__global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* fit_off, uint64_t* out) {
+    constexpr uint32_t W = sizeof(RunDev) / 8;
+    static_assert(sizeof(RunDev) % 8 == 0, "RunDev is copied as 8-byte words");
+    const uint32_t r = blockIdx.x;
+    if (r >= n) return;
+    const RunDev& R = runs[r];
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(&R);
+    for (uint32_t k = threadIdx.x; k < W; k += blockDim.x) out[(uint64_t)r * W + k] = src[k];
+    double* fit = reinterpret_cast<double*>(out + (uint64_t)n * W);
+    const uint32_t total = fit_off[n];
+    uint8_t* cur = reinterpret_cast<uint8_t*>(fit + total);
+    for (uint32_t i = threadIdx.x; i < R.P; i += blockDim.x) {
+        fit[fit_off[r] + i] = R.fit_old[i];
+        cur[fit_off[r] + i] = R.cur[i];
+    }
+}
+
 // ------------------------------------------------------------ PRNG table
 __global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow, uint32_t bits, uint64_t s0,
                                  uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S) {
