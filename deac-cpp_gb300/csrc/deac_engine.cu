@@ -367,7 +367,8 @@ const std::vector<uint64_t>& jump_powers(uint32_t bits) {
 // Host part of one run's set-up: constants, initial population, PRNG table.
 void prepare_run(RunHost& r) {
     const deac_config& c = r.cfg;
-    deac::build_model(c, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model);
+    // the kernel matrix is formed once per distinct one, after this
+    deac::build_model(c, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model, false);
     const uint64_t P = r.P, M = r.M;
     const int S = r.S;
     // initial population: one stream seeded with 1407513600 + seed
@@ -820,6 +821,23 @@ int deac_batch_setup(deac_batch* b) {
             pool.clear();
             for (unsigned t = 0; t < hw && next < b->runs.size(); ++t, ++next)
                 pool.emplace_back(prepare_run, std::ref(*b->runs[next]));
+            for (auto& th : pool) th.join();
+        }
+        // the kernel matrix of each distinct (model, T, tau and omega grid),
+        // in the first run that has it (the one upload_run takes it from),
+        // its rows spread over the host's threads
+        std::map<std::string, RunHost*> owners;
+        for (auto& rp : b->runs) owners.emplace(kernel_key(*rp), rp.get());
+        for (auto& kv : owners) {
+            RunHost& r = *kv.second;
+            r.model.k_pos.assign(r.Nt * r.M, 0.0);
+            if (r.S == 2) r.model.k_neg.assign(r.Nt * r.M, 0.0);
+            const uint64_t per = (r.Nt + hw - 1) / hw;
+            pool.clear();
+            for (uint64_t i0 = 0; i0 < r.Nt; i0 += per)
+                pool.emplace_back([&r, i0, per] {
+                    deac::kernel_rows(r.cfg, r.model, r.tau.data(), r.freq.data(), r.M, i0, std::min(r.Nt, i0 + per));
+                });
             for (auto& th : pool) th.join();
         }
     }

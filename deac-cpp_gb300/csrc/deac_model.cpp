@@ -44,28 +44,13 @@ std::string check_config(const deac_config& c) {
     return std::string();
 }
 
-void build_model(const deac_config& c, const double* tau, const double* isf,
-                 const double* err, uint64_t nt, const double* freq, uint64_t m,
-                 Model& o) {
-    o = Model();
-    o.sides = c.bosonic ? 1 : 2;
+// Rows [i0, i1) of the kernel matrix (deac.cpp:310-401) into o.k_pos /
+// o.k_neg, sized nt * m by the caller; o.beta and o.periodicity set.
+void kernel_rows(const deac_config& c, Model& o, const double* tau, const double* freq, uint64_t m, uint64_t i0,
+                 uint64_t i1) {
     const bool two = o.sides == 2;
-    if (!c.zero_temperature) {
-        o.beta = 1.0 / c.temperature;
-        o.periodicity = fermionic(c.spectra_type) ? -1.0 : 1.0;
-    }
-    o.zeroth_moment = isf[0];
-    o.use_first_moment = c.first_moment >= 0.0;
-    o.use_third_moment = c.third_moment >= 0.0;
-    // the negative first moment exists only for the one-sided genome and is
-    // switched off at zero temperature (deac.cpp:234-239, 868-924)
-    o.use_negative_first_moment = c.use_negative_first_moment && c.bosonic && !c.zero_temperature;
     const double beta = o.beta, per = o.periodicity;
-
-    // kernel matrix, deac.cpp:310-401
-    o.k_pos.assign(nt * m, 0.0);
-    if (two) o.k_neg.assign(nt * m, 0.0);
-    for (uint64_t i = 0; i < nt; ++i) {
+    for (uint64_t i = i0; i < i1; ++i) {
         const double t = tau[i];
         for (uint64_t j = 0; j < m; ++j) {
             const double f = freq[j];
@@ -109,6 +94,33 @@ void build_model(const deac_config& c, const double* tau, const double* isf,
                 }
             }
         }
+    }
+
+}
+
+void build_model(const deac_config& c, const double* tau, const double* isf,
+                 const double* err, uint64_t nt, const double* freq, uint64_t m,
+                 Model& o, bool with_kernel) {
+    o = Model();
+    o.sides = c.bosonic ? 1 : 2;
+    const bool two = o.sides == 2;
+    if (!c.zero_temperature) {
+        o.beta = 1.0 / c.temperature;
+        o.periodicity = fermionic(c.spectra_type) ? -1.0 : 1.0;
+    }
+    o.zeroth_moment = isf[0];
+    o.use_first_moment = c.first_moment >= 0.0;
+    o.use_third_moment = c.third_moment >= 0.0;
+    // the negative first moment exists only for the one-sided genome and is
+    // switched off at zero temperature (deac.cpp:234-239, 868-924)
+    o.use_negative_first_moment = c.use_negative_first_moment && c.bosonic && !c.zero_temperature;
+    const double beta = o.beta, per = o.periodicity;
+
+    // kernel matrix, deac.cpp:310-401
+    if (with_kernel) {
+        o.k_pos.assign(nt * m, 0.0);
+        if (two) o.k_neg.assign(nt * m, 0.0);
+        kernel_rows(c, o, tau, freq, m, 0, nt);
     }
 
     // normalisation terms, deac.cpp:493-538

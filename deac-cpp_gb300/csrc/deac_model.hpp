@@ -40,7 +40,13 @@ std::string check_config(const deac_config& cfg);
 // Build every constant term for one run.
 void build_model(const deac_config& cfg, const double* tau, const double* isf,
                  const double* isf_error, uint64_t nt, const double* freq,
-                 uint64_t m, Model& out);
+                 uint64_t m, Model& out, bool with_kernel = true);
+// Rows [i0, i1) of the kernel matrix into out.k_pos / out.k_neg (sized nt * m
+// by the caller; out.sides, beta and periodicity set, as build_model leaves
+// them): with_kernel = false and this, row blocks on several threads, give
+// build_model's matrix.
+void kernel_rows(const deac_config& cfg, Model& out, const double* tau, const double* freq, uint64_t m,
+                 uint64_t i0, uint64_t i1);
 
 // Best genome -> reported spectrum and frequency axis (deac.cpp:1594-1675).
 // xpos/xneg are the M genes of the best member (xneg ignored when one-sided).
