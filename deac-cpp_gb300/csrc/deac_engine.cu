@@ -467,8 +467,10 @@ int upload_run(deac_batch* b, RunHost& r) {
     CUDA_TRY(cudaMemcpy(base + o_cr, image.data() + o_cr, a.size - o_cr, cudaMemcpyHostToDevice));
     {
         const uint32_t bits = jump_bits(r.n_states);
-        const uint64_t blocks = std::min<uint64_t>((r.n_states + 255) / 256, 4096);
-        deac::rng_table_kernel<<<(unsigned)blocks, 256>>>(reinterpret_cast<uint64_t*>(base + o_rng), r.n_states,
+        // on the batch's stream: the host's set-up goes on meanwhile (the
+        // device is synchronised before the initial generation)
+        const uint64_t blocks = std::min<uint64_t>((r.n_states / 8 + 128) / 128, 4096);
+        deac::rng_table_kernel<<<(unsigned)blocks, 128, 0, b->stream>>>(reinterpret_cast<uint64_t*>(base + o_rng), r.n_states,
                                                           b->d_jpow, bits, r.rng_start[0], r.rng_start[1],
                                                           r.rng_start[2], r.rng_start[3], (uint32_t)P, (uint32_t)M,
                                                           (uint32_t)S);

@@ -354,10 +354,16 @@ __global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* 
 // ------------------------------------------------------------ PRNG table
 __global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow, uint32_t bits, uint64_t s0,
                                  uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S) {
-    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    // a thread forms kPerThread consecutive states: the first from the
+    // matrices of its index's set bits, the others one jump (J = jpow[0]) on
+    constexpr uint32_t kPerThread = 8;
+    const uint64_t groups = (n + kPerThread - 1) / kPerThread;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < groups;
+         g += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k0 = g * kPerThread;
         uint64_t v[4] = {s0, s1, s2, s3};
         for (uint32_t b = 0; b < bits; ++b)
-            if ((k >> b) & 1u) {
+            if ((k0 >> b) & 1u) {
                 uint64_t o[4];
                 gf2_matvec(jpow + (uint64_t)b * 1024, v, o);
                 v[0] = o[0];
@@ -365,9 +371,19 @@ __global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow
                 v[2] = o[2];
                 v[3] = o[3];
             }
-        const uint64_t slot = rng_slot(P, M, S, k);
+        for (uint32_t i = 0; i < kPerThread && k0 + i < n; ++i) {
+            if (i > 0) {
+                uint64_t o[4];
+                gf2_matvec(jpow, v, o);
+                v[0] = o[0];
+                v[1] = o[1];
+                v[2] = o[2];
+                v[3] = o[3];
+            }
+            const uint64_t slot = rng_slot(P, M, S, k0 + i);
 #pragma unroll
-        for (int w = 0; w < 4; ++w) rng[(uint64_t)w * n + slot] = v[w];
+            for (int w = 0; w < 4; ++w) rng[(uint64_t)w * n + slot] = v[w];
+        }
     }
 }
 
