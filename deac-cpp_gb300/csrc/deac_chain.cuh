@@ -807,33 +807,52 @@ __device__ __forceinline__ uint32_t group_predicted_pass(const double* x, const 
     int cbin_of[E];
     SegAll agg{0u, 1u, 0u, 0, 0};
     {
-        uint64_t prefix = pstart;
+        // each step's binade before and after it from the prefix (ds, 8 bits
+        // a step), its crossing, and the coarse terms to decode again on
+        // their step's grid
+        uint64_t prefix = pstart, ds_pack = 0;
+        uint32_t redo = 0, on_grid = 0;
 #pragma unroll
         for (uint32_t i = 0; i < E; ++i) {
-            Term t = unpack(tp[i]);
+            const Term t = unpack(tp[i]);
             const uint32_t s = my0 + i;
             const bool big = (t.flags & kBig) != 0;
             const uint64_t F = big ? t.F << kCoarse : t.F >> c;
             const uint64_t T = prefix + F + ((c == 0 && (t.flags & kGtZero)) ? 1u : 0u);
             const int ds = rel_binade(prefix, c), dk = rel_binade(T, c);
-            bool cr = s >= k0 && s < len && dk > ds;
-            bool on_grid = false;  // t already on the grid of binade ds
-            if (big && !cr && s >= k0 && s < len) {
-                // the coarse term on its own step's grid (a step still beyond
-                // it certainly changes binade: a crossing, run plainly)
-                const uint32_t q = chain_slot<W, E, kSwz>(s);
-                t = unpack(packed_term(x[q], w[q], ea + ds));
-                if (t.flags & (kNeg | kBad)) cr = true;
-                on_grid = true;
-            }
+            const bool live = s >= k0 && s < len;
+            const bool cr = live && dk > ds;
             cross_bits |= (cr ? 1u : 0u) << i;
+            redo |= (big && !cr && live ? 1u : 0u) << i;
+            ds_pack |= (uint64_t)(uint32_t)ds << (8 * i);
             cbin_of[i] = dk;
             prefix += F;
-            if (cr) {
+        }
+        // the coarse term on its own step's grid (a step still beyond it
+        // certainly changes binade: a crossing, run plainly); rare, and kept
+        // out of the loops around it
+        if (__any_sync(0xffffffffu, redo != 0)) {
+#pragma unroll
+            for (uint32_t i = 0; i < E; ++i) {
+                if (!((redo >> i) & 1u)) continue;
+                const uint32_t q = chain_slot<W, E, kSwz>(my0 + i);
+                const Term t = unpack(packed_term(x[q], w[q], ea + (int)((ds_pack >> (8 * i)) & 0xFFu)));
+                if (t.flags & (kNeg | kBad)) {
+                    cross_bits |= 1u << i;
+                } else {
+                    tp[i] = pack(t);
+                    on_grid |= 1u << i;
+                }
+            }
+        }
+#pragma unroll
+        for (uint32_t i = 0; i < E; ++i) {
+            if ((cross_bits >> i) & 1u) {
                 agg = seg_combine(agg, SegAll{1u, 1u, 0u, 0, 0});
                 tp[i] = 0ull;
             } else {
-                if (!on_grid) shift_term(t, ds);
+                Term t = unpack(tp[i]);
+                if (!((on_grid >> i) & 1u)) shift_term(t, (int)((ds_pack >> (8 * i)) & 0xFFu));
                 tp[i] = pack(t);
                 // the step for entering parity 0 and 1, and its map
                 const long long b0 = (long long)(t.F + ((t.flags & kGtHalf) ? 1u : 0u));
