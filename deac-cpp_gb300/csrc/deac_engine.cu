@@ -157,8 +157,9 @@ struct deac_batch {
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
-    double* h_genes = nullptr;          // pinned staging of a fetched member's genes
     uint32_t* d_fit_off = nullptr;      // snapshot_kernel: each run's first fitness slot (and the total)
+    uint64_t* d_gene_off = nullptr;     // snapshot_kernel: each run's first gene slot
+    std::vector<uint64_t> gene_off;     // its host copy
     uint64_t* d_snap = nullptr;         // snapshot_kernel output
     uint64_t* h_snap = nullptr;         // its pinned host copy
     size_t snap_bytes = 0;
@@ -296,13 +297,19 @@ int finalize_split(deac_batch* b) {
     if (!b->d_snap) {
         std::vector<uint32_t> off(n + 1, 0);
         for (size_t r = 0; r < n; ++r) off[r + 1] = off[r] + b->runs[r]->dev.P;
-        b->snap_bytes = n * sizeof(deac::RunDev) + (size_t)off[n] * 9;
+        b->gene_off.assign(n + 1, 0);
+        for (size_t r = 0; r < n; ++r) b->gene_off[r + 1] = b->gene_off[r] + (uint64_t)b->runs[r]->S * b->runs[r]->M;
+        b->snap_bytes = n * sizeof(deac::RunDev) + (size_t)off[n] * 8 + ((size_t)off[n] + 7) / 8 * 8 +
+                        (size_t)b->gene_off[n] * 8;
         CUDA_TRY(cudaMalloc(&b->d_fit_off, off.size() * 4));
         CUDA_TRY(cudaMemcpy(b->d_fit_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_gene_off, b->gene_off.size() * 8));
+        CUDA_TRY(cudaMemcpy(b->d_gene_off, b->gene_off.data(), b->gene_off.size() * 8, cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_snap, b->snap_bytes));
         CUDA_TRY(cudaMallocHost(&b->h_snap, b->snap_bytes));
     }
-    deac::snapshot_kernel<<<(unsigned)n, 128, 0, b->stream>>>(b->d_runs, (uint32_t)n, b->d_fit_off, b->d_snap);
+    deac::snapshot_kernel<<<(unsigned)n, 128, 0, b->stream>>>(b->d_runs, (uint32_t)n, b->d_fit_off, b->d_gene_off,
+                                                              b->d_snap);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(b->h_snap, b->d_snap, b->snap_bytes, cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
@@ -1123,20 +1130,16 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
     if (rc0) return rc0;
     const deac::RunDev& st = b->snap[run];
     const std::vector<double>& fit = b->snap_fit[run];
-    const std::vector<uint8_t>& cur = b->snap_cur[run];
     deac_run_result res;
     summarize(r, st, fit, &res);
-    const uint64_t best = res.best_index;
-    if (!b->h_genes) {
-        uint64_t most = 0;
-        for (auto& rp : b->runs) most = std::max<uint64_t>(most, (uint64_t)rp->S * rp->M);
-        CUDA_TRY(cudaMallocHost(&b->h_genes, most * 8));
-    }
-    double* const genes = b->h_genes;
-    for (uint64_t s = 0; s < S; ++s)
-        CUDA_TRY(cudaMemcpyAsync(&genes[s * M], st.pop + ((uint64_t)cur[best] * S * P + s * P + best) * M, M * 8,
-                                 cudaMemcpyDeviceToHost, b->stream));
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    // the best parent's genes (res.best_index, found by snapshot_kernel
+    // in the same values) are in the snapshot
+    size_t total = 0;
+    for (auto& rp : b->runs) total += rp->dev.P;
+    const double* const genes =
+        reinterpret_cast<const double*>(reinterpret_cast<const char*>(b->h_snap) + b->runs.size() * sizeof(deac::RunDev) +
+                                        total * 8 + (total + 7) / 8 * 8) +
+        b->gene_off[run];
     const uint64_t L = res.spectrum_length;
     std::vector<double> dsf(L), fr(L);
     deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes, S == 2 ? &genes[M] : nullptr, dsf.data(),
@@ -1241,8 +1244,8 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
     cudaFree(b->d_jpow);
-    if (b->h_genes) cudaFreeHost(b->h_genes);
     cudaFree(b->d_fit_off);
+    cudaFree(b->d_gene_off);
     cudaFree(b->d_snap);
     if (b->h_snap) cudaFreeHost(b->h_snap);
     cudaFree(b->d_runs);

@@ -334,9 +334,11 @@ trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles) {
 }
 
 // -------------------------------------------------------------- snapshot
-__global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* fit_off, uint64_t* out) {
+__global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* fit_off, const uint64_t* gene_off,
+                                uint64_t* out) {
     constexpr uint32_t W = sizeof(RunDev) / 8;
     static_assert(sizeof(RunDev) % 8 == 0, "RunDev is copied as 8-byte words");
+    __shared__ uint32_t s_best;
     const uint32_t r = blockIdx.x;
     if (r >= n) return;
     const RunDev& R = runs[r];
@@ -345,9 +347,30 @@ __global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* 
     double* fit = reinterpret_cast<double*>(out + (uint64_t)n * W);
     const uint32_t total = fit_off[n];
     uint8_t* cur = reinterpret_cast<uint8_t*>(fit + total);
+    double* genes = reinterpret_cast<double*>(out + (uint64_t)n * W + total + (total + 7) / 8);
     for (uint32_t i = threadIdx.x; i < R.P; i += blockDim.x) {
         fit[fit_off[r] + i] = R.fit_old[i];
         cur[fit_off[r] + i] = R.cur[i];
+    }
+    if (threadIdx.x == 0) {
+        // the first member of the strict minimum (deac.cpp:146-158), as the
+        // host's summary finds it in the same values
+        uint32_t best = 0;
+        double mn = R.fit_old[0];
+        for (uint32_t i = 0; i < R.P; ++i)
+            if (R.fit_old[i] < mn) {
+                mn = R.fit_old[i];
+                best = i;
+            }
+        s_best = best;
+    }
+    __syncthreads();
+    const uint32_t best = s_best;
+    const uint64_t PM = (uint64_t)R.P * R.M;
+    const double* row = R.pop + (uint64_t)R.cur[best] * R.S * PM + (uint64_t)best * R.M;
+    for (uint32_t k = threadIdx.x; k < R.S * R.M; k += blockDim.x) {
+        const uint32_t sd = k / R.M, j = k - sd * R.M;
+        genes[gene_off[r] + k] = row[(uint64_t)sd * PM + j];
     }
 }
 

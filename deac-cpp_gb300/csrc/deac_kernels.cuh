@@ -197,8 +197,11 @@ __device__ __forceinline__ void prefetch_l2(const T* p, uint64_t count, const T*
 __global__ void trial_kernel(RunDev* runs, const Work* work, int init_mode, int smem_doubles);
 // The result snapshot of n runs packed into one buffer: the RunDev
 // descriptors (as 8-byte words), then every run's parent fitness (offsets
-// fit_off), then their parent buffers (same offsets), for one copy to the host.
-__global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* fit_off, uint64_t* out);
+// fit_off), then their parent buffers (same offsets), then (8-byte aligned)
+// the genes of each run's best parent, both sides (offsets gene_off, in
+// doubles), for one copy to the host.
+__global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* fit_off, const uint64_t* gene_off,
+                                uint64_t* out);
 // the PRNG table of a run: state k = J^k s for the generator state s after
 // the initial draws, from the matrices J^(2^b) (jpow, 1024 words each), into
 // slot rng_slot(P, M, S, k) of the word-major table of n states
