@@ -11,6 +11,7 @@
 //   --allow_negative_spectral_weight             ALLOW_NEGATIVE_SPECTRAL_WEIGHT
 //   --device N                                   CUDA device
 //   --engine plain|split                         evaluation engine (same results)
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -61,6 +62,8 @@ const std::vector<Option>& options() {
         {"", "--stop_minimum_fitness", "Stopping criteria, if minimum fitness is below `stop_minimum_fitness` stop evolving.", "1", false},
         {"", "--seed", "Seed to pass to random number generator.", "0", false},
         {"", "--uuid", "UUID for run. If empty will be set to `seed`.", "", false},
+        {"", "--number_of_seeds", "Reconstructions run together, with seeds seed, seed+1, ...; each writes its own files, named by its seed.", "1", false},
+        {"", "--average_file", "File for the spectrum averaged over the seeds (float64, summed in the order of the seeds' names).", "", false},
         {"", "--save_state", "Save state of DEAC algorithm. Saves the random number generator, population, and population fitness.", "false", true},
         {"", "--save_directory", "Directory to save results in.", "./deacresults", false},
         {"", "--track_stats", "Track minimum fitness and other stats.", "false", true},
@@ -241,8 +244,21 @@ int main(int argc, char** argv) {
 
     const unsigned long seed_int = get_ulong(args, "--seed", 0);
     std::string uuid_str = args.has("--uuid") ? args.values.at("--uuid") : "";
-    if (uuid_str.empty()) uuid_str = std::to_string(seed_int);
-    std::cout << "uuid: " << uuid_str << std::endl;
+    // several seeds in one batch replace the reference's one process per
+    // seed (tools/generate_commands.sh:18-32); each seed's files keep the
+    // single-run names, with the seed as the uuid
+    const unsigned long n_seeds = get_ulong(args, "--number_of_seeds", 1);
+    if (n_seeds < 1) fail_with_error("number_of_seeds must be at least 1");
+    if (n_seeds > (1ul << 20)) fail_with_error("number_of_seeds must be at most 1048576");
+    if (n_seeds > 1 && !uuid_str.empty())
+        fail_with_error("uuid cannot be combined with number_of_seeds > 1: each seed's files are named by its seed");
+    std::vector<unsigned long> seeds(n_seeds);
+    std::vector<std::string> uuids(n_seeds);
+    for (unsigned long k = 0; k < n_seeds; ++k) {
+        seeds[k] = seed_int + k;
+        uuids[k] = uuid_str.empty() ? std::to_string(seeds[k]) : uuid_str;
+        std::cout << "uuid: " << uuids[k] << std::endl;
+    }
 
     // spectra type (deac.cpp:2040-2058)
     const std::string spectra_type =
@@ -338,11 +354,17 @@ int main(int argc, char** argv) {
     if (ec) fail_with_error("cannot create save_directory " + save_directory.string() + ": " + ec.message());
 
     const std::string prefix = (cfg.zero_temperature ? std::string("deac-zT") : std::string("deac-")) + spectra_type;
-    const fs::path log_filename = save_directory / (prefix + "_log_" + uuid_str + ".dat");
-    {
-        std::ofstream log(log_filename, std::ios_base::out | std::ios_base::app);
-        log << "uuid: " << uuid_str << std::endl;
+    auto log_filename = [&](unsigned long k) { return save_directory / (prefix + "_log_" + uuids[k] + ".dat"); };
+    for (unsigned long k = 0; k < n_seeds; ++k) {
+        std::ofstream log(log_filename(k), std::ios_base::out | std::ios_base::app);
+        log << "uuid: " << uuids[k] << std::endl;
         log << "isf_file: " << isf_file << std::endl;
+    }
+    const std::string average_file = args.has("--average_file") ? args.values.at("--average_file") : "";
+    if (!average_file.empty()) {
+        const fs::path parent = fs::path(average_file).parent_path();
+        if (!parent.empty() && !fs::is_directory(parent))
+            fail_with_error("average_file directory does not exist: " + parent.string());
     }
 
     // inside deac(): zero temperature disables the negative first moment
@@ -358,12 +380,27 @@ int main(int argc, char** argv) {
 
     deac_batch* batch = nullptr;
     int rc = deac_batch_create(device, nullptr, engine, &batch);
-    if (rc == DEAC_OK) rc = deac_batch_add_run(batch, &cfg, tau, isf, err, nt, frequency.data(), frequency.size(), nullptr);
+    for (unsigned long k = 0; k < n_seeds && rc == DEAC_OK; ++k) {
+        cfg.seed = seeds[k];
+        rc = deac_batch_add_run(batch, &cfg, tau, isf, err, nt, frequency.data(), frequency.size(), nullptr);
+    }
     if (rc == DEAC_OK) rc = deac_batch_run(batch);
-    deac_run_result res{};
-    if (rc == DEAC_OK) rc = deac_batch_result(batch, 0, &res);
+
+    // the seeds' outputs in the order of their names, which is the order the
+    // reference's averaging sums them in
+    // (tools/plot_simple_average_deac_results.py:10-27)
+    std::vector<unsigned long> order(n_seeds);
+    for (unsigned long k = 0; k < n_seeds; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](unsigned long a, unsigned long b) { return uuids[a] < uuids[b]; });
+    std::vector<double> average;
     std::vector<double> dsf, freq_out, s_mean, s_min, s_sq;
-    if (rc == DEAC_OK) {
+    static const char* build_names[] = {"USE_STANDARD_MODEL", "USE_HYPERBOLIC_MODEL", "USE_NORMALIZATION_MODEL"};
+    for (unsigned long n = 0; n < n_seeds && rc == DEAC_OK; ++n) {
+        const unsigned long k = order[n];
+        deac_run_result res{};
+        rc = deac_batch_result(batch, (uint32_t)k, &res);
+        if (rc != DEAC_OK) break;
         dsf.resize(res.spectrum_length);
         freq_out.resize(res.spectrum_length);
         if (cfg.track_stats) {
@@ -371,8 +408,66 @@ int main(int argc, char** argv) {
             s_min.resize(res.stats_length);
             s_sq.resize(res.stats_length);
         }
-        rc = deac_batch_fetch(batch, 0, dsf.data(), freq_out.data(), cfg.track_stats ? s_mean.data() : nullptr,
-                              cfg.track_stats ? s_min.data() : nullptr, cfg.track_stats ? s_sq.data() : nullptr);
+        rc = deac_batch_fetch(batch, (uint32_t)k, dsf.data(), freq_out.data(),
+                              cfg.track_stats ? s_mean.data() : nullptr, cfg.track_stats ? s_min.data() : nullptr,
+                              cfg.track_stats ? s_sq.data() : nullptr);
+        if (rc != DEAC_OK) break;
+        if (n == 0) {
+            average = dsf;
+        } else {
+            for (size_t i = 0; i < average.size(); ++i) average[i] += dsf[i];
+        }
+
+        // outputs (deac.cpp:1687-1769)
+        const std::string& uuid = uuids[k];
+        const fs::path dsf_filename = save_directory / (prefix + "_dsf_" + uuid + ".bin");
+        const fs::path frequency_filename = save_directory / (prefix + "_frequency_" + uuid + ".bin");
+        write_array(dsf_filename, dsf.data(), dsf.size());
+        write_array(frequency_filename, freq_out.data(), freq_out.size());
+        fs::path mean_fn, min_fn, sq_fn;
+        if (cfg.track_stats) {
+            mean_fn = save_directory / (prefix + "_stats_fitness-mean_" + uuid + ".bin");
+            min_fn = save_directory / (prefix + "_stats_fitness-minimum_" + uuid + ".bin");
+            sq_fn = save_directory / (prefix + "_stats_fitness-squared-mean_" + uuid + ".bin");
+            write_array(mean_fn, s_mean.data(), s_mean.size());
+            write_array(min_fn, s_min.data(), s_min.size());
+            write_array(sq_fn, s_sq.data(), s_sq.size());
+        }
+
+        std::ofstream log(log_filename(k), std::ios_base::out | std::ios_base::app);
+        log << "build: " << build_names[cfg.model] << std::endl;
+        log << "kernel: " << spectra_type << std::endl;
+        log << "temperature: " << cfg.temperature << std::endl;
+        log << "number_of_generations: " << cfg.number_of_generations << std::endl;
+        log << "number_of_timeslices: " << nt << std::endl;
+        log << "population_size: " << cfg.population_size << std::endl;
+        log << "genome_size: " << frequency.size() << std::endl;
+        log << "normalize: " << cfg.normalize << std::endl;
+        log << "use_negative_first_moment: " << cfg.use_negative_first_moment << std::endl;
+        log << "first_moment: " << cfg.first_moment << std::endl;
+        log << "third_moment: " << cfg.third_moment << std::endl;
+        log << "third_moment_error: " << cfg.third_moment_error << std::endl;
+        log << "crossover_probability: " << cfg.crossover_probability << std::endl;
+        log << "self_adapting_crossover_probability: " << cfg.self_adapting_crossover_probability << std::endl;
+        log << "differential_weight: " << cfg.differential_weight << std::endl;
+        log << "self_adapting_differential_weight_probability: " << cfg.self_adapting_differential_weight_probability
+            << std::endl;
+        log << "self_adapting_differential_weight_shift: " << cfg.self_adapting_differential_weight_shift << std::endl;
+        log << "self_adapting_differential_weight: " << cfg.self_adapting_differential_weight << std::endl;
+        log << "stop_minimum_fitness: " << cfg.stop_minimum_fitness << std::endl;
+        log << "track_stats: " << cfg.track_stats << std::endl;
+        log << "seed: " << seeds[k] << std::endl;
+        log << "best_dsf_filename: " << dsf_filename << std::endl;
+        log << "frequency_filename: " << frequency_filename << std::endl;
+        log << "generation: " << res.generation << std::endl;
+        std::cout << "generation: " << res.generation << std::endl;
+        log << "minimum_fitness: " << res.minimum_fitness << std::endl;
+        std::cout << "minimum_fitness: " << res.minimum_fitness << std::endl;
+        if (cfg.track_stats) {
+            log << "fitness_mean_filename: " << mean_fn << std::endl;
+            log << "fitness_minimum_filename: " << min_fn << std::endl;
+            log << "fitness_squared_mean_filename: " << sq_fn << std::endl;
+        }
     }
     if (rc != DEAC_OK) {
         std::cerr << "deac-gb300: " << deac_last_error() << std::endl;
@@ -380,56 +475,9 @@ int main(int argc, char** argv) {
         return 2;
     }
     deac_batch_destroy(batch);
-
-    // outputs (deac.cpp:1687-1769)
-    const fs::path dsf_filename = save_directory / (prefix + "_dsf_" + uuid_str + ".bin");
-    const fs::path frequency_filename = save_directory / (prefix + "_frequency_" + uuid_str + ".bin");
-    write_array(dsf_filename, dsf.data(), dsf.size());
-    write_array(frequency_filename, freq_out.data(), freq_out.size());
-    fs::path mean_fn, min_fn, sq_fn;
-    if (cfg.track_stats) {
-        mean_fn = save_directory / (prefix + "_stats_fitness-mean_" + uuid_str + ".bin");
-        min_fn = save_directory / (prefix + "_stats_fitness-minimum_" + uuid_str + ".bin");
-        sq_fn = save_directory / (prefix + "_stats_fitness-squared-mean_" + uuid_str + ".bin");
-        write_array(mean_fn, s_mean.data(), s_mean.size());
-        write_array(min_fn, s_min.data(), s_min.size());
-        write_array(sq_fn, s_sq.data(), s_sq.size());
-    }
-
-    std::ofstream log(log_filename, std::ios_base::out | std::ios_base::app);
-    static const char* build_names[] = {"USE_STANDARD_MODEL", "USE_HYPERBOLIC_MODEL", "USE_NORMALIZATION_MODEL"};
-    log << "build: " << build_names[cfg.model] << std::endl;
-    log << "kernel: " << spectra_type << std::endl;
-    log << "temperature: " << cfg.temperature << std::endl;
-    log << "number_of_generations: " << cfg.number_of_generations << std::endl;
-    log << "number_of_timeslices: " << nt << std::endl;
-    log << "population_size: " << cfg.population_size << std::endl;
-    log << "genome_size: " << frequency.size() << std::endl;
-    log << "normalize: " << cfg.normalize << std::endl;
-    log << "use_negative_first_moment: " << cfg.use_negative_first_moment << std::endl;
-    log << "first_moment: " << cfg.first_moment << std::endl;
-    log << "third_moment: " << cfg.third_moment << std::endl;
-    log << "third_moment_error: " << cfg.third_moment_error << std::endl;
-    log << "crossover_probability: " << cfg.crossover_probability << std::endl;
-    log << "self_adapting_crossover_probability: " << cfg.self_adapting_crossover_probability << std::endl;
-    log << "differential_weight: " << cfg.differential_weight << std::endl;
-    log << "self_adapting_differential_weight_probability: " << cfg.self_adapting_differential_weight_probability
-        << std::endl;
-    log << "self_adapting_differential_weight_shift: " << cfg.self_adapting_differential_weight_shift << std::endl;
-    log << "self_adapting_differential_weight: " << cfg.self_adapting_differential_weight << std::endl;
-    log << "stop_minimum_fitness: " << cfg.stop_minimum_fitness << std::endl;
-    log << "track_stats: " << cfg.track_stats << std::endl;
-    log << "seed: " << seed_int << std::endl;
-    log << "best_dsf_filename: " << dsf_filename << std::endl;
-    log << "frequency_filename: " << frequency_filename << std::endl;
-    log << "generation: " << res.generation << std::endl;
-    std::cout << "generation: " << res.generation << std::endl;
-    log << "minimum_fitness: " << res.minimum_fitness << std::endl;
-    std::cout << "minimum_fitness: " << res.minimum_fitness << std::endl;
-    if (cfg.track_stats) {
-        log << "fitness_mean_filename: " << mean_fn << std::endl;
-        log << "fitness_minimum_filename: " << min_fn << std::endl;
-        log << "fitness_squared_mean_filename: " << sq_fn << std::endl;
+    if (!average_file.empty()) {
+        for (double& v : average) v /= (double)n_seeds;
+        write_array(average_file, average.data(), average.size());
     }
     return 0;
 }

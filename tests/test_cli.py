@@ -126,3 +126,15 @@ def test_zero_temperature_two_sided_rejected(engine, tmp_path):
     r = run_exe(engine.EXE_PATH, ["--zero_temperature", "--spectra_type", "bfull", str(tmp_path / "isf.bin")],
                 tmp_path)
     assert r.returncode == 1 and "--bosonic" in r.stdout
+
+
+@pytest.mark.parametrize("extra,msg", [
+    (("--number_of_seeds", "0"), "number_of_seeds must be at least 1"),
+    (("--number_of_seeds", "2", "--uuid", "run"), "uuid cannot be combined with number_of_seeds > 1"),
+    (("--number_of_seeds", "2", "--average_file", "no-such-dir/avg.bin"), "average_file directory does not exist"),
+])
+def test_seed_range_validation(engine, tmp_path, extra, msg):
+    _fixture(tmp_path / "isf.bin")
+    r = run_exe(engine.EXE_PATH, _cmd(tmp_path, tmp_path / "isf.bin", extra=extra), tmp_path)
+    assert r.returncode == 1, r.stdout
+    assert msg in r.stdout
