@@ -112,6 +112,7 @@ struct RunHost {
     uint64_t n_states = 0;
     uint64_t trace_cap = 0;
     char* arena = nullptr;               // device allocation of this run
+    uint64_t arena_bytes = 0;            // its size
     char* split_arena = nullptr;         // split-engine buffers of this run
     deac::RunDev dev{};                  // host copy of the descriptor
     deac::SplitRun split{};              // host copy of the split descriptor
@@ -447,6 +448,7 @@ int upload_run(deac_batch* b, RunHost& r) {
     const uint64_t o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
     const uint64_t o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
     CUDA_TRY(cudaMalloc(&r.arena, a.size));
+    r.arena_bytes = a.size;
     char* base = r.arena;
     // the arena's initial contents as one host image (zeros but for the
     // inputs, the initial parents and CR / F), copied around the PRNG
@@ -1180,6 +1182,90 @@ int deac_batch_fetch_state(deac_batch* b, uint32_t run, double* population, doub
     if (crossover_rates) std::memcpy(crossover_rates, crfw.data(), SP * 8);
     if (differential_weights) std::memcpy(differential_weights, crfw.data() + 2 * SP, SP * 8);
     return DEAC_OK;
+}
+
+namespace {
+
+// A checkpoint: this header, then the run's evolving state as it lies in its
+// arena (both parent buffers, the parent selectors, the PRNG table, CR and F,
+// fitness, model ISF, moments, statistics and trace), from the population to
+// the end.  The constant inputs before it are not saved: a restore takes
+// them from the run it restores into.
+struct CheckpointHeader {
+    char magic[8];  // "DEACCKP1"
+    uint32_t P, M, Nt, S;
+    uint64_t N;
+    uint64_t state_bytes;
+    uint64_t ii, generation;
+    int32_t done;
+    uint32_t flags;
+};
+
+uint64_t state_offset(const RunHost& r) { return (uint64_t)(reinterpret_cast<char*>(r.dev.pop) - r.arena); }
+
+}  // namespace
+
+int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capacity, uint64_t* bytes) {
+    if (!b || run >= b->runs.size() || !bytes) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    if (b->engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "checkpoints are taken of the plain engine");
+    RunHost& r = *b->runs[run];
+    const uint64_t off = state_offset(r), state = r.arena_bytes - off;
+    *bytes = sizeof(CheckpointHeader) + state;
+    if (!out) return DEAC_OK;
+    if (capacity < *bytes) return fail(DEAC_E_INVALID, "checkpoint buffer too small (%llu < %llu bytes)",
+                                       (unsigned long long)capacity, (unsigned long long)*bytes);
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    deac::RunDev st;
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    CheckpointHeader h{};
+    std::memcpy(h.magic, "DEACCKP1", 8);
+    h.P = st.P;
+    h.M = st.M;
+    h.Nt = st.Nt;
+    h.S = st.S;
+    h.N = st.N;
+    h.state_bytes = state;
+    h.ii = st.ii;
+    h.generation = st.generation;
+    h.done = st.done;
+    h.flags = st.flags;
+    std::memcpy(out, &h, sizeof h);
+    CUDA_TRY(cudaMemcpy(static_cast<char*>(out) + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
+    return DEAC_OK;
+}
+
+int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t bytes) {
+    if (!b || run >= b->runs.size() || !in) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    if (b->engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "checkpoints are restored into the plain engine");
+    RunHost& r = *b->runs[run];
+    const uint64_t off = state_offset(r), state = r.arena_bytes - off;
+    CheckpointHeader h;
+    if (bytes < sizeof h) return fail(DEAC_E_INVALID, "checkpoint too short");
+    std::memcpy(&h, in, sizeof h);
+    const deac::RunDev& d = r.dev;
+    if (std::memcmp(h.magic, "DEACCKP1", 8) != 0) return fail(DEAC_E_INVALID, "not a checkpoint");
+    if (h.P != d.P || h.M != d.M || h.Nt != d.Nt || h.S != d.S || h.N != d.N || h.flags != d.flags ||
+        h.state_bytes != state || bytes != sizeof h + state)
+        return fail(DEAC_E_INVALID, "checkpoint of a different configuration");
+    // the values the kernels index with must lie in range
+    if (h.ii > h.N || h.generation > h.N || (h.done != 0 && h.done != 1))
+        return fail(DEAC_E_INVALID, "checkpoint counters out of range");
+    const char* body = static_cast<const char*>(in) + sizeof h;
+    const uint64_t cur_off = (uint64_t)(reinterpret_cast<char*>(d.cur) - r.arena) - off;
+    for (uint64_t i = 0; i < d.P; ++i)
+        if ((uint8_t)body[cur_off + i] > 1) return fail(DEAC_E_INVALID, "checkpoint parent selector out of range");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaMemcpy(r.arena + off, body, state, cudaMemcpyHostToDevice));
+    deac::RunDev st;
+    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    st.ii = h.ii;
+    st.generation = h.generation;
+    st.done = h.done;
+    CUDA_TRY(cudaMemcpy(b->d_runs + run, &st, sizeof st, cudaMemcpyHostToDevice));
+    b->snapped = false;
+    return refresh_status(b);
 }
 
 int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness, uint64_t capacity) {

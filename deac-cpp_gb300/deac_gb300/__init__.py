@@ -130,6 +130,9 @@ SIGNATURES = {
     "deac_batch_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(RunResult)]),
     "deac_batch_fetch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, _dp, _dp, _dp, _dp]),
     "deac_batch_fetch_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, _dp, _dp, _dp]),
+    "deac_batch_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                                             ctypes.POINTER(ctypes.c_uint64)]),
+    "deac_batch_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]),
     "deac_batch_enable_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]),
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
@@ -275,6 +278,18 @@ class Batch:
         _check(self._lib.deac_batch_fetch_state(self._h, run, _ptr(pop), _ptr(fit), _ptr(cr), _ptr(fw)))
         return {"population": pop.reshape(s, p, m), "fitness": fit, "crossover": cr.reshape(s, p),
                 "weights": fw.reshape(s, p)}
+
+    def checkpoint(self, run: int) -> bytes:
+        """The run's state as one byte block (plain engine, after setup)."""
+        n = ctypes.c_uint64(0)
+        _check(self._lib.deac_batch_checkpoint(self._h, run, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(self._lib.deac_batch_checkpoint(self._h, run, buf, n.value, ctypes.byref(n)))
+        return buf.raw
+
+    def restore(self, run: int, block: bytes):
+        """Continue run ``run`` from a checkpoint (after setup)."""
+        _check(self._lib.deac_batch_restore(self._h, run, block, len(block)))
 
     def fetch_trace(self, run: int, generations: int) -> np.ndarray:
         cfg = self._runs[run][0]

@@ -184,6 +184,22 @@ int deac_batch_fetch_state(deac_batch* b, uint32_t run, double* population,
                            double* fitness, double* crossover_rates,
                            double* differential_weights);
 
+/* Checkpoint of run `run` (plain engine, after setup): the state the
+ * reference's --save_state names (deac.cpp:2004-2007, declared there but
+ * never written) -- the PRNG states, both parent buffers, fitness, crossover
+ * rates and differential weights -- plus the generation counters, statistics
+ * and trace, as one byte block.  With out == NULL only *bytes (its size) is
+ * set; otherwise the block is written to out (capacity bytes at least). */
+int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out,
+                          uint64_t capacity, uint64_t* bytes);
+
+/* Resume from a checkpoint: after deac_batch_setup of a run added with the
+ * same configuration and inputs, overwrite its state with the block, so that
+ * the generations launched next continue the checkpointed run exactly (the
+ * same results as a run never interrupted).  A block of another configuration,
+ * or with counters out of range, is refused with DEAC_E_INVALID. */
+int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t bytes);
+
 /* Record, for run `run`, the trial fitness of every member at every
  * generation up to `max_generations` (a test aid; call before setup). */
 int deac_batch_enable_trace(deac_batch* b, uint32_t run, uint64_t max_generations);
