@@ -72,6 +72,20 @@ constexpr uint64_t kTailSlotsBytes = 4 * 1024 * 8;  // reduction slots of the fi
 
 uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`, never
+// lower it: batches set up in other host threads (and the allocation-free
+// fitness entry point) launch the same kernels with their own needs.
+template <typename Kernel>
+cudaError_t raise_smem_limit(Kernel kernel, size_t bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // smallest float >= |v| (infinity beyond the float range)
 float float_up(double v) {
     v = std::fabs(v);
@@ -879,11 +893,8 @@ int deac_batch_setup(deac_batch* b) {
     b->smem_doubles = (int)trial_doubles;
     b->trial_smem_bytes = trial_doubles * sizeof(double);
     b->contract_smem_bytes = contract_bytes;
-    CUDA_TRY(cudaFuncSetAttribute(deac::trial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::max<size_t>(b->trial_smem_bytes, 1024)));
-
-    CUDA_TRY(cudaFuncSetAttribute(deac::contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)b->contract_smem_bytes));
+    CUDA_TRY(raise_smem_limit(deac::trial_kernel, std::max<size_t>(b->trial_smem_bytes, 1024)));
+    CUDA_TRY(raise_smem_limit(deac::contract_kernel, b->contract_smem_bytes));
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
@@ -909,8 +920,7 @@ int deac_batch_setup(deac_batch* b) {
         CUDA_TRY(cudaMemcpy(b->d_part_work, pw.data(), pw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
         b->n_norm_ctas = (uint32_t)nw.size();
         if (!nw.empty()) {
-            CUDA_TRY(cudaFuncSetAttribute(deac::norm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)deac::kNormSmemBytes));
+            CUDA_TRY(raise_smem_limit(deac::norm_kernel, deac::kNormSmemBytes));
             CUDA_TRY(cudaMalloc(&b->d_norm_work, nw.size() * sizeof(deac::Work)));
             CUDA_TRY(cudaMemcpy(b->d_norm_work, nw.data(), nw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
         }
@@ -989,8 +999,7 @@ int deac_batch_setup(deac_batch* b) {
         CUDA_TRY(cudaMalloc(&b->d_partial, (uint64_t)blocks * deac::kPartialBlock * sizeof(float4)));
         CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
         CUDA_TRY(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaFuncSetAttribute(deac::split_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)deac::split_smem_bytes(2)));
+        CUDA_TRY(raise_smem_limit(deac::split_contract_kernel, deac::split_smem_bytes(2)));
     }
     CUDA_TRY(cudaDeviceSynchronize());
     // initial fitness, statistics of generation 0 and the first stop test
@@ -1192,16 +1201,36 @@ namespace {
 // the end.  The constant inputs before it are not saved: a restore takes
 // them from the run it restores into.
 struct CheckpointHeader {
-    char magic[8];  // "DEACCKP1"
+    char magic[8];  // "DEACCKP2"
     uint32_t P, M, Nt, S;
     uint64_t N;
     uint64_t state_bytes;
     uint64_t ii, generation;
     int32_t done;
     uint32_t flags;
+    uint64_t inputs;  // input_hash of the run
 };
 
 uint64_t state_offset(const RunHost& r) { return (uint64_t)(reinterpret_cast<char*>(r.dev.pop) - r.arena); }
+
+// FNV-1a over the run's whole configuration (seed, temperature, model,
+// spectra type, moment targets, jDE parameters, stop fitness ...) and its
+// input arrays (tau, F, sigma, frequency grid): a checkpoint continues only
+// a run with the same inputs, not merely the same sizes.
+uint64_t input_hash(const RunHost& r) {
+    uint64_t h = 1469598103934665603ull;
+    auto put = [&h](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        for (size_t k = 0; k < n; ++k) h = (h ^ c[k]) * 1099511628211ull;
+    };
+    put(&r.cfg, sizeof r.cfg);
+    for (const std::vector<double>* v : {&r.tau, &r.isf, &r.err, &r.freq}) {
+        const uint64_t n = v->size();
+        put(&n, sizeof n);
+        put(v->data(), n * sizeof(double));
+    }
+    return h;
+}
 
 }  // namespace
 
@@ -1219,7 +1248,7 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
     deac::RunDev st;
     CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     CheckpointHeader h{};
-    std::memcpy(h.magic, "DEACCKP1", 8);
+    std::memcpy(h.magic, "DEACCKP2", 8);
     h.P = st.P;
     h.M = st.M;
     h.Nt = st.Nt;
@@ -1230,6 +1259,7 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
     h.generation = st.generation;
     h.done = st.done;
     h.flags = st.flags;
+    h.inputs = input_hash(r);
     std::memcpy(out, &h, sizeof h);
     CUDA_TRY(cudaMemcpy(static_cast<char*>(out) + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
     return DEAC_OK;
@@ -1245,10 +1275,12 @@ int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t byt
     if (bytes < sizeof h) return fail(DEAC_E_INVALID, "checkpoint too short");
     std::memcpy(&h, in, sizeof h);
     const deac::RunDev& d = r.dev;
-    if (std::memcmp(h.magic, "DEACCKP1", 8) != 0) return fail(DEAC_E_INVALID, "not a checkpoint");
+    if (std::memcmp(h.magic, "DEACCKP2", 8) != 0) return fail(DEAC_E_INVALID, "not a checkpoint");
     if (h.P != d.P || h.M != d.M || h.Nt != d.Nt || h.S != d.S || h.N != d.N || h.flags != d.flags ||
         h.state_bytes != state || bytes != sizeof h + state)
         return fail(DEAC_E_INVALID, "checkpoint of a different configuration");
+    if (h.inputs != input_hash(r))
+        return fail(DEAC_E_INVALID, "checkpoint of a run with other inputs (seed, temperature, model, data or grid)");
     // the values the kernels index with must lie in range
     if (h.ii > h.N || h.generation > h.N || (h.done != 0 && h.done != 1))
         return fail(DEAC_E_INVALID, "checkpoint counters out of range");

@@ -16,7 +16,6 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
-#include <mutex>
 
 #include "deac_gb300.h"
 #include "deac_kernels.cuh"
@@ -31,10 +30,6 @@ __attribute__((visibility("hidden"))) int set_error(int code, const char* msg);
 }
 
 namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices];  // device address of g_fitness_scratch, per device
 
 int error(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int error(int code, const char* fmt, ...) {
@@ -79,18 +74,16 @@ __global__ void noalloc_prepare_kernel(deac::RunDev desc, deac::RunDev* run, dea
     for (uint32_t m = i; m < P; m += stride) cur[m] = 0;
 }
 
-// Once per device, with that device current: the device address of the
-// scratch array (its host-side name is only a stand-in) and the shared-memory
-// limit of contract_kernel.
-int set_up_device(int device, void** scratch) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[device]) {
-        void* p = nullptr;
-        NOALLOC_TRY(cudaGetSymbolAddress(&p, g_fitness_scratch));
-        if (!p) return error(DEAC_E_CUDA, "no device address for the fitness scratch on device %d", device);
-        g_scratch_address[device] = p;
-    }
-    *scratch = g_scratch_address[device];
+// With the target device current: the device address of the scratch array
+// in the current context (its host-side name is only a stand-in).  Looked up
+// on every call rather than cached, so that a context torn down and made
+// again (cudaDeviceReset, a new primary context) never leaves a stale
+// address behind; the lookup is cheap beside the launch.
+int scratch_address(int device, void** scratch) {
+    void* p = nullptr;
+    NOALLOC_TRY(cudaGetSymbolAddress(&p, g_fitness_scratch));
+    if (!p) return error(DEAC_E_CUDA, "no device address for the fitness scratch on device %d", device);
+    *scratch = p;
     return DEAC_OK;
 }
 
@@ -148,7 +141,7 @@ extern "C" int deac_population_fitness_noalloc(int device, void* cuda_stream, in
 
     // --- device
     int n_dev = 0;
-    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || device < 0 || device >= n_dev || device >= kMaxDevices) {
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || device < 0 || device >= n_dev) {
         cudaGetLastError();
         return error(DEAC_E_NODEVICE, "no CUDA device %d", device);
     }
@@ -163,7 +156,7 @@ extern "C" int deac_population_fitness_noalloc(int device, void* cuda_stream, in
     int rc = DEAC_OK;
     do {
         void* scratch = nullptr;
-        if ((rc = set_up_device(device, &scratch))) break;
+        if ((rc = scratch_address(device, &scratch))) break;
         cudaFuncAttributes fa;
         cudaError_t e = cudaFuncGetAttributes(&fa, deac::contract_kernel);
         if (e == cudaSuccess && (uint64_t)fa.maxDynamicSharedSizeBytes < smem)

@@ -264,10 +264,11 @@ int deac_reconstruct(const deac_config* cfg, const double* imaginary_time,
  * timeslice model-ISF matrix) lives in one static device array of
  * DEAC_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
  * the process exits: population_size x number_of_timeslices x 8 bytes plus a
- * few KB must fit in it, and larger calls fail with DEAC_E_INVALID.  The first
- * call on a device looks up the array's device address and raises the
- * kernel's shared-memory limit; make that first call before any stream
- * capture.  All calls on a device share the one array, which keeps the last
+ * few KB must fit in it, and larger calls fail with DEAC_E_INVALID.  Every
+ * call looks up the array's device address in the current context (so a
+ * context made again after cudaDeviceReset is handled); the first call on a
+ * device also raises the kernel's shared-memory limit, so make that first
+ * call before any stream capture.  All calls on a device share the one array, which keeps the last
  * call's contents: calls that overlap on the GPU (different streams or host
  * threads) race and must be ordered by the caller. */
 #define DEAC_NOALLOC_SCRATCH_BYTES (16u << 20)

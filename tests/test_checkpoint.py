@@ -69,3 +69,27 @@ def test_restore_refuses_another_configuration(engine):
             b.restore(r, block)
         with pytest.raises(engine.DeacError, match="too short"):
             b.restore(r, block[:16])
+
+
+@pytest.mark.parametrize("change", ["seed", "isf", "temperature"])
+def test_restore_refuses_a_run_with_other_inputs(engine, change):
+    """Same sizes and flags, other seed, data or temperature: refused."""
+    tau, isf, err, freq = _inputs()
+    with engine.Batch() as b:
+        r = b.add_run(_cfg(engine), tau, isf, err, freq)
+        b.setup()
+        block = b.checkpoint(r)
+    over, data = {}, (tau, isf, err, freq)
+    if change == "seed":
+        over = dict(seed=22)
+    elif change == "temperature":
+        over = dict(temperature=1.4)
+    else:
+        isf2 = isf.copy()
+        isf2[5] *= 1.0 + 1e-12
+        data = (tau, isf2, err, freq)
+    with engine.Batch() as b:
+        r = b.add_run(_cfg(engine, **over), *data)
+        b.setup()
+        with pytest.raises(engine.DeacError, match="other inputs"):
+            b.restore(r, block)

@@ -74,6 +74,25 @@ def test_noalloc_fitness_equals_batch_fitness_on_consecutive_calls(engine, oracl
         np.testing.assert_array_equal(fit, state["fitness"])
 
 
+@pytest.mark.gpu
+def test_noalloc_fitness_near_the_scratch_limit(engine, oracle):
+    """A population x timeslice model ISF of 16,384,000 bytes (P = 4000,
+    N_tau = 512), with its work list and buffer indices 16,646,656 of the
+    16 MiB static scratch: two calls in a row, each equal to the batch
+    engine's fitness of the same population."""
+    torch = pytest.importorskip("torch")
+    p, nt, m = 4000, 512, 1024
+    tau, isf, err = make_isf(nt, 1.35, [(0.7, 5.0, 1.0), (0.3, 20.0, 3.0)], 1e-4, 5)
+    freq = uniform_grid(m, 64.0)
+    cfg = engine.make_config(temperature=1.35, spectra_type="bfull", population_size=p,
+                             number_of_generations=100, seed=11, stop_minimum_fitness=0.0)
+    first, later = _batch_states(engine, cfg, (tau, isf, err), freq, 2)
+    k_pos, k_neg = oracle.kernel_matrix(cfg, tau, freq)
+    for state in (first, later):
+        fit = _noalloc(engine, torch, 2, state["population"], k_pos, k_neg, isf, err)
+        np.testing.assert_array_equal(fit, state["fitness"])
+
+
 @pytest.mark.parametrize("case,message", [
     ("sides", "sides must be 1 or 2"),
     ("empty", "must be positive"),
