@@ -143,6 +143,7 @@ struct deac_batch {
     bool own_stream = false;
     cudaStream_t capture_stream = nullptr;
     int32_t engine = DEAC_ENGINE_PLAIN_FP64;
+    int32_t streams = DEAC_STREAMS_REFERENCE;
     std::vector<std::unique_ptr<RunHost>> runs;
     std::map<std::string, KernelMatrix> kcache;
     deac::RunDev* d_runs = nullptr;
@@ -387,7 +388,7 @@ const std::vector<uint64_t>& jump_powers(uint32_t bits) {
 }
 
 // Host part of one run's set-up: constants, initial population, PRNG table.
-void prepare_run(RunHost& r) {
+void prepare_run(RunHost& r, int32_t streams) {
     const deac_config& c = r.cfg;
     // the kernel matrix is formed once per distinct one, after this
     deac::build_model(c, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model, false);
@@ -408,8 +409,9 @@ void prepare_run(RunHost& r) {
     if (S == 2)
         for (uint64_t i = 0; i < P; ++i) r.pop0[P * M + i * M] = r.pop0[i * M];
     // per-gene states: state k = jump^k(generator after the initial draws)
-    // (deac.cpp:1114-1126), formed on the device by rng_table_kernel
-    r.n_states = P * (1 + (uint64_t)S * M);
+    // (deac.cpp:1114-1126), formed on the device by rng_table_kernel; with
+    // counter streams one slot per member (its jDE step count, from 0)
+    r.n_states = streams == DEAC_STREAMS_COUNTER ? P : P * (1 + (uint64_t)S * M);
     for (int w = 0; w < 4; ++w) r.rng_start[w] = g.s[w];
 }
 
@@ -486,9 +488,15 @@ int upload_run(deac_batch* b, RunHost& r) {
     put(o_cr, crfw);
     for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
     put(o_fw, crfw);
-    CUDA_TRY(cudaMemcpy(base, image.data(), o_rng, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(base + o_cr, image.data() + o_cr, a.size - o_cr, cudaMemcpyHostToDevice));
-    {
+    const bool counter = b->streams == DEAC_STREAMS_COUNTER;
+    if (counter) {
+        // the members' jDE step counts start at zero (in the image)
+        CUDA_TRY(cudaMemcpy(base, image.data(), a.size, cudaMemcpyHostToDevice));
+    } else {
+        CUDA_TRY(cudaMemcpy(base, image.data(), o_rng, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(base + o_cr, image.data() + o_cr, a.size - o_cr, cudaMemcpyHostToDevice));
+    }
+    if (!counter) {
         const uint32_t bits = jump_bits(r.n_states);
         // on the batch's stream: the host's set-up goes on meanwhile (the
         // device is synchronised before the initial generation)
@@ -510,7 +518,9 @@ int upload_run(deac_batch* b, RunHost& r) {
               (m.use_third_moment ? deac::kThirdMoment : 0) |
               (m.use_negative_first_moment ? deac::kNegativeFirstMoment : 0) |
               (r.cfg.allow_negative_weight ? deac::kSignedWeights : 0) |
-              (r.cfg.track_stats ? deac::kTrackStats : 0) | (r.trace_cap ? deac::kTrace : 0);
+              (r.cfg.track_stats ? deac::kTrackStats : 0) | (r.trace_cap ? deac::kTrace : 0) |
+              (counter ? deac::kCounterStreams : 0);
+    if (counter) deac::stream_keys(1407513600ULL + r.cfg.seed, d.key_crossover, d.key_jde);
     // contraction tile: a power-of-two number of members times timeslices
     // filling the CTA's 64 (two-sided) or 128 (one-sided) chain pairs, and a
     // staging chunk that keeps two stages within 96 KB of shared memory
@@ -629,6 +639,15 @@ int upload_run(deac_batch* b, RunHost& r) {
     }
     // host copies are no longer needed
     return DEAC_OK;
+}
+
+// Counter streams address draws by (generation, member, side, gene): every
+// position of a run must stay below 2^63.  Null when they fit, else why not.
+const char* counter_streams_unfit(const RunHost& r) {
+    const long double n = (long double)r.cfg.number_of_generations, p = (long double)r.P;
+    if (n * p * (long double)r.S * (long double)r.M >= 0x1p62L || n * p * (long double)deac::kJdeSpan >= 0x1p62L)
+        return "number_of_generations x population_size x genome is too large for counter streams";
+    return nullptr;
 }
 
 int refresh_status(deac_batch* b) {
@@ -811,6 +830,13 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau,
     }
     auto r = std::make_unique<RunHost>();
     r->cfg = *cfg;
+    r->P = cfg->population_size;
+    r->M = m;
+    r->S = cfg->bosonic ? 1 : 2;
+    if (b->streams == DEAC_STREAMS_COUNTER) {
+        const char* why = counter_streams_unfit(*r);
+        if (why) return fail(DEAC_E_INVALID, "%s", why);
+    }
     r->tau.assign(tau, tau + nt);
     r->isf.assign(isf, isf + nt);
     r->err.assign(err, err + nt);
@@ -821,6 +847,20 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau,
     r->S = cfg->bosonic ? 1 : 2;
     if (run_index) *run_index = (uint32_t)b->runs.size();
     b->runs.push_back(std::move(r));
+    return DEAC_OK;
+}
+
+int deac_batch_set_streams(deac_batch* b, int32_t layout) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    if (b->set_up) return fail(DEAC_E_STATE, "choose the stream layout before deac_batch_setup");
+    if (layout != DEAC_STREAMS_REFERENCE && layout != DEAC_STREAMS_COUNTER)
+        return fail(DEAC_E_INVALID, "unknown stream layout %d", layout);
+    if (layout == DEAC_STREAMS_COUNTER)
+        for (auto& r : b->runs) {
+            const char* why = counter_streams_unfit(*r);
+            if (why) return fail(DEAC_E_INVALID, "%s", why);
+        }
+    b->streams = layout;
     return DEAC_OK;
 }
 
@@ -845,7 +885,7 @@ int deac_batch_setup(deac_batch* b) {
         while (next < b->runs.size()) {
             pool.clear();
             for (unsigned t = 0; t < hw && next < b->runs.size(); ++t, ++next)
-                pool.emplace_back(prepare_run, std::ref(*b->runs[next]));
+                pool.emplace_back(prepare_run, std::ref(*b->runs[next]), b->streams);
             for (auto& th : pool) th.join();
         }
         // the kernel matrix of each distinct (model, T, tau and omega grid),
@@ -866,7 +906,7 @@ int deac_batch_setup(deac_batch* b) {
             for (auto& th : pool) th.join();
         }
     }
-    {
+    if (b->streams == DEAC_STREAMS_REFERENCE) {
         uint32_t bits = 1;
         for (auto& r : b->runs) bits = std::max(bits, jump_bits(r->n_states));
         const std::vector<uint64_t>& jp = jump_powers(bits);

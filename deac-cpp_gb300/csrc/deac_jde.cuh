@@ -6,6 +6,10 @@
 // RNG slots of member i (base = i * (1 + S*M), word-major table of n states):
 // base (CR of side 0, then the mutant indices), base+1 (F of side 0),
 // base+2 / base+3 (CR / F of side 1) -- deac_gpu.cu's per-member states.
+// With counter streams (kCounterStreams) the table holds one slot per member
+// whose first word counts the member's jDE steps; step n draws from the jDE
+// stream at the positions deac_rng.cuh lists, and the slot's other words are
+// unused.
 #pragma once
 
 #include <cstdint>
@@ -25,8 +29,17 @@ __device__ __forceinline__ uint64_t mod_p(uint64_t x, uint64_t P, uint64_t m) {
     return r;
 }
 
-// the jDE slots of member i (every load at once)
+// the jDE slots of member i (every load at once); with counter streams the
+// member's step count in st[0][0]
 __device__ __forceinline__ void jde_load(const RunDev& R, uint32_t i, uint64_t (&st)[4][4]) {
+    if (R.flags & kCounterStreams) {
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q)
+#pragma unroll
+            for (uint32_t w = 0; w < 4; ++w) st[q][w] = 0ull;
+        st[0][0] = R.rng[i];
+        return;
+    }
     const uint64_t base = (uint64_t)i * (1ull + (uint64_t)R.S * R.M);
     const uint64_t n = R.n_states;
     const uint64_t* rng = R.rng;
@@ -60,6 +73,37 @@ __device__ __forceinline__ void jde_draws(const RunDev& R, uint32_t i, uint64_t 
     };
     d.cr_new[1] = d.fw_new[1] = false;
     d.cr[1] = d.fw[1] = 0.0;
+    if (R.flags & kCounterStreams) {
+        // jDE step n of member i: fixed positions of the run's jDE stream
+        const uint64_t n = st[0][0];
+        const uint64_t pos0 = kJdeSpan * (n * P + i);
+        auto at = [&](uint64_t k) { return stream_draw(R.key_jde, pos0 + k) >> 11; };
+#pragma unroll
+        for (uint32_t s = 0; s < 2; ++s)
+            if (s < R.S) {
+                d.cr_new[s] = at(4 * s) < thr_cr;
+                d.cr[s] = d.cr_new[s] ? (double)at(4 * s + 1) * 0x1.0p-53 : 0.0;
+                d.fw_new[s] = at(4 * s + 2) < thr_f;
+                d.fw[s] = d.fw_new[s] ? (double)at(4 * s + 3) * 0x1.0p-52 : 0.0;  // 2 * draw
+            }
+        // rejection sampling from draw 8 on (an admissible index has
+        // probability >= 1/4 per draw for P >= 4: the span of 2^16 - 8 draws
+        // is never exhausted in practice; if it were, the first admissible
+        // index is taken so that the result stays defined)
+        const uint64_t pm = R.p_magic;
+        uint64_t k = kJdeMutantDraw0, r[3] = {i, i, i};
+#pragma unroll
+        for (uint32_t q = 0; q < 3; ++q) {
+            auto bad = [&](uint64_t v) { return v == i || (q > 0 && v == r[0]) || (q > 1 && v == r[1]); };
+            while (bad(r[q]) && k < kJdeSpan) r[q] = mod_p(stream_draw(R.key_jde, pos0 + k++), P, pm);
+            for (uint64_t v = 0; bad(r[q]); ++v) r[q] = v;
+        }
+        d.mut[0] = (uint32_t)r[0];
+        d.mut[1] = (uint32_t)r[1];
+        d.mut[2] = (uint32_t)r[2];
+        st[0][0] = n + 1;
+        return;
+    }
     side(0, st[0], st[1]);
     if (R.S == 2) side(1, st[2], st[3]);
     // rejection sampling as in the reference; P >= 4 is enforced on the
@@ -109,11 +153,15 @@ __device__ __forceinline__ void jde_store(RunDev& R, uint32_t i, const uint64_t 
             R.cr[(uint64_t)S * P + s * P + i] = cr_new[s];
             R.fw[(uint64_t)S * P + s * P + i] = fw_new[s];
         }
+    if (R.flags & kCounterStreams) {
+        R.rng[i] = st[0][0];
+    } else {
 #pragma unroll
-    for (uint32_t q = 0; q < 4; ++q)
-        if (q < 2 * S)
+        for (uint32_t q = 0; q < 4; ++q)
+            if (q < 2 * S)
 #pragma unroll
-            for (uint32_t w = 0; w < 4; ++w) R.rng[w * n + base + q] = st[q][w];
+                for (uint32_t w = 0; w < 4; ++w) R.rng[w * n + base + q] = st[q][w];
+    }
     if (mutants)
         for (uint32_t q = 0; q < 3; ++q) R.mutants[3 * i + q] = mut[q];
 }

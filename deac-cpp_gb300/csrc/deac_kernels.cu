@@ -146,6 +146,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     __shared__ double s_fw[2], s_sum[4];
     __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
+    __shared__ uint64_t s_step;
     __shared__ ChainScratch s_chain[2];
 
     const Work w = work[blockIdx.x];
@@ -184,8 +185,10 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
     const bool row_sums_here = normalize && (init_mode || !(R.flags & kDeferNorm));
     if (row_sums_here) weights(R.norm_pos, R.norm_neg, norm_p, norm_n);
 
+    const bool counter = (R.flags & kCounterStreams) != 0;
     if (!init_mode && threadIdx.x == 0) {
         double cr[2], fw[2];
+        if (counter) s_step = R.rng[i];  // this trial's jDE step
         jde_member(R, i, cr, fw, s_mut);
 #pragma unroll
         for (uint32_t s = 0; s < 2; ++s)
@@ -221,6 +224,9 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
         const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
         const bool keep_sign = (R.flags & kSignedWeights) != 0;
         const uint64_t n = R.n_states;
+        // counter streams: gene j of side s draws position cpos + s*M + j
+        const uint64_t cpos = counter ? (s_step * P + i) * SM : 0;
+        const uint64_t key_x = R.key_crossover;
         constexpr uint32_t kGeneChunk = 256;
         const uint32_t nchunks = (M + kGeneChunk - 1) / kGeneChunk;
 
@@ -244,10 +250,12 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
                     sd[h] = ee / len;
                     jj[h] = j0 + (ee - sd[h] * len);
                     const uint64_t slot = base + 1 + (uint64_t)sd[h] * M + jj[h];
-                    st[h][0] = R.rng[slot];
-                    st[h][1] = R.rng[n + slot];
-                    st[h][2] = R.rng[2 * n + slot];
-                    st[h][3] = R.rng[3 * n + slot];
+                    if (!counter) {
+                        st[h][0] = R.rng[slot];
+                        st[h][1] = R.rng[n + slot];
+                        st[h][2] = R.rng[2 * n + slot];
+                        st[h][3] = R.rng[3 * n + slot];
+                    }
                     const uint64_t off = (uint64_t)sd[h] * PM + jj[h];
                     a[h] = pa[off];
                     b[h] = pb[off];
@@ -257,8 +265,13 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
 #pragma unroll
                 for (int h = 0; h < H; ++h) {
                     if (!ok[h]) continue;
-                    const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
-                    store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
+                    bool mutate;
+                    if (counter) {
+                        mutate = (stream_draw(key_x, cpos + (uint64_t)sd[h] * M + jj[h]) >> 11) < s_thr[sd[h]];
+                    } else {
+                        mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < s_thr[sd[h]];
+                        store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
+                    }
                     double v = x[h];
                     if (mutate) {
                         v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
@@ -437,6 +450,7 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     __shared__ double s_fw[2];
     __shared__ uint64_t s_thr[2];
     __shared__ uint32_t s_mut[3];
+    __shared__ uint64_t s_step;
     __shared__ uint8_t s_cur[kTrialPartThreads];
     __shared__ int s_digit_max[kTrialPartThreads / 32];
     // Before the wait only the static run description is read, and the
@@ -452,7 +466,8 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     const uint64_t n = R.n_states;
     const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
     const uint64_t buf = (uint64_t)S * PM;
-    if (threadIdx.x < 4 * S)
+    const bool counter = (R.flags & kCounterStreams) != 0;
+    if (!counter && threadIdx.x < 4 * S)
         prefetch_l2(R.rng + (threadIdx.x / S) * n + base + 1 + (uint64_t)(threadIdx.x % S) * M + j0, len,
                     R.rng + 4 * n);
     grid_dependency_wait();
@@ -468,6 +483,8 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
         s_fw[threadIdx.x] = R.fw[(uint64_t)S * P + threadIdx.x * P + i];
     } else if (threadIdx.x >= 32 && threadIdx.x < 35) {
         s_mut[threadIdx.x - 32] = R.mutants[3 * i + threadIdx.x - 32];
+    } else if (counter && threadIdx.x == 64) {
+        s_step = R.rng[i] - 1;  // the jDE step this trial's CR / F and mutants come from
     }
     __syncthreads();
     const uint32_t r0 = s_mut[0], r1 = s_mut[1], r2 = s_mut[2];
@@ -486,8 +503,11 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     const bool keep_sign = (R.flags & kSignedWeights) != 0;
     bool mutated = false;
     constexpr uint32_t H = 4;  // genes in flight per thread (one pass of a 512-gene side)
+    const uint64_t key_x = R.key_crossover;
     for (uint32_t s = 0; s < S; ++s) {
         uint64_t* st0 = R.rng + base + 1 + (uint64_t)s * M + j0;
+        // counter streams: gene j0 + k of side s draws position cpos + k
+        const uint64_t cpos = counter ? ((s_step * P + i) * S + s) * (uint64_t)M + j0 : 0;
         const uint64_t off = (uint64_t)s * PM + j0;
         const double *qa = pa + off, *qb = pb + off, *qc = pc + off, *qx = px + off;
         double* qd = dst + off;
@@ -501,10 +521,12 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
             for (uint32_t h = 0; h < H; ++h) {
                 const uint32_t jj = j + h * blockDim.x;
                 const uint32_t k = jj < len ? jj : j;
-                st[h][0] = st0[k];
-                st[h][1] = st0[n + k];
-                st[h][2] = st0[2 * n + k];
-                st[h][3] = st0[3 * n + k];
+                if (!counter) {
+                    st[h][0] = st0[k];
+                    st[h][1] = st0[n + k];
+                    st[h][2] = st0[2 * n + k];
+                    st[h][3] = st0[3 * n + k];
+                }
                 a[h] = qa[k];
                 b[h] = qb[k];
                 c[h] = qc[k];
@@ -514,12 +536,17 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
             for (uint32_t h = 0; h < H; ++h) {
                 const uint32_t jj = j + h * blockDim.x;
                 if (jj >= len) continue;
-                const bool mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < thr;
-                uint64_t* so = st0 + jj;
-                so[0] = st[h][0];
-                so[n] = st[h][1];
-                so[2 * n] = st[h][2];
-                so[3 * n] = st[h][3];
+                bool mutate;
+                if (counter) {
+                    mutate = (stream_draw(key_x, cpos + jj) >> 11) < thr;
+                } else {
+                    mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < thr;
+                    uint64_t* so = st0 + jj;
+                    so[0] = st[h][0];
+                    so[n] = st[h][1];
+                    so[2 * n] = st[h][2];
+                    so[3 * n] = st[h][3];
+                }
                 double v = x[h];
                 if (mutate) {
                     v = fma(fw, b[h] - c[h], a[h]);

@@ -44,6 +44,7 @@ enum : uint32_t {
     kTrace = 1u << 6,
     kDeferNorm = 1u << 7,  // split engine: normalisation applied after the decisions
     kNonNegProducts = 1u << 8,  // every gene x kernel product is >= 0 (unsigned genes, K >= 0)
+    kCounterStreams = 1u << 9,  // draws from counter streams (deac_rng.cuh), not the per-gene state table
 };
 
 // Per-run descriptor, resident in device memory.
@@ -76,7 +77,9 @@ struct RunDev {
     double* pop;             // [2 buffers][S][P][M]
     uint8_t* cur;            // [P] buffer holding each member's parent
     uint64_t* rng;           // 4 words x n_states, word-major
-    uint64_t n_states;       // P * (1 + S*M)
+    uint64_t n_states;       // P * (1 + S*M); P with counter streams (a jDE step count per member)
+    uint64_t key_crossover;  // counter streams: the keys of the run's crossover and jDE streams
+    uint64_t key_jde;
     double* cr;              // [old|new][S][P]
     double* fw;              // [old|new][S][P]
     double* fit_old;         // [P]

@@ -11,6 +11,7 @@
 //   --allow_negative_spectral_weight             ALLOW_NEGATIVE_SPECTRAL_WEIGHT
 //   --device N                                   CUDA device
 //   --engine plain|split                         evaluation engine (same results)
+//   --streams reference|counter                  draw layout (reference: its PRNG bit for bit)
 #include <algorithm>
 #include <cerrno>
 #include <cmath>
@@ -74,6 +75,7 @@ const std::vector<Option>& options() {
         {"", "--allow_negative_spectral_weight", "Do not take the absolute value of mutant genes.", "false", true},
         {"", "--device", "CUDA device to run on.", "0", false},
         {"", "--engine", "Evaluation engine: plain (FP64 throughout) or split (tensor-core contraction with exact FP64 decisions; genome_size a multiple of 32, no moment terms).", "plain", false},
+        {"", "--streams", "Random draws: reference (the reference's per-gene generator states, its draws bit for bit) or counter (compact counter streams for large batches; both engines agree).", "reference", false},
     };
     return o;
 }
@@ -347,6 +349,10 @@ int main(int argc, char** argv) {
     const std::string engine_name = args.has("--engine") ? args.values.at("--engine") : "plain";
     if (engine_name != "plain" && engine_name != "split") fail_with_error("--engine must be plain or split");
     const int32_t engine = engine_name == "split" ? DEAC_ENGINE_SPLIT_BF16 : DEAC_ENGINE_PLAIN_FP64;
+    const std::string streams_name = args.has("--streams") ? args.values.at("--streams") : "reference";
+    if (streams_name != "reference" && streams_name != "counter")
+        fail_with_error("--streams must be reference or counter");
+    const int32_t streams = streams_name == "counter" ? DEAC_STREAMS_COUNTER : DEAC_STREAMS_REFERENCE;
 
     const fs::path save_directory(args.has("--save_directory") ? args.values.at("--save_directory") : "./deacresults");
     std::error_code ec;
@@ -380,6 +386,7 @@ int main(int argc, char** argv) {
 
     deac_batch* batch = nullptr;
     int rc = deac_batch_create(device, nullptr, engine, &batch);
+    if (rc == DEAC_OK) rc = deac_batch_set_streams(batch, streams);
     for (unsigned long k = 0; k < n_seeds && rc == DEAC_OK; ++k) {
         cfg.seed = seeds[k];
         rc = deac_batch_add_run(batch, &cfg, tau, isf, err, nt, frequency.data(), frequency.size(), nullptr);

@@ -81,6 +81,47 @@ struct Xoshiro {
     }
 };
 
+// ---- counter streams (the batched forms' compact draw layout)
+//
+// SplitMix64 (Steele, Lea and Flood, "Fast splittable pseudorandom number
+// generators", OOPSLA 2014) is a Weyl sequence key + n * gamma passed through
+// a bijective 64-bit mixer; its n-th output depends on n alone.  A run's
+// per-generation draws are outputs of two such streams at positions computed
+// from (generation, member, side, gene), so no per-gene state is stored or
+// streamed: the draws are reproducible for any launch shape, and the plain
+// and split engines draw the same values.  The mixer is the one of the
+// splitmix step above.
+DEAC_HD uint64_t splitmix_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// Output `pos` (0, 1, ...) of the SplitMix64 stream whose state starts at key.
+DEAC_HD uint64_t stream_draw(uint64_t key, uint64_t pos) {
+    return splitmix_mix(key + (pos + 1) * 0x9E3779B97F4A7C15ULL);
+}
+
+// The two keys of a run (crossover draws, jDE draws): the third and fourth
+// outputs of the splitmix sequence seeded with the run's seed, whose first
+// two seed the initial population's generator (Xoshiro::seeded).
+inline void stream_keys(uint64_t seed, uint64_t& key_crossover, uint64_t& key_jde) {
+    uint64_t x = seed;
+    Xoshiro::splitmix(x);
+    Xoshiro::splitmix(x);
+    key_crossover = Xoshiro::splitmix(x);
+    key_jde = Xoshiro::splitmix(x);
+}
+
+// Positions within the streams.  jDE step n of member i (the draws for the
+// trial of its n-th generation) reads the jDE stream at kJdeSpan * (n P + i)
+// + k: k = 4s (CR test of side s), 4s+1 (new CR), 4s+2 (F test), 4s+3 (new
+// F), and k = 8, 9, ... the mutant-index draws of the rejection sampling.
+// Crossover draw of gene j, side s in that trial: ((n P + i) S + s) M + j of
+// the crossover stream.
+constexpr uint64_t kJdeSpan = 1ull << 16;
+constexpr uint64_t kJdeMutantDraw0 = 8;
+
 // The jump as a linear map of the 256-bit state over GF(2): a 256 x 256
 // matrix stored as 256 columns of 4 words (column i = jump(e_i)).  J^k s,
 // the state k jumps on, is then a product of the matrices J^(2^b) of k's

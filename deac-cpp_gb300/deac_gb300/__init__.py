@@ -27,6 +27,7 @@ MODEL = {"standard": 0, "hyperbolic": 1, "normalization": 2}
 SPECTRA = {"spbsf": 0, "spfsf": 1, "bfull": 2, "ffull": 3, "bdsf": 4}
 ENGINE_PLAIN_FP64 = 0
 ENGINE_SPLIT_BF16 = 1
+STREAMS = {"reference": 0, "counter": 1}
 
 
 class DeacConfig(ctypes.Structure):
@@ -133,6 +134,7 @@ SIGNATURES = {
     "deac_batch_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                              ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]),
+    "deac_batch_set_streams": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "deac_batch_enable_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]),
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
@@ -185,13 +187,19 @@ def _ptr(a):
 class Batch:
     """A batch of independent DEAC runs on one GPU (deac_batch_*)."""
 
-    def __init__(self, device: int = 0, stream: int | None = None, engine: int = ENGINE_PLAIN_FP64):
+    def __init__(self, device: int = 0, stream: int | None = None, engine: int = ENGINE_PLAIN_FP64,
+                 streams: str = "reference"):
+        """``streams``: "reference" (the reference's per-gene PRNG table, its
+        draws bit for bit) or "counter" (the compact counter-stream layout of
+        the batched forms, deac_batch_set_streams)."""
         lib = load_library()
         h = ctypes.c_void_p()
         _check(lib.deac_batch_create(device, ctypes.c_void_p(stream or 0), engine, ctypes.byref(h)))
         self._h = h
         self._lib = lib
         self._runs = []
+        if streams != "reference":
+            _check(lib.deac_batch_set_streams(h, STREAMS[streams]))
 
     def close(self):
         if self._h:

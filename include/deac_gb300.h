@@ -71,6 +71,22 @@ extern "C" {
 #define DEAC_ENGINE_PLAIN_FP64 0
 #define DEAC_ENGINE_SPLIT_BF16 1
 
+/* Draw layouts of a batch (deac_batch_set_streams).
+ *  REFERENCE: the reference's per-gene xoshiro256+ state table (deac.cpp:
+ *             1114-1135): 2 S P (M+1) states of 32 bytes, each read and
+ *             written by every draw; bit-identical to the reference's draws
+ *             (the default).
+ *  COUNTER:   the batched forms' compact layout: every per-generation draw
+ *             is the SplitMix64 output at a position computed from
+ *             (generation, member, side, gene), keyed by the run's seed; one
+ *             8-byte jDE step count per member replaces the table.  Draws
+ *             are statistically equivalent (uniform, independent positions of
+ *             one stream) but not the reference's values; both engines draw
+ *             the same values, so PLAIN_FP64 and SPLIT_BF16 still agree bit
+ *             for bit.  The initial population is drawn as in REFERENCE. */
+#define DEAC_STREAMS_REFERENCE 0
+#define DEAC_STREAMS_COUNTER 1
+
 /* Everything the reference reads from its command line (deac.cpp:1926-2024)
  * plus the compile-time variant switches. */
 typedef struct deac_config {
@@ -199,6 +215,12 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out,
  * same results as a run never interrupted).  A block of another configuration,
  * or with counters out of range, is refused with DEAC_E_INVALID. */
 int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t bytes);
+
+/* Choose the draw layout (DEAC_STREAMS_*) of every run of the batch; before
+ * deac_batch_setup.  No counterpart in the reference, which keeps one state
+ * per gene (deac.cpp:1114-1135); the counter layout is what lets thousands
+ * of runs at M = 16384 fit on one GPU. */
+int deac_batch_set_streams(deac_batch* b, int32_t layout);
 
 /* Record, for run `run`, the trial fitness of every member at every
  * generation up to `max_generations` (a test aid; call before setup). */

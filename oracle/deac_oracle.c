@@ -189,6 +189,7 @@ typedef struct {
     double *cr_old[2], *cr_new[2], *w_old[2], *w_new[2];
     double *fit_old, *fit_new, *E, *slots;
     uint64_t *states;       /* GPU order: table of xoshiro states, 4 words each */
+    uint64_t key_crossover, key_jde; /* GPU order with counter streams */
     uint64_t rng[4];        /* host stream */
     uint64_t *mutant;       /* 3*P */
     unsigned char *mask[2]; /* [P][M] */
@@ -537,6 +538,69 @@ static double mutate(const oracle_t* o, double* const old, uint64_t j, const uin
     return o->c->allow_negative_weight ? v : fabs(v);
 }
 
+/* Counter streams (the engine's DEAC_STREAMS_COUNTER layout, which the
+ * reference does not have): output `pos` of the SplitMix64 stream whose state
+ * starts at `key` -- the (pos+1)-th splitmix64_next() from that state, in one
+ * step (the state after n steps is key + n * gamma). */
+uint64_t deac_oracle_stream_draw(uint64_t key, uint64_t pos) {
+    uint64_t x = key + pos * 0x9E3779B97F4A7C15ULL;
+    return splitmix64_next(&x);
+}
+
+/* A run's two stream keys: the third and fourth splitmix64 outputs of the
+ * seed whose first two seed the population's xoshiro256+ (rng.hpp:46-59). */
+void deac_oracle_stream_keys(uint64_t seed, uint64_t keys[2]) {
+    uint64_t x = seed;
+    splitmix64_next(&x);
+    splitmix64_next(&x);
+    keys[0] = splitmix64_next(&x);
+    keys[1] = splitmix64_next(&x);
+}
+
+#define JDE_SPAN (1ULL << 16)
+
+/* One generation's trial vectors in GPU order from counter streams: jDE step
+ * n = ii of member i reads the jDE stream at JDE_SPAN (n P + i) + k (k = 4s:
+ * CR test of side s, 4s+1 new CR, 4s+2 F test, 4s+3 new F, 8.. the mutant
+ * draws); gene j of side s its crossover draw at ((n P + i) S + s) M + j.
+ * Arithmetic as trials_gpu. */
+static void trials_gpu_counter(oracle_t* o, uint64_t ii) {
+    const uint64_t P = o->P, M = o->M, S = (uint64_t)o->S;
+    const deac_config* c = o->c;
+    for (uint64_t i = 0; i < P; i++) {
+        const uint64_t pos0 = JDE_SPAN * (ii * P + i);
+        for (uint64_t s = 0; s < S; s++) {
+            if (u01(deac_oracle_stream_draw(o->key_jde, pos0 + 4 * s)) < c->self_adapting_crossover_probability)
+                o->cr_new[s][i] = u01(deac_oracle_stream_draw(o->key_jde, pos0 + 4 * s + 1));
+            else
+                o->cr_new[s][i] = o->cr_old[s][i];
+            if (u01(deac_oracle_stream_draw(o->key_jde, pos0 + 4 * s + 2)) <
+                c->self_adapting_differential_weight_probability)
+                o->w_new[s][i] = 2.0 * u01(deac_oracle_stream_draw(o->key_jde, pos0 + 4 * s + 3));
+            else
+                o->w_new[s][i] = o->w_old[s][i];
+        }
+        uint64_t k = 8, *r = o->mutant + 3 * i;
+        r[0] = r[1] = r[2] = i;
+        while (r[0] == i) r[0] = deac_oracle_stream_draw(o->key_jde, pos0 + k++) % P;
+        while (r[1] == i || r[1] == r[0]) r[1] = deac_oracle_stream_draw(o->key_jde, pos0 + k++) % P;
+        while (r[2] == i || r[2] == r[0] || r[2] == r[1]) r[2] = deac_oracle_stream_draw(o->key_jde, pos0 + k++) % P;
+        for (uint64_t s = 0; s < S; s++)
+            for (uint64_t j = 0; j < M; j++)
+                o->mask[s][i * M + j] =
+                    u01(deac_oracle_stream_draw(o->key_crossover, ((ii * P + i) * S + s) * M + j)) < o->cr_new[s][i];
+    }
+    for (uint64_t s = 0; s < S; s++)
+        for (uint64_t i = 0; i < P; i++)
+            for (uint64_t j = 0; j < M; j++)
+                o->pop_new[s][i * M + j] = o->mask[s][i * M + j]
+                                               ? mutate(o, o->pop_old[s], j, o->mutant + 3 * i, o->w_new[s][i])
+                                               : o->pop_old[s][i * M + j];
+    if (o->S == 2)
+        for (uint64_t i = 0; i < P; i++) o->pop_new[1][i * M] = o->pop_new[0][i * M];
+    if (c->normalize) normalize_gpu(o, o->pop_new);
+}
+
 /* One generation's trial vectors in GPU order (deac.cpp:1168-1259). */
 static void trials_gpu(oracle_t* o) {
     const uint64_t P = o->P, M = o->M;
@@ -722,6 +786,10 @@ int deac_oracle_run(const deac_config* c, int32_t order, const double* tau, cons
                     double* population, double* fitness, double* trace, uint64_t trace_capacity) {
     oracle_t o;
     memset(&o, 0, sizeof o);
+    /* GPU order with counter streams: the GPU order's arithmetic, its
+     * per-generation draws from the streams */
+    const int counter = order == DEAC_ORACLE_GPU_ORDER_COUNTER;
+    if (counter) order = DEAC_ORACLE_GPU_ORDER;
     if (!c || Nt < 2 || M < 2 || c->population_size < 4 || c->number_of_generations < 2) return -1;
     if (c->zero_temperature && !c->bosonic) return -1;
     o.c = c;
@@ -790,7 +858,12 @@ int deac_oracle_run(const deac_config* c, int32_t order, const double* tau, cons
             o.w_old[s][i] = c->differential_weight;
         }
 
-    if (order == DEAC_ORACLE_GPU_ORDER) {
+    if (counter) {
+        uint64_t keys[2];
+        deac_oracle_stream_keys(1407513600ULL + c->seed, keys);
+        o.key_crossover = keys[0];
+        o.key_jde = keys[1];
+    } else if (order == DEAC_ORACLE_GPU_ORDER) {
         /* state k = jump^k(state after the initial draws); only the first
          * P + S*P*M of the S*P*(M+1) states of deac.cpp:1116-1126 are read */
         const uint64_t nstates = P + (uint64_t)S * P * M;
@@ -818,7 +891,8 @@ int deac_oracle_run(const deac_config* c, int32_t order, const double* tau, cons
         }
         if (minimum_fitness <= c->stop_minimum_fitness) break;
 
-        if (order == DEAC_ORACLE_GPU_ORDER) trials_gpu(&o);
+        if (counter) trials_gpu_counter(&o, ii);
+        else if (order == DEAC_ORACLE_GPU_ORDER) trials_gpu(&o);
         else trials_cpu(&o);
         for (uint64_t i = 0; i < P; i++) o.fit_new[i] = fitness_of(&o, i, o.pop_new, 0);
         if (trace && ii < trace_capacity) memcpy(trace + ii * P, o.fit_new, P * sizeof(double));

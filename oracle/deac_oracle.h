@@ -22,6 +22,9 @@ extern "C" {
  *       CPU-only formulas, so it can be compared with the reference CPU build. */
 #define DEAC_ORACLE_GPU_ORDER 0
 #define DEAC_ORACLE_CPU_ORDER 1
+/* GPU order with the engine's counter streams (DEAC_STREAMS_COUNTER) in place
+ * of the per-gene state table: the batched forms' draw layout. */
+#define DEAC_ORACLE_GPU_ORDER_COUNTER 2
 
 typedef struct deac_oracle_out {
     uint64_t generation;
@@ -64,6 +67,11 @@ int deac_oracle_kernel_matrix(const deac_config* cfg,
 void deac_oracle_rng_init(uint64_t seed, uint64_t state[4]);
 uint64_t deac_oracle_rng_next(uint64_t state[4]);
 void deac_oracle_rng_jump(uint64_t state[4]);
+
+/* Counter streams: output `pos` of the SplitMix64 stream whose state starts
+ * at key, and a run's two keys (crossover, jDE) from its seed. */
+uint64_t deac_oracle_stream_draw(uint64_t key, uint64_t pos);
+void deac_oracle_stream_keys(uint64_t seed, uint64_t keys[2]);
 
 #ifdef __cplusplus
 }

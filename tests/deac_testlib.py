@@ -25,7 +25,7 @@ REPO = Path(__file__).resolve().parents[1]
 ORACLE_SO = REPO / "oracle" / "_build" / "libdeac_oracle.so"
 REF_DIR = REPO / "oracle" / "_ref"
 
-GPU_ORDER, CPU_ORDER = 0, 1
+GPU_ORDER, CPU_ORDER, GPU_ORDER_COUNTER = 0, 1, 2
 
 PKG_DIR = REPO / "deac-cpp_gb300"
 if str(PKG_DIR) not in sys.path:
@@ -75,6 +75,9 @@ class Oracle:
         self.lib.deac_oracle_rng_next.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
         self.lib.deac_oracle_rng_init.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
         self.lib.deac_oracle_rng_jump.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+        self.lib.deac_oracle_stream_draw.restype = ctypes.c_uint64
+        self.lib.deac_oracle_stream_draw.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        self.lib.deac_oracle_stream_keys.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
 
     def run(self, cfg: DeacConfig, tau, isf, err, freq, order=GPU_ORDER, trace=0,
             state=False):
@@ -124,6 +127,14 @@ class Oracle:
                                                 len(freq), _ptr(kp), _ptr(kn))
         assert rc == 0
         return kp, kn
+
+    def stream_draw(self, key: int, pos: int) -> int:
+        return self.lib.deac_oracle_stream_draw(key, pos)
+
+    def stream_keys(self, seed: int):
+        k = (ctypes.c_uint64 * 2)()
+        self.lib.deac_oracle_stream_keys(seed, k)
+        return k[0], k[1]
 
     def rng_stream(self, seed: int, n: int, jumps: int = 0):
         s = (ctypes.c_uint64 * 4)()
