@@ -1,29 +1,38 @@
 #!/usr/bin/env python3
-"""Benchmark: DEAC generations/s summed over runs on GB300.
+"""Benchmark: DEAC generations/s summed over runs on GB300, batched
+split-precision engine against the plain FP64 engine on the same runs.
 
-Workload (the reference's production scale, BASELINE config 1): 8 runs,
-seeds 1-8, standard model, two-sided (--spectra_type bfull), T = 1.35,
-N_tau = 128 on [0, beta], M = 4096 on omega in [0, 512], P = 8, --normalize,
-stop fitness 1.0 (not reached in the timed generations).  Synthetic data by
-the benchmark recipe (deac_gb300.data.config1_data).
+Workload (the batching form, 1024 independent runs in one batch): seeds
+1-1024; from each run's seed its genome size M in {1024, 4096, 16384} on
+[0, 64], population P in {8, 32, 64}, temperature T in {0.5, 1.35, 3.0} and
+model in {standard, hyperbolic, normalization}; two-sided (bfull), N_tau =
+128 on [0, beta], the single-run data recipe at its temperature (0.7 N(5,1) +
+0.3 N(20,3), sigma = 1e-4 F, noise from the seed; deac_gb300.data
+.config3_runs), stop fitness 1.0.  Both engines draw from counter streams
+(the batched forms' compact draw layout, deac_batch_set_streams), so the
+split engine's every decision equals the plain engine's and the line
+records whether every run ended with identical chi^2, best member and
+spectrum.
 
-A step is G generations of every run of the batch.  The headline is the
-split-precision engine (contraction from exact BF16 digit slices on the
-tcgen05 tensor cores, every selection decision equal to FP64); the plain
-FP64 engine runs the same generations beside it, and the line records
-whether both ended with identical chi^2 and spectra.  Timing: W untimed
-warm-up steps, then K steps, each bracketed by CUDA events on the batch
-stream, with a 256 MB L2 flush before each step (outside the events); the K
-steps sit between a barrier + device synchronize on both sides; value is
-the max over ranks.  With --gpus N (torchrun), each rank runs its own 8
-seeds (weak scaling, no data-path collective).
+A step is G = 16 generations of every run (one captured graph block).
+Timing: W untimed warm-up steps, then K steps, each bracketed by CUDA events
+on the batch stream; the working set (18 GB) is far larger than L2, so no
+flush is needed between steps; the K steps sit between a barrier + device
+synchronize on both sides; value is the max over ranks.  With --gpus N
+(torchrun), each rank runs its own 1024 seeds (weak scaling, no data-path
+collective).
+
+Secondary keys: the single-run production scale (8 runs of N_tau = 128,
+M = 4096, P = 8, --normalize, reference streams) over an early window and
+over a long window of 100,000 generations, where the exact FP64 passes of a
+converging population weigh more.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
 --impl reference times the reference's own CPU implementation of the path
 (the CPU-order oracle, a restatement of the reference's CPU code path, since
 the reference sources are not on the GPU host) on the host cores, one
-process per run, on the same workload.
+process per run, on a sample of the same runs.
 """
 from __future__ import annotations
 
@@ -45,27 +54,46 @@ for p in (REPO / "deac-cpp_gb300", REPO / "tests"):
 
 METRIC = "generations/s summed over runs: batched split-precision vs plain FP64, same χ²"
 UNIT = "generations/s"
-RUNS_PER_GPU = 8
-P, M, NT, OMEGA_MAX, T = 8, 4096, 128, 512.0, 1.35
-GENS_PER_STEP = 32
-WORKLOAD = ("deac config 1: 8 runs (seeds 1-8), standard model, two-sided bfull, T=1.35, "
-            "N_tau=128, M=4096 on [0,512], P=8, --normalize; split-precision engine, plain FP64 engine beside it")
-DATA = "synthetic (benchmark recipe: 0.7 N(5,1) + 0.3 N(20,3), sigma = 1e-4 F, numpy default_rng(seed))"
-CPU_SAMPLE_GENERATIONS = 1000
+RUNS_PER_GPU = 1024
+NT = 128
+GENS_PER_STEP = 16
+WORKLOAD = ("deac batching form: 1024 ragged runs in one batch (seeds 1-1024; M in {1024, 4096, 16384} on [0,64], "
+            "P in {8, 32, 64}, T in {0.5, 1.35, 3.0}, model in {standard, hyperbolic, normalization}, each drawn "
+            "from the seed; two-sided bfull, N_tau=128), counter streams; split-precision engine, plain FP64 "
+            "engine on the same runs beside it")
+DATA = ("synthetic (benchmark recipe per run: 0.7 N(5,1) + 0.3 N(20,3) at the run's temperature, sigma = 1e-4 F, "
+        "numpy default_rng(seed))")
+# the single-run production scale, for the secondary keys
+P1, M1, OMEGA1, T1 = 8, 4096, 512.0, 1.35
+LONG_WINDOW = 100_000
 
 
-def run_configs(rank):
+def run_specs(rank, n_runs=RUNS_PER_GPU):
+    """(config, tau, isf, err, frequency) of the workload's runs on `rank`."""
+    import deac_gb300
+    from deac_gb300.data import config3_runs
+
+    out = []
+    for r in config3_runs(n_runs, first_seed=rank * RUNS_PER_GPU + 1):
+        cfg = deac_gb300.make_config(model=r["model"], temperature=r["temperature"], spectra_type="bfull",
+                                     population_size=r["population_size"], number_of_generations=1_600_000,
+                                     stop_minimum_fitness=1.0, seed=r["seed"])
+        out.append((cfg, r["tau"], r["isf"], r["err"], r["frequency"]))
+    return out
+
+
+def config1_specs(rank):
     import deac_gb300
     from deac_gb300.data import config1_data, uniform_grid
 
-    freq = uniform_grid(M, OMEGA_MAX)
+    freq = uniform_grid(M1, OMEGA1)
     out = []
-    for k in range(RUNS_PER_GPU):
-        seed = rank * RUNS_PER_GPU + k + 1
-        cfg = deac_gb300.make_config(temperature=T, spectra_type="bfull", population_size=P,
+    for k in range(8):
+        seed = rank * 8 + k + 1
+        cfg = deac_gb300.make_config(temperature=T1, spectra_type="bfull", population_size=P1,
                                      number_of_generations=1_600_000, normalize=True, stop_minimum_fitness=1.0,
                                      seed=seed)
-        tau, isf, err = config1_data(seed, T)
+        tau, isf, err = config1_data(seed, T1)
         out.append((cfg, tau, isf, err, freq))
     return out
 
@@ -159,20 +187,18 @@ def barrier(world, device):
 # ------------------------------------------------------------------ CPU side
 
 def _cpu_worker(args):
-    """One reconstruction of `gens` generations with the CPU-order oracle (the
-    reference's CPU path); returns (generations executed, seconds)."""
-    seed, gens = args
+    """Run `index` of the workload on `rank` for `gens` generations with the
+    CPU-order oracle (the reference's CPU code path); returns (generations
+    executed, seconds)."""
+    rank, index, gens = args
     sys.path.insert(0, str(REPO / "tests"))
     sys.path.insert(0, str(REPO / "deac-cpp_gb300"))
     from deac_testlib import CPU_ORDER, Oracle
-    import deac_gb300
-    from deac_gb300.data import config1_data, uniform_grid
-    cfg = deac_gb300.make_config(temperature=T, spectra_type="bfull", population_size=P,
-                                 number_of_generations=gens + 1, normalize=True, stop_minimum_fitness=-1.0,
-                                 seed=seed)
-    tau, isf, err = config1_data(seed, T)
+    cfg, tau, isf, err, freq = run_specs(rank, index + 1)[index]
+    cfg.number_of_generations = gens + 1
+    cfg.stop_minimum_fitness = -1.0
     t0 = time.perf_counter()
-    r = Oracle().run(cfg, tau, isf, err, uniform_grid(M, OMEGA_MAX), order=CPU_ORDER)
+    r = Oracle().run(cfg, tau, isf, err, freq, order=CPU_ORDER)
     return r["executed"], time.perf_counter() - t0
 
 
@@ -180,43 +206,54 @@ def ensure_oracle():
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "all"], check=True)
 
 
-def cpu_baseline():
-    """Bounded single-core sample of the reference CPU path on the workload."""
+CPU_SAMPLE_RUNS = 16      # the workload's first 16 runs (its mix of M, P, T and models)
+CPU_SAMPLE_GENERATIONS = 2
+
+
+def cpu_sample(rank, pool_size, gens=CPU_SAMPLE_GENERATIONS, rounds=1):
+    """Generations/s of the reference's CPU path on the workload's first
+    CPU_SAMPLE_RUNS runs, one process per run on `pool_size` host cores."""
+    import multiprocessing as mp
     ensure_oracle()
-    gens, secs = _cpu_worker((1, CPU_SAMPLE_GENERATIONS))
-    return {"value": gens / secs, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"seed 1 of the workload, {gens} generations, one core "
-                      f"(CPU-order oracle = the reference's CPU code path), {secs:.1f} s"}
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(pool_size) as pool:
+        t0 = time.perf_counter()
+        total = 0
+        for _ in range(rounds):
+            res = pool.map(_cpu_worker, [(rank, k, gens) for k in range(CPU_SAMPLE_RUNS)])
+            total += sum(g for g, _ in res)
+        dt = time.perf_counter() - t0
+    return total, dt
+
+
+def cpu_baseline(rank):
+    """Bounded sample of the reference CPU path on the workload (all host cores)."""
+    cores = min(CPU_SAMPLE_RUNS, os.cpu_count() or 1)
+    total, dt = cpu_sample(rank, cores)
+    return {"value": total / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the workload's first {CPU_SAMPLE_RUNS} runs x {CPU_SAMPLE_GENERATIONS} generations, one "
+                      f"process per run on {cores} host cores (CPU-order oracle = the reference's CPU code path, "
+                      f"including its set-up), {dt:.1f} s"}
 
 
 def reference_arm(args, world, rank):
     if rank != 0:
         return
-    import multiprocessing as mp
-    ensure_oracle()
-    gens = 48  # per run per step: ~0.6 s of CPU work per run
-    cores = min(RUNS_PER_GPU, os.cpu_count() or 1)
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
-            pool.map(_cpu_worker, [(s + 1, gens) for s in range(RUNS_PER_GPU)])
-        t0 = time.perf_counter()
-        total = 0
-        for _ in range(args.steps):
-            res = pool.map(_cpu_worker, [(s + 1, gens) for s in range(RUNS_PER_GPU)])
-            total += sum(g for g, _ in res)
-        dt = time.perf_counter() - t0
+    cores = min(CPU_SAMPLE_RUNS, os.cpu_count() or 1)
+    for _ in range(args.warmup):
+        cpu_sample(0, cores)
+    total, dt = cpu_sample(0, cores, rounds=args.steps)
     value = total / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": {"workload": WORKLOAD + " (reference CPU path)", "runs": RUNS_PER_GPU,
-                   "generations_per_run_per_step": gens, "processes": cores},
+        "config": {"workload": WORKLOAD + " (reference CPU path on a sample of the runs)", "runs": CPU_SAMPLE_RUNS,
+                   "generations_per_run_per_step": CPU_SAMPLE_GENERATIONS, "processes": cores},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{RUNS_PER_GPU} runs x {gens} generations per step, one process per run "
-                                   f"(CPU-order oracle: the reference's CPU code path restated; the reference "
-                                   f"sources are not present on the GPU host)"},
+                         "sample": f"the workload's first {CPU_SAMPLE_RUNS} runs x {CPU_SAMPLE_GENERATIONS} "
+                                   f"generations per step, one process per run (CPU-order oracle: the reference's "
+                                   f"CPU code path restated; the reference sources are not present on the GPU host)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -224,42 +261,42 @@ def reference_arm(args, world, rank):
 
 # ---------------------------------------------------------------- GPU side
 
-# Algorithmic work per launch of each kernel kind of the split engine
-# (deac_batch_kernel_time kinds), for the roofline of the dominant one.
-BYTES_PER_TRIAL_GENE = 4 * 8 + 2 * 32 + 8 + 7 * 2   # parent+3 donors, PRNG state in/out, gene out, 7 BF16 digits out
-BYTES_PER_NORM_GENE = 8 + 8                         # raw gene and its weight in
-KEPT_DIGIT_PAIRS = 28                               # digit pairs a+b <= 6 of seven 7-bit digits
+KEPT_DIGIT_PAIRS = 28   # digit pairs a+b <= 6 of seven 7-bit digits
+KERNEL_NAMES = {0: "trial_part_kernel", 1: "contract_kernel (exact pass)", 2: "norm_kernel",
+                3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
 
 
-def kernel_roofline(kind, launch_s, peaks, split_ctas):
-    S, rows = 2, RUNS_PER_GPU * P
-    genes = RUNS_PER_GPU * P * S * M
+def workload_sizes(configs):
+    rows = sum(c.population_size for c, *_ in configs)
+    genes = sum(c.population_size * 2 * len(f) for c, _, _, _, f in configs)  # S = 2 (two-sided)
+    # sum over runs of rows x N_tau x M x S: the contraction's products
+    products = sum(c.population_size * len(t) * len(f) * 2 for c, t, _, _, f in configs)
+    return rows, genes, products
+
+
+def kernel_roofline(kind, launch_s, peaks, configs):
+    """Algorithmic work per launch of kernel kind `kind` and the rate it
+    reached, against the measured peak of what bounds it."""
+    rows, genes, products = workload_sizes(configs)
     if kind == 0:
-        work, unit, bound, peak = genes * BYTES_PER_TRIAL_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
+        # counter streams: three donors and the parent in, the trial gene
+        # and its seven BF16 digits out
+        work, unit, bound, peak = genes * (4 * 8 + 8 + 7 * 2), "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "trial_part_kernel"
-    elif kind == 2:
-        # exact normalisation row sums: each trial's raw genes and the weights
-        work, unit, bound, peak = genes * BYTES_PER_NORM_GENE, "GB/s", "hbm", peaks["hbm_gbs"]
-        achieved = work / launch_s / 1e9
-        name = "norm_kernel"
     elif kind == 3:
-        work = 2.0 * rows * NT * M * S * KEPT_DIGIT_PAIRS
+        work = 2.0 * products * KEPT_DIGIT_PAIRS  # BF16 digit-pair MMA flops (the precision form's algorithm)
         unit, bound, peak = "TFLOP/s", "tensor", peaks["bf16_tflops"]
         achieved = work / launch_s / 1e12
-        name = "split_contract_kernel"
     elif kind == 4:
-        work = 16.0 * rows * NT * split_ctas + rows * NT * 16  # partial sums in, estimate + bound out
+        work = rows * NT * (16 + 16 + 8)  # partial sums in, estimate + bound out, data / errors in
         unit, bound, peak = "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
-        name = "split_combine_kernel+split_select_kernel"
-    else:  # kind 1
-        work = 2.0 * 2 * rows * NT * M  # FP64 FMA chains, were every trial re-evaluated
+    else:  # the exact pass, were every trial re-evaluated; norm_kernel does not run here
+        work = 2.0 * products
         unit, bound, peak = "TFLOP/s", "fp64", 1.196
         achieved = work / launch_s / 1e12
-        name = "contract_kernel (exact pass)"
     return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-            "kernel": name, "work_per_launch": work, "launch_us": launch_s * 1e6}
+            "kernel": KERNEL_NAMES[kind], "work_per_launch": work, "launch_us": launch_s * 1e6}
 
 
 def load_peaks():
@@ -270,18 +307,21 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def timed_engine(engine_kind, configs, args, local, stream, flush, world, sample_clocks):
-    """Set up a batch of the workload on `engine_kind`, run the warm-up steps,
-    then time K steps of G generations (events on the batch stream, L2
-    flushed before every step)."""
-    import torch
+def make_batch(engine_kind, configs, local, stream, streams):
     import deac_gb300
-
-    G = args.generations_per_step
-    batch = deac_gb300.Batch(engine=engine_kind, device=local, stream=stream.cuda_stream)
+    b = deac_gb300.Batch(engine=engine_kind, device=local, stream=stream.cuda_stream, streams=streams)
     for cfg, tau, isf, err, freq in configs:
-        batch.add_run(cfg, tau, isf, err, freq)
-    batch.setup()
+        b.add_run(cfg, tau, isf, err, freq)
+    b.setup()
+    return b
+
+
+def timed_engine(engine_kind, configs, args, local, stream, world, sample_clocks, G, streams, flush=None):
+    """Set up a batch on `engine_kind`, run the warm-up steps, then time K
+    steps of G generations (events on the batch stream)."""
+    import torch
+
+    batch = make_batch(engine_kind, configs, local, stream, streams)
     for _ in range(args.warmup):
         batch.launch(G)
     torch.cuda.synchronize()
@@ -293,8 +333,9 @@ def timed_engine(engine_kind, configs, args, local, stream, flush, world, sample
         clocks.__enter__()
     try:
         for e0, e1 in events:
-            with torch.cuda.stream(stream):
-                flush.zero_()
+            if flush is not None:
+                with torch.cuda.stream(stream):
+                    flush.zero_()
             e0.record(stream)
             batch.launch(G)
             e1.record(stream)
@@ -309,8 +350,8 @@ def timed_engine(engine_kind, configs, args, local, stream, flush, world, sample
 
 
 def same_results(a, b, runs):
-    """Both batches ran the same generations: identical minimum fitness (chi^2),
-    best member and best spectrum for every run."""
+    """Both batches ran the same generations: identical generation count,
+    minimum fitness (chi^2), best member and best spectrum for every run."""
     import numpy as np
     for r in range(runs):
         x, y = a.fetch(r), b.fetch(r)
@@ -321,6 +362,46 @@ def same_results(a, b, runs):
     return True
 
 
+def long_window(configs, local, stream, window):
+    """Summed generations/s of both engines over generations 0..window of the
+    production-scale runs (reference streams), and the split engine's
+    decision counts: the exact FP64 passes grow as the populations converge."""
+    import torch
+    import deac_gb300
+    out = {}
+    for name, kind in (("split", deac_gb300.ENGINE_SPLIT_BF16), ("plain", deac_gb300.ENGINE_PLAIN_FP64)):
+        b = make_batch(kind, configs, local, stream, "reference")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        b.launch(window)
+        e1.record(stream)
+        stream.synchronize()
+        done = b.sync()
+        ms = e0.elapsed_time(e1)
+        # a run that reached its stop executed its reported generations
+        executed = 0
+        for r in range(len(configs)):
+            res_r = b.result(r)
+            executed += res_r["generation"] if res_r["finished"] else window
+        res = {"value": executed / (ms / 1e3), "seconds": ms / 1e3, "runs_finished": done,
+               "generations_executed": executed}
+        if kind == deac_gb300.ENGINE_SPLIT_BF16:
+            c = [b.split_counts(r) for r in range(len(configs))]
+            res["decisions"] = {k: sum(x[k] for x in c) for k in c[0]}
+            tot = sum(res["decisions"].values())
+            res["exact_fraction"] = res["decisions"]["exact"] / tot if tot else 0.0
+        out[name] = (b, res)
+    same = same_results(out["split"][0], out["plain"][0], len(configs))
+    line = {"generations": window, "runs": len(configs),
+            "split": out["split"][1], "plain": out["plain"][1],
+            "split_over_plain": out["split"][1]["value"] / out["plain"][1]["value"],
+            "same_chi2_and_spectra": same}
+    for b, _ in out.values():
+        b.close()
+    return line
+
+
 def engine_arm(args, world, rank, local):
     import torch
     import deac_gb300
@@ -328,87 +409,95 @@ def engine_arm(args, world, rank, local):
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=device)
-    configs = run_configs(rank)
+    configs = run_specs(rank, args.runs)
     G = args.generations_per_step
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    n = len(configs)
 
     # the headline: the split-precision engine; beside it the plain FP64
     # engine on the same runs and the same generations
-    split, ms, clocks = timed_engine(deac_gb300.ENGINE_SPLIT_BF16, configs, args, local, stream, flush, world, True)
-    plain, ms_plain, _ = timed_engine(deac_gb300.ENGINE_PLAIN_FP64, configs, args, local, stream, flush, world,
-                                      False)
-    identical = same_results(split, plain, len(configs))
-    counts = [split.split_counts(r) for r in range(len(configs))]
+    split, ms, clocks = timed_engine(deac_gb300.ENGINE_SPLIT_BF16, configs, args, local, stream, world, True, G,
+                                     "counter")
+    counts = [split.split_counts(r) for r in range(n)]
+    # per-kernel device time (kernels launched one by one, bracketed by
+    # events on the batch stream), for the roofline of the dominant kernel
+    split.enable_timing(True)
+    split.launch(1)
+    kt = {k: split.kernel_time(k) for k in range(5)}
+    split.enable_timing(False)
+    plain, ms_plain, _ = timed_engine(deac_gb300.ENGINE_PLAIN_FP64, configs, args, local, stream, world, False, G,
+                                      "counter")
+    plain.launch(1)  # the generation the timing pass added to the split batch
+    plain.sync()
+    identical = same_results(split, plain, n)
     plain.close()
+    split.close()
     ms = barrier_max(ms, world, device)
     ms_plain = barrier_max(ms_plain, world, device)
-    gens_total = world * RUNS_PER_GPU * args.steps * G
+    gens_total = world * n * args.steps * G
     value = gens_total / (ms / 1e3)
     value_plain = gens_total / (ms_plain / 1e3)
 
-    # per-kernel device time (separate pass, kernels launched one by one and
-    # bracketed by events on the batch stream)
-    split.enable_timing(True)
-    split.launch(G)
-    kt = {k: split.kernel_time(k) for k in range(5)}
-    split.enable_timing(False)
-    split.close()
-    # CTAs of the split contraction: one tile (64 rows x 128 timeslices) whose
-    # M/32 chunks are spread over the SMs the normalisation row sums (one CTA
-    # per trial, beside it) leave free
-    chunks = M // 32
-    sms = torch.cuda.get_device_properties(device).multi_processor_count
-    free = sms - min(RUNS_PER_GPU * P, sms // 2)
-    per = -(-chunks // min(max(1, free), chunks))
-    split_ctas = -(-chunks // per)
-    per_gen_us = {k: ms_k / G * 1e3 for k, (ms_k, n) in kt.items() if n}
+    per_gen_us = {k: ms_k * 1e3 for k, (ms_k, cnt) in kt.items() if cnt}
     dominant = max(per_gen_us, key=per_gen_us.get)
     ms_d, n_d = kt[dominant]
     peaks = load_peaks()
-    roof = kernel_roofline(dominant, ms_d / n_d / 1e3, peaks, split_ctas)
+    roof = kernel_roofline(dominant, ms_d / n_d / 1e3, peaks, configs)
     roof["peak_source"] = peaks["source"] + (" burst figure" if roof["bound"] != "fp64" else
-                                             "; FP64: measured DFMA throughput (profiles/fp64_pipe_gb300.md)")
-    tpath = REPO / "profiles" / f"{roof['kernel'].split('+')[0].split(' ')[0]}_config1_traffic.json"
-    roof["traffic"] = json.loads(tpath.read_text()).get("bytes_per_launch") if tpath.exists() else None
-    names = {0: "trial_part_kernel", 1: "contract_kernel (exact pass)", 2: "norm_kernel",
-             3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
-    roof["per_generation_us"] = {names[k]: round(v, 2) for k, v in per_gen_us.items()}
+                                             "; FP64: measured DFMA throughput")
+    # DRAM bytes per launch are read from an ncu capture, not from this run
+    roof["traffic"] = None
+    roof["per_generation_us"] = {KERNEL_NAMES[k]: round(v, 1) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs
     # (host arrays) + setup (host build, H2D) + K steps of (G generations,
-    # then every run's best spectrum and minimum fitness read back)
+    # then every run's status read back), then every run's result fetched
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b2 = deac_gb300.Batch(engine=deac_gb300.ENGINE_SPLIT_BF16, device=local, stream=stream.cuda_stream)
-    h2d = 0
+    b2 = deac_gb300.Batch(engine=deac_gb300.ENGINE_SPLIT_BF16, device=local, stream=stream.cuda_stream,
+                          streams="counter")
     for cfg, tau, isf, err, freq in configs:
         b2.add_run(cfg, tau, isf, err, freq)
-        # isf and its errors, the normalisation weights of both sides, the
-        # initial parents, CR and F (the PRNG table and K's digit planes
-        # are formed on the device)
-        s = 2
-        h2d += 8 * (2 * NT + s * M + s * P * M + 4 * s * P)
-    h2d += 8 * 2 * NT * M  # the shared kernel matrix
     b2.setup()
-    d2h = 0
     for _ in range(args.steps):
         b2.launch(G)
-        for r in range(len(configs)):
-            out = b2.fetch(r)
-            d2h += 8 * (len(out["dsf"]) + P) + P
+        b2.sync()
+    for r in range(n):
+        b2.fetch(r)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    # every byte the engine copied (inputs, initial parents, kernel matrices,
+    # work lists, status reads, result snapshot), as it counted them
+    h2d, d2h = b2.transfer_bytes()
     b2.close()
     e2e_value = gens_total / barrier_max(e2e_s, world, device)
+
+    # secondary: the single-run production scale, 8 runs
+    c1 = config1_specs(rank)
+    early = {}
+    if not args.no_secondary:
+        import copy
+        a1 = copy.copy(args)
+        a1.steps, a1.warmup = 10, 3
+        s1, ms1, _ = timed_engine(deac_gb300.ENGINE_SPLIT_BF16, c1, a1, local, stream, world, False, 32, "reference")
+        p1, ms1p, _ = timed_engine(deac_gb300.ENGINE_PLAIN_FP64, c1, a1, local, stream, world, False, 32,
+                                   "reference")
+        early = {"generations": "32 x 10 after 96 warm-up", "split": 8 * 320 / (ms1 / 1e3),
+                 "plain": 8 * 320 / (ms1p / 1e3), "same_chi2_and_spectra": same_results(s1, p1, 8)}
+        early["split_over_plain"] = early["split"] / early["plain"]
+        s1.close()
+        p1.close()
+        longw = long_window(c1, local, stream, args.long_window)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 (FP64-identical results; contraction from exact bf16 digit slices)",
         "data": DATA,
-        "config": {"workload": WORKLOAD, "runs_per_gpu": RUNS_PER_GPU, "population_size": P, "genome_size": M,
-                   "number_of_timeslices": NT, "normalize": True, "generations_per_step": G,
-                   "engine": "split_bf16", "l2": "flushed before every timed step (256 MB write, untimed)"},
+        "config": {"workload": WORKLOAD if n == RUNS_PER_GPU else f"the first {n} runs of: " + WORKLOAD,
+                   "runs_per_gpu": n, "number_of_timeslices": NT,
+                   "population_rows": sum(c.population_size for c, *_ in configs),
+                   "generations_per_step": G, "engine": "split_bf16", "streams": "counter",
+                   "l2": "no flush: the batch's working set (18 GB) is far larger than L2"},
         "plain_fp64": {"value": value_plain, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
                        "split_over_plain": value / value_plain,
                        "same_chi2_and_spectra": identical},
@@ -417,14 +506,19 @@ def engine_arm(args, world, rank, local):
                             "by_exact_fp64": sum(c["exact"] for c in counts)},
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
-                "d2h_bytes_per_step": d2h // args.steps},
-        # per generation: trial parts, normalisation row sums, tensor
-        # contraction, combine, selection, the exact pass
-        "gpu_launches": 6 * G * args.steps,
+                "d2h_bytes_per_step": d2h // args.steps,
+                "includes": "batch creation, set-up from host arrays, K steps with a status read each, "
+                            "every run's result fetched at the end"},
+        # per generation: trial parts, tensor contraction, combine, selection,
+        # the exact pass
+        "gpu_launches": 5 * G * args.steps,
         "clocks": clocks,
     }
+    if early:
+        line["config1_early_window"] = early
+        line["config1_long_window"] = longw
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -432,11 +526,15 @@ def engine_arm(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--generations-per-step", type=int, default=GENS_PER_STEP)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the single-run production-scale keys")
+    ap.add_argument("--long-window", type=int, default=LONG_WINDOW)
+    ap.add_argument("--runs", type=int, default=RUNS_PER_GPU,
+                    help="the workload's first RUNS runs (smaller cases for profiling; the line is for 1024)")
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU only: rank 0 measures, the other ranks exit without work

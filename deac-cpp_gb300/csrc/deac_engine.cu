@@ -196,9 +196,30 @@ struct deac_batch {
     size_t part_smem_bytes = 0;
     double kernel_ms[5] = {};
     uint64_t kernel_launches[5] = {};
+    // bytes copied between host and device by this batch's calls
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
 };
 
 namespace {
+
+// cudaMemcpy / cudaMemcpyAsync that count the bytes crossing the bus
+cudaError_t copy(deac_batch* b, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    const cudaError_t e = cudaMemcpy(dst, src, bytes, kind);
+    if (e == cudaSuccess) {
+        if (kind == cudaMemcpyHostToDevice) b->h2d_bytes += bytes;
+        if (kind == cudaMemcpyDeviceToHost) b->d2h_bytes += bytes;
+    }
+    return e;
+}
+cudaError_t copy_async(deac_batch* b, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
+                       cudaStream_t s) {
+    const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, s);
+    if (e == cudaSuccess) {
+        if (kind == cudaMemcpyHostToDevice) b->h2d_bytes += bytes;
+        if (kind == cudaMemcpyDeviceToHost) b->d2h_bytes += bytes;
+    }
+    return e;
+}
 
 // A launch that may start while the previous kernel on the stream is still
 // running (`early`: programmatic stream serialisation); the kernel's first
@@ -318,16 +339,16 @@ int finalize_split(deac_batch* b) {
         b->snap_bytes = n * sizeof(deac::RunDev) + (size_t)off[n] * 8 + ((size_t)off[n] + 7) / 8 * 8 +
                         (size_t)b->gene_off[n] * 8;
         CUDA_TRY(cudaMalloc(&b->d_fit_off, off.size() * 4));
-        CUDA_TRY(cudaMemcpy(b->d_fit_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_fit_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_gene_off, b->gene_off.size() * 8));
-        CUDA_TRY(cudaMemcpy(b->d_gene_off, b->gene_off.data(), b->gene_off.size() * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_gene_off, b->gene_off.data(), b->gene_off.size() * 8, cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_snap, b->snap_bytes));
         CUDA_TRY(cudaMallocHost(&b->h_snap, b->snap_bytes));
     }
     deac::snapshot_kernel<<<(unsigned)n, 128, 0, b->stream>>>(b->d_runs, (uint32_t)n, b->d_fit_off, b->d_gene_off,
                                                               b->d_snap);
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaMemcpyAsync(b->h_snap, b->d_snap, b->snap_bytes, cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(copy_async(b, b->h_snap, b->d_snap, b->snap_bytes, cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->snap.resize(n);
     b->snap_fit.resize(n);
@@ -425,10 +446,10 @@ int upload_run(deac_batch* b, RunHost& r) {
     if (it == b->kcache.end()) {
         KernelMatrix km;
         CUDA_TRY(cudaMalloc(&km.k_pos, Nt * M * sizeof(double)));
-        CUDA_TRY(cudaMemcpy(km.k_pos, m.k_pos.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, km.k_pos, m.k_pos.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
         if (S == 2) {
             CUDA_TRY(cudaMalloc(&km.k_neg, Nt * M * sizeof(double)));
-            CUDA_TRY(cudaMemcpy(km.k_neg, m.k_neg.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
+            CUDA_TRY(copy(b, km.k_neg, m.k_neg.data(), Nt * M * sizeof(double), cudaMemcpyHostToDevice));
         }
         km.nonneg = true;
         for (double v : m.k_pos) km.nonneg = km.nonneg && v >= 0.0;
@@ -489,13 +510,13 @@ int upload_run(deac_batch* b, RunHost& r) {
     for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
     put(o_fw, crfw);
     const bool counter = b->streams == DEAC_STREAMS_COUNTER;
-    if (counter) {
-        // the members' jDE step counts start at zero (in the image)
-        CUDA_TRY(cudaMemcpy(base, image.data(), a.size, cudaMemcpyHostToDevice));
-    } else {
-        CUDA_TRY(cudaMemcpy(base, image.data(), o_rng, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(base + o_cr, image.data() + o_cr, a.size - o_cr, cudaMemcpyHostToDevice));
-    }
+    // zeros are written on the device; only the inputs, the initial parents
+    // (buffer 0) and the initial CR / F cross the bus
+    CUDA_TRY(cudaMemsetAsync(base, 0, a.size, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(copy(b, base, image.data(), o_pop + (uint64_t)S * P * M * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, base + o_cr, image.data() + o_cr, (uint64_t)S * P * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, base + o_fw, image.data() + o_fw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice));
     if (!counter) {
         const uint32_t bits = jump_bits(r.n_states);
         // on the batch's stream: the host's set-up goes on meanwhile (the
@@ -618,8 +639,8 @@ int upload_run(deac_batch* b, RunHost& r) {
                 ie[t] = 1.0 / r.err[t];
                 ief[t] = float_up(ie[t]);
             }
-            CUDA_TRY(cudaMemcpy(sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
-            CUDA_TRY(cudaMemcpy(sb + o_ief, ief.data(), Nt * 4, cudaMemcpyHostToDevice));
+            CUDA_TRY(copy(b, sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
+            CUDA_TRY(copy(b, sb + o_ief, ief.data(), Nt * 4, cudaMemcpyHostToDevice));
             x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
             x.inv_err_up = reinterpret_cast<const float*>(sb + o_ief);
             x.inv_nt = 1.0 / (double)Nt;
@@ -652,7 +673,7 @@ const char* counter_streams_unfit(const RunHost& r) {
 
 int refresh_status(deac_batch* b) {
     b->status.resize(b->runs.size());
-    CUDA_TRY(cudaMemcpyAsync(b->status.data(), b->d_runs, b->runs.size() * sizeof(deac::RunDev),
+    CUDA_TRY(copy_async(b, b->status.data(), b->d_runs, b->runs.size() * sizeof(deac::RunDev),
                              cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     return DEAC_OK;
@@ -739,7 +760,7 @@ int make_group_planes(deac_batch* b) {
         if (rc) return rc;
     }
     CUDA_TRY(cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)));
-    CUDA_TRY(cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
     return DEAC_OK;
 }
 
@@ -911,7 +932,7 @@ int deac_batch_setup(deac_batch* b) {
         for (auto& r : b->runs) bits = std::max(bits, jump_bits(r->n_states));
         const std::vector<uint64_t>& jp = jump_powers(bits);
         CUDA_TRY(cudaMalloc(&b->d_jpow, (size_t)bits * 1024 * 8));
-        CUDA_TRY(cudaMemcpy(b->d_jpow, jp.data(), (size_t)bits * 1024 * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_jpow, jp.data(), (size_t)bits * 1024 * 8, cudaMemcpyHostToDevice));
     }
     uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
@@ -957,18 +978,18 @@ int deac_batch_setup(deac_batch* b) {
         b->n_part_ctas = (uint32_t)pw.size();
         b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
         CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::Work)));
-        CUDA_TRY(cudaMemcpy(b->d_part_work, pw.data(), pw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
         b->n_norm_ctas = (uint32_t)nw.size();
         if (!nw.empty()) {
             CUDA_TRY(raise_smem_limit(deac::norm_kernel, deac::kNormSmemBytes));
             CUDA_TRY(cudaMalloc(&b->d_norm_work, nw.size() * sizeof(deac::Work)));
-            CUDA_TRY(cudaMemcpy(b->d_norm_work, nw.data(), nw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+            CUDA_TRY(copy(b, b->d_norm_work, nw.data(), nw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
         }
     }
     CUDA_TRY(cudaMalloc(&b->d_trial_work, tw.size() * sizeof(deac::Work)));
     CUDA_TRY(cudaMalloc(&b->d_contract_work, cw.size() * sizeof(deac::Work)));
-    CUDA_TRY(cudaMemcpy(b->d_trial_work, tw.data(), tw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(b->d_contract_work, cw.data(), cw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_trial_work, tw.data(), tw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_contract_work, cw.data(), cw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
         int rc = make_group_planes(b);
         if (rc) return rc;
@@ -976,14 +997,14 @@ int deac_batch_setup(deac_batch* b) {
     std::vector<deac::RunDev> descs;
     for (auto& r : b->runs) descs.push_back(r->dev);
     CUDA_TRY(cudaMalloc(&b->d_runs, descs.size() * sizeof(deac::RunDev)));
-    CUDA_TRY(cudaMemcpy(b->d_runs, descs.data(), descs.size() * sizeof(deac::RunDev), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_runs, descs.data(), descs.size() * sizeof(deac::RunDev), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&b->d_status, sizeof(int)));
     CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int)));
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
         std::vector<deac::SplitRun> xs;
         for (auto& r : b->runs) xs.push_back(r->split);
         CUDA_TRY(cudaMalloc(&b->d_split, xs.size() * sizeof(deac::SplitRun)));
-        CUDA_TRY(cudaMemcpy(b->d_split, xs.data(), xs.size() * sizeof(deac::SplitRun), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_split, xs.data(), xs.size() * sizeof(deac::SplitRun), cudaMemcpyHostToDevice));
         // output tiles: the members of all runs that share a kernel matrix,
         // 64 rows at a time, times 128 timeslices
         std::vector<deac::SplitRow> rows;
@@ -1032,13 +1053,13 @@ int deac_batch_setup(deac_batch* b) {
         b->n_tiles = (uint32_t)tiles.size();
         b->n_split_ctas = (uint32_t)work.size();
         CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
-        CUDA_TRY(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_split_work, work.size() * sizeof(deac::SplitWork)));
-        CUDA_TRY(cudaMemcpy(b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork),
+        CUDA_TRY(copy(b, b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork),
                             cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_partial, (uint64_t)blocks * deac::kPartialBlock * sizeof(float4)));
         CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
-        CUDA_TRY(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
         CUDA_TRY(raise_smem_limit(deac::split_contract_kernel, deac::split_smem_bytes(2)));
     }
     CUDA_TRY(cudaDeviceSynchronize());
@@ -1062,10 +1083,19 @@ int deac_batch_launch(deac_batch* b, uint64_t generations) {
         CUDA_TRY(cudaGetLastError());
         return DEAC_OK;
     }
-    int rc = build_graph(b);
-    if (rc) return rc;
+    // whole blocks as the captured graph, the remainder launched directly
+    const uint64_t blocks = generations / kGraphBlock, rest = generations % kGraphBlock;
+    if (blocks) {
+        int rc = build_graph(b);
+        if (rc) return rc;
+    }
     b->snapped = false;
-    for (uint64_t g = 0; g < generations; g += kGraphBlock) CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+    for (uint64_t g = 0; g < blocks; ++g) CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+    for (uint64_t g = 0; g < rest; ++g) {
+        int rc = launch_generation(b, b->stream, 0);
+        if (rc) return rc;
+    }
+    CUDA_TRY(cudaGetLastError());
     return DEAC_OK;
 }
 
@@ -1075,7 +1105,7 @@ int deac_batch_sync(deac_batch* b, uint32_t* runs_finished) {
     CUDA_TRY(cudaGetLastError());
     if (b->d_status) {
         int st = 0;
-        CUDA_TRY(cudaMemcpy(&st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
+        CUDA_TRY(copy(b, &st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
         if (st) return fail(DEAC_E_CUDA, "a tensor-core wait gave up (status %d)", st);
     }
     int rc = refresh_status(b);
@@ -1114,22 +1144,22 @@ static int gather(deac_batch* b, uint32_t run, std::vector<double>& pop, std::ve
     RunHost& r = *b->runs[run];
     int rc = finalize_split(b);
     if (rc) return rc;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     const uint64_t P = r.P, M = r.M, S = r.S;
     std::vector<uint8_t> cur(P);
     std::vector<double> both(2 * S * P * M);
     fit.assign(P, 0.0);
-    CUDA_TRY(cudaMemcpy(cur.data(), st.cur, P, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(both.data(), st.pop, both.size() * 8, cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(fit.data(), st.fit_old, P * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, cur.data(), st.cur, P, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, both.data(), st.pop, both.size() * 8, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, fit.data(), st.fit_old, P * 8, cudaMemcpyDeviceToHost));
     pop.assign(S * P * M, 0.0);
     for (uint64_t s = 0; s < S; ++s)
         for (uint64_t i = 0; i < P; ++i)
             std::memcpy(&pop[(s * P + i) * M], &both[((uint64_t)cur[i] * S * P + s * P + i) * M], M * 8);
     if (crfw) {
         crfw->assign(4 * S * P, 0.0);
-        CUDA_TRY(cudaMemcpy(crfw->data(), st.cr, S * P * 8, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(crfw->data() + 2 * S * P, st.fw, S * P * 8, cudaMemcpyDeviceToHost));
+        CUDA_TRY(copy(b, crfw->data(), st.cr, S * P * 8, cudaMemcpyDeviceToHost));
+        CUDA_TRY(copy(b, crfw->data() + 2 * S * P, st.fw, S * P * 8, cudaMemcpyDeviceToHost));
     }
     return DEAC_OK;
 }
@@ -1201,7 +1231,7 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
         const uint64_t N = r.cfg.number_of_generations, n = res.stats_length;
         std::vector<double> stats(3 * n);
         for (int k = 0; k < 3; ++k)
-            if (n) CUDA_TRY(cudaMemcpy(&stats[k * n], st.stats + k * N, n * 8, cudaMemcpyDeviceToHost));
+            if (n) CUDA_TRY(copy(b, &stats[k * n], st.stats + k * N, n * 8, cudaMemcpyDeviceToHost));
         if (st.done && st.generation == N - 2) {
             // last entry from the host, with the sequential mean
             // (deac.cpp:1677-1685)
@@ -1286,7 +1316,7 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
                                        (unsigned long long)capacity, (unsigned long long)*bytes);
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     deac::RunDev st;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     CheckpointHeader h{};
     std::memcpy(h.magic, "DEACCKP2", 8);
     h.P = st.P;
@@ -1301,7 +1331,7 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
     h.flags = st.flags;
     h.inputs = input_hash(r);
     std::memcpy(out, &h, sizeof h);
-    CUDA_TRY(cudaMemcpy(static_cast<char*>(out) + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, static_cast<char*>(out) + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
     return DEAC_OK;
 }
 
@@ -1329,13 +1359,13 @@ int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t byt
     for (uint64_t i = 0; i < d.P; ++i)
         if ((uint8_t)body[cur_off + i] > 1) return fail(DEAC_E_INVALID, "checkpoint parent selector out of range");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
-    CUDA_TRY(cudaMemcpy(r.arena + off, body, state, cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, r.arena + off, body, state, cudaMemcpyHostToDevice));
     deac::RunDev st;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     st.ii = h.ii;
     st.generation = h.generation;
     st.done = h.done;
-    CUDA_TRY(cudaMemcpy(b->d_runs + run, &st, sizeof st, cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_runs + run, &st, sizeof st, cudaMemcpyHostToDevice));
     b->snapped = false;
     return refresh_status(b);
 }
@@ -1346,9 +1376,9 @@ int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness, u
     if (!b->set_up || !r.trace_cap) return fail(DEAC_E_STATE, "no trace recorded");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     deac::RunDev st;
-    CUDA_TRY(cudaMemcpy(&st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     const uint64_t rows = std::min(std::min(st.ii, r.trace_cap), capacity);
-    if (rows) CUDA_TRY(cudaMemcpy(trial_fitness, st.trace, rows * r.P * 8, cudaMemcpyDeviceToHost));
+    if (rows) CUDA_TRY(copy(b, trial_fitness, st.trace, rows * r.P * 8, cudaMemcpyDeviceToHost));
     return DEAC_OK;
 }
 
@@ -1356,7 +1386,14 @@ int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]) {
     if (!b || run >= b->runs.size() || !counts) return fail(DEAC_E_INVALID, "bad argument");
     if (b->engine != DEAC_ENGINE_SPLIT_BF16 || !b->set_up) return fail(DEAC_E_STATE, "not a set-up split batch");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
-    CUDA_TRY(cudaMemcpy(counts, b->runs[run]->split.counts, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(copy(b, counts, b->runs[run]->split.counts, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return DEAC_OK;
+}
+
+int deac_batch_transfer_bytes(const deac_batch* b, uint64_t* host_to_device, uint64_t* device_to_host) {
+    if (!b) return fail(DEAC_E_INVALID, "null batch");
+    if (host_to_device) *host_to_device = b->h2d_bytes;
+    if (device_to_host) *device_to_host = b->d2h_bytes;
     return DEAC_OK;
 }
 

@@ -138,6 +138,8 @@ SIGNATURES = {
     "deac_batch_enable_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]),
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "deac_batch_transfer_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                                 ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_split_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -251,6 +253,12 @@ class Batch:
         n = ctypes.c_uint64()
         _check(self._lib.deac_batch_kernel_time(self._h, kind, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def transfer_bytes(self):
+        """(host -> device, device -> host) bytes this batch has copied."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib.deac_batch_transfer_bytes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def split_counts(self, run: int) -> dict:
         c = (ctypes.c_uint64 * 3)()

@@ -168,9 +168,10 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg,
  * fitness (deac.cpp:829-976).  Synchronous. */
 int deac_batch_setup(deac_batch* b);
 
-/* Enqueue up to `generations` generations of every unfinished run on the
- * batch stream and return without waiting.  Runs that reach their stop
- * fitness or their generation limit stop on the device. */
+/* Enqueue `generations` generations of every unfinished run on the batch
+ * stream and return without waiting (whole blocks of 16 as a captured CUDA
+ * graph, the rest launched directly).  Runs that reach their stop fitness or
+ * their generation limit stop on the device. */
 int deac_batch_launch(deac_batch* b, uint64_t generations);
 
 /* Wait for the stream, then report how many runs have finished. */
@@ -235,6 +236,11 @@ int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness,
  * counts[0] equal to their parent (no gene changed), counts[1] settled by the
  * tensor-core estimate's interval, counts[2] settled by the exact FP64 value. */
 int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]);
+
+/* Bytes this batch has copied host -> device and device -> host so far
+ * (set-up uploads, status reads, result and state fetches).  No counterpart
+ * in the reference. */
+int deac_batch_transfer_bytes(const deac_batch* b, uint64_t* host_to_device, uint64_t* device_to_host);
 
 /* Device time of the kernels launched since timing was enabled, per kernel
  * kind, measured with CUDA events on the batch stream (ms): 0 trial kernel,
