@@ -540,7 +540,8 @@ int upload_run(deac_batch* b, RunHost& r) {
               (m.use_negative_first_moment ? deac::kNegativeFirstMoment : 0) |
               (r.cfg.allow_negative_weight ? deac::kSignedWeights : 0) |
               (r.cfg.track_stats ? deac::kTrackStats : 0) | (r.trace_cap ? deac::kTrace : 0) |
-              (counter ? deac::kCounterStreams : 0);
+              (counter ? deac::kCounterStreams : 0) |
+              (m.use_first_moment && r.cfg.first_moment_formula == DEAC_FIRST_MOMENT_CPU ? deac::kFirstMomentCpu : 0);
     if (counter) deac::stream_keys(1407513600ULL + r.cfg.seed, d.key_crossover, d.key_jde);
     // contraction tile: a power-of-two number of members times timeslices
     // filling the CTA's 64 (two-sided) or 128 (one-sided) chain pairs, and a

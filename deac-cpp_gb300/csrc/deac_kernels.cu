@@ -823,7 +823,12 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
                 const double term = (R.negfirst_target - mom) / R.negfirst_error;
                 fit = fma(term, term, fit);
             }
-            if (R.flags & kFirstMoment) {
+            if (R.flags & kFirstMomentCpu) {
+                // the CPU build's term (deac.cpp:969): a rounded square, a
+                // rounded quotient and a rounded sum
+                const double d = R.moments[2 * m] - R.first_target;
+                fit = fit + (d * d) / R.first_target;
+            } else if (R.flags & kFirstMoment) {
                 const double term = (R.first_target - R.moments[2 * m]) / 1.0;
                 fit = fma(term, term, fit);
             }

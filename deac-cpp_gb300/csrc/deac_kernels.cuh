@@ -45,6 +45,7 @@ enum : uint32_t {
     kDeferNorm = 1u << 7,  // split engine: normalisation applied after the decisions
     kNonNegProducts = 1u << 8,  // every gene x kernel product is >= 0 (unsigned genes, K >= 0)
     kCounterStreams = 1u << 9,  // draws from counter streams (deac_rng.cuh), not the per-gene state table
+    kFirstMomentCpu = 1u << 10,  // the first-moment term of the reference's CPU build, (m_i - m)^2 / m
 };
 
 // Per-run descriptor, resident in device memory.

@@ -75,6 +75,7 @@ const std::vector<Option>& options() {
         {"", "--allow_negative_spectral_weight", "Do not take the absolute value of mutant genes.", "false", true},
         {"", "--device", "CUDA device to run on.", "0", false},
         {"", "--engine", "Evaluation engine: plain (FP64 throughout) or split (tensor-core contraction with exact FP64 decisions; genome_size a multiple of 32, no moment terms).", "plain", false},
+        {"", "--first_moment_formula", "First-moment fitness term: gpu ((m - m_i)/1.0)^2, the reference's GPU build, or cpu (m_i - m)^2/m, its CPU build.", "gpu", false},
         {"", "--streams", "Random draws: reference (the reference's per-gene generator states, its draws bit for bit) or counter (compact counter streams for large batches; both engines agree).", "reference", false},
     };
     return o;
@@ -349,6 +350,9 @@ int main(int argc, char** argv) {
     const std::string engine_name = args.has("--engine") ? args.values.at("--engine") : "plain";
     if (engine_name != "plain" && engine_name != "split") fail_with_error("--engine must be plain or split");
     const int32_t engine = engine_name == "split" ? DEAC_ENGINE_SPLIT_BF16 : DEAC_ENGINE_PLAIN_FP64;
+    const std::string fm_name = args.has("--first_moment_formula") ? args.values.at("--first_moment_formula") : "gpu";
+    if (fm_name != "gpu" && fm_name != "cpu") fail_with_error("--first_moment_formula must be gpu or cpu");
+    cfg.first_moment_formula = fm_name == "cpu" ? DEAC_FIRST_MOMENT_CPU : DEAC_FIRST_MOMENT_GPU;
     const std::string streams_name = args.has("--streams") ? args.values.at("--streams") : "reference";
     if (streams_name != "reference" && streams_name != "counter")
         fail_with_error("--streams must be reference or counter");
@@ -382,7 +386,8 @@ int main(int argc, char** argv) {
         cfg.use_negative_first_moment = 0;
         cfg.temperature = 0.0;
     }
-    if (cfg.first_moment >= 0.0) std::cout << "WARNING: setting first_moment_error to 1.0." << std::endl;
+    if (cfg.first_moment >= 0.0 && cfg.first_moment_formula == DEAC_FIRST_MOMENT_GPU)
+        std::cout << "WARNING: setting first_moment_error to 1.0." << std::endl;
 
     deac_batch* batch = nullptr;
     int rc = deac_batch_create(device, nullptr, engine, &batch);

@@ -41,6 +41,8 @@ std::string check_config(const deac_config& c) {
     if (!std::isfinite(c.third_moment)) return "third_moment must be finite";
     if (c.third_moment >= 0.0 && (!std::isfinite(c.third_moment_error) || c.third_moment_error <= 0.0))
         return "third_moment_error must be positive when third_moment is used";
+    if (c.first_moment_formula != DEAC_FIRST_MOMENT_GPU && c.first_moment_formula != DEAC_FIRST_MOMENT_CPU)
+        return "first_moment_formula must be gpu or cpu";
     return std::string();
 }
 

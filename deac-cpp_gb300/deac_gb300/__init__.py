@@ -28,6 +28,7 @@ SPECTRA = {"spbsf": 0, "spfsf": 1, "bfull": 2, "ffull": 3, "bdsf": 4}
 ENGINE_PLAIN_FP64 = 0
 ENGINE_SPLIT_BF16 = 1
 STREAMS = {"reference": 0, "counter": 1}
+FIRST_MOMENT_FORMULA = {"gpu": 0, "cpu": 1}
 
 
 class DeacConfig(ctypes.Structure):
@@ -56,6 +57,7 @@ class DeacConfig(ctypes.Structure):
         ("number_of_generations", ctypes.c_uint64),
         ("population_size", ctypes.c_uint64),
         ("seed", ctypes.c_uint64),
+        ("first_moment_formula", ctypes.c_int32),
     ]
 
 
@@ -101,6 +103,8 @@ def make_config(**kw) -> DeacConfig:
             v = MODEL[v]
         if k == "spectra_type" and isinstance(v, str):
             v = SPECTRA[v]
+        if k == "first_moment_formula" and isinstance(v, str):
+            v = FIRST_MOMENT_FORMULA[v]
         if isinstance(v, bool):
             v = int(v)
         if not hasattr(c, k):

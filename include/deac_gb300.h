@@ -87,6 +87,12 @@ extern "C" {
 #define DEAC_STREAMS_REFERENCE 0
 #define DEAC_STREAMS_COUNTER 1
 
+/* The first-moment term of the fitness differs between the reference's
+ * builds: the GPU build adds ((m - m_i) / 1.0)^2 (deac.cpp:623, 949;
+ * deac_gpu.cu:450-456), the CPU build (m_i - m)^2 / m (deac.cpp:969). */
+#define DEAC_FIRST_MOMENT_GPU 0
+#define DEAC_FIRST_MOMENT_CPU 1
+
 /* Everything the reference reads from its command line (deac.cpp:1926-2024)
  * plus the compile-time variant switches. */
 typedef struct deac_config {
@@ -112,6 +118,7 @@ typedef struct deac_config {
     uint64_t number_of_generations; /* -N */
     uint64_t population_size;       /* -P */
     uint64_t seed;                  /* --seed; the PRNG is seeded with 1407513600 + seed */
+    int32_t first_moment_formula;   /* DEAC_FIRST_MOMENT_GPU (default) or DEAC_FIRST_MOMENT_CPU */
 } deac_config;
 
 /* Result of one run, as the reference reports it (deac.cpp:1592, 1677-1685,

@@ -468,7 +468,12 @@ static double fitness_of(oracle_t* o, uint64_t i, double* pop[2], int setup) {
         fit = fma(term, term, fit);
     }
     if (o->use_fm) {
-        if (o->order == DEAC_ORACLE_GPU_ORDER) {
+        if (o->order == DEAC_ORACLE_GPU_ORDER && o->c->first_moment_formula == DEAC_FIRST_MOMENT_CPU) {
+            /* the CPU build's term on the GPU order's moment */
+            const double m = gemv_gpu(o, i, pop, o->fmp, o->fmn, 1.0);
+            const double d = m - o->c->first_moment;
+            fit = fit + (d * d) / o->c->first_moment; /* deac.cpp:969 */
+        } else if (o->order == DEAC_ORACLE_GPU_ORDER) {
             const double m = gemv_gpu(o, i, pop, o->fmp, o->fmn, 1.0);
             const double term = (o->c->first_moment - m) / 1.0; /* deac.cpp:623 */
             fit = fma(term, term, fit);

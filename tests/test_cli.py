@@ -132,6 +132,9 @@ def test_zero_temperature_two_sided_rejected(engine, tmp_path):
     (("--number_of_seeds", "0"), "number_of_seeds must be at least 1"),
     (("--number_of_seeds", "2", "--uuid", "run"), "uuid cannot be combined with number_of_seeds > 1"),
     (("--number_of_seeds", "2", "--average_file", "no-such-dir/avg.bin"), "average_file directory does not exist"),
+    (("--first_moment_formula", "mixed"), "--first_moment_formula must be gpu or cpu"),
+    (("--streams", "table"), "--streams must be reference or counter"),
+    (("--engine", "fast"), "--engine must be plain or split"),
 ])
 def test_seed_range_validation(engine, tmp_path, extra, msg):
     _fixture(tmp_path / "isf.bin")

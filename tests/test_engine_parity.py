@@ -38,6 +38,13 @@ CASES = {
                                dict(spectra_type="ffull", first_moment=2.0, third_moment=50.0,
                                     third_moment_error=2.0)),
     "bosonic-standard-negfirst": ("cfg0", 64, 64.0, 400, dict(bosonic=True, use_negative_first_moment=True)),
+    # the reference CPU build's first-moment term, (m_i - m)^2 / m (deac.cpp:969)
+    "first-moment-cpu-formula": ("cfg0", 64, 64.0, 400, dict(spectra_type="bfull", first_moment=2.0,
+                                                             first_moment_formula="cpu")),
+    "first-moment-cpu-formula-bosonic-normalize": ("cfg0", 64, 64.0, 400,
+                                                   dict(bosonic=True, normalize=True, first_moment=1.5,
+                                                        third_moment=40.0, third_moment_error=3.0,
+                                                        first_moment_formula="cpu")),
     "bosonic-hyperbolic-normalize": ("cfg0", 64, 64.0, 400, dict(bosonic=True, model="hyperbolic", normalize=True)),
     "bosonic-normalization": ("cfg0", 64, 64.0, 400, dict(bosonic=True, model="normalization")),
     "zero-temperature": ("cfg0", 64, 64.0, 400, dict(bosonic=True, zero_temperature=True)),
