@@ -742,16 +742,19 @@ int make_group_planes(deac_batch* b) {
                 rp->dev.xdig_plane = M * R;
                 row += rp->P;
             }
-        // dims: 8 genes, rows, units of 8 genes, planes; box: one chunk of
-        // one tile (128 timeslices resp. 64 trial rows) of every plane
+        // A unit's rows (8 genes = 16 bytes each) are consecutive in memory,
+        // so the innermost dimension is all rows of a unit, in 8-byte
+        // elements (two per row): dims rows*2, units of 8 genes, planes; box:
+        // one tile's rows (128 timeslices resp. 64 trial rows) of one chunk's
+        // units of every plane -- 2 KB resp. 1 KB contiguous per line
         auto make = [&](CUtensorMap* m, void* base, uint64_t rows, uint32_t box_rows) -> int {
-            const cuuint64_t dims[4] = {8, rows, units, planes};
-            const cuuint64_t strides[3] = {16, rows * 16, units * rows * 16};
-            const cuuint32_t box[4] = {8, box_rows, deac::kChunk / 8, (cuuint32_t)planes};
-            const cuuint32_t estr[4] = {1, 1, 1, 1};
-            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, base, dims, strides, box, estr,
+            const cuuint64_t dims[3] = {rows * 2, units, planes};
+            const cuuint64_t strides[2] = {rows * 16, units * rows * 16};
+            const cuuint32_t box[3] = {2 * box_rows, deac::kChunk / 8, (cuuint32_t)planes};
+            const cuuint32_t estr[3] = {1, 1, 1};
+            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, dims, strides, box, estr,
                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return fail(DEAC_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
             return DEAC_OK;
         };
@@ -1280,7 +1283,14 @@ struct CheckpointHeader {
     int32_t done;
     uint32_t flags;
     uint64_t inputs;  // input_hash of the run
+    int32_t kind;     // kCheckpointPlain or kCheckpointSplit
+    uint32_t reserved;
 };
+// A plain-engine block is taken at a generation boundary before the next
+// jDE step; a split-engine block after it, with the next generation's mutant
+// indices ([P][3] uint32) and the run's decision counts (3 uint64) appended.
+constexpr int32_t kCheckpointPlain = 0, kCheckpointSplit = 1;
+uint64_t split_extra_bytes(const RunHost& r) { return r.P * 3 * sizeof(uint32_t) + 3 * sizeof(uint64_t); }
 
 uint64_t state_offset(const RunHost& r) { return (uint64_t)(reinterpret_cast<char*>(r.dev.pop) - r.arena); }
 
@@ -1308,13 +1318,18 @@ uint64_t input_hash(const RunHost& r) {
 int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capacity, uint64_t* bytes) {
     if (!b || run >= b->runs.size() || !bytes) return fail(DEAC_E_INVALID, "bad argument");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
-    if (b->engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "checkpoints are taken of the plain engine");
     RunHost& r = *b->runs[run];
+    const bool split = b->engine == DEAC_ENGINE_SPLIT_BF16;
     const uint64_t off = state_offset(r), state = r.arena_bytes - off;
-    *bytes = sizeof(CheckpointHeader) + state;
+    *bytes = sizeof(CheckpointHeader) + state + (split ? split_extra_bytes(r) : 0);
     if (!out) return DEAC_OK;
     if (capacity < *bytes) return fail(DEAC_E_INVALID, "checkpoint buffer too small (%llu < %llu bytes)",
                                        (unsigned long long)capacity, (unsigned long long)*bytes);
+    if (split) {
+        // every parent's fitness exact (the checkpoint holds no intervals)
+        int rc = finalize_split(b);
+        if (rc) return rc;
+    }
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     deac::RunDev st;
     CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
@@ -1329,29 +1344,43 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
     h.ii = st.ii;
     h.generation = st.generation;
     h.done = st.done;
-    h.flags = st.flags;
+    h.flags = st.flags & ~(deac::kDeferNorm | deac::kNonNegProducts);  // engine-specific flags
     h.inputs = input_hash(r);
-    std::memcpy(out, &h, sizeof h);
-    CUDA_TRY(copy(b, static_cast<char*>(out) + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
+    h.kind = split ? kCheckpointSplit : kCheckpointPlain;
+    char* dst = static_cast<char*>(out);
+    std::memcpy(dst, &h, sizeof h);
+    CUDA_TRY(copy(b, dst + sizeof h, r.arena + off, state, cudaMemcpyDeviceToHost));
+    if (split) {
+        char* extra = dst + sizeof h + state;
+        CUDA_TRY(copy(b, extra, r.dev.mutants, r.P * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        CUDA_TRY(copy(b, extra + r.P * 3 * sizeof(uint32_t), r.split.counts, 3 * sizeof(uint64_t),
+                      cudaMemcpyDeviceToHost));
+    }
     return DEAC_OK;
 }
 
 int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t bytes) {
     if (!b || run >= b->runs.size() || !in) return fail(DEAC_E_INVALID, "bad argument");
     if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
-    if (b->engine != DEAC_ENGINE_PLAIN_FP64) return fail(DEAC_E_INVALID, "checkpoints are restored into the plain engine");
     RunHost& r = *b->runs[run];
+    const bool split = b->engine == DEAC_ENGINE_SPLIT_BF16;
     const uint64_t off = state_offset(r), state = r.arena_bytes - off;
     CheckpointHeader h;
     if (bytes < sizeof h) return fail(DEAC_E_INVALID, "checkpoint too short");
     std::memcpy(&h, in, sizeof h);
     const deac::RunDev& d = r.dev;
     if (std::memcmp(h.magic, "DEACCKP2", 8) != 0) return fail(DEAC_E_INVALID, "not a checkpoint");
-    if (h.P != d.P || h.M != d.M || h.Nt != d.Nt || h.S != d.S || h.N != d.N || h.flags != d.flags ||
-        h.state_bytes != state || bytes != sizeof h + state)
+    if (h.kind != kCheckpointPlain && h.kind != kCheckpointSplit) return fail(DEAC_E_INVALID, "not a checkpoint");
+    const uint64_t want = sizeof h + state + (h.kind == kCheckpointSplit ? split_extra_bytes(r) : 0);
+    const uint32_t flags = d.flags & ~(deac::kDeferNorm | deac::kNonNegProducts);
+    if (h.P != d.P || h.M != d.M || h.Nt != d.Nt || h.S != d.S || h.N != d.N || h.flags != flags ||
+        h.state_bytes != state || bytes != want)
         return fail(DEAC_E_INVALID, "checkpoint of a different configuration");
     if (h.inputs != input_hash(r))
         return fail(DEAC_E_INVALID, "checkpoint of a run with other inputs (seed, temperature, model, data or grid)");
+    if (h.kind == kCheckpointSplit && !split)
+        return fail(DEAC_E_INVALID,
+                    "a split-engine checkpoint (its next jDE step already drawn) continues only in the split engine");
     // the values the kernels index with must lie in range
     if (h.ii > h.N || h.generation > h.N || (h.done != 0 && h.done != 1))
         return fail(DEAC_E_INVALID, "checkpoint counters out of range");
@@ -1359,6 +1388,11 @@ int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t byt
     const uint64_t cur_off = (uint64_t)(reinterpret_cast<char*>(d.cur) - r.arena) - off;
     for (uint64_t i = 0; i < d.P; ++i)
         if ((uint8_t)body[cur_off + i] > 1) return fail(DEAC_E_INVALID, "checkpoint parent selector out of range");
+    if (h.kind == kCheckpointSplit) {
+        const uint32_t* mut = reinterpret_cast<const uint32_t*>(body + state);
+        for (uint64_t k = 0; k < 3 * d.P; ++k)
+            if (mut[k] >= d.P) return fail(DEAC_E_INVALID, "checkpoint mutant index out of range");
+    }
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(copy(b, r.arena + off, body, state, cudaMemcpyHostToDevice));
     deac::RunDev st;
@@ -1366,7 +1400,36 @@ int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t byt
     st.ii = h.ii;
     st.generation = h.generation;
     st.done = h.done;
+    st.ticket = 0;
     CUDA_TRY(copy(b, b->d_runs + run, &st, sizeof st, cudaMemcpyHostToDevice));
+    if (split) {
+        // the split state of a generation boundary: exact parents (their
+        // intervals are points), no trial sliced or pending, the selection
+        // tallies cleared
+        const uint64_t P = r.P;
+        const double* fit = reinterpret_cast<const double*>(body + ((reinterpret_cast<char*>(d.fit_old) - r.arena) - off));
+        CUDA_TRY(copy(b, r.split.f_lo, fit, P * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, r.split.f_hi, fit, P * 8, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemset(r.split.changed, 0, P));
+        CUDA_TRY(cudaMemset(r.split.recheck, 0, P));
+        CUDA_TRY(cudaMemset(r.split.xexp_max, 0x80, P * 4));
+        CUDA_TRY(copy(b, b->d_split + run, &r.split, sizeof r.split, cudaMemcpyHostToDevice));
+        if (h.kind == kCheckpointSplit) {
+            CUDA_TRY(copy(b, d.mutants, body + state, P * 3 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(copy(b, r.split.counts, body + state + P * 3 * sizeof(uint32_t), 3 * sizeof(uint64_t),
+                          cudaMemcpyHostToDevice));
+        } else {
+            CUDA_TRY(cudaMemset(r.split.counts, 0, 3 * sizeof(uint64_t)));
+            // a plain block stops before the next jDE step: draw it for this
+            // run's members (its slice of the trial work list), as after set-up
+            uint64_t first = 0;
+            for (uint32_t k = 0; k < run; ++k) first += b->runs[k]->P;
+            deac::jde_kernel<<<(unsigned)((P + 127) / 128), 128, 0, b->stream>>>(
+                b->d_runs, static_cast<const deac::Work*>(b->d_trial_work) + first, (uint32_t)P);
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaStreamSynchronize(b->stream));
+        }
+    }
     b->snapped = false;
     return refresh_status(b);
 }

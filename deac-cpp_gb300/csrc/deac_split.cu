@@ -77,14 +77,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
                  : "r"(taddr));
 }
 
-// one 4-D tiled TMA load into shared memory, completing on `bar` (tensor map
-// in global memory, coordinates innermost first)
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+// one 3-D tiled TMA load into shared memory, completing on `bar` (tensor map
+// in global memory, coordinates innermost first; the innermost one, in
+// 8-byte elements, is even: a 16-byte multiple)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             uint64_t* bar) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-        "%5}], [%6];\n" ::"r"(smem_u32(dst)),
-        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -223,12 +224,14 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     for (uint32_t e = tid; e < (kTauTile + kRowTile) * 16; e += blockDim.x)
         reinterpret_cast<uint16_t*>(sAb)[e] = 0;
 
-    // one thread loads a chunk's planes of both operands: two TMA boxes
-    // (timeslices beyond Nt and rows beyond the group read as zero)
+    // one thread loads a chunk's planes of both operands: two TMA boxes whose
+    // innermost extent is a unit's rows, 2 KB (K) and 1 KB (trials) of
+    // consecutive bytes (timeslices beyond Nt and rows beyond the group read
+    // as zero)
     const uint32_t a_bytes = (uint32_t)kDigits * S * a_tile, b_bytes = (uint32_t)kDigits * S * b_tile;
-    auto load_k = [&](uint32_t c) { tma_load_4d(sA, map_k, 0, (int)tau0, (int)(c * (kChunk / 8)), 0, &s_full); };
+    auto load_k = [&](uint32_t c) { tma_load_3d(sA, map_k, (int)(2 * tau0), (int)(c * (kChunk / 8)), 0, &s_full); };
     auto load_x = [&](uint32_t c) {
-        tma_load_4d(sB, map_x, 0, (int)tile.grow0, (int)(c * (kChunk / 8)), 0, &s_full);
+        tma_load_3d(sB, map_x, (int)(2 * tile.grow0), (int)(c * (kChunk / 8)), 0, &s_full);
     };
     auto stage = [&](uint32_t c) {
         mbar_expect_tx(&s_full, stage_bytes);

@@ -23,10 +23,12 @@
 // q = digit*S + side, then units of 8 genes, then rows, then the 8 genes
 // (16 bytes), i.e. element (q, row, gene j) at
 //     ((q * M/8 + j/8) * rows + row) * 8 + j%8.
-// One 4-D TMA box {8 genes, 128 or 64 rows, 4 units, 7S planes} then lands in
-// shared memory as [plane][unit][row][8]: the canonical K-major no-swizzle
-// operand layout with 16-byte rows, core matrices 8 rows apart (128 bytes)
-// and units one row-block apart.
+// A unit's rows are consecutive, so one 3-D TMA box {all rows of the tile x
+// 16 bytes (as 8-byte elements), 4 units, 7S planes} -- lines of 2 KB (128
+// timeslices) or 1 KB (64 trial rows) -- lands in shared memory as
+// [plane][unit][row][8]: the canonical K-major no-swizzle operand layout with
+// 16-byte rows, core matrices 8 rows apart (128 bytes) and units one
+// row-block apart.
 #pragma once
 
 #include <cuda.h>

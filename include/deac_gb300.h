@@ -208,20 +208,27 @@ int deac_batch_fetch_state(deac_batch* b, uint32_t run, double* population,
                            double* fitness, double* crossover_rates,
                            double* differential_weights);
 
-/* Checkpoint of run `run` (plain engine, after setup): the state the
- * reference's --save_state names (deac.cpp:2004-2007, declared there but
- * never written) -- the PRNG states, both parent buffers, fitness, crossover
- * rates and differential weights -- plus the generation counters, statistics
- * and trace, as one byte block.  With out == NULL only *bytes (its size) is
- * set; otherwise the block is written to out (capacity bytes at least). */
+/* Checkpoint of run `run` (after setup): the state the reference's
+ * --save_state names (deac.cpp:2004-2007, declared there but never written)
+ * -- the PRNG states, both parent buffers, fitness, crossover rates and
+ * differential weights -- plus the generation counters, statistics and
+ * trace, as one byte block.  A split-engine batch first makes every parent's
+ * fitness exact and also saves the next generation's mutant indices and its
+ * decision counts (its next jDE step is drawn when a selection becomes
+ * final, a generation ahead of the plain engine).  With out == NULL only
+ * *bytes (its size) is set; otherwise the block is written to out (capacity
+ * bytes at least). */
 int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out,
                           uint64_t capacity, uint64_t* bytes);
 
 /* Resume from a checkpoint: after deac_batch_setup of a run added with the
  * same configuration and inputs, overwrite its state with the block, so that
  * the generations launched next continue the checkpointed run exactly (the
- * same results as a run never interrupted).  A block of another configuration,
- * or with counters out of range, is refused with DEAC_E_INVALID. */
+ * same results as a run never interrupted).  A plain-engine block restores
+ * into either engine (the split engine draws the next jDE step on restore);
+ * a split-engine block only into the split engine.  A block of another
+ * configuration or other inputs, or with counters out of range, is refused
+ * with DEAC_E_INVALID. */
 int deac_batch_restore(deac_batch* b, uint32_t run, const void* in, uint64_t bytes);
 
 /* Choose the draw layout (DEAC_STREAMS_*) of every run of the batch; before

@@ -93,3 +93,49 @@ def test_restore_refuses_a_run_with_other_inputs(engine, change):
         b.setup()
         with pytest.raises(engine.DeacError, match="other inputs"):
             b.restore(r, block)
+
+
+@pytest.mark.parametrize("engine_from,engine_to,after,stats", [
+    ("split", "split", 16, True), ("split", "split", 112, False), ("plain", "split", 48, False),
+    ("plain", "split", 112, True)])
+def test_split_engine_checkpoints(engine, engine_from, engine_to, after, stats):
+    """A split-engine run checkpointed and restored into a new split batch,
+    and a plain-engine checkpoint continued by the split engine, end exactly
+    as the plain run never interrupted (the split engine's decisions are the
+    FP64 ones).  Without statistics most decisions are the intervals'."""
+    kinds = {"plain": engine.ENGINE_PLAIN_FP64, "split": engine.ENGINE_SPLIT_BF16}
+    cfg = _cfg(engine, track_stats=stats)
+    data = _inputs()
+    with engine.Batch() as b:
+        r = b.add_run(cfg, *data)
+        b.run()
+        want, want_state = b.fetch(r), b.fetch_state(r)
+    with engine.Batch(engine=kinds[engine_from]) as b:
+        r = b.add_run(cfg, *data)
+        b.setup()
+        b.launch(after)
+        assert b.sync() == 0
+        block = b.checkpoint(r)
+    with engine.Batch(engine=kinds[engine_to]) as b:
+        r = b.add_run(cfg, *data)
+        b.setup()
+        b.restore(r, block)
+        b.run()
+        got, got_state = b.fetch(r), b.fetch_state(r)
+    _same(got, want)
+    for k in want_state:
+        assert np.array_equal(got_state[k], want_state[k]), k
+
+
+def test_split_checkpoint_refused_by_the_plain_engine(engine):
+    data = _inputs()
+    with engine.Batch(engine=engine.ENGINE_SPLIT_BF16) as b:
+        r = b.add_run(_cfg(engine), *data)
+        b.setup()
+        b.launch(16)
+        block = b.checkpoint(r)
+    with engine.Batch() as b:
+        r = b.add_run(_cfg(engine), *data)
+        b.setup()
+        with pytest.raises(engine.DeacError, match="continues only in the split engine"):
+            b.restore(r, block)
