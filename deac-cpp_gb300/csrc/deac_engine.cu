@@ -191,7 +191,7 @@ struct deac_batch {
     deac::Work* d_norm_work = nullptr;
     uint32_t n_norm_ctas = 0;
     // split engine: the raw trials in parts (trial_part_kernel)
-    deac::Work* d_part_work = nullptr;
+    deac::PartWork* d_part_work = nullptr;
     uint32_t n_part_ctas = 0;
     size_t part_smem_bytes = 0;
     double kernel_ms[5] = {};
@@ -272,8 +272,9 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
             b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
     } else {
-        launch(deac::trial_part_kernel, b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early,
-               b->d_runs, static_cast<const deac::Work*>(b->d_part_work));
+        launch(b->streams == DEAC_STREAMS_COUNTER ? deac::trial_part_counter_kernel : deac::trial_part_kernel,
+               b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early,
+               b->d_runs, static_cast<const deac::PartWork*>(b->d_part_work));
     }
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
@@ -970,19 +971,20 @@ int deac_batch_setup(deac_batch* b) {
             if (!(r.dev.flags & deac::kDeferNorm)) continue;
             for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
         }
-        std::vector<deac::Work> pw;
+        std::vector<deac::PartWork> pw;
         uint32_t smax = 1;
         for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
             const RunHost& r = *b->runs[ri];
             const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
             smax = std::max<uint32_t>(smax, (uint32_t)r.S);
             for (uint32_t i = 0; i < r.dev.P; ++i)
-                for (uint32_t q = 0; q < parts; ++q) pw.push_back({ri, (q << 20) | i});
+                for (uint32_t q = 0; q < parts; q += deac::kPartsPerCta)
+                    pw.push_back({ri, i, q, std::min<uint32_t>(deac::kPartsPerCta, parts - q)});
         }
         b->n_part_ctas = (uint32_t)pw.size();
         b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
-        CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::Work)));
-        CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::Work), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::PartWork)));
+        CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
         b->n_norm_ctas = (uint32_t)nw.size();
         if (!nw.empty()) {
             CUDA_TRY(raise_smem_limit(deac::norm_kernel, deac::kNormSmemBytes));

@@ -441,11 +441,17 @@ __global__ void __launch_bounds__(128) jde_kernel(RunDev* runs, const Work* work
 }
 
 // Split engine: the raw trial of member i, genes [part*kTrialPart, ...) of
-// both sides, per CTA -- the crossover draw and DE/rand/1 mutation of each
-// gene as in trial_kernel, then the part's BF16 digit slices.  Sets the
-// trial's `changed` flag when a gene mutated and raises its maximum chunk
-// exponent (split_select_kernel resets both after use).
-__global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev* runs, const Work* work) {
+// both sides for each part of the CTA's range -- the crossover draw and
+// DE/rand/1 mutation of each gene as in trial_kernel, then the part's BF16
+// digit slices.  The member's CR / F, mutants and the run's parent buffers
+// are read once for the range, and each part's rows are prefetched into L2
+// while the part before it is formed.  Sets the trial's `changed` flag when a
+// gene mutated and raises its maximum chunk exponent (split_select_kernel
+// resets both after use).
+// kCounter: the batch draws from counter streams (no per-gene states in
+// registers, so more CTAs fit on an SM); otherwise from the state table.
+template <bool kCounter>
+__device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* work) {
     extern __shared__ __align__(16) double part_s[];  // [S][len] the part's trial genes
     __shared__ double s_fw[2];
     __shared__ uint64_t s_thr[2];
@@ -454,22 +460,28 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     __shared__ uint8_t s_cur[kTrialPartThreads];
     __shared__ int s_digit_max[kTrialPartThreads / 32];
     // Before the wait only the static run description is read, and the
-    // part's PRNG states are prefetched into L2 meanwhile (a hint: their
-    // values are read after the wait).
-    const Work wk = work[blockIdx.x];
+    // first part's PRNG states are prefetched into L2 meanwhile (a hint:
+    // their values are read after the wait).
+    const PartWork wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
-    const uint32_t i = wk.index & 0xFFFFFu, part = wk.index >> 20;
+    const uint32_t i = wk.member;
     const uint32_t P = R.P, M = R.M, S = R.S;
     const uint64_t PM = (uint64_t)P * M;
-    const uint32_t j0 = part * kTrialPart;
-    const uint32_t len = M - j0 < kTrialPart ? M - j0 : kTrialPart;
     const uint64_t n = R.n_states;
     const uint64_t base = (uint64_t)i * (1ull + (uint64_t)S * M);
     const uint64_t buf = (uint64_t)S * PM;
-    const bool counter = (R.flags & kCounterStreams) != 0;
-    if (!counter && threadIdx.x < 4 * S)
-        prefetch_l2(R.rng + (threadIdx.x / S) * n + base + 1 + (uint64_t)(threadIdx.x % S) * M + j0, len,
-                    R.rng + 4 * n);
+    constexpr bool counter = kCounter;
+    auto part_len = [&](uint32_t part) {
+        const uint32_t j0 = part * kTrialPart;
+        return M - j0 < kTrialPart ? M - j0 : kTrialPart;
+    };
+    auto prefetch_states = [&](uint32_t part) {
+        if (!counter && threadIdx.x < 4 * S)
+            prefetch_l2(R.rng + (threadIdx.x / S) * n + base + 1 + (uint64_t)(threadIdx.x % S) * M +
+                            part * kTrialPart,
+                        part_len(part), R.rng + 4 * n);
+    };
+    prefetch_states(wk.part0);
     grid_dependency_wait();
     if (R.done) return;
     // one round trip: the member's CR / F and mutant indices, and the
@@ -495,79 +507,99 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev
     const double* pb = R.pop + cur(r1) * buf + (uint64_t)r1 * M;
     const double* pc = R.pop + cur(r2) * buf + (uint64_t)r2 * M;
     const double* px = R.pop + (uint64_t)parent_buf * buf + (uint64_t)i * M;
-    if (S == 2 && threadIdx.x < 4) {
-        // the second side's rows, read after the first side's pass
-        const double* rows[4] = {pa, pb, pc, px};
-        prefetch_l2(rows[threadIdx.x] + PM + j0, len, R.pop + 2 * buf);
-    }
     const bool keep_sign = (R.flags & kSignedWeights) != 0;
+    const uint64_t key_x = R.key_crossover;
+    const double* rows[4] = {pa, pb, pc, px};
     bool mutated = false;
     constexpr uint32_t H = 4;  // genes in flight per thread (one pass of a 512-gene side)
-    const uint64_t key_x = R.key_crossover;
-    for (uint32_t s = 0; s < S; ++s) {
-        uint64_t* st0 = R.rng + base + 1 + (uint64_t)s * M + j0;
-        // counter streams: gene j0 + k of side s draws position cpos + k
-        const uint64_t cpos = counter ? ((s_step * P + i) * S + s) * (uint64_t)M + j0 : 0;
-        const uint64_t off = (uint64_t)s * PM + j0;
-        const double *qa = pa + off, *qb = pb + off, *qc = pc + off, *qx = px + off;
-        double* qd = dst + off;
-        double* qs = part_s + s * len;
-        const uint64_t thr = s_thr[s];
-        const double fw = s_fw[s];
-        for (uint32_t j = threadIdx.x; j < len; j += H * blockDim.x) {
-            uint64_t st[H][4];
-            double a[H], b[H], c[H], x[H];
+    for (uint32_t part = wk.part0; part < wk.part0 + wk.nparts; ++part) {
+        const uint32_t j0 = part * kTrialPart;
+        const uint32_t len = part_len(part);
+        // into L2 while this part is formed: this part's second side, and
+        // both sides of the next part (and its PRNG states)
+        if (threadIdx.x < 4 * S) {
+            const uint32_t q = threadIdx.x & 3u, sd = threadIdx.x >> 2;
+            if (sd == 1) prefetch_l2(rows[q] + PM + j0, len, R.pop + 2 * buf);
+            if (part + 1 < wk.part0 + wk.nparts)
+                prefetch_l2(rows[q] + (uint64_t)sd * PM + j0 + kTrialPart, part_len(part + 1), R.pop + 2 * buf);
+        }
+        if (part + 1 < wk.part0 + wk.nparts) prefetch_states(part + 1);
+        for (uint32_t s = 0; s < S; ++s) {
+            uint64_t* st0 = R.rng + base + 1 + (uint64_t)s * M + j0;
+            // counter streams: gene j0 + k of side s draws position cpos + k
+            const uint64_t cpos = counter ? ((s_step * P + i) * S + s) * (uint64_t)M + j0 : 0;
+            const uint64_t off = (uint64_t)s * PM + j0;
+            const double *qa = pa + off, *qb = pb + off, *qc = pc + off, *qx = px + off;
+            double* qd = dst + off;
+            double* qs = part_s + s * len;
+            const uint64_t thr = s_thr[s];
+            const double fw = s_fw[s];
+            for (uint32_t j = threadIdx.x; j < len; j += H * blockDim.x) {
+                uint64_t st[H][4];
+                double a[H], b[H], c[H], x[H];
 #pragma unroll
-            for (uint32_t h = 0; h < H; ++h) {
-                const uint32_t jj = j + h * blockDim.x;
-                const uint32_t k = jj < len ? jj : j;
-                if (!counter) {
-                    st[h][0] = st0[k];
-                    st[h][1] = st0[n + k];
-                    st[h][2] = st0[2 * n + k];
-                    st[h][3] = st0[3 * n + k];
+                for (uint32_t h = 0; h < H; ++h) {
+                    const uint32_t jj = j + h * blockDim.x;
+                    const uint32_t k = jj < len ? jj : j;
+                    if (!counter) {
+                        st[h][0] = st0[k];
+                        st[h][1] = st0[n + k];
+                        st[h][2] = st0[2 * n + k];
+                        st[h][3] = st0[3 * n + k];
+                    }
+                    a[h] = qa[k];
+                    b[h] = qb[k];
+                    c[h] = qc[k];
+                    x[h] = qx[k];
                 }
-                a[h] = qa[k];
-                b[h] = qb[k];
-                c[h] = qc[k];
-                x[h] = qx[k];
-            }
 #pragma unroll
-            for (uint32_t h = 0; h < H; ++h) {
-                const uint32_t jj = j + h * blockDim.x;
-                if (jj >= len) continue;
-                bool mutate;
-                if (counter) {
-                    mutate = (stream_draw(key_x, cpos + jj) >> 11) < thr;
-                } else {
-                    mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < thr;
-                    uint64_t* so = st0 + jj;
-                    so[0] = st[h][0];
-                    so[n] = st[h][1];
-                    so[2 * n] = st[h][2];
-                    so[3 * n] = st[h][3];
+                for (uint32_t h = 0; h < H; ++h) {
+                    const uint32_t jj = j + h * blockDim.x;
+                    if (jj >= len) continue;
+                    bool mutate;
+                    if (counter) {
+                        mutate = (stream_draw(key_x, cpos + jj) >> 11) < thr;
+                    } else {
+                        mutate = (xoshiro_next(st[h][0], st[h][1], st[h][2], st[h][3]) >> 11) < thr;
+                        uint64_t* so = st0 + jj;
+                        so[0] = st[h][0];
+                        so[n] = st[h][1];
+                        so[2 * n] = st[h][2];
+                        so[3 * n] = st[h][3];
+                    }
+                    double v = x[h];
+                    if (mutate) {
+                        v = fma(fw, b[h] - c[h], a[h]);
+                        if (!keep_sign)
+                            v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
+                        mutated = true;
+                    }
+                    qd[jj] = v;
+                    qs[part_slot(jj, s)] = v;
                 }
-                double v = x[h];
-                if (mutate) {
-                    v = fma(fw, b[h] - c[h], a[h]);
-                    if (!keep_sign) v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
-                    mutated = true;
-                }
-                qd[jj] = v;
-                qs[part_slot(jj, s)] = v;
             }
         }
-    }
-    __syncthreads();
-    if (S == 2 && j0 == 0 && threadIdx.x == 0) {
-        // gpu_match_population_zero (deac_gpu.cu:541-549)
-        dst[PM] = part_s[part_slot(0, 0)];
-        part_s[len + part_slot(0, 1)] = part_s[part_slot(0, 0)];
+        __syncthreads();
+        if (S == 2 && j0 == 0 && threadIdx.x == 0) {
+            // gpu_match_population_zero (deac_gpu.cu:541-549)
+            dst[PM] = part_s[part_slot(0, 0)];
+            part_s[len + part_slot(0, 1)] = part_s[part_slot(0, 0)];
+        }
+        __syncthreads();
+        // (ends with a barrier after its last read of part_s)
+        digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * 8 + (uint64_t)(j0 >> 3) * R.xdig_unit,
+                       R.xdig_plane, R.xdig_unit, R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk,
+                       R.xexp_max + i, s_digit_max);
     }
     if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;
-    digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * 8 + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_plane,
-                   R.xdig_unit,
-                   R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk, R.xexp_max + i, s_digit_max);
+}
+
+__global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_kernel(RunDev* runs, const PartWork* work) {
+    trial_part_body<false>(runs, work);
+}
+__global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_counter_kernel(RunDev* runs,
+                                                                                  const PartWork* work) {
+    trial_part_body<true>(runs, work);
 }
 
 // ---------------------------------------------------------------- norm

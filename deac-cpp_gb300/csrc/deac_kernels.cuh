@@ -213,11 +213,18 @@ __global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow
                                  uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S);
 // split engine: jDE of every member (one thread each) after the initial
 // population; each generation's raw trials in parts of kTrialPart genes per
-// side (work index = part << 20 | member), each with its BF16 digit slices
+// side, each with its BF16 digit slices, up to kPartsPerCta consecutive
+// parts of one member per CTA
 constexpr uint32_t kTrialPart = 512;
+constexpr uint32_t kPartsPerCta = 4;
 constexpr int kTrialPartThreads = 128;
+struct PartWork {
+    uint32_t run, member, part0, nparts;
+};
 __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
-__global__ void trial_part_kernel(RunDev* runs, const Work* work);
+__global__ void trial_part_kernel(RunDev* runs, const PartWork* work);
+// the same for batches that draw from counter streams
+__global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
 // split engine, kDeferNorm runs: the exact normalisation row sums of one raw
 // trial per CTA (both sides), the reciprocal norm and the final `changed`
 // flag

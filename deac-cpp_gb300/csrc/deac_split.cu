@@ -238,26 +238,30 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         load_k(c);
         load_x(c);
     };
-    // chunk exponents and the bound operands 2^(e - max) at k = 0
-    auto scales = [&](uint32_t c) {
+    // chunk exponents and the bound operands 2^(e - max) at k = 0: thread t
+    // < 128 holds timeslice t's, 128 <= t < 192 trial row t - 128's.  A
+    // chunk's exponent is loaded (scale_load) while the chunk before it is
+    // in the tensor cores and stored (scale_store) after that chunk's fold.
+    const bool scale_k = tid < kTauTile && tau0 + tid < Nt;
+    const bool scale_x = tid >= kTauTile && tid < kTauTile + kRowTile && tid - kTauTile < tile.rows;
+    const int16_t* scale_row = nullptr;  // this thread's exponents, one per chunk
+    if (scale_k) scale_row = X0.kexp + (uint64_t)(tau0 + tid) * C;
+    if (scale_x) {
+        const SplitRow rw = rows[tile.first_row + (tid - kTauTile)];
+        scale_row = split[rw.run].xexp + (uint64_t)rw.member * C;
+    }
+    auto scale_load = [&](uint32_t c) -> int { return scale_row ? (int)scale_row[c] : -1000; };
+    auto scale_store = [&](int e) {
         if (tid < kTauTile) {
-            const bool ok = tau0 + tid < Nt;
-            const int ek = ok ? X0.kexp[(uint64_t)(tau0 + tid) * C + c] : -1000;
-            s_ek[tid] = ek;
-            const int d = ek - s_kmax[tid];
-            const float v = (ok && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
+            s_ek[tid] = e;
+            const int d = e - s_kmax[tid];
+            const float v = (scale_k && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
             *reinterpret_cast<uint16_t*>(sAb + canon(tid, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
         } else if (tid < kTauTile + kRowTile) {
             const uint32_t r = tid - kTauTile;
-            const bool ok = r < tile.rows;
-            int e = -1000;
-            if (ok) {
-                const SplitRow rw = rows[tile.first_row + r];
-                e = split[rw.run].xexp[(uint64_t)rw.member * C + c];
-            }
             s_ex[r] = e;
             const int d = e - s_xmax[r];
-            const float v = (ok && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
+            const float v = (scale_x && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
             *reinterpret_cast<uint16_t*>(sBb + canon(r, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
         }
     };
@@ -327,7 +331,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         mbar_expect_tx(&s_full, b_bytes);
         load_x(wk.c0);
     }
-    scales(wk.c0);
+    scale_store(scale_load(wk.c0));
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
@@ -355,6 +359,8 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 smem_u32(&s_bar)));
         }
+        // the next chunk's exponents, loaded while the tensor cores work
+        const int next_e = c + 1 < wk.c1 ? scale_load(c + 1) : -1000;
         ok = __syncthreads_and(mbar_wait(&s_bar, it & 1u)) != 0;  // uniform across the CTA
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         if (!ok) break;
@@ -396,7 +402,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();  // every read of s_ek/s_ex and of TMEM is done
         if (c + 1 < wk.c1) {
-            scales(c + 1);
+            scale_store(next_e);
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n");
