@@ -171,6 +171,11 @@ struct deac_batch {
     deac::SplitRow* d_rows = nullptr;
     float4* d_partial = nullptr;       // partial sums of the split contraction CTAs
     uint32_t n_tiles = 0, n_split_ctas = 0;
+    int sms = 0;                             // the device's multiprocessors
+    uint64_t* d_exact_list = nullptr;        // split engine: the exact pass's items
+    uint32_t* d_exact_count = nullptr;
+    uint32_t n_combine_tiles = 0;            // tiles split over several contraction CTAs
+    uint32_t* d_combine_tiles = nullptr;     // their indices
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
     uint32_t* d_fit_off = nullptr;      // snapshot_kernel: each run's first fitness slot (and the total)
@@ -241,9 +246,15 @@ void launch(void (*kernel)(Params...), uint32_t grid, uint32_t block, size_t sme
 }
 
 void launch_contract(deac_batch* b, cudaStream_t s, int mode, bool early = false) {
-    const uint32_t grid = mode == deac::kModeRecheck ? 2 * b->n_contract_ctas : b->n_contract_ctas;
-    launch(deac::contract_kernel, grid, deac::kContractThreads, b->contract_smem_bytes, s, early, b->d_runs,
-           static_cast<const deac::Work*>(b->d_contract_work), mode);
+    if (mode == deac::kModeRecheck) {
+        // the listed items, over at most one CTA per SM (one fits per SM)
+        const uint32_t grid = std::min<uint32_t>(2 * b->n_contract_ctas, (uint32_t)b->sms);
+        launch(deac::exact_pass_kernel, grid, deac::kContractThreads, b->contract_smem_bytes, s, early, b->d_runs,
+               static_cast<const uint64_t*>(b->d_exact_list), static_cast<const uint32_t*>(b->d_exact_count));
+        return;
+    }
+    launch(deac::contract_kernel, b->n_contract_ctas, deac::kContractThreads, b->contract_smem_bytes, s, early,
+           b->d_runs, static_cast<const deac::Work*>(b->d_contract_work), mode);
 }
 
 // One generation of every run: two launches for the plain engine; for the
@@ -306,9 +317,11 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     if ((rc = mark(3))) return rc;
     // not scheduled early: its waiting CTAs would hold the SMs that the
     // normalisation row sums need
-    launch(deac::split_combine_kernel, b->n_tiles * deac::kCombineCtasPerTile, 256, 0, s, early && !fork, b->d_runs,
-           b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
-           static_cast<const float4*>(b->d_partial));
+    if (b->n_combine_tiles)
+        launch(deac::split_combine_kernel, b->n_combine_tiles * deac::kCombineCtasPerTile, 256, 0, s, early && !fork,
+               b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
+               static_cast<const uint32_t*>(b->d_combine_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
+               static_cast<const float4*>(b->d_partial));
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
                                                                                b->d_trial_work);
@@ -961,6 +974,8 @@ int deac_batch_setup(deac_batch* b) {
     b->contract_smem_bytes = contract_bytes;
     CUDA_TRY(raise_smem_limit(deac::trial_kernel, std::max<size_t>(b->trial_smem_bytes, 1024)));
     CUDA_TRY(raise_smem_limit(deac::contract_kernel, b->contract_smem_bytes));
+    CUDA_TRY(raise_smem_limit(deac::exact_pass_kernel, b->contract_smem_bytes));
+    CUDA_TRY(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
@@ -999,6 +1014,15 @@ int deac_batch_setup(deac_batch* b) {
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
         int rc = make_group_planes(b);
         if (rc) return rc;
+    }
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        CUDA_TRY(cudaMalloc(&b->d_exact_list, std::max<uint64_t>(2ull * b->n_contract_ctas, 1) * sizeof(uint64_t)));
+        CUDA_TRY(cudaMalloc(&b->d_exact_count, sizeof(uint32_t)));
+        CUDA_TRY(cudaMemset(b->d_exact_count, 0, sizeof(uint32_t)));
+        for (auto& r : b->runs) {
+            r->dev.exact_list = b->d_exact_list;
+            r->dev.exact_count = b->d_exact_count;
+        }
     }
     std::vector<deac::RunDev> descs;
     for (auto& r : b->runs) descs.push_back(r->dev);
@@ -1046,24 +1070,36 @@ int deac_batch_setup(deac_batch* b) {
             if (r->cfg.normalize) norm_ctas += r->P;
         const uint64_t free_sms = (uint64_t)sms - std::min<uint64_t>(norm_ctas, (uint64_t)sms / 2);
         const uint64_t want = std::max<uint64_t>(1, free_sms / tiles.size());
+        // partial-sum blocks only for tiles split over several CTAs; a tile
+        // with one CTA has its estimates formed by that CTA
         std::vector<deac::SplitWork> work;
+        std::vector<uint32_t> combine_tiles;
         uint32_t blocks = 0;
         for (uint32_t t = 0; t < tiles.size(); ++t) {
             const uint32_t C = tile_chunks[t];
             const uint32_t per = (uint32_t)((C + std::min<uint64_t>(want, C) - 1) / std::min<uint64_t>(want, C));
-            tiles[t].block0 = blocks;
-            for (uint32_t c0 = 0; c0 < C; c0 += per) work.push_back({t, c0, std::min(C, c0 + per), blocks++});
-            tiles[t].nsplit = blocks - tiles[t].block0;
+            const uint32_t nsplit = (C + per - 1) / per;
+            tiles[t].block0 = nsplit > 1 ? blocks : ~0u;
+            tiles[t].nsplit = nsplit;
             tiles[t].per = per;
+            for (uint32_t c0 = 0; c0 < C; c0 += per)
+                work.push_back({t, c0, std::min(C, c0 + per), nsplit > 1 ? blocks++ : ~0u});
+            if (nsplit > 1) combine_tiles.push_back(t);
         }
         b->n_tiles = (uint32_t)tiles.size();
+        b->n_combine_tiles = (uint32_t)combine_tiles.size();
         b->n_split_ctas = (uint32_t)work.size();
+        if (!combine_tiles.empty()) {
+            CUDA_TRY(cudaMalloc(&b->d_combine_tiles, combine_tiles.size() * sizeof(uint32_t)));
+            CUDA_TRY(copy(b, b->d_combine_tiles, combine_tiles.data(), combine_tiles.size() * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice));
+        }
         CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
         CUDA_TRY(copy(b, b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMalloc(&b->d_split_work, work.size() * sizeof(deac::SplitWork)));
         CUDA_TRY(copy(b, b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork),
                             cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMalloc(&b->d_partial, (uint64_t)blocks * deac::kPartialBlock * sizeof(float4)));
+        CUDA_TRY(cudaMalloc(&b->d_partial, std::max<uint64_t>(blocks, 1) * deac::kPartialBlock * sizeof(float4)));
         CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
         CUDA_TRY(copy(b, b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
         CUDA_TRY(raise_smem_limit(deac::split_contract_kernel, deac::split_smem_bytes(2)));
@@ -1502,6 +1538,9 @@ int deac_batch_destroy(deac_batch* b) {
     for (uint16_t* x : b->group_xdig) cudaFree(x);
     cudaFree(b->d_maps);
     cudaFree(b->d_partial);
+    cudaFree(b->d_combine_tiles);
+    cudaFree(b->d_exact_list);
+    cudaFree(b->d_exact_count);
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
     cudaFree(b->d_jpow);

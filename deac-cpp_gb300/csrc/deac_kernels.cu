@@ -483,6 +483,8 @@ __device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* wo
     };
     prefetch_states(wk.part0);
     grid_dependency_wait();
+    // the previous generation's exact pass is done with its item list
+    if (blockIdx.x == 0 && threadIdx.x == 0) *R.exact_count = 0;
     if (R.done) return;
     // one round trip: the member's CR / F and mutant indices, and the
     // parent buffer of every member of the run (of the mutants on demand
@@ -683,24 +685,11 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // row the CTA needs ([S][member_tile] pop rows, then [S][tau_tile] K rows,
 // row stride chunk+2), reused by the finishing CTA as 4 x 1024 reduction
 // slots.
-__global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int mode) {
-    if (mode == kModeRecheck) {
-        // the next generation's trial parts read nothing before their own
-        // wait: let them be scheduled while the selection still runs
-        asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
-        asm volatile("griddepcontrol.wait;\n" ::: "memory");
-    } else {
-        grid_dependency_wait();
-    }
-    extern __shared__ __align__(16) double dyn[];
+// One contraction item: tile w of run w.run in mode `mode`; in
+// kModeRecheck the item's pass `pmode` is kModeParents or kModeTrials.
+__device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mode, int pmode, double* dyn) {
     __shared__ int s_last, s_any;
-
-    // kModeRecheck: the first half of the grid evaluates what kModeParents
-    // does, the second half what kModeTrials does
     const bool both = mode == kModeRecheck;
-    const uint32_t half_n = both ? gridDim.x / 2 : gridDim.x;
-    const int pmode = both ? (blockIdx.x < half_n ? kModeParents : kModeTrials) : mode;  // this CTA's pass
-    const Work w = work[blockIdx.x % half_n];
     RunDev& R = runs[w.run];
     if (R.done && mode != kModeFinal) return;
     if ((mode == kModeParents || mode == kModeTrials || both) && R.exact_idle) return;
@@ -955,6 +944,32 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
         }
     }
     if (threadIdx.x == 0) R.ticket = 0;
+}
+
+__global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs, const Work* work, int mode) {
+    grid_dependency_wait();
+    extern __shared__ __align__(16) double dyn[];
+    contract_body(runs, work[blockIdx.x], mode, mode, dyn);
+}
+
+// The split engine's exact pass: the items the selections left open, listed
+// by split_select_kernel (run << 32 | pass << 31 | tile, both passes of each
+// listed run), shared out over a grid of at most one CTA per SM; with nothing
+// listed every CTA returns at once.
+__global__ void __launch_bounds__(kContractThreads) exact_pass_kernel(RunDev* runs, const uint64_t* list,
+                                                                      const uint32_t* count) {
+    // the next generation's trial parts read nothing before their own wait:
+    // let them be scheduled while the selection still runs
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    extern __shared__ __align__(16) double dyn[];
+    const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(count);
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint64_t e = list[k];
+        const Work w{(uint32_t)(e >> 32), (uint32_t)e & 0x7FFFFFFFu};
+        contract_body(runs, w, kModeRecheck, (e >> 31) & 1u ? kModeTrials : kModeParents, dyn);
+        __syncthreads();  // shared memory is reused by the next item
+    }
 }
 
 }  // namespace deac

@@ -105,6 +105,10 @@ struct RunDev {
     // split engine with --normalize (kDeferNorm): the trials stay raw until
     // the decisions; norm_kernel forms each trial's exact reciprocal norm
     double* recip;           // [P] 1/norm of each trial
+    // split engine: the batch's list of exact-pass items (shared by all
+    // runs; see exact_pass_kernel) and its length
+    uint64_t* exact_list;
+    uint32_t* exact_count;
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
@@ -170,8 +174,8 @@ enum ContractMode : int {
     kModeParents = 2,     // split engine: exact fitness of undecided members' inexact parents
     kModeTrials = 3,      // split engine: exact fitness and selection of undecided trials, bookkeeping
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
-    kModeRecheck = 5,     // split engine, a grid of two halves: kModeParents, then kModeTrials,
-                          // one CTA finishing both
+    kModeRecheck = 5,     // split engine (exact_pass_kernel): kModeParents and kModeTrials items
+                          // of a run, one CTA finishing both
 };
 
 // Programmatic dependent launch: a kernel launched with the programmatic
@@ -233,5 +237,8 @@ constexpr uint32_t kNormStage = kChainWarps * 32 * kChainSteps;  // steps staged
 constexpr uint32_t kNormSmemBytes = 2 * 2 * kNormStage * sizeof(double);  // dynamic shared memory of norm_kernel
 __global__ void norm_kernel(RunDev* runs, const Work* work);
 __global__ void contract_kernel(RunDev* runs, const Work* work, int mode);
+// split engine: the exact pass over the items split_select_kernel listed
+// (entry = run << 32 | pass << 31 | tile, pass 1 = the trials; count entries)
+__global__ void exact_pass_kernel(RunDev* runs, const uint64_t* list, const uint32_t* count);
 
 }  // namespace deac

@@ -177,6 +177,41 @@ __device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
 
 }  // namespace
 
+// The estimate of output (row rw, timeslice t) and its bound from the
+// tile's summed double-float (hi, lo) and bound accumulator b (see below).
+__device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, const SplitRow rw, uint32_t t,
+                                               const SplitTile& tile, float hi, float lo, float b) {
+    const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
+    const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
+    // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
+    // below 2^-23 per addition), terms under 2^-126 dropped
+    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
+    // Error of the estimate against the FP64 chain value, in parts:
+    //  digits: dropped digit pairs and remainders, 2^-45.9 2^(e_x+e_K) per
+    //    product, 64 products a chunk:                     2^-39 B
+    //  digit-group sums in FP32 (TwoSum cascade of seven exact terms):
+    //    30 u^2 times the chunk's |terms| <= 64 2^(e_x+e_K):  2^-37 B
+    //  double-float additions, 3 u^2 |partial| each, along the longest
+    //    path (a split's chunks, then the combine):  depth 3 u^2 |sum|
+    //  the FP64 chains themselves, 2^-53 per step of |partial sum|, and
+    //    the final FP64 sum.
+    // |sum| is at most 64 B in general; when every product is >= 0 the
+    // partial sums are at most the value itself, bounded by E' below.
+    const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
+    const double e = (double)hi + (double)lo;
+    const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
+    double eb;
+    if (R.flags & kNonNegProducts) {
+        const double Ep = (fabs(e) + bsum * gen * 1.01) * (1.0 + 0x1p-40);
+        eb = bsum * 0x1p-39 + Ep * ((M + 1.0) * 0x1p-53 + 0x1p-43 + depth * 3.0 * 0x1p-48 + 0x1p-51);
+    } else {
+        eb = bsum * (gen + M * 0x1p-47 + 0x1p-46);
+    }
+    const uint64_t o = (uint64_t)rw.member * R.Nt + t;
+    X.e_mp[o] = e;
+    X.e_bound[o] = eb * (1.0 + 0x1p-40) + (C + ks + 10.0) * 0x1p-140;
+}
+
 // ----------------------------------------------------- split contraction
 // One CTA per (tile, chunk range).  The tile is 128 timeslices (MMA M, one
 // TMEM lane each) x 64 trial rows (MMA N) of runs that share K.  Per 32-gene
@@ -410,7 +445,26 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         asm volatile("tcgen05.fence::after_thread_sync;\n");
     }
 
-    if (ok) {
+    if (ok && tile.nsplit == 1) {
+        // the tile's only CTA: its sums are the tile's, so the estimates and
+        // their bounds are formed here (no partial sums, no combine)
+#pragma unroll
+        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
+            uint32_t d[8];
+            tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const uint32_t r = r0 + j8 + j;
+                const uint32_t t = tau0 + tl;
+                if (r >= tile.rows || t >= Nt) continue;
+                const SplitRow rw = rows[tile.first_row + r];
+                const RunDev& R = runs[rw.run];
+                if (R.done) continue;
+                store_estimate(R, split[rw.run], rw, t, tile, acc_hi[j8 + j], acc_lo[j8 + j], __uint_as_float(d[j]));
+            }
+        }
+    } else if (ok) {
         // partial sums and the bound accumulator sum_c 2^(e_x-max_x + e_K-max_K)
         float4* out = partial + (uint64_t)wk.block * kPartialBlock;
 #pragma unroll
@@ -438,10 +492,11 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
 // loads, eight in flight), then lane-wise the eight warps' sums are added in
 // a fixed order and turned into the estimate and its error bound.
 __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
-                                                            const SplitRow* rows, const float4* partial) {
+                                                            const uint32_t* combine_tiles, const SplitRow* rows,
+                                                            const float4* partial) {
     grid_dependency_wait();
     __shared__ float4 s_part[8][32];
-    const SplitTile tile = tiles[blockIdx.x / kCombineCtasPerTile];
+    const SplitTile tile = tiles[combine_tiles[blockIdx.x / kCombineCtasPerTile]];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t idx = (blockIdx.x % kCombineCtasPerTile) * 32 + lane;
     const uint32_t r = idx / kTauTile, tl = idx % kTauTile;
@@ -477,35 +532,7 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     SplitRun& X = split[rw.run];
     const uint32_t t = tile.tau0 + tl;
     if (R.done || t >= R.Nt) return;
-    const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
-    const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
-    // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
-    // below 2^-23 per addition), terms under 2^-126 dropped
-    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
-    // Error of the estimate against the FP64 chain value, in parts:
-    //  digits: dropped digit pairs and remainders, 2^-45.9 2^(e_x+e_K) per
-    //    product, 64 products a chunk:                     2^-39 B
-    //  digit-group sums in FP32 (TwoSum cascade of seven exact terms):
-    //    30 u^2 times the chunk's |terms| <= 64 2^(e_x+e_K):  2^-37 B
-    //  double-float additions, 3 u^2 |partial| each, along the longest
-    //    path (a split's chunks, then the combine):  depth 3 u^2 |sum|
-    //  the FP64 chains themselves, 2^-53 per step of |partial sum|, and
-    //    the final FP64 sum.
-    // |sum| is at most 64 B in general; when every product is >= 0 the
-    // partial sums are at most the value itself, bounded by E' below.
-    const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
-    const double e = (double)hi + (double)lo;
-    const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
-    double eb;
-    if (R.flags & kNonNegProducts) {
-        const double Ep = (fabs(e) + bsum * gen * 1.01) * (1.0 + 0x1p-40);
-        eb = bsum * 0x1p-39 + Ep * ((M + 1.0) * 0x1p-53 + 0x1p-43 + depth * 3.0 * 0x1p-48 + 0x1p-51);
-    } else {
-        eb = bsum * (gen + M * 0x1p-47 + 0x1p-46);
-    }
-    const uint64_t o = (uint64_t)rw.member * R.Nt + t;
-    X.e_mp[o] = e;
-    X.e_bound[o] = eb * (1.0 + 0x1p-40) + (C + ks + 10.0) * 0x1p-140;
+    store_estimate(R, X, rw, t, tile, hi, lo, b);
 }
 
 // ---------------------------------------------------------------- select
@@ -782,6 +809,15 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         X.sel_min_bits = ~0ull;
         const bool idle = nre == 0 && !force_exact;
         R.exact_idle = idle ? 1 : 0;
+        if (!idle) {
+            // list both passes of every tile of this run for the exact pass
+            const uint32_t n = R.contract_ctas;
+            const uint32_t base = atomicAdd(R.exact_count, 2 * n);
+            for (uint32_t k = 0; k < 2 * n; ++k) {
+                const uint64_t pass = k >= n ? 1u : 0u;
+                R.exact_list[base + k] = ((uint64_t)wk.run << 32) | (pass << 31) | (pass ? k - n : k);
+            }
+        }
         if (idle) {
             const uint64_t ii = ii0 + 1;
             R.ii = ii;

@@ -112,8 +112,10 @@ constexpr uint64_t kPartialBlock = (uint64_t)kRowTile * kTauTile;
 // [2g+1] the trial digit planes (box 64 rows)
 __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
                                       const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status);
-__global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitRow* rows,
-                                     const float4* partial);
+// combine_tiles: the tiles split over several CTAs (a tile with one CTA
+// has its estimates formed by that CTA)
+__global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
+                                     const uint32_t* combine_tiles, const SplitRow* rows, const float4* partial);
 __global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* work);
 // The digit planes of K (kn null for one-sided K), one CTA per timeslice t:
 // per 32-gene chunk the scale exponent shared by both sides (kexp[t][c]),
