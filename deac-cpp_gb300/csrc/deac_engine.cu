@@ -157,6 +157,7 @@ struct deac_batch {
     // snapshot of every run's status, parent fitness and parent buffers,
     // taken after the last launch (finalised: split-engine parents exact)
     bool snapped = false;
+    bool snapped_all = false;  // every parent's fitness exact in the snapshot
     std::vector<deac::RunDev> snap;
     std::vector<std::vector<double>> snap_fit;
     std::vector<std::vector<uint8_t>> snap_cur;
@@ -332,16 +333,20 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
 
 int launch_generation_timed(deac_batch* b) { return launch_generation(b, b->stream, 0, true); }
 
-// Split engine: make every parent's fitness exact (the final argmin, the
-// reported minimum and the state fetches read them).
-// Make every split-engine parent's fitness exact and take the snapshot the
-// result and fetch calls read; nothing is done again until the next launch.
-int finalize_split(deac_batch* b) {
-    if (b->snapped) return DEAC_OK;
+// Take the snapshot the result and fetch calls read; nothing is done again
+// until the next launch.  Split engine: first make exact the fitness of the
+// parents that may hold each run's minimum (the best member, the reported
+// minimum and spectrum), or with `all` of every parent (state fetches,
+// checkpoints).  A parent whose interval starts above another's upper end
+// cannot hold the minimum, so its midpoint stays in the snapshot: above the
+// exact minimum, it changes neither the argmin nor the minimum.
+int finalize_split(deac_batch* b, bool all = false) {
+    if (b->snapped && (b->snapped_all || !all)) return DEAC_OK;
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        launch_contract(b, b->stream, deac::kModeFinal);
+        launch_contract(b, b->stream, all ? deac::kModeFinal : deac::kModeFinalBest);
         CUDA_TRY(cudaGetLastError());
     }
+    b->snapped_all = all || b->engine != DEAC_ENGINE_SPLIT_BF16;
     // every run's descriptor, parent fitness and parent buffers packed on
     // the device and read back in one copy
     const size_t n = b->runs.size();
@@ -422,11 +427,15 @@ const std::vector<uint64_t>& jump_powers(uint32_t bits) {
     return tab;
 }
 
-// Host part of one run's set-up: constants, initial population, PRNG table.
-void prepare_run(RunHost& r, int32_t streams) {
+// Host part of one run's set-up: its constants (the kernel matrix is formed
+// once per distinct one, after this).
+void prepare_model(RunHost& r) {
+    deac::build_model(r.cfg, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model, false);
+}
+
+// Host part of one run's set-up: initial population and PRNG start state.
+void prepare_population(RunHost& r, int32_t streams) {
     const deac_config& c = r.cfg;
-    // the kernel matrix is formed once per distinct one, after this
-    deac::build_model(c, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model, false);
     const uint64_t P = r.P, M = r.M;
     const int S = r.S;
     // initial population: one stream seeded with 1407513600 + seed
@@ -915,18 +924,16 @@ int deac_batch_setup(deac_batch* b) {
     if (b->set_up) return DEAC_OK;
     if (b->runs.empty()) return fail(DEAC_E_STATE, "empty batch");
     CUDA_TRY(cudaSetDevice(b->device));
-    // host preparation, one thread per run (the PRNG table is a serial chain
-    // of jumps per run, as in the reference)
+    // host preparation of the runs' constants, spread over the host's threads
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     {
-        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         std::vector<std::thread> pool;
-        size_t next = 0;
-        while (next < b->runs.size()) {
-            pool.clear();
-            for (unsigned t = 0; t < hw && next < b->runs.size(); ++t, ++next)
-                pool.emplace_back(prepare_run, std::ref(*b->runs[next]), b->streams);
-            for (auto& th : pool) th.join();
-        }
+        for (unsigned t = 0; t < hw && t < b->runs.size(); ++t)
+            pool.emplace_back([b, t, hw] {
+                for (size_t k = t; k < b->runs.size(); k += hw) prepare_model(*b->runs[k]);
+            });
+        for (auto& th : pool) th.join();
+        pool.clear();
         // the kernel matrix of each distinct (model, T, tau and omega grid),
         // in the first run that has it (the one upload_run takes it from),
         // its rows spread over the host's threads
@@ -945,6 +952,8 @@ int deac_batch_setup(deac_batch* b) {
             for (auto& th : pool) th.join();
         }
     }
+    for (auto& r : b->runs)
+        r->n_states = b->streams == DEAC_STREAMS_COUNTER ? r->P : r->P * (1 + (uint64_t)r->S * r->M);
     if (b->streams == DEAC_STREAMS_REFERENCE) {
         uint32_t bits = 1;
         for (auto& r : b->runs) bits = std::max(bits, jump_bits(r->n_states));
@@ -956,8 +965,17 @@ int deac_batch_setup(deac_batch* b) {
     std::vector<deac::Work> tw, cw;
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         RunHost& r = *b->runs[ri];
+        if (ri % hw == 0) {
+            // the initial populations of the next window of runs, one host
+            // thread each (only a window is held on the host at a time)
+            std::vector<std::thread> pool;
+            for (uint32_t k = ri; k < b->runs.size() && k < ri + hw; ++k)
+                pool.emplace_back(prepare_population, std::ref(*b->runs[k]), b->streams);
+            for (auto& th : pool) th.join();
+        }
         int rc = upload_run(b, r);
         if (rc) return rc;
+        std::vector<double>().swap(r.pop0);  // uploaded
         for (uint32_t i = 0; i < r.dev.P; ++i) tw.push_back({ri, i});
         for (uint32_t k = 0; k < r.dev.contract_ctas; ++k) cw.push_back({ri, k});
         // trial genes, plus one row of weights when a row sum is formed
@@ -1184,7 +1202,7 @@ int deac_batch_size(const deac_batch* b, uint32_t* runs) {
 static int gather(deac_batch* b, uint32_t run, std::vector<double>& pop, std::vector<double>& fit,
                   std::vector<double>* crfw, deac::RunDev& st) {
     RunHost& r = *b->runs[run];
-    int rc = finalize_split(b);
+    int rc = finalize_split(b, true);
     if (rc) return rc;
     CUDA_TRY(copy(b, &st, b->d_runs + run, sizeof st, cudaMemcpyDeviceToHost));
     const uint64_t P = r.P, M = r.M, S = r.S;
@@ -1365,7 +1383,7 @@ int deac_batch_checkpoint(deac_batch* b, uint32_t run, void* out, uint64_t capac
                                        (unsigned long long)capacity, (unsigned long long)*bytes);
     if (split) {
         // every parent's fitness exact (the checkpoint holds no intervals)
-        int rc = finalize_split(b);
+        int rc = finalize_split(b, true);
         if (rc) return rc;
     }
     CUDA_TRY(cudaStreamSynchronize(b->stream));

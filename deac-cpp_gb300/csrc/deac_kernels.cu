@@ -115,6 +115,17 @@ __device__ __forceinline__ uint32_t pow2_ceil(uint32_t n) {
     return w;
 }
 
+// min of a shared double with v (a CAS loop: no native double atomicMin)
+__device__ __forceinline__ void atomic_min_double_smem(double* p, double v) {
+    unsigned long long* a = reinterpret_cast<unsigned long long*>(p);
+    unsigned long long old = *a;
+    while (v < __longlong_as_double((long long)old)) {
+        const unsigned long long seen = atomicCAS(a, old, (unsigned long long)__double_as_longlong(v));
+        if (seen == old) break;
+        old = seen;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- trial
@@ -691,15 +702,31 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     __shared__ int s_last, s_any;
     const bool both = mode == kModeRecheck;
     RunDev& R = runs[w.run];
-    if (R.done && mode != kModeFinal) return;
+    const bool final_mode = mode == kModeFinal || mode == kModeFinalBest;
+    if (R.done && !final_mode) return;
     if ((mode == kModeParents || mode == kModeTrials || both) && R.exact_idle) return;
     const bool init_mode = mode == kModeInit;
     // members evaluated by a pass, and which of their two buffers
-    auto parents_of = [](int pm) { return pm == kModeInit || pm == kModeParents || pm == kModeFinal; };
+    auto parents_of = [](int pm) {
+        return pm == kModeInit || pm == kModeParents || pm == kModeFinal || pm == kModeFinalBest;
+    };
+    // kModeFinalBest: the lowest upper end of the parents' intervals (a
+    // parent whose interval starts above it cannot hold the minimum)
+    __shared__ double s_min_hi;
+    if (mode == kModeFinalBest) {
+        double mh = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+        for (uint32_t m = threadIdx.x; m < R.P; m += blockDim.x) mh = fmin(mh, R.f_hi[m]);
+        for (int o = 16; o > 0; o >>= 1) mh = fmin(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+        if (threadIdx.x == 0) s_min_hi = mh;
+        __syncthreads();
+        if ((threadIdx.x & 31u) == 0) atomic_min_double_smem(&s_min_hi, mh);
+        __syncthreads();
+    }
     auto wanted_in = [&](int pm, uint32_t m) -> bool {
         if (pm == kModeGeneration || pm == kModeInit) return true;
         if (pm == kModeTrials) return R.recheck[m] != 0;
         const bool inexact = R.f_lo[m] != R.f_hi[m];
+        if (pm == kModeFinalBest) return inexact && R.f_lo[m] <= s_min_hi;
         return pm == kModeFinal ? inexact : (R.recheck[m] != 0 && inexact);
     };
     const bool use_parent = parents_of(pmode);
@@ -864,7 +891,7 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     }
     __syncthreads();
     }
-    if (mode == kModeParents || mode == kModeFinal) {
+    if (mode == kModeParents || final_mode) {
         if (threadIdx.x == 0) R.ticket = 0;
         return;  // no selection and no bookkeeping in these passes
     }

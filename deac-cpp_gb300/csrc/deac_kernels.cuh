@@ -174,6 +174,8 @@ enum ContractMode : int {
     kModeParents = 2,     // split engine: exact fitness of undecided members' inexact parents
     kModeTrials = 3,      // split engine: exact fitness and selection of undecided trials, bookkeeping
     kModeFinal = 4,       // split engine: exact fitness of every inexact parent (finished runs too)
+    kModeFinalBest = 6,   // split engine: the same for the parents that may hold the minimum (an
+                          // interval reaching below every other parent's upper end)
     kModeRecheck = 5,     // split engine (exact_pass_kernel): kModeParents and kModeTrials items
                           // of a run, one CTA finishing both
 };
