@@ -634,6 +634,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
         const uint64_t o_cnt = sa.take(3 * 8);
         const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
+        const uint64_t o_pm = sa.take(2 * P * 8);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
         char* sb = r.split_arena;
@@ -678,6 +679,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         d.f_lo = x.f_lo;
         d.f_hi = x.f_hi;
         d.recip = reinterpret_cast<double*>(sb + o_rcp);
+        d.pmoments = reinterpret_cast<double*>(sb + o_pm);
         // with --normalize the trials stay raw until the decisions
         if (r.cfg.normalize) d.flags |= deac::kDeferNorm;
         if (it->second.nonneg && !r.cfg.allow_negative_weight) d.flags |= deac::kNonNegProducts;
@@ -869,13 +871,8 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau,
     if (cfg->population_size > (1u << 20) || m > (1u << 26) || nt > (1u << 20))
         return fail(DEAC_E_INVALID, "problem size beyond the engine's limits");
     if (isf[0] == 0.0 && cfg->normalize) return fail(DEAC_E_INVALID, "--normalize needs a nonzero F(0)");
-    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        if (m % deac::kChunk != 0)
-            return fail(DEAC_E_INVALID, "the split engine needs genome_size a multiple of %d", deac::kChunk);
-        if (cfg->first_moment >= 0.0 || cfg->third_moment >= 0.0 ||
-            (cfg->use_negative_first_moment && cfg->bosonic && !cfg->zero_temperature))
-            return fail(DEAC_E_INVALID, "the split engine does not support moment terms; use the plain engine");
-    }
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16 && m % deac::kChunk != 0)
+        return fail(DEAC_E_INVALID, "the split engine needs genome_size a multiple of %d", deac::kChunk);
     auto r = std::make_unique<RunHost>();
     r->cfg = *cfg;
     r->P = cfg->population_size;
@@ -997,11 +994,12 @@ int deac_batch_setup(deac_batch* b) {
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        // one CTA per trial of every --normalize run
+        // one CTA per trial of every run that normalises or has moment
+        // terms (their exact row sums)
         std::vector<deac::Work> nw;
         for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
             const RunHost& r = *b->runs[ri];
-            if (!(r.dev.flags & deac::kDeferNorm)) continue;
+            if (!(r.dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment))) continue;
             for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
         }
         std::vector<deac::PartWork> pw;
@@ -1085,7 +1083,7 @@ int deac_batch_setup(deac_batch* b) {
         // kernel: leave them their SMs (up to half)
         uint64_t norm_ctas = 0;
         for (auto& r : b->runs)
-            if (r->cfg.normalize) norm_ctas += r->P;
+            if (r->dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment)) norm_ctas += r->P;
         const uint64_t free_sms = (uint64_t)sms - std::min<uint64_t>(norm_ctas, (uint64_t)sms / 2);
         const uint64_t want = std::max<uint64_t>(1, free_sms / tiles.size());
         // partial-sum blocks only for tiles split over several CTAs; a tile

@@ -616,15 +616,18 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_counter_kerne
 }
 
 // ---------------------------------------------------------------- norm
-// Split engine, kDeferNorm runs: one CTA per raw trial forms the exact
-// normalisation row sums (warps 0-7 the positive side, 8-15 the negative
-// side, staged kNormStage genes at a time in shared memory), then
-// norm = gemv_pair(...) and 1/norm exactly as trial_kernel does, and sets
-// the trial's `changed` flag (a mutated gene or a scale other than 1).
+// Split engine, runs that normalise (kDeferNorm) or have moment terms: one
+// CTA per raw trial forms its exact row sums (warps 0-7 the positive side,
+// 8-15 the negative side, staged kNormStage genes at a time in shared
+// memory).  First the normalisation sums, then norm = gemv_pair(...) and
+// 1/norm exactly as trial_kernel does, setting the trial's `changed` flag
+// (a mutated gene or a scale other than 1); then the first and third moment
+// sums of the normalised trial -- each gene RN(x / norm) as trial_kernel
+// forms it, so the moments are trial_kernel's to the bit.
 __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const Work* work) {
     grid_dependency_wait();
     __shared__ ChainScratch s_chain[2];
-    __shared__ double s_sum[2];
+    __shared__ double s_sum[2], s_recip;
     extern __shared__ __align__(16) double norm_s[];  // per side: [kNormStage] genes, [kNormStage] weights
     const Work wk = work[blockIdx.x];
     RunDev& R = runs[wk.run];
@@ -635,60 +638,85 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
     const uint32_t buf = 1u - R.cur[i];
     const uint32_t side = (threadIdx.x >> 5) / kChainWarps;
     const double* x = R.pop + ((uint64_t)buf * S + side) * PM + (uint64_t)i * M;
-    const double* wts = side == 0 ? R.norm_pos : R.norm_neg;
     double* s_x = norm_s + (uint64_t)side * 2 * kNormStage;
     double* s_w = s_x + kNormStage;
     const uint32_t tg = threadIdx.x - side * kChainWarps * 32;
     // the later stages' genes into L2 while the first stage's chain runs
     if (tg == 0 && side < S && M > kNormStage) prefetch_l2(x + kNormStage, M - kNormStage, x + M);
-    double sum = 0.0;
-    // each side's group runs on its own: its staging and chain synchronise
-    // with the group's named barrier only
-    for (uint32_t k0 = 0; side < S && k0 < M; k0 += kNormStage) {
-        const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
-        chain_detail::group_bar(1 + (int)side, kChainWarps * 32);  // the chain is done with the stage buffer
-        {
-            // this thread's steps tg*E .. tg*E+E-1 of the stage, all loads in
-            // flight at once, stored step-major (chain_slot order) so that
-            // the chain's threads read them without bank conflicts
-            constexpr uint32_t E = kChainSteps, NT = kChainWarps * 32;
-            double vx[E], vw[E];
-            const uint32_t k = tg * E;
-            if (k + E <= len) {
-                const double2* px = reinterpret_cast<const double2*>(x + k0 + k);
-                const double2* pw = reinterpret_cast<const double2*>(wts + k0 + k);
+    // this side's row sum over weights wts, of the genes times rc when
+    // `scaled`; each side's group runs on its own: its staging and chain
+    // synchronise with the group's named barrier only
+    auto side_sum = [&](const double* wts, bool scaled, double rc) -> double {
+        double sum = 0.0;
+        for (uint32_t k0 = 0; side < S && k0 < M; k0 += kNormStage) {
+            const uint32_t len = M - k0 < kNormStage ? M - k0 : kNormStage;
+            chain_detail::group_bar(1 + (int)side, kChainWarps * 32);  // the chain is done with the stage buffer
+            {
+                // this thread's steps tg*E .. tg*E+E-1 of the stage, all loads
+                // in flight at once, stored step-major (chain_slot order) so
+                // that the chain's threads read them without bank conflicts
+                constexpr uint32_t E = kChainSteps, NT = kChainWarps * 32;
+                double vx[E], vw[E];
+                const uint32_t k = tg * E;
+                if (k + E <= len) {
+                    const double2* px = reinterpret_cast<const double2*>(x + k0 + k);
+                    const double2* pw = reinterpret_cast<const double2*>(wts + k0 + k);
 #pragma unroll
-                for (uint32_t u = 0; u < E / 2; ++u) {
-                    const double2 a = px[u], b = pw[u];
-                    vx[2 * u] = a.x;
-                    vx[2 * u + 1] = a.y;
-                    vw[2 * u] = b.x;
-                    vw[2 * u + 1] = b.y;
+                    for (uint32_t u = 0; u < E / 2; ++u) {
+                        const double2 a = px[u], b = pw[u];
+                        vx[2 * u] = a.x;
+                        vx[2 * u + 1] = a.y;
+                        vw[2 * u] = b.x;
+                        vw[2 * u + 1] = b.y;
+                    }
+                } else {
+#pragma unroll
+                    for (uint32_t u = 0; u < E; ++u) {
+                        vx[u] = k + u < len ? x[k0 + k + u] : 0.0;
+                        vw[u] = k + u < len ? wts[k0 + k + u] : 0.0;
+                    }
                 }
-            } else {
 #pragma unroll
                 for (uint32_t u = 0; u < E; ++u) {
-                    vx[u] = k + u < len ? x[k0 + k + u] : 0.0;
-                    vw[u] = k + u < len ? wts[k0 + k + u] : 0.0;
+                    s_x[u * NT + tg] = scaled ? vx[u] * rc : vx[u];
+                    s_w[u * NT + tg] = vw[u];
                 }
             }
-#pragma unroll
-            for (uint32_t u = 0; u < E; ++u) {
-                s_x[u * NT + tg] = vx[u];
-                s_w[u * NT + tg] = vw[u];
-            }
+            chain_detail::group_bar(1 + (int)side, kChainWarps * 32);
+            sum = group_fma_chain<kChainWarps, kChainSteps, true, true>(s_x, s_w, len, sum, side * kChainWarps,
+                                                                        1 + (int)side, s_chain[side],
+                                                                        k0 == 0 ? 32u : 0u);
         }
-        chain_detail::group_bar(1 + (int)side, kChainWarps * 32);
-        sum = group_fma_chain<kChainWarps, kChainSteps, true, true>(s_x, s_w, len, sum, side * kChainWarps,
-                                                                    1 + (int)side, s_chain[side], k0 == 0 ? 32u : 0u);
+        return sum;
+    };
+    const bool defer = (R.flags & kDeferNorm) != 0;
+    if (defer) {
+        const double sum = side_sum(side == 0 ? R.norm_pos : R.norm_neg, false, 1.0);
+        if (tg == 0 && side < S) s_sum[side] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
+            const double recip = 1.0 / norm;
+            R.recip[i] = recip;
+            s_recip = recip;
+            if (recip != 1.0) R.changed[i] = 1;
+        }
+        __syncthreads();
     }
-    if (tg == 0 && side < S) s_sum[side] = sum;
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    const double norm = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, R.alpha, S == 2);
-    const double recip = 1.0 / norm;
-    R.recip[i] = recip;
-    if (recip != 1.0) R.changed[i] = 1;
+    // moment row sums with alpha = 1 (deac.cpp:1418-1477), of the trial as
+    // it is kept: normalised when the run normalises
+    const double rc = defer ? s_recip : 1.0;
+    for (int which = 0; which < 2; ++which) {
+        const uint32_t flag = which == 0 ? kFirstMoment : kThirdMoment;
+        if (!(R.flags & flag)) continue;
+        const double* wp = which == 0 ? R.first_pos : R.third_pos;
+        const double* wn = which == 0 ? R.first_neg : R.third_neg;
+        const double sum = side_sum(side == 0 ? wp : wn, defer, rc);
+        if (tg == 0 && side < S) s_sum[side] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) R.moments[2 * i + which] = gemv_pair(s_sum[0], S == 2 ? s_sum[1] : 0.0, 1.0, S == 2);
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------- contract
@@ -871,18 +899,25 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
                 const double term = (R.negfirst_target - mom) / R.negfirst_error;
                 fit = fma(term, term, fit);
             }
+            // the split engine keeps its parents' moments apart from the
+            // trials' (an interval-accepted parent is evaluated again later)
+            const double* mom = fit_parent && R.pmoments && fmode != kModeInit ? R.pmoments : R.moments;
             if (R.flags & kFirstMomentCpu) {
                 // the CPU build's term (deac.cpp:969): a rounded square, a
                 // rounded quotient and a rounded sum
-                const double d = R.moments[2 * m] - R.first_target;
+                const double d = mom[2 * m] - R.first_target;
                 fit = fit + (d * d) / R.first_target;
             } else if (R.flags & kFirstMoment) {
-                const double term = (R.first_target - R.moments[2 * m]) / 1.0;
+                const double term = (R.first_target - mom[2 * m]) / 1.0;
                 fit = fma(term, term, fit);
             }
             if (R.flags & kThirdMoment) {
-                const double term = (R.third_target - R.moments[2 * m + 1]) / R.third_error;
+                const double term = (R.third_target - mom[2 * m + 1]) / R.third_error;
                 fit = fma(term, term, fit);
+            }
+            if (fmode == kModeInit && R.pmoments) {
+                R.pmoments[2 * m] = R.moments[2 * m];
+                R.pmoments[2 * m + 1] = R.moments[2 * m + 1];
             }
             fit_dst[m] = fit;
             if (fit_parent && R.f_lo) R.f_lo[m] = R.f_hi[m] = fit;  // now exact
@@ -908,6 +943,10 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
             if (fn <= R.fit_old[m]) {
                 R.fit_old[m] = fn;
                 if (R.f_lo) R.f_lo[m] = R.f_hi[m] = fn;
+                if (R.pmoments) {
+                    R.pmoments[2 * m] = R.moments[2 * m];
+                    R.pmoments[2 * m + 1] = R.moments[2 * m + 1];
+                }
                 for (uint32_t s = 0; s < S; ++s) {
                     R.cr[s * P + m] = R.cr[(uint64_t)S * P + s * P + m];
                     R.fw[s * P + m] = R.fw[(uint64_t)S * P + s * P + m];

@@ -87,7 +87,8 @@ struct RunDev {
     double* fit_new;         // [P]
     double* model_isf;       // [P][Nt]
     double* model_isf2;      // [P][Nt] kModeRecheck: the trials' (model_isf holds the parents')
-    double* moments;         // [P][2]: first, third
+    double* moments;         // [P][2]: first, third (of the trials, in the split engine)
+    double* pmoments;        // split engine: [P][2] of the parents (null in the plain engine)
     double* stats;           // [mean|minimum|squared mean][N]
     double* trace;           // [trace_cap][P]
     uint64_t trace_cap;
@@ -231,9 +232,9 @@ __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const PartWork* work);
 // the same for batches that draw from counter streams
 __global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
-// split engine, kDeferNorm runs: the exact normalisation row sums of one raw
-// trial per CTA (both sides), the reciprocal norm and the final `changed`
-// flag
+// split engine, runs that normalise (kDeferNorm) or have moment terms: the
+// exact normalisation row sums of one raw trial per CTA (both sides), the
+// reciprocal norm and the final `changed` flag, then its moment row sums
 constexpr int kNormThreads = 2 * kChainWarps * 32;
 constexpr uint32_t kNormStage = kChainWarps * 32 * kChainSteps;  // steps staged in shared memory at a time
 constexpr uint32_t kNormSmemBytes = 2 * 2 * kNormStage * sizeof(double);  // dynamic shared memory of norm_kernel

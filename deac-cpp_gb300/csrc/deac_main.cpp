@@ -74,7 +74,7 @@ const std::vector<Option>& options() {
         {"", "--bosonic", "One-sided genome with the bosonic detailed-balance kernel (spectra_type bdsf).", "false", true},
         {"", "--allow_negative_spectral_weight", "Do not take the absolute value of mutant genes.", "false", true},
         {"", "--device", "CUDA device to run on.", "0", false},
-        {"", "--engine", "Evaluation engine: plain (FP64 throughout) or split (tensor-core contraction with exact FP64 decisions; genome_size a multiple of 32, no moment terms).", "plain", false},
+        {"", "--engine", "Evaluation engine: plain (FP64 throughout) or split (tensor-core contraction with exact FP64 decisions; genome_size a multiple of 32).", "plain", false},
         {"", "--first_moment_formula", "First-moment fitness term: gpu ((m - m_i)/1.0)^2, the reference's GPU build, or cpu (m_i - m)^2/m, its CPU build.", "gpu", false},
         {"", "--streams", "Random draws: reference (the reference's per-gene generator states, its draws bit for bit) or counter (compact counter streams for large batches; both engines agree).", "reference", false},
     };

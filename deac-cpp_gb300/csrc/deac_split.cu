@@ -560,7 +560,9 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const uint32_t i = wk.index;
     const uint32_t P = R.P, Nt = R.Nt, S = R.S, M = R.M;
     const bool defer = (R.flags & kDeferNorm) != 0;
-    const bool force_exact = (R.flags & kTrackStats) != 0;
+    // statistics need every parent's exact fitness; the negative first
+    // moment is formed from the model ISF itself: both decided exactly
+    const bool force_exact = (R.flags & (kTrackStats | kNegativeFirstMoment)) != 0;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     constexpr uint32_t kJdeThread = kSelectThreads - 32;
     // read by every thread before thread 0 may change them, in one round
@@ -578,6 +580,9 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     // the decision's other operands (thread 0)
     const double f_lo0 = tid == 0 ? X.f_lo[i] : 0.0, f_hi0 = tid == 0 ? X.f_hi[i] : 0.0;
     const double inv_nt = tid == 0 ? X.inv_nt : 0.0, stop = tid == 0 ? R.stop : 0.0;
+    // the trial's exact moments (norm_kernel) for the moment terms
+    const double mom1 = tid == 0 && (R.flags & kFirstMoment) ? R.moments[2 * i] : 0.0;
+    const double mom3 = tid == 0 && (R.flags & kThirdMoment) ? R.moments[2 * i + 1] : 0.0;
     const float inv_nt_up = tid == 0 ? X.inv_nt_up : 0.0f;
     double cr_t[2] = {0.0, 0.0}, fw_t[2] = {0.0, 0.0};  // the trial's CR / F, kept on acceptance
     if (tid == 0) {
@@ -751,7 +756,24 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             // quotient has one, covered by two more units of the slack below
             chi *= inv_nt;
             const double dchi_d = (double)__fmul_ru(dchi, inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
-            const double lo = chi - dchi_d, hi = chi + dchi_d;
+            double lo = chi - dchi_d, hi = chi + dchi_d;
+            // the moment terms, exact (norm_kernel's sums equal trial_kernel's),
+            // added as contract_kernel adds them: each step is monotone in the
+            // fitness so far, so the interval's ends map to the ends
+            if (R.flags & kFirstMomentCpu) {
+                const double d = mom1 - R.first_target, q = (d * d) / R.first_target;
+                lo = lo + q;
+                hi = hi + q;
+            } else if (R.flags & kFirstMoment) {
+                const double t1 = (R.first_target - mom1) / 1.0;
+                lo = fma(t1, t1, lo);
+                hi = fma(t1, t1, hi);
+            }
+            if (R.flags & kThirdMoment) {
+                const double t3 = (R.third_target - mom3) / R.third_error;
+                lo = fma(t3, t3, lo);
+                hi = fma(t3, t3, hi);
+            }
             X.t_lo[i] = lo;
             X.t_hi[i] = hi;
             int outcome;
@@ -763,6 +785,10 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
                 X.f_hi[i] = hi;
                 fit_kept = 0.5 * (lo + hi);
                 R.fit_old[i] = fit_kept;
+                if (R.flags & (kFirstMoment | kThirdMoment)) {
+                    R.pmoments[2 * i] = mom1;
+                    R.pmoments[2 * i + 1] = mom3;
+                }
 #pragma unroll
                 for (uint32_t s = 0; s < 2; ++s)
                     if (s < S) {

@@ -67,7 +67,9 @@ extern "C" {
  *              decisions that bound leaves open are settled by the FP64
  *              chains.  Selection, generation count, minimum fitness and
  *              spectrum are identical to PLAIN_FP64.  Needs genome_size a
- *              multiple of 32 and no moment terms. */
+ *              multiple of 32.  First and third moment terms enter the
+ *              interval decisions exactly; runs with the negative first
+ *              moment or statistics are decided by the FP64 chains. */
 #define DEAC_ENGINE_PLAIN_FP64 0
 #define DEAC_ENGINE_SPLIT_BF16 1
 

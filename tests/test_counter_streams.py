@@ -132,8 +132,8 @@ def test_counter_streams_plain_matches_oracle_and_split_matches_plain(engine, or
     assert np.array_equal(plain["fitness"], ref["fitness"])
     for k in ("stats_mean", "stats_minimum", "stats_squared_mean"):
         assert np.array_equal(plain[k], ref[k]), k
-    if m % 32 or cfg.first_moment >= 0 or cfg.third_moment >= 0:
-        return  # the split engine needs M a multiple of 32 and no moment terms
+    if m % 32:
+        return  # the split engine needs M a multiple of 32
     split = _run(engine, engine.ENGINE_SPLIT_BF16, cfg, data, freq, n, False)
     for k in ("generation", "minimum_fitness", "best_index"):
         assert split[k] == plain[k], k

@@ -143,12 +143,41 @@ def test_split_ragged_batch_with_normalization(engine):
 
 
 def test_split_rejects_unsupported(engine):
-    cfg = engine.make_config(temperature=1.35, spectra_type="bfull", population_size=8, number_of_generations=10,
-                             first_moment=1.0)
+    cfg = engine.make_config(temperature=1.35, spectra_type="bfull", population_size=8, number_of_generations=10)
     tau, isf, err = config0_data(1)
     with engine.Batch(engine=engine.ENGINE_SPLIT_BF16) as b:
-        with pytest.raises(engine.DeacError):
-            b.add_run(cfg, tau, isf, err, uniform_grid(64, 64.0))
-        cfg.first_moment = -1.0
-        with pytest.raises(engine.DeacError):
+        with pytest.raises(engine.DeacError, match="multiple of 32"):
             b.add_run(cfg, tau, isf, err, uniform_grid(50, 64.0))
+
+
+# Moment terms (deac.cpp:605-924): the first and third moments of each trial
+# come from exact row sums beside the tensor cores and enter the interval
+# decision exactly; the negative first moment (from the model ISF) is decided
+# by the FP64 chains.  Every case must equal the plain engine.
+MOMENT_CASES = {
+    "first-moment": ("cfg0", 64, 64.0, 800, dict(spectra_type="bfull", first_moment=2.0)),
+    "first-moment-cpu-formula": ("cfg0", 64, 64.0, 800, dict(spectra_type="bfull", first_moment=2.0,
+                                                             first_moment_formula="cpu")),
+    "first-and-third-normalize": ("cfg0", 96, 64.0, 600, dict(spectra_type="ffull", normalize=True,
+                                                              first_moment=1.5, third_moment=50.0,
+                                                              third_moment_error=2.0)),
+    "third-moment-bosonic": ("cfg0", 64, 64.0, 600, dict(bosonic=True, third_moment=40.0, third_moment_error=3.0)),
+    "negative-first-moment": ("cfg0", 64, 64.0, 600, dict(bosonic=True, use_negative_first_moment=True)),
+    "moments-wide-genome": ("tight", 512, 512.0, 200, dict(spectra_type="bfull", population_size=32,
+                                                          first_moment=40.0, normalize=True)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MOMENT_CASES))
+def test_split_moment_terms_match_plain(name, engine):
+    kind, m, omax, n, over = MOMENT_CASES[name]
+    kw = dict(temperature=1.35, population_size=8, number_of_generations=n, seed=6, stop_minimum_fitness=1.0)
+    kw.update(over)
+    cfg = engine.make_config(**kw)
+    spec = [(cfg, _data(kind), uniform_grid(m, omax))]
+    plain = _results(engine, engine.ENGINE_PLAIN_FP64, spec)[0]
+    split = _results(engine, engine.ENGINE_SPLIT_BF16, spec)[0]
+    _same(plain, split)
+    c = split["counts"]
+    if not over.get("use_negative_first_moment"):
+        assert c["interval"] > 0, c
