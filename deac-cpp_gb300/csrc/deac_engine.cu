@@ -173,6 +173,14 @@ struct deac_batch {
     float4* d_partial = nullptr;       // partial sums of the split contraction CTAs
     uint32_t n_tiles = 0, n_split_ctas = 0;
     int sms = 0;                             // the device's multiprocessors
+    // split engine launch shapes (what deac_batch_autotune varies): trial
+    // parts per CTA, and the contraction split so that its CTAs number about
+    // split_waves x the SMs it has; the tiles before splitting kept to rebuild
+    uint32_t parts_per_cta = deac::kPartsPerCta;
+    uint32_t split_waves = 1;
+    std::vector<deac::SplitTile> tiles_host;
+    std::vector<uint32_t> tile_chunks;
+    uint64_t free_sms = 1;
     uint64_t* d_exact_list = nullptr;        // split engine: the exact pass's items
     uint32_t* d_exact_count = nullptr;
     uint32_t n_combine_tiles = 0;            // tiles split over several contraction CTAs
@@ -793,6 +801,93 @@ int make_group_planes(deac_batch* b) {
     return DEAC_OK;
 }
 
+// Split engine: the trial-part work list, up to b->parts_per_cta
+// consecutive 512-gene parts of one member per CTA.
+int build_part_work(deac_batch* b) {
+    std::vector<deac::PartWork> pw;
+    uint32_t smax = 1;
+    for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+        const RunHost& r = *b->runs[ri];
+        const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
+        smax = std::max<uint32_t>(smax, (uint32_t)r.S);
+        for (uint32_t i = 0; i < r.dev.P; ++i)
+            for (uint32_t q = 0; q < parts; q += b->parts_per_cta)
+                pw.push_back({ri, i, q, std::min<uint32_t>(b->parts_per_cta, parts - q)});
+    }
+    cudaFree(b->d_part_work);
+    b->d_part_work = nullptr;
+    b->n_part_ctas = (uint32_t)pw.size();
+    b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
+    CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::PartWork)));
+    CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
+    return DEAC_OK;
+}
+
+// Split engine: every tile's chunks split over CTAs so that the launch has
+// about split_waves x the SMs the row sums leave free (one CTA per SM: the
+// kernel uses ~214 KB of shared memory and all of TMEM); partial-sum blocks
+// only for tiles split over several CTAs (a tile with one CTA has its
+// estimates formed by that CTA).
+int build_split_work(deac_batch* b) {
+    std::vector<deac::SplitTile> tiles = b->tiles_host;
+    const std::vector<uint32_t>& tile_chunks = b->tile_chunks;
+    const uint64_t want = std::max<uint64_t>(1, b->split_waves * b->free_sms / tiles.size());
+    std::vector<deac::SplitWork> work;
+    std::vector<uint32_t> combine_tiles;
+    uint32_t blocks = 0;
+    for (uint32_t t = 0; t < tiles.size(); ++t) {
+        const uint32_t C = tile_chunks[t];
+        const uint32_t per = (uint32_t)((C + std::min<uint64_t>(want, C) - 1) / std::min<uint64_t>(want, C));
+        const uint32_t nsplit = (C + per - 1) / per;
+        tiles[t].block0 = nsplit > 1 ? blocks : ~0u;
+        tiles[t].nsplit = nsplit;
+        tiles[t].per = per;
+        for (uint32_t c0 = 0; c0 < C; c0 += per)
+            work.push_back({t, c0, std::min(C, c0 + per), nsplit > 1 ? blocks++ : ~0u});
+        if (nsplit > 1) combine_tiles.push_back(t);
+    }
+    for (void* p : {(void*)b->d_combine_tiles, (void*)b->d_tiles, (void*)b->d_split_work, (void*)b->d_partial})
+        cudaFree(p);
+    b->d_combine_tiles = nullptr;
+    b->d_tiles = nullptr;
+    b->d_split_work = nullptr;
+    b->d_partial = nullptr;
+    b->n_tiles = (uint32_t)tiles.size();
+    b->n_combine_tiles = (uint32_t)combine_tiles.size();
+    b->n_split_ctas = (uint32_t)work.size();
+    if (!combine_tiles.empty()) {
+        CUDA_TRY(cudaMalloc(&b->d_combine_tiles, combine_tiles.size() * sizeof(uint32_t)));
+        CUDA_TRY(copy(b, b->d_combine_tiles, combine_tiles.data(), combine_tiles.size() * sizeof(uint32_t),
+                      cudaMemcpyHostToDevice));
+    }
+    CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
+    CUDA_TRY(copy(b, b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&b->d_split_work, work.size() * sizeof(deac::SplitWork)));
+    CUDA_TRY(copy(b, b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&b->d_partial, std::max<uint64_t>(blocks, 1) * deac::kPartialBlock * sizeof(float4)));
+    return DEAC_OK;
+}
+
+// The shapes autotuning chose for batches of the same mix (sizes, sides and
+// row sums of their runs), for this process.
+std::mutex g_tune_mutex;
+std::map<std::string, std::pair<uint32_t, uint32_t>> g_tune_cache;
+
+std::string tune_key(const deac_batch* b) {
+    std::vector<std::string> parts;
+    for (auto& r : b->runs) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "%d/%llu/%llu/%llu/%u;", r->S, (unsigned long long)r->M, (unsigned long long)r->Nt,
+                 (unsigned long long)r->P,
+                 (unsigned)(r->dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment)));
+        parts.emplace_back(buf);
+    }
+    std::sort(parts.begin(), parts.end());
+    std::string k = std::to_string(b->kcache.size()) + "|" + std::to_string(b->streams) + "|";
+    for (auto& p : parts) k += p;
+    return k;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1002,20 +1097,8 @@ int deac_batch_setup(deac_batch* b) {
             if (!(r.dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment))) continue;
             for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
         }
-        std::vector<deac::PartWork> pw;
-        uint32_t smax = 1;
-        for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
-            const RunHost& r = *b->runs[ri];
-            const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
-            smax = std::max<uint32_t>(smax, (uint32_t)r.S);
-            for (uint32_t i = 0; i < r.dev.P; ++i)
-                for (uint32_t q = 0; q < parts; q += deac::kPartsPerCta)
-                    pw.push_back({ri, i, q, std::min<uint32_t>(deac::kPartsPerCta, parts - q)});
-        }
-        b->n_part_ctas = (uint32_t)pw.size();
-        b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
-        CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::PartWork)));
-        CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
+        int rc = build_part_work(b);
+        if (rc) return rc;
         b->n_norm_ctas = (uint32_t)nw.size();
         if (!nw.empty()) {
             CUDA_TRY(raise_smem_limit(deac::norm_kernel, deac::kNormSmemBytes));
@@ -1074,48 +1157,16 @@ int deac_batch_setup(deac_batch* b) {
             }
             rows.insert(rows.end(), grp.begin(), grp.end());
         }
-        // split every tile's chunks over CTAs so that the launch fills the
-        // SMs about once (one CTA per SM: the kernel uses ~214 KB of shared
-        // memory and all of TMEM)
-        int sms = 0;
-        CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-        // the normalisation row sums of --normalize runs run beside this
-        // kernel: leave them their SMs (up to half)
+        // the normalisation and moment row sums run beside the contraction:
+        // leave them their SMs (up to half)
         uint64_t norm_ctas = 0;
         for (auto& r : b->runs)
             if (r->dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment)) norm_ctas += r->P;
-        const uint64_t free_sms = (uint64_t)sms - std::min<uint64_t>(norm_ctas, (uint64_t)sms / 2);
-        const uint64_t want = std::max<uint64_t>(1, free_sms / tiles.size());
-        // partial-sum blocks only for tiles split over several CTAs; a tile
-        // with one CTA has its estimates formed by that CTA
-        std::vector<deac::SplitWork> work;
-        std::vector<uint32_t> combine_tiles;
-        uint32_t blocks = 0;
-        for (uint32_t t = 0; t < tiles.size(); ++t) {
-            const uint32_t C = tile_chunks[t];
-            const uint32_t per = (uint32_t)((C + std::min<uint64_t>(want, C) - 1) / std::min<uint64_t>(want, C));
-            const uint32_t nsplit = (C + per - 1) / per;
-            tiles[t].block0 = nsplit > 1 ? blocks : ~0u;
-            tiles[t].nsplit = nsplit;
-            tiles[t].per = per;
-            for (uint32_t c0 = 0; c0 < C; c0 += per)
-                work.push_back({t, c0, std::min(C, c0 + per), nsplit > 1 ? blocks++ : ~0u});
-            if (nsplit > 1) combine_tiles.push_back(t);
-        }
-        b->n_tiles = (uint32_t)tiles.size();
-        b->n_combine_tiles = (uint32_t)combine_tiles.size();
-        b->n_split_ctas = (uint32_t)work.size();
-        if (!combine_tiles.empty()) {
-            CUDA_TRY(cudaMalloc(&b->d_combine_tiles, combine_tiles.size() * sizeof(uint32_t)));
-            CUDA_TRY(copy(b, b->d_combine_tiles, combine_tiles.data(), combine_tiles.size() * sizeof(uint32_t),
-                          cudaMemcpyHostToDevice));
-        }
-        CUDA_TRY(cudaMalloc(&b->d_tiles, tiles.size() * sizeof(deac::SplitTile)));
-        CUDA_TRY(copy(b, b->d_tiles, tiles.data(), tiles.size() * sizeof(deac::SplitTile), cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMalloc(&b->d_split_work, work.size() * sizeof(deac::SplitWork)));
-        CUDA_TRY(copy(b, b->d_split_work, work.data(), work.size() * sizeof(deac::SplitWork),
-                            cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMalloc(&b->d_partial, std::max<uint64_t>(blocks, 1) * deac::kPartialBlock * sizeof(float4)));
+        b->free_sms = (uint64_t)b->sms - std::min<uint64_t>(norm_ctas, (uint64_t)b->sms / 2);
+        b->tiles_host = tiles;
+        b->tile_chunks = tile_chunks;
+        int rc = build_split_work(b);
+        if (rc) return rc;
         CUDA_TRY(cudaMalloc(&b->d_rows, rows.size() * sizeof(deac::SplitRow)));
         CUDA_TRY(copy(b, b->d_rows, rows.data(), rows.size() * sizeof(deac::SplitRow), cudaMemcpyHostToDevice));
         CUDA_TRY(raise_smem_limit(deac::split_contract_kernel, deac::split_smem_bytes(2)));
@@ -1505,6 +1556,87 @@ int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]) {
     if (b->engine != DEAC_ENGINE_SPLIT_BF16 || !b->set_up) return fail(DEAC_E_STATE, "not a set-up split batch");
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(copy(b, counts, b->runs[run]->split.counts, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return DEAC_OK;
+}
+
+int deac_batch_autotune(deac_batch* b, uint64_t generations, deac_tune_report* out) {
+    if (!b || !out) return fail(DEAC_E_INVALID, "null argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    std::memset(out, 0, sizeof *out);
+    if (b->engine != DEAC_ENGINE_SPLIT_BF16) return DEAC_OK;  // the plain engine's shapes are fixed
+    if (b->timing) return fail(DEAC_E_STATE, "disable kernel timing before autotuning");
+    CUDA_TRY(cudaSetDevice(b->device));
+    const std::string key = tune_key(b);
+    auto apply = [&](uint32_t parts, uint32_t waves) -> int {
+        if (parts == b->parts_per_cta && waves == b->split_waves) return DEAC_OK;
+        CUDA_TRY(cudaStreamSynchronize(b->stream));
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        b->parts_per_cta = parts;
+        b->split_waves = waves;
+        int rc = build_part_work(b);
+        if (rc) return rc;
+        return build_split_work(b);
+    };
+    // time `generations` real generations of the batch in the current
+    // shapes (the shapes change no result)
+    auto time_it = [&](double& ms) -> int {
+        cudaEvent_t e0 = b->ev[6], e1 = b->ev[7];
+        CUDA_TRY(cudaEventRecord(e0, b->stream));
+        int rc = deac_batch_launch(b, generations);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(e1, b->stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float f = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&f, e0, e1));
+        ms = (double)f / (double)generations;
+        return DEAC_OK;
+    };
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end() || generations == 0) {
+            const uint32_t parts = it != g_tune_cache.end() ? it->second.first : b->parts_per_cta;
+            const uint32_t waves = it != g_tune_cache.end() ? it->second.second : b->split_waves;
+            int rc = apply(parts, waves);
+            if (rc) return rc;
+            out->parts_per_cta = parts;
+            out->split_waves = waves;
+            out->from_cache = it != g_tune_cache.end() ? 1 : 0;
+            return DEAC_OK;
+        }
+    }
+    static const uint32_t kParts[] = {1, 2, 4, 8};
+    static const uint32_t kWaves[] = {1, 2, 4};
+    double best_ms = 0.0;
+    uint32_t best_parts = b->parts_per_cta, best_waves = b->split_waves;
+    // the defaults first (also warms the caches), then every other candidate
+    std::vector<std::pair<uint32_t, uint32_t>> cands{{b->parts_per_cta, b->split_waves}};
+    for (uint32_t p : kParts)
+        for (uint32_t w : kWaves)
+            if (p != b->parts_per_cta || w != b->split_waves) cands.emplace_back(p, w);
+    for (size_t k = 0; k < cands.size(); ++k) {
+        int rc = apply(cands[k].first, cands[k].second);
+        if (rc) return rc;
+        double ms = 0.0;
+        if ((rc = time_it(ms))) return rc;
+        if (k == 0) out->ms_per_generation_default = ms;
+        if (k == 0 || ms < best_ms) {
+            best_ms = ms;
+            best_parts = cands[k].first;
+            best_waves = cands[k].second;
+        }
+        out->candidates += 1;
+    }
+    int rc = apply(best_parts, best_waves);
+    if (rc) return rc;
+    out->parts_per_cta = best_parts;
+    out->split_waves = best_waves;
+    out->ms_per_generation = best_ms;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = {best_parts, best_waves};
     return DEAC_OK;
 }
 

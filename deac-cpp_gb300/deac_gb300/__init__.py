@@ -61,6 +61,19 @@ class DeacConfig(ctypes.Structure):
     ]
 
 
+class TuneReport(ctypes.Structure):
+    """Mirror of ``deac_tune_report``."""
+
+    _fields_ = [
+        ("parts_per_cta", ctypes.c_uint32),
+        ("split_waves", ctypes.c_uint32),
+        ("candidates", ctypes.c_uint32),
+        ("from_cache", ctypes.c_uint32),
+        ("ms_per_generation", ctypes.c_double),
+        ("ms_per_generation_default", ctypes.c_double),
+    ]
+
+
 class RunResult(ctypes.Structure):
     """Mirror of ``deac_run_result``."""
 
@@ -142,6 +155,7 @@ SIGNATURES = {
     "deac_batch_enable_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]),
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "deac_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(TuneReport)]),
     "deac_batch_transfer_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
                                                  ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_split_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
@@ -257,6 +271,12 @@ class Batch:
         n = ctypes.c_uint64()
         _check(self._lib.deac_batch_kernel_time(self._h, kind, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def autotune(self, generations: int = 16) -> dict:
+        """Choose the split engine's launch shapes (deac_batch_autotune)."""
+        r = TuneReport()
+        _check(self._lib.deac_batch_autotune(self._h, generations, ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in TuneReport._fields_}
 
     def transfer_bytes(self):
         """(host -> device, device -> host) bytes this batch has copied."""

@@ -253,6 +253,28 @@ int deac_batch_fetch_trace(deac_batch* b, uint32_t run, double* trial_fitness,
  * tensor-core estimate's interval, counts[2] settled by the exact FP64 value. */
 int deac_batch_split_counts(deac_batch* b, uint32_t run, uint64_t counts[3]);
 
+/* Launch shapes of the split engine that deac_batch_autotune chooses. */
+typedef struct deac_tune_report {
+    uint32_t parts_per_cta;   /* trial-part CTAs: consecutive 512-gene parts of one member */
+    uint32_t split_waves;     /* tensor-core contraction: about split_waves x SMs CTAs */
+    uint32_t candidates;      /* shapes timed (0: taken from this process's cache) */
+    uint32_t from_cache;      /* 1 when a batch of the same mix was tuned before */
+    double ms_per_generation;          /* the chosen shapes' */
+    double ms_per_generation_default;  /* the default shapes' */
+} deac_tune_report;
+
+/* Choose the split engine's launch shapes for this batch's mix of runs:
+ * after setup, time `generations` generations in each candidate shape (trial
+ * parts per CTA 1, 2, 4, 8 x contraction CTAs 1, 2, 4 waves of the SMs) and
+ * keep the fastest.  The timed generations are real generations of the runs
+ * (shapes change no result, only speed).  The choice is cached per mix (run
+ * sizes, sides and row sums) for the process: a later batch of the same mix
+ * takes it without timing, and generations == 0 applies a cached choice
+ * only.  No counterpart in the reference, whose block and stream sizes are
+ * compile-time constants (src/deac/CMakeLists.txt:86-95).  The plain engine
+ * has nothing to tune (report all zero). */
+int deac_batch_autotune(deac_batch* b, uint64_t generations, deac_tune_report* out);
+
 /* Bytes this batch has copied host -> device and device -> host so far
  * (set-up uploads, status reads, result and state fetches).  No counterpart
  * in the reference. */
