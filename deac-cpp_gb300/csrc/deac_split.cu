@@ -159,6 +159,22 @@ __device__ __forceinline__ float f32_up(double x) {
     return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
 }
 
+// A float upper bound of |x| 2^k from integer operations alone (as f32_up;
+// zero and subnormal x are bounded by 2^(k-1022)).
+__device__ __forceinline__ float f32_up_s(double x, int k) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    const int ef = (int)(b >> 52);
+    if (ef == 0) {
+        const int e = k - 1022 + 127;
+        if (e >= 255) return __uint_as_float(0x7f800000u);
+        return e <= 0 ? 0x1p-126f : __uint_as_float((uint32_t)e << 23);
+    }
+    const int e = ef - 1023 + k + 127;
+    if (e >= 255) return __uint_as_float(0x7f800000u);
+    if (e <= 0) return 0x1p-126f;
+    return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
+}
+
 __device__ __forceinline__ float exp2_int(int n) {  // 2^n for -126 <= n <= 127
     return __uint_as_float((uint32_t)(n + 127) << 23);
 }
@@ -198,7 +214,8 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
     // |sum| is at most 64 B in general; when every product is >= 0 the
     // partial sums are at most the value itself, bounded by E' below.
     const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
-    const double e = (double)hi + (double)lo;
+    // (hi, lo) count in units of 2^emax (the fold's scaling)
+    const double e = ldexp((double)hi + (double)lo, emax);
     const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
     double eb;
     if (R.flags & kNonNegProducts) {
@@ -207,9 +224,16 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
     } else {
         eb = bsum * (gen + M * 0x1p-47 + 0x1p-46);
     }
+    // Absolute terms: subnormal roundings of the scaled chunk sums (2^-149
+    // each, a few per chunk, in units of 2^emax), and the values below the
+    // double's normal range, which the digits drop: at most M genes or K
+    // entries per output, each product below 2^-1022 times the other
+    // operand's largest scale.
+    const double absolute = ldexp((C + ks + 10.0) * 0x1p-140, emax) + ldexp(M, X.xexp_max[rw.member] - 1022) +
+                            ldexp(M, X.kexp_max[t] - 1022);
     const uint64_t o = (uint64_t)rw.member * R.Nt + t;
     X.e_mp[o] = e;
-    X.e_bound[o] = eb * (1.0 + 0x1p-40) + (C + ks + 10.0) * 0x1p-140;
+    X.e_bound[o] = eb * (1.0 + 0x1p-40) + absolute * (1.0 + 0x1p-40);
 }
 
 // ----------------------------------------------------- split contraction
@@ -423,8 +447,11 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
                 }
                 float hi, lo;
                 fast_two_sum(sh, sl, hi, lo);
-                // weight of the lowest kept group: 2^(e_x + e_K - 56)
-                const int k = s_ex[r] + ek - 7 * (kKept + 1);
+                // weight of the lowest kept group, 2^(e_x + e_K - 56), in
+                // units of the output's largest scale 2^(max_x + max_K): the
+                // accumulators stay inside the FP32 range whatever the
+                // magnitude of K (e^{-tau omega} spans hundreds of binades)
+                const int k = (s_ex[r] - s_xmax[r]) + (ek - s_kmax[tl]) - 7 * (kKept + 1);
                 if (k > 50) {  // beyond any sane data: make the estimate unusable
                     hi = __int_as_float(0x7fc00000);
                     lo = 0.0f;
@@ -575,6 +602,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const double em0 = t0_ok ? X.e_mp[o0] : 0.0, eb00 = t0_ok ? X.e_bound[o0] : 0.0;
     const double f0 = t0_ok ? R.isf[tid] : 0.0, ie0 = t0_ok ? X.inv_err[tid] : 0.0;
     const float ief0 = t0_ok ? X.inv_err_up[tid] : 0.0f;
+    const int iek0 = t0_ok ? X.inv_err_exp[tid] : 0;
     const uint64_t ii0 = tid == 0 ? R.ii : 0;  // changed only by the run's bookkeeping below
     double fit_kept = tid == 0 ? R.fit_old[i] : 0.0;  // the member's fitness after the selection
     // the decision's other operands (thread 0)
@@ -720,23 +748,26 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         // FP32 operands taken as upper bounds by integer operations
         double chi = 0.0;
         float dchi = 0.0f;
-        auto term = [&](double em, double eb0, double f, double ie, float ief) {
+        // 1/sigma is carried as ief 2^iek (ief in [1, 2]): the bound's
+        // E-unit quantities are scaled by 2^iek before they become floats,
+        // so neither side leaves the FP32 range however small sigma is
+        auto term = [&](double em, double eb0, double f, double ie, float ief, int iek) {
             const double e = defer ? em * rc : em;
             // r carries up to three roundings of 2^-53 each
             const double r = (f - e) * ie;
             chi = fma(r, r, chi);
             const float ar = f32_up(r);
-            const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up(eb0)), rc_up),
-                                               __fmul_ru(f32_up(e), 0x1.0p-51f))
-                                   : f32_up(eb0);
+            const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up_s(eb0, iek)), rc_up),
+                                               __fmul_ru(f32_up_s(e, iek), 0x1.0p-51f))
+                                   : f32_up_s(eb0, iek);
             const float dr =
                 __fadd_ru(__fmul_ru(__fmul_ru(eb, ief), 1.0f + 0x1.0p-20f), __fmul_ru(ar, 0x1.0p-51f));
             dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
         };
-        if (t0_ok) term(em0, eb00, f0, ie0, ief0);
+        if (t0_ok) term(em0, eb00, f0, ie0, ief0, iek0);
         for (uint32_t t = tid + kChiThreads; t < Nt; t += kChiThreads) {
             const uint64_t o = (uint64_t)i * Nt + t;
-            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], X.inv_err_up[t]);
+            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], X.inv_err_up[t], X.inv_err_exp[t]);
         }
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);

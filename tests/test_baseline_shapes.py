@@ -15,6 +15,9 @@ the same runs, at:
   three peaks, sigma = 1e-5 F): the trial kernel's global-memory path
   (S*M beyond its shared-memory cap), 128 shared-memory stages, two
   128-timeslice tiles of the tensor-core contraction;
+* a run of the batched split configuration (N_tau = 512, M = 16384 on
+  [0, 1024], P = 64, sigma = 1e-5 F): four 128-timeslice tiles, K values
+  down to e^{-760};
 * a non-uniform frequency grid (trapezoid weights, deac.cpp:351-358).
 
 Reference loops: deac.cpp:1137-1574 (generation), deac_gpu.cu:277-315
@@ -45,6 +48,11 @@ CASES = {
     "cfg2": ("cfg2", ("uniform", 16384, 512.0), 12, dict(spectra_type="bfull", population_size=64)),
     "cfg2-normalize": ("cfg2", ("uniform", 16384, 512.0), 8,
                        dict(spectra_type="bfull", population_size=64, normalize=True)),
+    # the batched split configuration's runs: N_tau = 512, M = 16384 on
+    # [0, 1024], P = 64, a random mixture of 1-4 peaks up to omega = 800,
+    # sigma = 1e-5 F (the ISF falls by ~11 decades towards mid-tau), K down
+    # to e^{-760}
+    "cfg4-run": ("cfg4", ("uniform", 16384, 1024.0), 4, dict(spectra_type="bfull", population_size=64)),
     "nonuniform-grid": ("cfg0", ("quadratic", 512, 64.0), 300, dict(spectra_type="bfull", normalize=True)),
     "nonuniform-grid-bosonic": ("cfg0", ("quadratic", 256, 64.0), 300, dict(bosonic=True)),
 }
@@ -56,7 +64,13 @@ def _setup(engine, name):
               track_stats=True)
     kw.update(over)
     cfg = engine.make_config(**kw)
-    data = {"cfg0": config0_data, "cfg1": config1_data, "cfg2": config2_data}[kind](5)
+    if kind == "cfg4":
+        from deac_gb300.data import config4_runs
+        tau, _, runs = config4_runs(3)
+        _, isf, err = runs[2]
+        data = (tau, isf, err)
+    else:
+        data = {"cfg0": config0_data, "cfg1": config1_data, "cfg2": config2_data}[kind](5)
     freq = uniform_grid(m, omax) if grid == "uniform" else _quadratic_grid(m, omax)
     return cfg, data, freq, n
 
