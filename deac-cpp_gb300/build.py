@@ -1,8 +1,9 @@
 """Build the GB300 DEAC engine in-tree.
 
 Produces, under deac-cpp_gb300/:
-  lib/libdeac_gb300.so   the C-ABI library (include/deac_gb300.h)
-  bin/deac.e             the deac.e command-line front end
+  lib/libdeac_gb300.so        the C-ABI library (include/deac_gb300.h)
+  lib/libdeac_gb300_debug.so  test aids (include/deac_gb300_debug.h)
+  bin/deac.e                  the deac.e command-line front end
 
 Device code is compiled for sm_103a only, with --fmad=false (every fused
 multiply-add in the kernels is an explicit fma()), host code with
@@ -22,6 +23,7 @@ REPO = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "libdeac_gb300.so"
+DEBUG_LIB = PKG / "lib" / "libdeac_gb300_debug.so"  # test aids (deac_debug.cu), apart from the engine
 EXE = PKG / "bin" / "deac.e"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -67,9 +69,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
     if ptxas_verbose:
         cu_flags += ["-Xptxas", "-v"]
     objs, cmds = [], []
+    debug_obj = BUILD / "deac_debug.o"
     for src in sorted(CSRC.glob("*.cu")):
         obj = BUILD / (src.stem + ".o")
-        objs.append(obj)
+        if obj != debug_obj:
+            objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmds.append([nv] + cu_flags + ["-c", str(src), "-o", str(obj)])
     host_srcs = [CSRC / "deac_model.cpp"]
@@ -83,8 +87,12 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
         for c in cmds:
             print("$", " ".join(c))
     _run_all(cmds)
+    links = []
     if force or cmds or _stale(LIB, objs):
-        _run_all([[nv] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lpthread"]])
+        links.append([nv] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lpthread"])
+    if force or _stale(DEBUG_LIB, [debug_obj]):
+        links.append([nv] + ARCH + ["-shared", "-o", str(DEBUG_LIB), str(debug_obj)])
+    _run_all(links)
     main_src = CSRC / "deac_main.cpp"
     if force or _stale(EXE, [main_src, LIB, REPO / "include" / "deac_gb300.h"]):
         _run_all([["g++", "-O2", "-std=c++17", "-Wall"] + inc + [str(main_src), "-o", str(EXE),

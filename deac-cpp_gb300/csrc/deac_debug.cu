@@ -1,7 +1,9 @@
-// deac_debug.cu -- test aids (include/deac_gb300_debug.h).
+// deac_debug.cu -- test aids (include/deac_gb300_debug.h), built into their
+// own library (lib/libdeac_gb300_debug.so), not into the engine's.
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <string>
 
 #include "deac_chain.cuh"
 #include "deac_gb300.h"
@@ -9,8 +11,16 @@
 #include "deac_kernels.cuh"
 
 namespace deac {
-__attribute__((visibility("hidden"))) int set_error(int code, const char* msg);
+namespace {
+thread_local std::string g_debug_error;
+int set_error(int code, const char* msg) {
+    g_debug_error = msg;
+    return code;
 }
+}  // namespace
+}  // namespace deac
+
+extern "C" const char* deac_debug_last_error(void) { return deac::g_debug_error.c_str(); }
 
 namespace {
 

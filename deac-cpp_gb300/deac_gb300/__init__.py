@@ -21,6 +21,7 @@ import numpy as np
 
 PKG = Path(__file__).resolve().parents[1]
 LIB_PATH = PKG / "lib" / "libdeac_gb300.so"
+DEBUG_LIB_PATH = PKG / "lib" / "libdeac_gb300_debug.so"
 EXE_PATH = PKG / "bin" / "deac.e"
 
 MODEL = {"standard": 0, "hyperbolic": 1, "normalization": 2}
@@ -184,6 +185,16 @@ def load_library(path: Path = LIB_PATH):
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    return lib
+
+
+def load_debug_library(path: Path = DEBUG_LIB_PATH):
+    """The test aids' library (include/deac_gb300_debug.h); not the engine."""
+    if not Path(path).exists():
+        raise RuntimeError(f"{path} is not built; run `python deac-cpp_gb300/build.py`")
+    lib = ctypes.CDLL(str(path))
+    lib.deac_debug_last_error.restype = ctypes.c_char_p
+    lib.deac_debug_last_error.argtypes = []
     return lib
 
 

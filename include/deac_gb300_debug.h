@@ -1,5 +1,6 @@
 /*
- * deac_gb300_debug.h -- test aids of the GB300 DEAC engine.  Not part of the
+ * deac_gb300_debug.h -- test aids of the GB300 DEAC engine, in their own
+ * library (lib/libdeac_gb300_debug.so).  Not part of the
  * drop-in boundary (include/deac_gb300.h) and with no counterpart in the
  * reference: they expose single device routines so that tests can check
  * them on inputs the full engine would rarely produce.
@@ -20,6 +21,9 @@ extern "C" {
  * synchronous.  Returns 0 or a DEAC_E_* code. */
 int deac_debug_fma_chains(const double* x, const double* w, uint64_t n, const double* start, uint32_t count,
                           double* fast_out, double* plain_out);
+
+/* Message for the last failing call of this library on this thread. */
+const char* deac_debug_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -74,3 +74,16 @@ def test_defaults_match_reference_cli(engine):
     assert (c.differential_weight, c.self_adapting_differential_weight_probability) == (0.9, 0.1)
     assert (c.stop_minimum_fitness, c.first_moment, c.third_moment) == (1.0, -1.0, -1.0)
     assert c.spectra_type == engine.SPECTRA["spfsf"]
+
+
+def test_test_aids_live_in_their_own_library(engine):
+    """The debug hooks (include/deac_gb300_debug.h) are not linked into the
+    engine's library; their own library exports them."""
+    out = subprocess.run(["nm", "-D", "--defined-only", str(engine.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    assert "deac_debug_" not in out
+    dbg = subprocess.run(["nm", "-D", "--defined-only", str(engine.DEBUG_LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    for name in ("deac_debug_fma_chains", "deac_debug_last_error"):
+        assert name in dbg
+    engine.load_debug_library()

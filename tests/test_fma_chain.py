@@ -86,7 +86,7 @@ def _chains(kind, n, count, rng):
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 7, 256, 257, 4096, 5000, 12288])
 def test_warp_chain_matches_sequential_fma(engine, n):
-    lib = engine.load_library()
+    lib = engine.load_debug_library()
     fn = lib.deac_debug_fma_chains
     dp = ctypes.POINTER(ctypes.c_double)
     fn.restype = ctypes.c_int
@@ -98,6 +98,6 @@ def test_warp_chain_matches_sequential_fma(engine, n):
         plain = np.zeros(len(start))
         p = lambda a: a.ctypes.data_as(dp)
         rc = fn(p(x), p(w), n, p(start), len(start), p(fast), p(plain))
-        assert rc == 0, lib.deac_last_error().decode()
+        assert rc == 0, lib.deac_debug_last_error().decode()
         same = (fast.view(np.uint64) == plain.view(np.uint64)) | (np.isnan(fast) & np.isnan(plain))
         assert same.all(), (kind, np.flatnonzero(~same)[:5], fast[~same][:3], plain[~same][:3])
