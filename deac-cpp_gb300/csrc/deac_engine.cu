@@ -86,14 +86,6 @@ cudaError_t raise_smem_limit(Kernel kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-// smallest float >= |v| (infinity beyond the float range)
-float float_up(double v) {
-    v = std::fabs(v);
-    float f = (float)v;
-    if ((double)f < v) f = std::nextafter(f, std::numeric_limits<float>::infinity());
-    return f;
-}
-
 struct Arena {
     uint64_t size = 0;
     uint64_t take(uint64_t bytes) {
@@ -641,8 +633,7 @@ int upload_run(deac_batch* b, RunHost& r) {
         const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
         const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
         const uint64_t o_cnt = sa.take(3 * 8);
-        const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8), o_ief = sa.take(Nt * 4);
-        const uint64_t o_iek = sa.take(Nt * 2);
+        const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8);
         const uint64_t o_pm = sa.take(2 * P * 8);
         CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
         CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
@@ -667,26 +658,12 @@ int upload_run(deac_batch* b, RunHost& r) {
         {
             // 1/sigma as the decisions use it, and float upper bounds for
             // their error bounds
-            // 1/sigma as ief 2^iek with ief a float upper bound in [1, 2]
-            // (sigma may be far below the float range: F spans hundreds of
-            // binades when the spectrum reaches high frequencies)
+            // 1/sigma as the decisions use it
             std::vector<double> ie(Nt);
-            std::vector<float> ief(Nt);
-            std::vector<int16_t> iek(Nt);
-            for (uint64_t t = 0; t < Nt; ++t) {
-                ie[t] = 1.0 / r.err[t];
-                const int k = std::isfinite(ie[t]) && ie[t] > 0.0 ? std::ilogb(ie[t]) : 0;
-                iek[t] = (int16_t)k;
-                ief[t] = float_up(std::ldexp(ie[t], -k));
-            }
+            for (uint64_t t = 0; t < Nt; ++t) ie[t] = 1.0 / r.err[t];
             CUDA_TRY(copy(b, sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
-            CUDA_TRY(copy(b, sb + o_ief, ief.data(), Nt * 4, cudaMemcpyHostToDevice));
-            CUDA_TRY(copy(b, sb + o_iek, iek.data(), Nt * 2, cudaMemcpyHostToDevice));
             x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
-            x.inv_err_up = reinterpret_cast<const float*>(sb + o_ief);
-            x.inv_err_exp = reinterpret_cast<const int16_t*>(sb + o_iek);
             x.inv_nt = 1.0 / (double)Nt;
-            x.inv_nt_up = float_up(x.inv_nt);
         }
         d.changed = x.changed;
         d.xexp = x.xexp;

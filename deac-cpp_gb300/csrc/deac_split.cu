@@ -147,34 +147,6 @@ __device__ __forceinline__ void dw_add(float& ah, float& al, float bh, float bl)
     fast_two_sum(vh, vl, ah, al);
 }
 
-// A float upper bound of |x| from integer operations alone (the FP64 pipe is
-// the scarce one): the leading 24 bits of |x| truncated, plus one unit in the
-// last place; 2^-126 below the float normal range, infinity above it (and
-// for NaN, which the FP64 part of the decision rejects on its own).
-__device__ __forceinline__ float f32_up(double x) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-    const int e = (int)(b >> 52) - 1023 + 127;
-    if (e >= 255) return __uint_as_float(0x7f800000u);
-    if (e <= 0) return 0x1p-126f;
-    return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
-}
-
-// A float upper bound of |x| 2^k from integer operations alone (as f32_up;
-// zero and subnormal x are bounded by 2^(k-1022)).
-__device__ __forceinline__ float f32_up_s(double x, int k) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-    const int ef = (int)(b >> 52);
-    if (ef == 0) {
-        const int e = k - 1022 + 127;
-        if (e >= 255) return __uint_as_float(0x7f800000u);
-        return e <= 0 ? 0x1p-126f : __uint_as_float((uint32_t)e << 23);
-    }
-    const int e = ef - 1023 + k + 127;
-    if (e >= 255) return __uint_as_float(0x7f800000u);
-    if (e <= 0) return 0x1p-126f;
-    return __uint_as_float((((uint32_t)e << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu)) + 1u);
-}
-
 __device__ __forceinline__ float exp2_int(int n) {  // 2^n for -126 <= n <= 127
     return __uint_as_float((uint32_t)(n + 127) << 23);
 }
@@ -577,7 +549,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     grid_dependency_wait();
     constexpr uint32_t kChiWarps = 4, kChiThreads = kChiWarps * 32;
     __shared__ double s_chi[kChiWarps];
-    __shared__ float s_dchi[kChiWarps];
+    __shared__ double s_dchi[kChiWarps];
     __shared__ int s_outcome;
     enum { kReject = 0, kAccept = 1, kRecheck = 2, kSame = 3 };
     const Work wk = work[blockIdx.x];
@@ -601,8 +573,6 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     const uint64_t o0 = (uint64_t)i * Nt + tid;
     const double em0 = t0_ok ? X.e_mp[o0] : 0.0, eb00 = t0_ok ? X.e_bound[o0] : 0.0;
     const double f0 = t0_ok ? R.isf[tid] : 0.0, ie0 = t0_ok ? X.inv_err[tid] : 0.0;
-    const float ief0 = t0_ok ? X.inv_err_up[tid] : 0.0f;
-    const int iek0 = t0_ok ? X.inv_err_exp[tid] : 0;
     const uint64_t ii0 = tid == 0 ? R.ii : 0;  // changed only by the run's bookkeeping below
     double fit_kept = tid == 0 ? R.fit_old[i] : 0.0;  // the member's fitness after the selection
     // the decision's other operands (thread 0)
@@ -611,7 +581,6 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     // the trial's exact moments (norm_kernel) for the moment terms
     const double mom1 = tid == 0 && (R.flags & kFirstMoment) ? R.moments[2 * i] : 0.0;
     const double mom3 = tid == 0 && (R.flags & kThirdMoment) ? R.moments[2 * i + 1] : 0.0;
-    const float inv_nt_up = tid == 0 ? X.inv_nt_up : 0.0f;
     double cr_t[2] = {0.0, 0.0}, fw_t[2] = {0.0, 0.0};  // the trial's CR / F, kept on acceptance
     if (tid == 0) {
 #pragma unroll
@@ -742,36 +711,31 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         // two), 0.001 of it more for the per-gene roundings (at most
         // 2^-47 B while the raw bound is at least 2^-33 B), and 2^-51 |E|
         // for the product's rounding.
-        const float rc_up = f32_up(rc);
-        // chi^2 in FP64; its error bound in FP32 rounded upward (every term
-        // is non-negative, so each rounding up keeps an upper bound), the
-        // FP32 operands taken as upper bounds by integer operations
-        double chi = 0.0;
-        float dchi = 0.0f;
-        // 1/sigma is carried as ief 2^iek (ief in [1, 2]): the bound's
-        // E-unit quantities are scaled by 2^iek before they become floats,
-        // so neither side leaves the FP32 range however small sigma is
-        auto term = [&](double em, double eb0, double f, double ie, float ief, int iek) {
+        // chi^2 in FP64, and its error bound in FP64 rounded upward (every
+        // term is non-negative, so each rounding up keeps an upper bound).
+        // Early in a run with sigma far below F's scale the residuals reach
+        // 1e130 sigma and more: the bound needs the double's range.
+        const double rc_abs = fabs(rc);
+        double chi = 0.0, dchi = 0.0;
+        auto term = [&](double em, double eb0, double f, double ie) {
             const double e = defer ? em * rc : em;
             // r carries up to three roundings of 2^-53 each
             const double r = (f - e) * ie;
             chi = fma(r, r, chi);
-            const float ar = f32_up(r);
-            const float eb = defer ? __fadd_ru(__fmul_ru(__fmul_ru(2.001f, f32_up_s(eb0, iek)), rc_up),
-                                               __fmul_ru(f32_up_s(e, iek), 0x1.0p-51f))
-                                   : f32_up_s(eb0, iek);
-            const float dr =
-                __fadd_ru(__fmul_ru(__fmul_ru(eb, ief), 1.0f + 0x1.0p-20f), __fmul_ru(ar, 0x1.0p-51f));
-            dchi = __fmaf_ru(__fadd_ru(__fmul_ru(2.0f, ar), dr), dr, dchi);
+            const double ar = fabs(r);
+            const double eb = defer ? __dadd_ru(__dmul_ru(__dmul_ru(2.001, eb0), rc_abs), __dmul_ru(fabs(e), 0x1p-51))
+                                    : eb0;
+            const double dr = __dadd_ru(__dmul_ru(__dmul_ru(eb, ie), 1.0 + 0x1p-20), __dmul_ru(ar, 0x1p-51));
+            dchi = __fma_ru(__dadd_ru(2.0 * ar, dr), dr, dchi);
         };
-        if (t0_ok) term(em0, eb00, f0, ie0, ief0, iek0);
+        if (t0_ok) term(em0, eb00, f0, ie0);
         for (uint32_t t = tid + kChiThreads; t < Nt; t += kChiThreads) {
             const uint64_t o = (uint64_t)i * Nt + t;
-            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], X.inv_err_up[t], X.inv_err_exp[t]);
+            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t]);
         }
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
-            dchi = __fadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
+            dchi = __dadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
         }
         if (lane == 0) {
             s_chi[warp] = chi;
@@ -781,13 +745,14 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         if (tid == 0) {
             // the warps' sums (any order: the bound covers it)
             chi = (s_chi[0] + s_chi[1]) + (s_chi[2] + s_chi[3]);
-            dchi = __fadd_ru(__fadd_ru(s_dchi[0], s_dchi[1]), __fadd_ru(s_dchi[2], s_dchi[3]));
+            dchi = __dadd_ru(__dadd_ru(s_dchi[0], s_dchi[1]), __dadd_ru(s_dchi[2], s_dchi[3]));
             X.recheck[i] = 0;
             // /Nt as a product with 1/Nt rounded once: two roundings where a
             // quotient has one, covered by two more units of the slack below
             chi *= inv_nt;
-            const double dchi_d = (double)__fmul_ru(dchi, inv_nt_up) + chi * (double)(Nt + 10) * 0x1p-52;
-            double lo = chi - dchi_d, hi = chi + dchi_d;
+            const double dchi_d = __dadd_ru(__dmul_ru(__dmul_ru(dchi, inv_nt), 1.0 + 0x1p-50),
+                                            __dmul_ru(__dmul_ru(chi, (double)(Nt + 10)), 0x1p-52));
+            double lo = __dsub_rd(chi, dchi_d), hi = __dadd_ru(chi, dchi_d);
             // the moment terms, exact (norm_kernel's sums equal trial_kernel's),
             // added as contract_kernel adds them: each step is monotone in the
             // fitness so far, so the interval's ends map to the ends

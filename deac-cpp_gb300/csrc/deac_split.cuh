@@ -79,10 +79,7 @@ struct SplitRun {
                                     // word) and of them left for the exact pass (high word)
     unsigned long long sel_min_bits;  // their fitness minimum (bits; all ones: none yet)
     const double* inv_err;  // [Nt] 1/sigma, rounded once
-    const float* inv_err_up;  // [Nt] float upper bounds of inv_err / 2^inv_err_exp (in [1, 2])
-    const int16_t* inv_err_exp;  // [Nt] the binade of inv_err
     double inv_nt;            // 1/Nt, rounded once
-    float inv_nt_up;          // a float upper bound of 1/Nt
 };
 
 // One output tile: up to 64 (run, member) rows sharing one K, x 128
