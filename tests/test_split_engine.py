@@ -23,6 +23,8 @@ def _data(kind, seed=1):
     if kind == "high":  # peaks up to omega = 700, sigma = 1e-5 F: F(tau) ~ 1e-100 mid-range
         return make_isf(64, 1.35, [(0.5, 700.0, 30.0), (0.3, 300.0, 20.0), (0.2, 40.0, 5.0)], 1e-5, seed,
                         omega_max_data=1500.0)
+    if kind == "only-high":  # all weight above omega = 400: F(mid tau) ~ 1e-80, residuals ~ 1e84 sigma
+        return make_isf(64, 1.35, [(0.6, 700.0, 30.0), (0.4, 500.0, 20.0)], 1e-5, seed, omega_max_data=1500.0)
     if kind == "tight":  # sigma = 1e-5 F, three peaks
         return make_isf(96, 1.35, [(0.5, 3.0, 0.5), (0.3, 40.0, 5.0), (0.2, 200.0, 30.0)], 1e-5, seed,
                         omega_max_data=512.0)
@@ -45,6 +47,7 @@ CASES = {
     # binades below the float range in mid-tau (accumulators in scaled
     # units, 1/sigma carried as a float times a power of two)
     "high-frequencies-tiny-sigma": ("high", 1024, 1024.0, 300, dict(spectra_type="bfull", population_size=16)),
+    "only-high-frequencies": ("only-high", 1024, 1024.0, 300, dict(spectra_type="bfull", population_size=16)),
     "early-stop": ("cfg0", 64, 64.0, 20000, dict(spectra_type="bfull", stop_minimum_fitness=5e4)),
     # --normalize: the trials stay raw until the decisions, their exact
     # normalisation row sums run beside the tensor-core contraction
