@@ -746,41 +746,54 @@ int make_group_planes(deac_batch* b) {
                 S = rp->S;
             }
         if (R == 0) continue;
-        const uint64_t planes = (uint64_t)deac::kDigits * S, units = M / 8;
-        CUDA_TRY(cudaMalloc(&b->group_xdig[g], planes * units * R * 8 * 2));
-        CUDA_TRY(cudaMemset(b->group_xdig[g], 0, planes * units * R * 8 * 2));
+        const uint64_t units = M / 8;
+        // trial planes [side][unit][64-row tile, half][digit][32 rows][8]
+        const uint64_t halves = 2 * ((R + deac::kRowTile - 1) / deac::kRowTile);
+        const uint64_t unit_elems = halves * deac::kDigits * deac::kHalfRows * 8;
+        const uint64_t elems = (uint64_t)S * units * unit_elems;
+        CUDA_TRY(cudaMalloc(&b->group_xdig[g], elems * 2));
+        CUDA_TRY(cudaMemset(b->group_xdig[g], 0, elems * 2));
         uint64_t row = 0;
         for (auto& rp : b->runs)
             if (rp->kgroup == g) {
-                uint16_t* x = b->group_xdig[g] + row * 8;
-                rp->split.xdig = x;
-                rp->split.xdig_unit = R * 8;
-                rp->split.xdig_plane = M * R;
-                rp->dev.xdig = x;
-                rp->dev.xdig_unit = R * 8;
-                rp->dev.xdig_plane = M * R;
+                rp->dev.xdig = b->group_xdig[g];
+                rp->dev.xdig_unit = unit_elems;
+                rp->dev.xdig_side = units * unit_elems;
+                rp->dev.xdig_row0 = (uint32_t)row;
                 row += rp->P;
             }
-        // A unit's rows (8 genes = 16 bytes each) are consecutive in memory,
-        // so the innermost dimension is all rows of a unit, in 8-byte
-        // elements (two per row): dims rows*2, units of 8 genes, planes; box:
-        // one tile's rows (128 timeslices resp. 64 trial rows) of one chunk's
-        // units of every plane -- 2 KB resp. 1 KB contiguous per line
-        auto make = [&](CUtensorMap* m, void* base, uint64_t rows, uint32_t box_rows) -> int {
-            const cuuint64_t dims[3] = {rows * 2, units, planes};
-            const cuuint64_t strides[2] = {rows * 16, units * rows * 16};
-            const cuuint32_t box[3] = {2 * box_rows, deac::kChunk / 8, (cuuint32_t)planes};
-            const cuuint32_t estr[3] = {1, 1, 1};
-            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, dims, strides, box, estr,
+        auto encode_map = [&](CUtensorMap* m, void* base, uint32_t rank, const cuuint64_t* dims,
+                              const cuuint64_t* strides, const cuuint32_t* box) -> int {
+            const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+            const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, rank, base, dims, strides, box, estr,
                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return fail(DEAC_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
             return DEAC_OK;
         };
-        int rc = make(&maps[2 * g], kms[g]->kdig, Nt, deac::kTauTile);
-        if (rc) return rc;
-        rc = make(&maps[2 * g + 1], b->group_xdig[g], R, deac::kRowTile);
-        if (rc) return rc;
+        // K: a unit's timeslices are consecutive; the innermost dimension is
+        // all of them (two 8-byte elements per 16-byte row): dims Nt*2,
+        // units, planes; box one tile of 128 timeslices, the two units of a
+        // 16-gene MMA step (one operand stage), every plane (2 KB lines)
+        {
+            const uint64_t planes = (uint64_t)deac::kDigits * S;
+            const cuuint64_t dims[3] = {Nt * 2, units, planes};
+            const cuuint64_t strides[2] = {Nt * 16, units * Nt * 16};
+            const cuuint32_t box[3] = {2 * deac::kTauTile, 2, (cuuint32_t)planes};
+            int rc = encode_map(&maps[2 * g], kms[g]->kdig, 3, dims, strides, box);
+            if (rc) return rc;
+        }
+        // trials: dims 32 rows * 2, digits, (tile, half), units, sides; box
+        // one tile's two halves of one 16-gene MMA step, every digit and side
+        // (512-byte lines)
+        {
+            const cuuint64_t dims[5] = {deac::kHalfRows * 2, deac::kDigits, halves, units, (cuuint64_t)S};
+            const cuuint64_t strides[4] = {deac::kHalfRows * 16, deac::kDigits * deac::kHalfRows * 16,
+                                           unit_elems * 2, units * unit_elems * 2};
+            const cuuint32_t box[5] = {2 * deac::kHalfRows, deac::kDigits, 2, 2, (cuuint32_t)S};
+            int rc = encode_map(&maps[2 * g + 1], b->group_xdig[g], 5, dims, strides, box);
+            if (rc) return rc;
+        }
     }
     CUDA_TRY(cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)));
     CUDA_TRY(copy(b, b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));

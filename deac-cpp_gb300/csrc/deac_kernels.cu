@@ -600,8 +600,9 @@ __device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* wo
         }
         __syncthreads();
         // (ends with a barrier after its last read of part_s)
-        digitize_trial(part_s, len, S, len, R.xdig + (uint64_t)i * 8 + (uint64_t)(j0 >> 3) * R.xdig_unit,
-                       R.xdig_plane, R.xdig_unit, R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk,
+        digitize_trial(part_s, len, S, len,
+                       R.xdig + xdig_row_offset(R.xdig_row0 + i) + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_unit,
+                       R.xdig_side, R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk,
                        R.xexp_max + i, s_digit_max);
     }
     if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;

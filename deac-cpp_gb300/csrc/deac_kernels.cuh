@@ -97,9 +97,10 @@ struct RunDev {
     const uint8_t* recheck;  // [P] decision left to the exact FP64 value
     double* f_lo;            // [P] interval holding the parent's exact fitness
     double* f_hi;
-    uint16_t* xdig;          // tiled digit planes of the trials (member 0's row)
+    uint16_t* xdig;          // digit planes of the trials of the runs sharing K (deac_split.cuh)
     uint64_t xdig_unit;      // elements between units of 8 genes
-    uint64_t xdig_plane;     // elements between planes
+    uint64_t xdig_side;      // elements between the sides
+    uint32_t xdig_row0;      // row of member 0 among the group's rows
     int16_t* xexp;           // [P][M/32] their chunk scale exponents
     int32_t* xexp_max;       // [P] their maximum (raised per part, reset after the decisions)
     uint32_t* mutants;       // [P][3] mutant indices of this generation

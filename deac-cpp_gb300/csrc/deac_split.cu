@@ -15,7 +15,6 @@ namespace {
 
 constexpr int kKept = kDigits;            // digit-pair groups a+b = 0..6 kept
 constexpr uint32_t kTmemCols = 512;       // 7 groups x 64 rows + bound x 64 rows = 512
-constexpr uint32_t kBoundCol = kKept * kRowTile;
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier waits: 2 s
 constexpr int kStatusWait = 1;             // status: a tensor-core completion wait gave up
 
@@ -69,6 +68,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
         if (global_ns() - t0 > kWaitNs) return false;
         __nanosleep(64);
     }
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t v[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                 : "r"(taddr));
 }
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
@@ -165,6 +170,14 @@ __device__ __forceinline__ void scale_pow2(float& hi, float& lo, int k) {
 
 }  // namespace
 
+// x 2^k as two multiplications by powers of two (exact but where the
+// result leaves the double's normal range; no library call)
+__device__ __forceinline__ double times_pow2(double x, int k) {
+    k = k > 2046 ? 2046 : (k < -2044 ? -2044 : k);
+    const int k1 = k / 2, k2 = k - k1;  // each in [-1022, 1023]
+    return x * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+}
+
 // The estimate of output (row rw, timeslice t) and its bound from the
 // tile's summed double-float (hi, lo) and bound accumulator b (see below).
 __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, const SplitRow rw, uint32_t t,
@@ -173,7 +186,7 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
     const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
     // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
     // below 2^-23 per addition), terms under 2^-126 dropped
-    const double bsum = ldexp(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
+    const double bsum = times_pow2(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
     // Error of the estimate against the FP64 chain value, in parts:
     //  digits: dropped digit pairs and remainders, 2^-45.9 2^(e_x+e_K) per
     //    product, 64 products a chunk:                     2^-39 B
@@ -187,7 +200,7 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
     // partial sums are at most the value itself, bounded by E' below.
     const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
     // (hi, lo) count in units of 2^emax (the fold's scaling)
-    const double e = ldexp((double)hi + (double)lo, emax);
+    const double e = times_pow2((double)hi + (double)lo, emax);
     const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
     double eb;
     if (R.flags & kNonNegProducts) {
@@ -201,32 +214,83 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
     // double's normal range, which the digits drop: at most M genes or K
     // entries per output, each product below 2^-1022 times the other
     // operand's largest scale.
-    const double absolute = ldexp((C + ks + 10.0) * 0x1p-140, emax) + ldexp(M, X.xexp_max[rw.member] - 1022) +
-                            ldexp(M, X.kexp_max[t] - 1022);
+    const double absolute = times_pow2((C + ks + 10.0) * 0x1p-140, emax) + times_pow2(M, X.xexp_max[rw.member] - 1022) +
+                            times_pow2(M, X.kexp_max[t] - 1022);
     const uint64_t o = (uint64_t)rw.member * R.Nt + t;
     X.e_mp[o] = e;
     X.e_bound[o] = eb * (1.0 + 0x1p-40) + absolute * (1.0 + 0x1p-40);
 }
 
 // ----------------------------------------------------- split contraction
+// Wait for the mbarrier phase with parity `phase` to complete, giving up when
+// another role of the CTA gave up (*abort) or after kWaitNs (then setting
+// *abort, which makes every role of the CTA leave its loop).
+__device__ __forceinline__ bool mbar_wait_or(uint64_t* bar, uint32_t phase, volatile int* abort) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+        if (global_ns() - t0 > kWaitNs) {
+            *abort = 1;
+            return false;
+        }
+        __nanosleep(32);
+    }
+}
+
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5, %6}], [%7];\n" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar)));
+}
+
 // One CTA per (tile, chunk range).  The tile is 128 timeslices (MMA M, one
-// TMEM lane each) x 64 trial rows (MMA N) of runs that share K.  Per 32-gene
-// chunk: stage the digit planes of both operands, issue the kept digit pairs
-// into six TMEM group accumulators plus one rank-1 MMA of the chunk scales
-// into the bound accumulator, wait, and fold the exact group sums into
-// double-float accumulators in shared memory; the next chunk's digits load
-// while the current one is folded.  The CTA ends by writing its partial sums
-// (hi, lo, bound) for the combine kernel.
+// TMEM lane each) x 64 trial rows in two halves of 32, each half with its own
+// TMEM buffer of 256 columns: seven group accumulators of 32 columns and the
+// bound accumulator.  A chunk's operands arrive in two 16-gene stages (one
+// per MMA K step), each with its own full / empty barriers.  Warp roles:
+//  producer warp: per chunk the exponents of its 128 timeslices and 64 rows
+//    and the bound operands 2^(e - max) (two buffers; written once the fold
+//    is done with the chunk two before), then per stage, once the MMAs of the
+//    chunk before are done with it, the digit planes of both operands by TMA;
+//  MMA warp (one thread): per stage and half -- the half's buffer free once
+//    the fold has read the chunk before -- for each K digit d and side one
+//    MMA over the trial digits 0..6-d (N = 32(7-d)) into groups d..6, the
+//    half's bound MMA with the second stage; commits per half (accumulators
+//    full) and per stage (operands free);
+//  16 fold warps: per half, read the seven exact group sums, release the
+//    buffer and fold the sums into double-float accumulators while the tensor
+//    cores work on the other half.
+// Every wait is bounded; a CTA that gives up reports it in *status.
 __global__ void __launch_bounds__(kSplitThreads, 1)
 split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
                       const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t s_tmem;
-    __shared__ __align__(8) uint64_t s_bar;   // MMA completion
-    __shared__ __align__(8) uint64_t s_full;  // the chunk's digit planes have landed
-    __shared__ int s_ek[kTauTile], s_kmax[kTauTile];
-    __shared__ int s_ex[kRowTile], s_xmax[kRowTile];
+    __shared__ __align__(8) uint64_t s_full[2];    // a stage's digit planes have landed
+    __shared__ __align__(8) uint64_t s_empty[2];   // the MMAs are done with a stage
+    __shared__ __align__(8) uint64_t s_scales[2];  // a chunk's exponents and bound operands are written
+    __shared__ __align__(8) uint64_t s_tfull[2];   // a half's accumulators hold the chunk's sums
+    __shared__ __align__(8) uint64_t s_tempty[2];  // the fold warps have read a half's accumulators
+    __shared__ __align__(8) uint64_t s_mma_done;   // every MMA issued has completed
+    __shared__ int s_ek[2][kTauTile], s_ex[2][kRowTile];
+    __shared__ int s_kmax[kTauTile], s_xmax[kRowTile];
     __shared__ int s_live;
+    __shared__ int s_abort;
+    __shared__ uint32_t s_armed[2];  // phases of each stage armed (arrivals made) so far
 
     const SplitWork wk = work[blockIdx.x];
     const SplitTile tile = tiles[wk.tile];
@@ -236,101 +300,80 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     const uint32_t S = R0.S, M = R0.M, Nt = R0.Nt;
     const uint32_t C = M / kChunk;
     const uint32_t tau0 = tile.tau0;
+    const uint32_t nchunks = wk.c1 - wk.c0;
+    constexpr uint32_t kProducerWarp = kFoldWarps, kMmaWarp = kFoldWarps + 1;
+    constexpr uint32_t kBufCols = 256;  // TMEM columns per half: 7 x 32 group sums, then the bound
+    constexpr uint32_t kBoundCol = kKept * kHalfRows;
 
-    // shared memory: K digits [7S planes] x (128 x 32), trial digits [7S]
-    // x (64 x 32), each plane [unit][row][8 genes] as the TMA box lands
-    // (core matrices 8 rows = 128 bytes apart, units one row block apart),
-    // and the bound operands (128 x 16) and (64 x 16)
-    const uint32_t a_tile = kTauTile * kChunk * 2;  // 8 KB
-    const uint32_t b_tile = kRowTile * kChunk * 2;  // 4 KB
-    uint8_t* sA = smem;
-    uint8_t* sB = sA + kDigits * S * a_tile;
-    uint8_t* sAb = sB + kDigits * S * b_tile;
-    uint8_t* sBb = sAb + kTauTile * 16 * 2;
-    const uint32_t stage_bytes = (uint32_t)kDigits * S * (a_tile + b_tile);
+    // shared memory: two stages of [K digits: 7S planes x 2 units x 128 x 16 B]
+    // [trials: S x 2 units x 2 halves x 7 digits x 32 x 16 B], then two
+    // buffers of the bound operands (128 x 16 and 64 x 16, canonical)
+    const uint32_t a_stage = kDigits * S * (2 * kTauTile * 16);  // 56 KB for two sides
+    const uint32_t b_stage = kDigits * S * (2 * kRowTile * 16);  // 28 KB
+    auto sA = [&](uint32_t ks) { return smem + ks * (a_stage + b_stage); };
+    auto sB = [&](uint32_t ks) { return smem + ks * (a_stage + b_stage) + a_stage; };
+    constexpr uint32_t kBoundBytes = (kTauTile + kRowTile) * 16 * 2;
+    uint8_t* const sBound = smem + 2 * (a_stage + b_stage);
+    auto sAb = [&](uint32_t buf) { return sBound + buf * kBoundBytes; };
+    auto sBb = [&](uint32_t buf) { return sBound + buf * kBoundBytes + kTauTile * 16 * 2; };
     const CUtensorMap* map_k = maps + 2 * tile.group;
     const CUtensorMap* map_x = maps + 2 * tile.group + 1;
-
-    // zero the rank-1 bound operands once (only k = 0 is written per chunk)
-    for (uint32_t e = tid; e < (kTauTile + kRowTile) * 16; e += blockDim.x)
-        reinterpret_cast<uint16_t*>(sAb)[e] = 0;
-
-    // one thread loads a chunk's planes of both operands: two TMA boxes whose
-    // innermost extent is a unit's rows, 2 KB (K) and 1 KB (trials) of
-    // consecutive bytes (timeslices beyond Nt and rows beyond the group read
-    // as zero)
-    const uint32_t a_bytes = (uint32_t)kDigits * S * a_tile, b_bytes = (uint32_t)kDigits * S * b_tile;
-    auto load_k = [&](uint32_t c) { tma_load_3d(sA, map_k, (int)(2 * tau0), (int)(c * (kChunk / 8)), 0, &s_full); };
-    auto load_x = [&](uint32_t c) {
-        tma_load_3d(sB, map_x, (int)(2 * tile.grow0), (int)(c * (kChunk / 8)), 0, &s_full);
+    // stage ks of chunk c: units 4c + 2ks and 4c + 2ks + 1 of both operands
+    auto load_k = [&](uint32_t c, uint32_t ks) {
+        tma_load_3d(sA(ks), map_k, (int)(2 * tau0), (int)(c * (kChunk / 8) + 2 * ks), 0, &s_full[ks]);
     };
-    auto stage = [&](uint32_t c) {
-        mbar_expect_tx(&s_full, stage_bytes);
-        load_k(c);
-        load_x(c);
-    };
-    // chunk exponents and the bound operands 2^(e - max) at k = 0: thread t
-    // < 128 holds timeslice t's, 128 <= t < 192 trial row t - 128's.  A
-    // chunk's exponent is loaded (scale_load) while the chunk before it is
-    // in the tensor cores and stored (scale_store) after that chunk's fold.
-    const bool scale_k = tid < kTauTile && tau0 + tid < Nt;
-    const bool scale_x = tid >= kTauTile && tid < kTauTile + kRowTile && tid - kTauTile < tile.rows;
-    const int16_t* scale_row = nullptr;  // this thread's exponents, one per chunk
-    if (scale_k) scale_row = X0.kexp + (uint64_t)(tau0 + tid) * C;
-    if (scale_x) {
-        const SplitRow rw = rows[tile.first_row + (tid - kTauTile)];
-        scale_row = split[rw.run].xexp + (uint64_t)rw.member * C;
-    }
-    auto scale_load = [&](uint32_t c) -> int { return scale_row ? (int)scale_row[c] : -1000; };
-    auto scale_store = [&](int e) {
-        if (tid < kTauTile) {
-            s_ek[tid] = e;
-            const int d = e - s_kmax[tid];
-            const float v = (scale_k && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
-            *reinterpret_cast<uint16_t*>(sAb + canon(tid, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
-        } else if (tid < kTauTile + kRowTile) {
-            const uint32_t r = tid - kTauTile;
-            s_ex[r] = e;
-            const int d = e - s_xmax[r];
-            const float v = (scale_x && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
-            *reinterpret_cast<uint16_t*>(sBb + canon(r, 0, 16)) = (uint16_t)(__float_as_uint(v) >> 16);
-        }
+    auto load_x = [&](uint32_t c, uint32_t ks) {
+        tma_load_5d(sB(ks), map_x, 0, 0, (int)(2 * (tile.grow0 / kRowTile)), (int)(c * (kChunk / 8) + 2 * ks), 0,
+                    &s_full[ks]);
     };
 
+    // the bound operands are written at k = 0 only: zero both buffers once
+    for (uint32_t e = tid; e < kBoundBytes; e += blockDim.x) reinterpret_cast<uint16_t*>(sBound)[e] = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_tmem)),
                      "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_bar)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_full)));
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_full[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_empty[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_scales[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_tfull[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&s_tempty[q])), "r"(kFoldWarps));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&s_mma_done)));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        // K is constant: its first chunk loads while the trial kernel ends
-        mbar_add_tx(&s_full, a_bytes);
-        load_k(wk.c0);
+        s_abort = 0;
+        s_armed[0] = s_armed[1] = 0;
+        // K is constant: the first chunk's K stages load while the trial kernel ends
+        for (uint32_t ks = 0; ks < 2; ++ks) {
+            mbar_add_tx(&s_full[ks], a_stage);
+            load_k(wk.c0, ks);
+        }
     }
     if (tid < kTauTile) s_kmax[tid] = (tau0 + tid < Nt) ? X0.kexp_max[tau0 + tid] : 0;
 
     // everything below reads what the trial kernel wrote
     grid_dependency_wait();
-    // is any row of the tile a changed trial of a running run?  (Nothing is
-    // done either after a failed wait in an earlier launch, until the host
-    // has seen the status; one thread reads it so the CTA agrees.)
+    // is any row of the tile a trial of a running run?  (Nothing is done
+    // either after a failed wait in an earlier launch, until the host has
+    // seen the status; one thread reads it so the CTA agrees.)
     if (tid == 0) s_live = *reinterpret_cast<volatile int*>(status) != 0 ? -1 : 0;
     __syncthreads();
     if (s_live == 0 && tid < tile.rows) {
-        // every trial of a running run is sliced (whether it changed is known
-        // only after the normalisation of kDeferNorm runs)
         const SplitRow rw = rows[tile.first_row + tid];
         if (!runs[rw.run].done) atomicOr(&s_live, 1);
     }
     __syncthreads();
     if (s_live <= 0) {
-        // nothing to do: let the K load land, then release TMEM
-        if (tid == 0) mbar_arrive(&s_full);
-        if (tid == 0) mbar_wait(&s_full, 0);
+        // nothing to do: let the K loads land, then release TMEM
+        if (tid == 0)
+            for (uint32_t ks = 0; ks < 2; ++ks) {
+                mbar_arrive(&s_full[ks]);
+                mbar_wait(&s_full[ks], 0);
+            }
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();
         if (warp == 0)
@@ -346,141 +389,251 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         }
         s_xmax[r] = m;
     }
-    // this thread's TMEM lane (timeslice) and rows: warp w reads lane
-    // quarter w % 4 (a tcgen05.ld rule), row slice w / 4
-    constexpr uint32_t kRows = kRowTile / (kSplitThreads / 128);  // rows per thread
-    const uint32_t quarter = warp & 3u, slice = warp >> 2;
-    const uint32_t tl = quarter * 32 + lane;  // timeslice within the tile
-    const uint32_t r0 = slice * kRows;        // first of this thread's rows
-    // double-float accumulators of this thread's (timeslice, row) outputs
-    float acc_hi[kRows], acc_lo[kRows];
-#pragma unroll
-    for (uint32_t r = 0; r < kRows; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
-
-    __syncthreads();  // s_kmax / s_xmax
-    if (tid == 0) {
-        mbar_expect_tx(&s_full, b_bytes);
-        load_x(wk.c0);
-    }
-    scale_store(scale_load(wk.c0));
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n");
-    __syncthreads();
+    __syncthreads();  // s_kmax, s_xmax, the barriers, the TMEM address
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     const uint32_t tmem = s_tmem;
-    const uint32_t idesc = idesc_bf16(kTauTile, kRowTile);
-    const uint32_t lane_base = tmem + ((quarter * 32u) << 16);
-
+    volatile int* abort = &s_abort;
     bool ok = true;
-    for (uint32_t c = wk.c0; c < wk.c1; ++c) {
-        const uint32_t it = c - wk.c0;
-        // the chunk's planes (one thread waits; the CTA agrees on the outcome)
-        ok = __syncthreads_and(tid == 0 ? mbar_wait(&s_full, it & 1u) : true) != 0;
-        if (!ok) break;
-        // --- MMAs (one thread): group g accumulates every digit pair a+b=g
-        if (tid == 0) {
-            // K-adjacent core matrices one unit apart, row blocks 128 bytes
-            const uint64_t dA = smem_desc(smem_u32(sA), kTauTile * 16, 128);
-            const uint64_t dB = smem_desc(smem_u32(sB), kRowTile * 16, 128);
-            if (S == 2) issue_chunk_mmas<2>(tmem, dA, dB, idesc);
-            else issue_chunk_mmas<1>(tmem, dA, dB, idesc);
-            const uint64_t dab = smem_desc(smem_u32(sAb), 128, 256);
-            const uint64_t dbb = smem_desc(smem_u32(sBb), 128, 256);
-            mma_bf16(tmem + kBoundCol, dab, dbb, idesc, it > 0 ? 1u : 0u);
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                smem_u32(&s_bar)));
-        }
-        // the next chunk's exponents, loaded while the tensor cores work
-        const int next_e = c + 1 < wk.c1 ? scale_load(c + 1) : -1000;
-        ok = __syncthreads_and(mbar_wait(&s_bar, it & 1u)) != 0;  // uniform across the CTA
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-        if (!ok) break;
-        // the staging buffers are free again: load the next chunk meanwhile
-        if (tid == 0 && c + 1 < wk.c1) stage(c + 1);
 
-        // --- fold the seven exact group sums of this chunk into the accumulators
-        const int ek = s_ek[tl];
+    if (warp == kProducerWarp) {
+        // ---- producer: exponents, bound operands and operand stages
+        // lane l: timeslices l + 32q (q < 4), rows l + 32q (q < 2)
+        const int16_t* krow[4];
+        const int16_t* xrow[2];
 #pragma unroll
-        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
-            uint32_t d[kKept][8];
-#pragma unroll
-            for (int g = 0; g < kKept; ++g) tmem_ld8(lane_base + g * kRowTile + r0 + j8, d[g]);
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint32_t r = r0 + j8 + j;
-                // sum_g D_g 2^(7(6-g)) as a double-float: every term is exact
-                float sh = __uint_as_float(d[0][j]) * exp2_int(7 * (kKept - 1)), sl = 0.0f;
-#pragma unroll
-                for (int g = 1; g < kKept; ++g) {
-                    float e;
-                    two_sum(sh, __uint_as_float(d[g][j]) * exp2_int(7 * (kKept - 1 - g)), sh, e);
-                    sl += e;
-                }
-                float hi, lo;
-                fast_two_sum(sh, sl, hi, lo);
-                // weight of the lowest kept group, 2^(e_x + e_K - 56), in
-                // units of the output's largest scale 2^(max_x + max_K): the
-                // accumulators stay inside the FP32 range whatever the
-                // magnitude of K (e^{-tau omega} spans hundreds of binades)
-                const int k = (s_ex[r] - s_xmax[r]) + (ek - s_kmax[tl]) - 7 * (kKept + 1);
-                if (k > 50) {  // beyond any sane data: make the estimate unusable
-                    hi = __int_as_float(0x7fc00000);
-                    lo = 0.0f;
-                } else {
-                    scale_pow2(hi, lo, k);
-                }
-                dw_add(acc_hi[j8 + j], acc_lo[j8 + j], hi, lo);
-            }
+        for (uint32_t q = 0; q < 4; ++q) {
+            const uint32_t t = lane + 32 * q;
+            krow[q] = tau0 + t < Nt ? X0.kexp + (uint64_t)(tau0 + t) * C : nullptr;
         }
-        asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();  // every read of s_ek/s_ex and of TMEM is done
-        if (c + 1 < wk.c1) {
-            scale_store(next_e);
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-    }
-
-    if (ok && tile.nsplit == 1) {
-        // the tile's only CTA: its sums are the tile's, so the estimates and
-        // their bounds are formed here (no partial sums, no combine)
 #pragma unroll
-        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
-            uint32_t d[8];
-            tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint32_t r = r0 + j8 + j;
-                const uint32_t t = tau0 + tl;
-                if (r >= tile.rows || t >= Nt) continue;
+        for (uint32_t q = 0; q < 2; ++q) {
+            const uint32_t r = lane + 32 * q;
+            xrow[q] = nullptr;
+            if (r < tile.rows) {
                 const SplitRow rw = rows[tile.first_row + r];
-                const RunDev& R = runs[rw.run];
-                if (R.done) continue;
-                store_estimate(R, split[rw.run], rw, t, tile, acc_hi[j8 + j], acc_lo[j8 + j], __uint_as_float(d[j]));
+                xrow[q] = split[rw.run].xexp + (uint64_t)rw.member * C;
             }
         }
-    } else if (ok) {
-        // partial sums and the bound accumulator sum_c 2^(e_x-max_x + e_K-max_K)
-        float4* out = partial + (uint64_t)wk.block * kPartialBlock;
+        int pk[4], px[2];
+        auto load_scales = [&](uint32_t c) {
 #pragma unroll
-        for (uint32_t j8 = 0; j8 < kRows; j8 += 8) {
-            uint32_t d[8];
-            tmem_ld8(lane_base + kBoundCol + r0 + j8, d);
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+            for (uint32_t q = 0; q < 4; ++q) pk[q] = krow[q] ? (int)krow[q][c] : -1000;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint32_t r = r0 + j8 + j;
-                out[(uint64_t)r * kTauTile + tl] =
-                    make_float4(acc_hi[j8 + j], acc_lo[j8 + j], __uint_as_float(d[j]), 0.0f);
+            for (uint32_t q = 0; q < 2; ++q) px[q] = xrow[q] ? (int)xrow[q][c] : -1000;
+        };
+        auto pow2_bf16 = [](int d, bool valid) -> uint16_t {
+            const float v = (valid && d >= -126) ? __uint_as_float((uint32_t)(d + 127) << 23) : 0.0f;
+            return (uint16_t)(__float_as_uint(v) >> 16);
+        };
+        load_scales(wk.c0);
+        for (uint32_t it = 0; it < nchunks && ok; ++it) {
+            const uint32_t c = wk.c0 + it, buf = it & 1u;
+            // the operand stages, each once the MMAs of the chunk before are
+            // done with it (the first stage while they work on the second)
+            if (lane == 0) {
+                for (uint32_t ks = 0; ks < 2 && ok; ++ks) {
+                    if (it == 0) {
+                        mbar_expect_tx(&s_full[ks], b_stage);  // K in flight since the start
+                        load_x(c, ks);
+                    } else {
+                        if (!mbar_wait_or(&s_empty[ks], (it - 1) & 1u, abort)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_expect_tx(&s_full[ks], a_stage + b_stage);
+                        load_k(c, ks);
+                        load_x(c, ks);
+                    }
+                    s_armed[ks] = it + 1;
+                }
+                // the exponents' buffer is free once the fold warps are done
+                // with the chunk before's second half (so with the chunk two
+                // before, the buffer's last user)
+                if (ok && it > 0) ok = mbar_wait_or(&s_tempty[1], (it - 1) & 1u, abort);
+            }
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                const uint32_t t = lane + 32 * q;
+                s_ek[buf][t] = pk[q];
+                *reinterpret_cast<uint16_t*>(sAb(buf) + canon(t, 0, 16)) = pow2_bf16(pk[q] - s_kmax[t], krow[q]);
+            }
+#pragma unroll
+            for (uint32_t q = 0; q < 2; ++q) {
+                const uint32_t r = lane + 32 * q;
+                s_ex[buf][r] = px[q];
+                *reinterpret_cast<uint16_t*>(sBb(buf) + canon(r, 0, 16)) = pow2_bf16(px[q] - s_xmax[r], xrow[q]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&s_scales[buf]);
+            if (it + 1 < nchunks) load_scales(c + 1);
+        }
+    } else if (warp == kMmaWarp) {
+        // ---- MMA issue (one thread)
+        if (lane == 0) {
+            const uint32_t idesc_b = idesc_bf16(kTauTile, kHalfRows);
+            for (uint32_t it = 0; it < nchunks && ok; ++it) {
+                const uint32_t buf = it & 1u;
+                for (uint32_t ks = 0; ks < 2 && ok; ++ks) {
+                    ok = mbar_wait_or(&s_full[ks], it & 1u, abort);
+                    if (ok && ks == 1) ok = mbar_wait_or(&s_scales[buf], (it >> 1) & 1u, abort);
+                    for (uint32_t h = 0; h < 2 && ok; ++h) {
+                        // the buffer of half h: read by the fold for the chunk before
+                        if (ks == 0 && it > 0) ok = mbar_wait_or(&s_tempty[h], (it - 1) & 1u, abort);
+                        if (!ok) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;\n");
+                        const uint32_t d_half = tmem + h * kBufCols;
+                        // K planes: units 128 timeslice rows apart; trial
+                        // digits of half h: units 2 x 7 x 32 rows apart,
+                        // digits 32 rows apart, rows 16 bytes
+                        const uint64_t dA = smem_desc(smem_u32(sA(ks)), kTauTile * 16, 128);
+                        const uint64_t dB = smem_desc(smem_u32(sB(ks)) + h * kDigits * kHalfRows * 16,
+                                                      2 * kDigits * kHalfRows * 16, 128);
+                        constexpr uint32_t a_plane = 2 * kTauTile * 16 / 16;          // a K plane, 16-byte units
+                        constexpr uint32_t b_side = 2 * 2 * kDigits * kHalfRows;     // a side of the trials
+#pragma unroll
+                        for (uint32_t d = 0; d < (uint32_t)kDigits; ++d)
+#pragma unroll
+                            for (uint32_t s2 = 0; s2 < 2; ++s2) {
+                                if (s2 >= S) continue;
+                                const uint64_t da = dA + (uint64_t)((d * S + s2) * a_plane);
+                                const uint64_t db = dB + (uint64_t)(s2 * b_side);
+                                // groups d..6 (trial digits 0..6-d); the chunk's
+                                // first MMA of a half clears its groups
+                                mma_bf16(d_half + d * kHalfRows, da, db, idesc_bf16(kTauTile, kHalfRows * (kDigits - d)),
+                                         (ks | d | s2) ? 1u : 0u);
+                            }
+                        if (ks == 1) {
+                            // the bound: sum_c 2^(e_x-max_x) 2^(e_K-max_K), rank 1
+                            const uint64_t dab = smem_desc(smem_u32(sAb(buf)), 128, 256);
+                            const uint64_t dbb = smem_desc(smem_u32(sBb(buf)) + h * (kHalfRows / 8) * 256, 128, 256);
+                            mma_bf16(d_half + kBoundCol, dab, dbb, idesc_b, it > 0 ? 1u : 0u);
+                            mma_commit(&s_tfull[h]);
+                        }
+                    }
+                    if (ok) mma_commit(&s_empty[ks]);
+                }
+            }
+            // every MMA issued completes before TMEM is released
+            mma_commit(&s_mma_done);
+            if (!mbar_wait_or(&s_mma_done, 0, abort)) ok = false;
+        }
+    } else {
+        // ---- fold warps
+        // warp w reads TMEM lane quarter w % 4 (a tcgen05.ld rule): timeslice
+        // tl; of each half the 8 rows 8 (w / 4) .. 8 (w / 4) + 7
+        const uint32_t quarter = warp & 3u, slice = warp >> 2;
+        const uint32_t tl = quarter * 32 + lane;
+        const uint32_t lane_base = tmem + ((quarter * 32u) << 16);
+        float acc_hi[16], acc_lo[16];  // [h * 8 + j]: row 32 h + 8 slice + j
+#pragma unroll
+        for (uint32_t r = 0; r < 16; ++r) acc_hi[r] = acc_lo[r] = 0.0f;
+        for (uint32_t it = 0; it < nchunks && ok; ++it) {
+            const uint32_t buf = it & 1u;
+            ok = mbar_wait_or(&s_scales[buf], (it >> 1) & 1u, abort);
+            if (!ok) break;
+            const int kd = s_ek[buf][tl] - s_kmax[tl];
+#pragma unroll
+            for (uint32_t h = 0; h < 2; ++h) {
+                ok = mbar_wait_or(&s_tfull[h], it & 1u, abort);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                // the half's 8 rows in two passes of 4 (the group sums of 4
+                // rows in registers at a time); the buffer is released after
+                // the second pass's loads, while the tensor cores work on the
+                // other half
+#pragma unroll
+                for (uint32_t pass = 0; pass < 2; ++pass) {
+                    uint32_t dg[kKept][4];
+#pragma unroll
+                    for (int g = 0; g < kKept; ++g)
+                        tmem_ld4(lane_base + h * kBufCols + g * kHalfRows + 8 * slice + 4 * pass, dg[g]);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+                    if (pass == 1) {
+                        asm volatile("tcgen05.fence::before_thread_sync;\n");
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&s_tempty[h]);  // the buffer is free for the next chunk
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const uint32_t jj = 4 * pass + j;
+                        const uint32_t r = h * kHalfRows + 8 * slice + jj;
+                        // sum_g D_g 2^(7(6-g)) as a double-float: every term is exact
+                        float sh = __uint_as_float(dg[0][j]) * exp2_int(7 * (kKept - 1)), sl = 0.0f;
+#pragma unroll
+                        for (int g = 1; g < kKept; ++g) {
+                            float e;
+                            two_sum(sh, __uint_as_float(dg[g][j]) * exp2_int(7 * (kKept - 1 - g)), sh, e);
+                            sl += e;
+                        }
+                        float hi, lo;
+                        fast_two_sum(sh, sl, hi, lo);
+                        // weight of the lowest kept group, 2^(e_x + e_K - 56), in
+                        // units of the output's largest scale 2^(max_x + max_K):
+                        // the accumulators stay inside the FP32 range whatever
+                        // the magnitude of K (e^{-tau omega} spans hundreds of
+                        // binades)
+                        scale_pow2(hi, lo, (s_ex[buf][r] - s_xmax[r]) + kd - 7 * (kKept + 1));
+                        dw_add(acc_hi[h * 8 + jj], acc_lo[h * 8 + jj], hi, lo);
+                    }
+                }
+            }
+        }
+        if (ok) {
+            // the estimates (a tile with one CTA) or the partial sums, and the
+            // bound accumulators sum_c 2^(e_x-max_x + e_K-max_K)
+#pragma unroll
+            for (uint32_t h = 0; h < 2; ++h) {
+                uint32_t bd[8];
+                tmem_ld8(lane_base + h * kBufCols + kBoundCol + 8 * slice, bd);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const uint32_t r = h * kHalfRows + 8 * slice + j;
+                    if (tile.nsplit == 1) {
+                        const uint32_t t = tau0 + tl;
+                        if (r >= tile.rows || t >= Nt) continue;
+                        const SplitRow rw = rows[tile.first_row + r];
+                        const RunDev& R = runs[rw.run];
+                        if (R.done) continue;
+                        store_estimate(R, split[rw.run], rw, t, tile, acc_hi[h * 8 + j], acc_lo[h * 8 + j],
+                                       __uint_as_float(bd[j]));
+                    } else {
+                        partial[(uint64_t)wk.block * kPartialBlock + (uint64_t)r * kTauTile + tl] =
+                            make_float4(acc_hi[h * 8 + j], acc_lo[h * 8 + j], __uint_as_float(bd[j]), 0.0f);
+                    }
+                }
             }
         }
     }
-    if (!ok && tid == 0) atomicCAS(status, 0, kStatusWait);
+
+    if (*abort && tid == 0) atomicCAS(status, 0, kStatusWait);
     asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (*abort && tid == kProducerWarp * 32) {
+        // a CTA that gave up: the copies it issued land before it exits
+        // (bounded; the MMA thread has waited for its MMAs above).  A stage's
+        // latest armed phase is the only one that can be in flight.
+        for (uint32_t ks = 0; ks < 2; ++ks) {
+            const uint32_t n = s_armed[ks];
+            if (n == 0) continue;
+            const uint64_t t0 = global_ns();
+            for (;;) {
+                uint32_t done;
+                asm volatile(
+                    "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, "
+                    "p;\n}\n"
+                    : "=r"(done)
+                    : "r"(smem_u32(&s_full[ks])), "r"((n - 1) & 1u)
+                    : "memory");
+                if (done || global_ns() - t0 > kWaitNs) break;
+                __nanosleep(64);
+            }
+        }
+    }
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
 }

@@ -9,26 +9,36 @@
 // weight (a+b = g, g <= 6) summed over 32 genes x 2 sides is < 2^23, so the
 // tensor core's FP32 accumulation of each group is exact.  Per chunk the
 // seven group sums are combined into a double-float (FP32 pair) value,
-// scaled by 2^(e_x + e_K - 56) and added to double-float accumulators; CTAs
-// split the chunks of a tile and a combine kernel adds their partial sums.
-// What is dropped -- remainders and digit pairs with a+b > 6 -- is below
-// 2^-45.9 * 2^(e_x+e_K) per product, and the bound's chunk sums
-// B = sum_c 2^(e_x+e_K) are accumulated by one extra rank-1 MMA per chunk.
-// With the rounding bounds of the double-float steps and of the FP64 chain
-// itself this gives an interval that contains the value the plain FP64
-// engine computes, so selection decisions made from it are the FP64
-// decisions (deac_kernels.cuh, contract_kernel).
+// scaled by 2^(e_x + e_K - 56) relative to the output's largest scale and
+// added to double-float accumulators; CTAs split the chunks of a tile and a
+// combine kernel adds their partial sums when a tile has several.  What is
+// dropped -- remainders and digit pairs with a+b > 6 -- is below 2^-45.9 *
+// 2^(e_x+e_K) per product, and the bound's chunk sums B = sum_c 2^(e_x+e_K)
+// are accumulated by one extra rank-1 MMA per chunk.  With the rounding
+// bounds of the double-float steps and of the FP64 chain itself this gives
+// an interval that contains the value the plain FP64 engine computes, so
+// selection decisions made from it are the FP64 decisions (deac_kernels.cuh,
+// contract_kernel).
 //
-// Digit planes are stored pre-tiled for the tensor memory accelerator: plane
-// q = digit*S + side, then units of 8 genes, then rows, then the 8 genes
-// (16 bytes), i.e. element (q, row, gene j) at
-//     ((q * M/8 + j/8) * rows + row) * 8 + j%8.
-// A unit's rows are consecutive, so one 3-D TMA box {all rows of the tile x
-// 16 bytes (as 8-byte elements), 4 units, 7S planes} -- lines of 2 KB (128
-// timeslices) or 1 KB (64 trial rows) -- lands in shared memory as
-// [plane][unit][row][8]: the canonical K-major no-swizzle operand layout with
-// 16-byte rows, core matrices 8 rows apart (128 bytes) and units one
-// row-block apart.
+// Digit planes are stored pre-tiled for the tensor memory accelerator, rows
+// 16 bytes (8 genes) wide.
+//  K (the A operand, rows = timeslices): plane q = digit*S + side, then
+//    units of 8 genes, then timeslices: element (q, t, gene j) at
+//        ((q * M/8 + j/8) * Nt + t) * 8 + j%8.
+//    A unit's timeslices are consecutive, so one 3-D box {128 timeslices x
+//    16 bytes (as 8-byte elements), 4 units, 7S planes} -- 2 KB lines --
+//    lands in shared memory as [plane][unit][timeslice][8].
+//  Trials (the B operand, rows = members of the runs sharing K, in 64-row
+//    tiles of two 32-row halves): side, then unit, then (tile, half), then
+//    digit, then the half's 32 rows: element (s, row, digit d, gene j) at
+//        ((((s * M/8 + j/8) * H + row/32) * 7 + d) * 32 + row%32) * 8 + j%8
+//    with H = 2 * (64-row tiles).  One 5-D box {32 rows x 16 bytes, 7
+//    digits, 2 halves, 4 units, S sides} -- 512-byte lines -- lands as
+//    [side][unit][half][digit][row][8]: for a half, the rows of consecutive
+//    digits follow each other, so one MMA of N = 32 n rows takes n digits.
+// Both are the canonical K-major no-swizzle operand layout: core matrices 8
+// rows apart (128 bytes), the two 8-gene halves of a 16-gene MMA step one
+// unit apart.
 #pragma once
 
 #include <cuda.h>
@@ -43,23 +53,30 @@ constexpr int kDigits = 7;         // 7-bit digits per value (49 bits)
 constexpr int kDigitBits = 7 * kDigits;
 constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
-constexpr int kRowTile = 64;       // MMA N: trial rows
-constexpr int kSplitThreads = 512; // four warps per TMEM lane quarter, 16 rows each
+constexpr int kRowTile = 64;       // trial rows per output tile
+constexpr int kHalfRows = 32;      // rows per TMEM buffer (a tile's half)
+constexpr int kFoldWarps = 16;     // fold warps: four per TMEM lane quarter, 8 rows of each half each
+// split_contract_kernel: the fold warps, a producer warp (TMA loads and the
+// chunk scales) and an MMA warp
+constexpr int kSplitThreads = (kFoldWarps + 2) * 32;
+// elements between a half's digit blocks in the trial planes (32 rows x 8)
+constexpr uint64_t kXdigDigit = (uint64_t)kHalfRows * 8;
+// the trial planes' element offset of `row` (within its group) at unit 0,
+// side 0, digit 0
+__host__ __device__ inline uint64_t xdig_row_offset(uint32_t row) {
+    return ((uint64_t)(row >> 5) * kDigits * kHalfRows + (row & 31u)) * 8;
+}
 constexpr int kSelectThreads = 512;
 // dynamic shared memory of split_contract_kernel for S sides: K digits
-// [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and the two bound
-// operands (128 x 16, 64 x 16)
+// [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and two buffers of
+// the bound operands (128 x 16, 64 x 16)
 constexpr uint32_t split_smem_bytes(uint32_t S) {
     return (uint32_t)kDigits * S * (kTauTile * kChunk * 2) + (uint32_t)kDigits * S * (kRowTile * kChunk * 2) +
-           (kTauTile + kRowTile) * 16 * 2;
+           2 * (kTauTile + kRowTile) * 16 * 2;
 }
 
 // Split-engine buffers of one run (device pointers).
 struct SplitRun {
-    uint16_t* xdig;      // BF16 digits of the trial genes: member 0's row of the
-                         // tiled planes of all runs sharing K (rows R)
-    uint64_t xdig_unit;  // elements between units of 8 genes (R * 8)
-    uint64_t xdig_plane; // elements between planes (M * R)
     int16_t* xexp;       // [P][M/kChunk] chunk scale exponents of the trial
     const uint16_t* kdig;  // tiled digit planes of K, rows = timeslices (shared)
     const int16_t* kexp;   // [Nt][M/kChunk]
@@ -170,15 +187,16 @@ __device__ __forceinline__ uint32_t digit_bits(uint64_t f, int shift, float sg) 
 // one side.  A chunk's scale exponent is the maximum over both sides; each
 // gene gets seven 7-bit digits, written as one 16-byte store per digit plane;
 // the part's maximum exponent is raised into *xexp_max.  `xdig` points at the
-// trial's row in the tiled planes at the part's first unit.  `s_max` is
-// shared scratch of one int per warp.
+// trial's row in the tiled planes at the part's first unit; units are
+// unit_stride elements apart, sides xside_stride, digits kXdigDigit.
+// `s_max` is shared scratch of one int per warp.
 __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_stride, uint32_t S, uint32_t len,
-                                               uint16_t* xdig, uint64_t plane_stride, uint64_t unit_stride,
+                                               uint16_t* xdig, uint64_t unit_stride, uint64_t xside_stride,
                                                int16_t* xexp, int32_t* xexp_max, int* s_max) {
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t s = (threadIdx.x >> 2) & 1u, uq = threadIdx.x & 3u;
     const uint32_t C = len / kChunk, per_pass = blockDim.x >> 3;
-    const uint64_t digit_step = (uint64_t)S * plane_stride;  // from one digit plane to the next
+    constexpr uint64_t digit_step = kXdigDigit;  // from one digit plane to the next
     int wmax = -2000;
     for (uint32_t c0 = 0; c0 < C; c0 += per_pass) {
         const uint32_t c = c0 + (threadIdx.x >> 3);
@@ -210,7 +228,7 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
                 // FP64 pipe); -0 and zero digits give +0 either way
                 sg[k] = __double_as_longlong(v[k]) < 0 ? -1.0f : 1.0f;
             }
-            uint16_t* q = xdig + s * plane_stride + (uint64_t)u * unit_stride;
+            uint16_t* q = xdig + s * xside_stride + (uint64_t)u * unit_stride;
 #pragma unroll
             for (int b = 0; b < kDigits; ++b) {
                 const int sh = 7 * (kDigits - 1 - b);
