@@ -113,7 +113,6 @@ struct RunHost {
     uint64_t Nt = 0, M = 0, P = 0;
     int S = 2;
     deac::Model model;
-    std::vector<double> pop0;            // [S][P][M] initial parents
     uint64_t rng_start[4] = {0, 0, 0, 0};  // generator state after the initial draws
     uint64_t n_states = 0;
     uint64_t trace_cap = 0;
@@ -433,8 +432,40 @@ void prepare_model(RunHost& r) {
     deac::build_model(r.cfg, r.tau.data(), r.isf.data(), r.err.data(), r.Nt, r.freq.data(), r.M, r.model, false);
 }
 
-// Host part of one run's set-up: initial population and PRNG start state.
-void prepare_population(RunHost& r, int32_t streams) {
+// Byte offsets of a run's arena (one device allocation).
+struct ArenaLayout {
+    uint64_t o_isf, o_err, o_tw, o_np, o_nn, o_fp, o_fn, o_tp, o_tn, o_pop, o_cur, o_rng, o_cr, o_fw, o_fo, o_fnw,
+        o_E, o_E2, o_mom, o_stats, o_trace, size;
+    // bytes of the host image copied to the device: everything before the
+    // population, buffer 0 of it, then the initial CR and F
+    uint64_t pop_bytes, image_bytes;
+};
+
+ArenaLayout arena_layout(const RunHost& r) {
+    const uint64_t P = r.P, M = r.M, Nt = r.Nt, N = r.cfg.number_of_generations;
+    const int S = r.S;
+    Arena a;
+    ArenaLayout L;
+    L.o_isf = a.take(Nt * 8), L.o_err = a.take(Nt * 8), L.o_tw = a.take(Nt * 8);
+    L.o_np = a.take(M * 8), L.o_nn = a.take(M * 8), L.o_fp = a.take(M * 8), L.o_fn = a.take(M * 8);
+    L.o_tp = a.take(M * 8), L.o_tn = a.take(M * 8);
+    L.o_pop = a.take(2ull * S * P * M * 8);
+    L.o_cur = a.take(P);
+    L.o_rng = a.take(4 * r.n_states * 8);
+    L.o_cr = a.take(2ull * S * P * 8), L.o_fw = a.take(2ull * S * P * 8);
+    L.o_fo = a.take(P * 8), L.o_fnw = a.take(P * 8);
+    L.o_E = a.take(P * Nt * 8), L.o_E2 = a.take(P * Nt * 8), L.o_mom = a.take(2 * P * 8);
+    L.o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
+    L.o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
+    L.size = a.size;
+    L.pop_bytes = (uint64_t)S * P * M * 8;
+    L.image_bytes = L.o_pop + L.pop_bytes + 2ull * S * P * 8;
+    return L;
+}
+
+// Host part of one run's set-up: initial population (into pop, S*P*M
+// doubles) and PRNG start state.
+void prepare_population(RunHost& r, int32_t streams, double* pop) {
     const deac_config& c = r.cfg;
     const uint64_t P = r.P, M = r.M;
     const int S = r.S;
@@ -442,16 +473,15 @@ void prepare_population(RunHost& r, int32_t streams) {
     // (deac.cpp:2089-2091), member-major, a draw per side per gene
     // (deac.cpp:429-446), zero frequency matched (deac.cpp:447-456)
     deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + c.seed);
-    r.pop0.assign((uint64_t)S * P * M, 0.0);
     for (uint64_t i = 0; i < P; ++i)
         for (uint64_t j = 0; j < M; ++j)
             for (int s = 0; s < S; ++s) {
                 double v = deac::to_unit(g.next());
                 if (c.allow_negative_weight) v -= 0.5;
-                r.pop0[(uint64_t)s * P * M + i * M + j] = v;
+                pop[(uint64_t)s * P * M + i * M + j] = v;
             }
     if (S == 2)
-        for (uint64_t i = 0; i < P; ++i) r.pop0[P * M + i * M] = r.pop0[i * M];
+        for (uint64_t i = 0; i < P; ++i) pop[P * M + i * M] = pop[i * M];
     // per-gene states: state k = jump^k(generator after the initial draws)
     // (deac.cpp:1114-1126), formed on the device by rng_table_kernel; with
     // counter streams one slot per member (its jDE step count, from 0)
@@ -459,10 +489,41 @@ void prepare_population(RunHost& r, int32_t streams) {
     for (int w = 0; w < 4; ++w) r.rng_start[w] = g.s[w];
 }
 
-int upload_run(deac_batch* b, RunHost& r) {
+// The host image of a run's arena (pinned; ArenaLayout::image_bytes): the
+// inputs and the constant terms before the population, buffer 0 of the
+// population (drawn in place) and the initial CR / F after it.
+void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
+    const uint64_t P = r.P, S = (uint64_t)r.S;
+    const deac::Model& m = r.model;
+    std::memset(img, 0, L.o_pop);
+    auto put = [&](uint64_t off, const std::vector<double>& v) {
+        if (!v.empty()) std::memcpy(img + off, v.data(), v.size() * 8);
+    };
+    put(L.o_isf, r.isf);
+    put(L.o_err, r.err);
+    put(L.o_tw, m.tau_weight);
+    put(L.o_np, m.norm_pos);
+    put(L.o_nn, m.norm_neg);
+    put(L.o_fp, m.first_pos);
+    put(L.o_fn, m.first_neg);
+    put(L.o_tp, m.third_pos);
+    put(L.o_tn, m.third_neg);
+    prepare_population(r, streams, reinterpret_cast<double*>(img + L.o_pop));
+    double* crfw = reinterpret_cast<double*>(img + L.o_pop + L.pop_bytes);
+    for (uint64_t k = 0; k < S * P; ++k) {
+        crfw[k] = r.cfg.crossover_probability;
+        crfw[S * P + k] = r.cfg.differential_weight;
+    }
+}
+
+// Device part of one run's set-up from its host image `img` (pinned; the
+// copies are asynchronous on the batch stream: the image stays untouched
+// until the stream has been synchronised).
+int upload_run(deac_batch* b, RunHost& r, const char* img) {
     const uint64_t P = r.P, M = r.M, Nt = r.Nt, N = r.cfg.number_of_generations;
     const int S = r.S;
     const deac::Model& m = r.model;
+    (void)N;
     // constant kernel matrix, shared between runs with the same inputs
     const std::string key = kernel_key(r);
     auto it = b->kcache.find(key);
@@ -495,51 +556,23 @@ int upload_run(deac_batch* b, RunHost& r) {
     }
     r.kgroup = it->second.group;
 
-    Arena a;
-    const uint64_t o_isf = a.take(Nt * 8), o_err = a.take(Nt * 8), o_tw = a.take(Nt * 8);
-    const uint64_t o_np = a.take(M * 8), o_nn = a.take(M * 8), o_fp = a.take(M * 8), o_fn = a.take(M * 8);
-    const uint64_t o_tp = a.take(M * 8), o_tn = a.take(M * 8);
-    const uint64_t o_pop = a.take(2ull * S * P * M * 8);
-    const uint64_t o_cur = a.take(P);
-    const uint64_t o_rng = a.take(4 * r.n_states * 8);
-    const uint64_t o_cr = a.take(2ull * S * P * 8), o_fw = a.take(2ull * S * P * 8);
-    const uint64_t o_fo = a.take(P * 8), o_fnw = a.take(P * 8);
-    const uint64_t o_E = a.take(P * Nt * 8), o_E2 = a.take(P * Nt * 8), o_mom = a.take(2 * P * 8);
-    const uint64_t o_stats = a.take(r.cfg.track_stats ? 3 * N * 8 : 8);
-    const uint64_t o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
-    CUDA_TRY(cudaMalloc(&r.arena, a.size));
-    r.arena_bytes = a.size;
+    const ArenaLayout L = arena_layout(r);
+    const uint64_t o_isf = L.o_isf, o_err = L.o_err, o_tw = L.o_tw, o_np = L.o_np, o_nn = L.o_nn, o_fp = L.o_fp,
+                   o_fn = L.o_fn, o_tp = L.o_tp, o_tn = L.o_tn, o_pop = L.o_pop, o_cur = L.o_cur, o_rng = L.o_rng,
+                   o_cr = L.o_cr, o_fw = L.o_fw, o_fo = L.o_fo, o_fnw = L.o_fnw, o_E = L.o_E, o_E2 = L.o_E2,
+                   o_mom = L.o_mom, o_stats = L.o_stats, o_trace = L.o_trace;
+    CUDA_TRY(cudaMalloc(&r.arena, L.size));
+    r.arena_bytes = L.size;
     char* base = r.arena;
-    // the arena's initial contents as one host image (zeros but for the
-    // inputs, the initial parents and CR / F), copied around the PRNG
-    // table, which rng_table_kernel forms on the device
-    std::vector<char> image(a.size, 0);
-    auto put = [&](uint64_t off, const std::vector<double>& v) {
-        if (!v.empty()) std::memcpy(image.data() + off, v.data(), v.size() * 8);
-    };
-    put(o_isf, r.isf);
-    put(o_err, r.err);
-    put(o_tw, m.tau_weight);
-    put(o_np, m.norm_pos);
-    put(o_nn, m.norm_neg);
-    put(o_fp, m.first_pos);
-    put(o_fn, m.first_neg);
-    put(o_tp, m.third_pos);
-    put(o_tn, m.third_neg);
-    put(o_pop, r.pop0);
-    std::vector<double> crfw(2ull * S * P, 0.0);
-    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.crossover_probability;
-    put(o_cr, crfw);
-    for (uint64_t k = 0; k < (uint64_t)S * P; ++k) crfw[k] = r.cfg.differential_weight;
-    put(o_fw, crfw);
     const bool counter = b->streams == DEAC_STREAMS_COUNTER;
     // zeros are written on the device; only the inputs, the initial parents
     // (buffer 0) and the initial CR / F cross the bus
-    CUDA_TRY(cudaMemsetAsync(base, 0, a.size, b->stream));
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
-    CUDA_TRY(copy(b, base, image.data(), o_pop + (uint64_t)S * P * M * 8, cudaMemcpyHostToDevice));
-    CUDA_TRY(copy(b, base + o_cr, image.data() + o_cr, (uint64_t)S * P * 8, cudaMemcpyHostToDevice));
-    CUDA_TRY(copy(b, base + o_fw, image.data() + o_fw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemsetAsync(base, 0, L.size, b->stream));
+    CUDA_TRY(copy_async(b, base, img, o_pop + L.pop_bytes, cudaMemcpyHostToDevice, b->stream));
+    const char* crfw = img + o_pop + L.pop_bytes;
+    CUDA_TRY(copy_async(b, base + o_cr, crfw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice, b->stream));
+    CUDA_TRY(copy_async(b, base + o_fw, crfw + (uint64_t)S * P * 8, (uint64_t)S * P * 8, cudaMemcpyHostToDevice,
+                        b->stream));
     if (!counter) {
         const uint32_t bits = jump_bits(r.n_states);
         // on the batch's stream: the host's set-up goes on meanwhile (the
@@ -1054,19 +1087,35 @@ int deac_batch_setup(deac_batch* b) {
     }
     uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
+    // pinned host images, one per host thread: a window of runs is drawn in
+    // parallel straight into them, then copied asynchronously (the next
+    // window waits for the copies)
+    uint64_t image_max = 0;
+    for (auto& rp : b->runs) image_max = std::max(image_max, arena_layout(*rp).image_bytes);
+    const uint32_t window = std::min<uint32_t>(hw, (uint32_t)b->runs.size());
+    std::vector<char*> images(window, nullptr);
+    struct PinnedFree {
+        std::vector<char*>* v;
+        ~PinnedFree() {
+            for (char* p : *v)
+                if (p) cudaFreeHost(p);
+        }
+    } pinned_free{&images};
+    for (auto& p : images) CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&p), image_max));
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         RunHost& r = *b->runs[ri];
-        if (ri % hw == 0) {
-            // the initial populations of the next window of runs, one host
-            // thread each (only a window is held on the host at a time)
+        if (ri % window == 0) {
+            CUDA_TRY(cudaStreamSynchronize(b->stream));  // the window before has been copied
             std::vector<std::thread> pool;
-            for (uint32_t k = ri; k < b->runs.size() && k < ri + hw; ++k)
-                pool.emplace_back(prepare_population, std::ref(*b->runs[k]), b->streams);
+            for (uint32_t k = ri; k < b->runs.size() && k < ri + window; ++k)
+                pool.emplace_back([b, k, ri, &images] {
+                    RunHost& rk = *b->runs[k];
+                    fill_image(rk, arena_layout(rk), b->streams, images[k - ri]);
+                });
             for (auto& th : pool) th.join();
         }
-        int rc = upload_run(b, r);
+        int rc = upload_run(b, r, images[ri % window]);
         if (rc) return rc;
-        std::vector<double>().swap(r.pop0);  // uploaded
         for (uint32_t i = 0; i < r.dev.P; ++i) tw.push_back({ri, i});
         for (uint32_t k = 0; k < r.dev.contract_ctas; ++k) cw.push_back({ri, k});
         // trial genes, plus one row of weights when a row sum is formed
