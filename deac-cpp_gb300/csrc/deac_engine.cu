@@ -199,6 +199,12 @@ struct deac_batch {
     deac::PartWork* d_part_work = nullptr;
     uint32_t n_part_ctas = 0;
     size_t part_smem_bytes = 0;
+    // split engine on counter streams: the trial slices (trial_slice_kernel)
+    // of the runs with at most kSliceRows members, segments of items per
+    // persistent CTA
+    deac::SliceSeg* d_slice_segs = nullptr;
+    uint32_t* d_slice_start = nullptr;
+    uint32_t n_slice_ctas = 0;
     double kernel_ms[5] = {};
     uint64_t kernel_launches[5] = {};
     // bytes copied between host and device by this batch's calls
@@ -283,9 +289,14 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
         deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(
             b->d_runs, b->d_trial_work, init_mode, b->smem_doubles);
     } else {
-        launch(b->streams == DEAC_STREAMS_COUNTER ? deac::trial_part_counter_kernel : deac::trial_part_kernel,
-               b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early,
-               b->d_runs, static_cast<const deac::PartWork*>(b->d_part_work));
+        if (b->n_part_ctas)
+            launch(b->streams == DEAC_STREAMS_COUNTER ? deac::trial_part_counter_kernel : deac::trial_part_kernel,
+                   b->n_part_ctas, deac::kTrialPartThreads, b->part_smem_bytes, s, early, b->d_runs,
+                   static_cast<const deac::PartWork*>(b->d_part_work));
+        if (b->n_slice_ctas)
+            launch(deac::trial_slice_kernel, b->n_slice_ctas, deac::kSliceThreads, deac::kSliceSmemBytes, s, early,
+                   b->d_runs, static_cast<const deac::SliceSeg*>(b->d_slice_segs),
+                   static_cast<const uint32_t*>(b->d_slice_start), b->d_status);
     }
     if ((rc = mark(0))) return rc;
     if (b->engine == DEAC_ENGINE_PLAIN_FP64 || init_mode) {
@@ -833,13 +844,26 @@ int make_group_planes(deac_batch* b) {
     return DEAC_OK;
 }
 
-// Split engine: the trial-part work list, up to b->parts_per_cta
-// consecutive 512-gene parts of one member per CTA.
+// Split engine: the trial work lists.  On counter streams the runs with at
+// most kSliceRows members go to trial_slice_kernel: their items, in run
+// order, spread over its persistent CTAs (as many as fit on the SMs) in
+// contiguous ranges of about equal gene counts, as segments of consecutive
+// items of one run.  Every other run goes to trial_part_kernel, up to
+// b->parts_per_cta consecutive 512-gene parts of one member per CTA.
 int build_part_work(deac_batch* b) {
     std::vector<deac::PartWork> pw;
+    std::vector<uint32_t> slice_runs;
+    uint64_t slice_genes = 0, slice_items = 0;
     uint32_t smax = 1;
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         const RunHost& r = *b->runs[ri];
+        if (b->streams == DEAC_STREAMS_COUNTER && r.dev.P <= deac::kSliceRows) {
+            const uint64_t len = (uint64_t)deac::slice_chunks(r.dev.P) * deac::kChunk;
+            slice_runs.push_back(ri);
+            slice_genes += (uint64_t)r.dev.P * r.S * r.M;
+            slice_items += (r.M + len - 1) / len;
+            continue;
+        }
         const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
         smax = std::max<uint32_t>(smax, (uint32_t)r.S);
         for (uint32_t i = 0; i < r.dev.P; ++i)
@@ -850,8 +874,50 @@ int build_part_work(deac_batch* b) {
     b->d_part_work = nullptr;
     b->n_part_ctas = (uint32_t)pw.size();
     b->part_smem_bytes = (size_t)smax * deac::kTrialPart * sizeof(double);
-    CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::PartWork)));
-    CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
+    if (!pw.empty()) {
+        CUDA_TRY(cudaMalloc(&b->d_part_work, pw.size() * sizeof(deac::PartWork)));
+        CUDA_TRY(copy(b, b->d_part_work, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
+    }
+    cudaFree(b->d_slice_segs);
+    cudaFree(b->d_slice_start);
+    b->d_slice_segs = nullptr;
+    b->d_slice_start = nullptr;
+    b->n_slice_ctas = 0;
+    if (slice_runs.empty()) return DEAC_OK;
+    CUDA_TRY(raise_smem_limit(deac::trial_slice_kernel, deac::kSliceSmemBytes));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, deac::trial_slice_kernel, deac::kSliceThreads,
+                                                           deac::kSliceSmemBytes));
+    const uint32_t G = (uint32_t)std::min<uint64_t>(slice_items, (uint64_t)std::max(per_sm, 1) * b->sms);
+    std::vector<deac::SliceSeg> segs;
+    std::vector<uint32_t> start(G + 1, 0);
+    uint64_t acc = 0;
+    int64_t last = -1;  // CTA of the last segment
+    for (uint32_t ri : slice_runs) {
+        const RunHost& r = *b->runs[ri];
+        const uint32_t P = r.dev.P, S = (uint32_t)r.S, M = (uint32_t)r.M;
+        const uint32_t len = deac::slice_chunks(P) * deac::kChunk;
+        const uint32_t items = (M + len - 1) / len;
+        for (uint32_t it = 0; it < items; ++it) {
+            const uint64_t w = (uint64_t)P * S * std::min(len, M - it * len);
+            // the CTA whose share of the genes holds this item's middle
+            const int64_t cta = (int64_t)std::min<uint64_t>(G - 1, (acc + w / 2) * G / slice_genes);
+            acc += w;
+            if (segs.empty() || cta != last || segs.back().run != ri) {
+                for (int64_t q = last + 1; q <= cta; ++q) start[q] = (uint32_t)segs.size();
+                segs.push_back({ri, it, it + 1});
+                last = cta;
+            } else {
+                segs.back().item1 = it + 1;
+            }
+        }
+    }
+    for (int64_t q = last + 1; q <= (int64_t)G; ++q) start[q] = (uint32_t)segs.size();
+    CUDA_TRY(cudaMalloc(&b->d_slice_segs, segs.size() * sizeof(deac::SliceSeg)));
+    CUDA_TRY(cudaMalloc(&b->d_slice_start, start.size() * sizeof(uint32_t)));
+    CUDA_TRY(copy(b, b->d_slice_segs, segs.data(), segs.size() * sizeof(deac::SliceSeg), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy(b, b->d_slice_start, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    b->n_slice_ctas = G;
     return DEAC_OK;
 }
 
@@ -1662,9 +1728,12 @@ int deac_batch_autotune(deac_batch* b, uint64_t generations, deac_tune_report* o
     uint32_t best_parts = b->parts_per_cta, best_waves = b->split_waves;
     // the defaults first (also warms the caches), then every other candidate
     std::vector<std::pair<uint32_t, uint32_t>> cands{{b->parts_per_cta, b->split_waves}};
+    // (parts per CTA only shape trial_part_kernel: no choice when every run
+    // goes to trial_slice_kernel)
     for (uint32_t p : kParts)
         for (uint32_t w : kWaves)
-            if (p != b->parts_per_cta || w != b->split_waves) cands.emplace_back(p, w);
+            if ((p != b->parts_per_cta || w != b->split_waves) && (b->n_part_ctas || p == b->parts_per_cta))
+                cands.emplace_back(p, w);
     for (size_t k = 0; k < cands.size(); ++k) {
         int rc = apply(cands[k].first, cands[k].second);
         if (rc) return rc;
@@ -1753,6 +1822,8 @@ int deac_batch_destroy(deac_batch* b) {
     if (b->ev_join) cudaEventDestroy(b->ev_join);
     cudaFree(b->d_norm_work);
     cudaFree(b->d_part_work);
+    cudaFree(b->d_slice_segs);
+    cudaFree(b->d_slice_start);
     if (b->side_stream) cudaStreamDestroy(b->side_stream);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->own_stream) cudaStreamDestroy(b->stream);

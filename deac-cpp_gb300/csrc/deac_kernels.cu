@@ -24,15 +24,6 @@ __device__ __forceinline__ void store_state(const RunDev& R, uint64_t slot, cons
 }
 
 
-// Integer form of the crossover test  (x >> 11) * 2^-53 < cr
-// (deac_gpu.cu:641): with m = x >> 11 < 2^53 and X = cr * 2^53 (exact),
-// m < X  <=>  m < ceil(X).  Keeps the FP64 pipe free for the row-sum chain.
-__device__ __forceinline__ uint64_t crossover_threshold(double cr) {
-    if (!(cr > 0.0)) return 0;
-    if (cr >= 1.0) return 1ull << 53;
-    return (uint64_t)ceil(cr * 0x1.0p53);
-}
-
 // k-ascending FMA chain continuing from `acc` (the inner loops of
 // gpu_matmul and gpu_deac_gemv, deac_gpu.cu:302-304, 359-363).  Operands of
 // the next 8 steps are loaded while the current 8 are fused, so a dependent

@@ -193,6 +193,15 @@ __device__ __forceinline__ void grid_dependency_wait() {
     asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
+// Integer form of the crossover test  (x >> 11) * 2^-53 < cr
+// (deac_gpu.cu:641): with m = x >> 11 < 2^53 and X = cr * 2^53 (exact),
+// m < X  <=>  m < ceil(X).  Keeps the FP64 pipe free for the row-sum chain.
+__device__ __forceinline__ uint64_t crossover_threshold(double cr) {
+    if (!(cr > 0.0)) return 0;
+    if (cr >= 1.0) return 1ull << 53;
+    return (uint64_t)ceil(cr * 0x1.0p53);
+}
+
 // Asynchronous L2 prefetch of the `count` elements at p, rounded out to the
 // 16-byte units a bulk copy addresses and clipped at `end` (one past the
 // buffer's last element), so that it never reaches beyond the buffer.

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "deac_async.cuh"
 #include "deac_jde.cuh"
 #include "deac_split.cuh"
 
@@ -15,10 +16,7 @@ namespace {
 
 constexpr int kKept = kDigits;            // digit-pair groups a+b = 0..6 kept
 constexpr uint32_t kTmemCols = 512;       // 7 groups x 64 rows + bound x 64 rows = 512
-constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier waits: 2 s
 constexpr int kStatusWait = 1;             // status: a tensor-core completion wait gave up
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // canonical K-major, no-swizzle layout of a [rows x kdim] BF16 tile: core
 // matrix (8 rows x 16 bytes) of row group rg and k group kg at
@@ -47,29 +45,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Wait for the completion of the mbarrier phase with parity `phase`, giving
-// up after kWaitNs of wall time (the caller then reports an error).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    const uint64_t t0 = global_ns();
-    for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(phase)
-            : "memory");
-        if (done) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
-        __nanosleep(64);
-    }
-}
-
 __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t v[4]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
@@ -92,18 +67,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
         "[%5];\n" ::"r"(smem_u32(dst)),
         "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
         : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-// more bytes to come in the current phase, without an arrival
-__device__ __forceinline__ void mbar_add_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // The digit-pair MMAs of one chunk (one thread): group g accumulates every

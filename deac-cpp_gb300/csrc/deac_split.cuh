@@ -180,6 +180,30 @@ __device__ __forceinline__ uint32_t digit_bits(uint64_t f, int shift, float sg) 
     return __float_as_uint(__fmaf_rn(sg, __uint_as_float(0x4B000000u | d), -sg * 8388608.0f));
 }
 
+// The seven digit planes of one 16-byte unit (8 genes v) at scale 2^e:
+// one 16-byte store per plane at q, q + kXdigDigit, ...
+__device__ __forceinline__ void store_unit_digits(const double v[8], int e, uint16_t* q) {
+    uint64_t f[8];
+    float sg[8];
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) {
+        f[k] = frac_digits(v[k], e);
+        // the sign bit (integer test: FP64 compares share the narrow FP64
+        // pipe); -0 and zero digits give +0 either way
+        sg[k] = __double_as_longlong(v[k]) < 0 ? -1.0f : 1.0f;
+    }
+#pragma unroll
+    for (int b = 0; b < kDigits; ++b) {
+        const int sh = 7 * (kDigits - 1 - b);
+        uint32_t w[4];
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k)
+            w[k] = __byte_perm(digit_bits(f[2 * k], sh, sg[2 * k]), digit_bits(f[2 * k + 1], sh, sg[2 * k + 1]),
+                               0x7632);
+        *reinterpret_cast<uint4*>(q + b * kXdigDigit) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
 // The digit planes of the `len` genes (a multiple of kChunk) of one trial
 // part, both sides, read from shared memory `x` (side s at s * side_stride,
 // gene j at part_slot(j, s)) by the calling CTA (blockDim.x a multiple of
@@ -196,7 +220,6 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t s = (threadIdx.x >> 2) & 1u, uq = threadIdx.x & 3u;
     const uint32_t C = len / kChunk, per_pass = blockDim.x >> 3;
-    constexpr uint64_t digit_step = kXdigDigit;  // from one digit plane to the next
     int wmax = -2000;
     for (uint32_t c0 = 0; c0 < C; c0 += per_pass) {
         const uint32_t c = c0 + (threadIdx.x >> 3);
@@ -219,26 +242,7 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
         for (int o = 1; o < 8; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
         e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
         if (live) {
-            uint64_t f[8];
-            float sg[8];
-#pragma unroll
-            for (uint32_t k = 0; k < 8; ++k) {
-                f[k] = frac_digits(v[k], e);
-                // the sign bit (integer test: FP64 compares share the narrow
-                // FP64 pipe); -0 and zero digits give +0 either way
-                sg[k] = __double_as_longlong(v[k]) < 0 ? -1.0f : 1.0f;
-            }
-            uint16_t* q = xdig + s * xside_stride + (uint64_t)u * unit_stride;
-#pragma unroll
-            for (int b = 0; b < kDigits; ++b) {
-                const int sh = 7 * (kDigits - 1 - b);
-                uint32_t w[4];
-#pragma unroll
-                for (uint32_t k = 0; k < 4; ++k)
-                    w[k] = __byte_perm(digit_bits(f[2 * k], sh, sg[2 * k]), digit_bits(f[2 * k + 1], sh, sg[2 * k + 1]),
-                                       0x7632);
-                *reinterpret_cast<uint4*>(q + b * digit_step) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
+            store_unit_digits(v, e, xdig + s * xside_stride + (uint64_t)u * unit_stride);
             if ((threadIdx.x & 7u) == 0) xexp[c] = (int16_t)e;
         }
         if (c < C) wmax = max(wmax, e);
@@ -252,6 +256,32 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
         atomicMax(xexp_max, m);
     }
 }
+
+// ---- trial slices: the split engine's trials for batches on counter
+// streams, runs of at most kSliceRows members.  An item of a run is
+// slice_chunks(P) consecutive 32-gene chunks of every member, both sides.
+// trial_slice_kernel is persistent: each CTA walks its items (seg_start[b]
+// .. seg_start[b+1] of the segment list), staging the members' parent rows
+// of an item in shared memory by bulk copies, two items in flight, so each
+// parent gene leaves HBM once however many trials use it as a donor; then it
+// forms every trial gene of the item (written once, coalesced) and its
+// digit planes, whose stores cover consecutive members' 16-byte rows.
+constexpr int kSliceThreads = 256;
+constexpr uint32_t kSliceRows = 64;  // largest population of a sliced run
+// one stage: the parents of an item, [member][side][slice_chunks(P) x 32]
+constexpr uint32_t kSliceStageDoubles = kSliceRows * 2 * kChunk;
+// the item's trials, rows padded by 2 doubles (16 bytes: an odd number of
+// 16-byte units per row spreads the digit pass's row reads over the banks)
+constexpr uint32_t kSliceTrialDoubles = kSliceStageDoubles + 2 * kSliceRows;
+// two stages, the trials, and one chunk exponent per (member, chunk)
+constexpr uint32_t kSliceSmemBytes = (2 * kSliceStageDoubles + kSliceTrialDoubles) * 8 + kSliceRows * 4;
+__host__ __device__ inline uint32_t slice_chunks(uint32_t P) { return kSliceRows / P; }
+struct SliceSeg {
+    uint32_t run, item0, item1;  // items [item0, item1) of one run
+};
+__global__ void trial_slice_kernel(RunDev* runs, const SliceSeg* segs, const uint32_t* seg_start, int* status);
+// status value of a CTA whose bulk-copy wait gave up
+constexpr int kStatusSliceWait = 2;
 
 // host-side digit decomposition of one value for a given scale exponent
 void digits_of(double v, int e, uint16_t out[kDigits]);

@@ -144,14 +144,21 @@ def test_counter_streams_plain_matches_oracle_and_split_matches_plain(engine, or
 @pytest.mark.gpu
 def test_counter_streams_ragged_batch(engine, oracle):
     """A ragged batch (models, sides, sizes, stops) on counter streams: every
-    run equals its own oracle run, in the plain and the split engine."""
+    run equals its own oracle run, in the plain and the split engine.  In the
+    split engine the runs of at most 64 members take the slice path (items of
+    64/P chunks: P = 13 on M = 96 is one short item of three chunks, P = 5 on
+    M = 416 is two items, the second short) and the run of 100 members the
+    per-member part path, in the same generations."""
     specs = []
     for k, (over, m) in enumerate([(dict(spectra_type="bfull", population_size=8), 64),
                                    (dict(model="hyperbolic", spectra_type="bfull", population_size=32), 128),
                                    (dict(bosonic=True, population_size=13), 96),
                                    (dict(model="normalization", spectra_type="bfull", population_size=64,
                                          normalize=True), 256),
-                                   (dict(spectra_type="bfull", population_size=8, stop_minimum_fitness=1e5), 64)]):
+                                   (dict(spectra_type="bfull", population_size=8, stop_minimum_fitness=1e5), 64),
+                                   (dict(spectra_type="bfull", population_size=100), 160),
+                                   (dict(bosonic=True, population_size=5, allow_negative_weight=True), 416),
+                                   (dict(spectra_type="bfull", population_size=4), 32)]):
         kw = dict(temperature=1.35, number_of_generations=300, seed=40 + k, stop_minimum_fitness=1.0)
         kw.update(over)
         specs.append((engine.make_config(**kw), config0_data(40 + k), uniform_grid(m, 64.0)))
