@@ -262,7 +262,7 @@ def reference_arm(args, world, rank):
 # ---------------------------------------------------------------- GPU side
 
 KEPT_DIGIT_PAIRS = 28   # digit pairs a+b <= 6 of seven 7-bit digits
-KERNEL_NAMES = {0: "trial_part_kernel", 1: "contract_kernel (exact pass)", 2: "norm_kernel",
+KERNEL_NAMES = {0: "trial_slice_kernel", 1: "contract_kernel (exact pass)", 2: "norm_kernel",
                 3: "split_contract_kernel", 4: "split_combine_kernel+split_select_kernel"}
 
 
@@ -279,9 +279,10 @@ def kernel_roofline(kind, launch_s, peaks, configs):
     reached, against the measured peak of what bounds it."""
     rows, genes, products = workload_sizes(configs)
     if kind == 0:
-        # counter streams: three donors and the parent in, the trial gene
-        # and its seven BF16 digits out
-        work, unit, bound, peak = genes * (4 * 8 + 8 + 7 * 2), "GB/s", "hbm", peaks["hbm_gbs"]
+        # counter streams (trial slices): every parent gene in once (the
+        # donors are read from the staged parents), the trial gene and its
+        # seven BF16 digits out
+        work, unit, bound, peak = genes * (8 + 8 + 7 * 2), "GB/s", "hbm", peaks["hbm_gbs"]
         achieved = work / launch_s / 1e9
     elif kind == 3:
         work = 2.0 * products * KEPT_DIGIT_PAIRS  # BF16 digit-pair MMA flops (the precision form's algorithm)
@@ -402,6 +403,79 @@ def long_window(configs, local, stream, window):
     return line
 
 
+C4_RUNS, C4_PLAIN_RUNS, C4_WARMUP, C4_STEPS = 4096, 256, 2, 4
+C4_GB = 272  # device memory the full-size split batch needs
+
+
+def config4_key(local, stream):
+    """The batched split-precision form at full size: 4096 runs of M = 16384,
+    P = 64, N_tau = 512 in one split batch (270 GB), C4_STEPS generations
+    timed after C4_WARMUP; beside it the plain FP64 engine on the first 256 of
+    the same runs (the plain engine's per-run rate does not depend on how
+    many identical-shape runs share the batch), whose chi^2, best member and
+    spectrum must equal the split engine's on those runs."""
+    import numpy as np
+    import torch
+    import deac_gb300
+    from deac_gb300.data import config4_runs
+
+    free = torch.cuda.mem_get_info(local)[0] / 1e9
+    if free < C4_GB:
+        return {"skipped": f"needs {C4_GB} GB of device memory, {free:.0f} GB free"}
+    tau, freq, runs = config4_runs(C4_RUNS)
+    cfgs = [deac_gb300.make_config(temperature=1.35, spectra_type="bfull", population_size=64,
+                                   number_of_generations=1_000_000, stop_minimum_fitness=1.0, seed=seed)
+            for seed, _, _ in runs]
+    out = {"runs": C4_RUNS, "genome_size": len(freq), "population_size": 64, "number_of_timeslices": len(tau),
+           "generations_timed": C4_STEPS, "warmup_generations": C4_WARMUP}
+
+    def arm(kind, n):
+        b = deac_gb300.Batch(engine=kind, device=local, stream=stream.cuda_stream, streams="counter")
+        for cfg, (seed, isf, err) in zip(cfgs[:n], runs[:n]):
+            b.add_run(cfg, tau, isf, err, freq)
+        t0 = time.perf_counter()
+        b.setup()
+        setup_s = time.perf_counter() - t0
+        b.launch(C4_WARMUP)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.launch(C4_STEPS)
+        e1.record(stream)
+        stream.synchronize()
+        assert b.sync() == 0, "a run finished inside the timed window"
+        ms = e0.elapsed_time(e1)
+        return b, {"value": n * C4_STEPS / (ms / 1e3), "unit": UNIT, "ms_per_generation": ms / C4_STEPS,
+                   "setup_s": setup_s}
+
+    split, out["split"] = arm(deac_gb300.ENGINE_SPLIT_BF16, C4_RUNS)
+    c = [split.split_counts(r) for r in range(C4_RUNS)]
+    out["split"]["decisions"] = {k: sum(x[k] for x in c) for k in c[0]}
+    split.enable_timing(True)
+    split.launch(1)
+    out["split"]["kernel_ms_per_generation"] = {KERNEL_NAMES[k]: round(ms_k / cnt, 3)
+                                                for k, (ms_k, cnt) in
+                                                ((k, split.kernel_time(k)) for k in range(5)) if cnt}
+    split.enable_timing(False)
+    ref = [split.fetch(r) for r in range(C4_PLAIN_RUNS)]
+    split.close()
+    del split
+    torch.cuda.empty_cache()
+    plain, out["plain"] = arm(deac_gb300.ENGINE_PLAIN_FP64, C4_PLAIN_RUNS)
+    out["plain"]["runs"] = C4_PLAIN_RUNS
+    plain.launch(1)  # the generation the timing pass added to the split batch
+    plain.sync()
+    same = True
+    for r in range(C4_PLAIN_RUNS):
+        y = plain.fetch(r)
+        x = ref[r]
+        same = same and x["generation"] == y["generation"] and x["minimum_fitness"] == y["minimum_fitness"] \
+            and x["best_index"] == y["best_index"] and np.array_equal(x["dsf"], y["dsf"])
+    plain.close()
+    out["same_chi2_and_spectra_on_plain_runs"] = same
+    out["split_over_plain_per_run"] = (out["split"]["value"] / C4_RUNS) / (out["plain"]["value"] / C4_PLAIN_RUNS)
+    return out
+
+
 def engine_arm(args, world, rank, local):
     import torch
     import deac_gb300
@@ -517,6 +591,8 @@ def engine_arm(args, world, rank, local):
     if early:
         line["config1_early_window"] = early
         line["config1_long_window"] = longw
+    if not args.no_config4 and world == 1:
+        line["config4_full_size"] = config4_key(local, stream)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(rank)
     if rank == 0:
@@ -533,6 +609,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the single-run production-scale keys")
     ap.add_argument("--long-window", type=int, default=LONG_WINDOW)
+    ap.add_argument("--no-config4", action="store_true", help="skip the full-size batched split key (270 GB)")
     ap.add_argument("--runs", type=int, default=RUNS_PER_GPU,
                     help="the workload's first RUNS runs (smaller cases for profiling; the line is for 1024)")
     args = ap.parse_args()

@@ -102,7 +102,7 @@ struct KernelMatrix {
     double* k_neg = nullptr;
     uint16_t* kdig = nullptr;   // tiled digit planes (rows = timeslices)
     bool nonneg = false;        // every entry >= 0
-    int16_t* kexp = nullptr;    // [Nt][M/kChunk]
+    int16_t* kexp = nullptr;    // [Nt][split_chunks(M)]
     int16_t* kexp_max = nullptr;  // [Nt]
     uint32_t group = 0;         // index of the runs sharing it (split tiles)
 };
@@ -551,10 +551,10 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
         if (S == 2)
             for (double v : m.k_neg) km.nonneg = km.nonneg && v >= 0.0;
         if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-            // digit planes of K: one scale per (timeslice, 32-gene chunk)
+            // digit planes of K: one scale per (timeslice, 64-gene chunk)
             // shared by both sides, seven 7-bit digits per value, tiled as
             // [plane][unit of 8 genes][timeslice][8]
-            const uint64_t C = M / deac::kChunk;
+            const uint64_t C = deac::split_chunks(M);
             CUDA_TRY(cudaMalloc(&km.kdig, (uint64_t)deac::kDigits * S * Nt * M * 2));
             CUDA_TRY(cudaMalloc(&km.kexp, Nt * C * 2));
             CUDA_TRY(cudaMalloc(&km.kexp_max, Nt * 2));
@@ -670,7 +670,7 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
     d.trace = ptr(o_trace);
     d.trace_cap = r.trace_cap;
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        const uint64_t C = M / deac::kChunk;
+        const uint64_t C = deac::split_chunks(M);
         Arena sa;
         const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 4), o_mu = sa.take(P * 3 * 4);
         const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
@@ -846,9 +846,8 @@ int make_group_planes(deac_batch* b) {
 
 // Split engine: the trial work lists.  On counter streams the runs with at
 // most kSliceRows members go to trial_slice_kernel: their items, in run
-// order, spread over its persistent CTAs (as many as fit on the SMs) in
-// contiguous ranges of about equal gene counts, as segments of consecutive
-// items of one run.  Every other run goes to trial_part_kernel, up to
+// order, spread over its persistent CTAs (one per SM) in contiguous ranges
+// of about equal gene counts, as segments of consecutive items of one run.  Every other run goes to trial_part_kernel, up to
 // b->parts_per_cta consecutive 512-gene parts of one member per CTA.
 int build_part_work(deac_batch* b) {
     std::vector<deac::PartWork> pw;
@@ -858,7 +857,7 @@ int build_part_work(deac_batch* b) {
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         const RunHost& r = *b->runs[ri];
         if (b->streams == DEAC_STREAMS_COUNTER && r.dev.P <= deac::kSliceRows) {
-            const uint64_t len = (uint64_t)deac::slice_chunks(r.dev.P) * deac::kChunk;
+            const uint64_t len = (uint64_t)deac::slice_chunks(r.dev.P, (uint32_t)r.S) * deac::kChunk;
             slice_runs.push_back(ri);
             slice_genes += (uint64_t)r.dev.P * r.S * r.M;
             slice_items += (r.M + len - 1) / len;
@@ -896,7 +895,7 @@ int build_part_work(deac_batch* b) {
     for (uint32_t ri : slice_runs) {
         const RunHost& r = *b->runs[ri];
         const uint32_t P = r.dev.P, S = (uint32_t)r.S, M = (uint32_t)r.M;
-        const uint32_t len = deac::slice_chunks(P) * deac::kChunk;
+        const uint32_t len = deac::slice_chunks(P, S) * deac::kChunk;
         const uint32_t items = (M + len - 1) / len;
         for (uint32_t it = 0; it < items; ++it) {
             const uint64_t w = (uint64_t)P * S * std::min(len, M - it * len);
@@ -1064,8 +1063,8 @@ int deac_batch_add_run(deac_batch* b, const deac_config* cfg, const double* tau,
     if (cfg->population_size > (1u << 20) || m > (1u << 26) || nt > (1u << 20))
         return fail(DEAC_E_INVALID, "problem size beyond the engine's limits");
     if (isf[0] == 0.0 && cfg->normalize) return fail(DEAC_E_INVALID, "--normalize needs a nonzero F(0)");
-    if (b->engine == DEAC_ENGINE_SPLIT_BF16 && m % deac::kChunk != 0)
-        return fail(DEAC_E_INVALID, "the split engine needs genome_size a multiple of %d", deac::kChunk);
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16 && m % deac::kGeneStep != 0)
+        return fail(DEAC_E_INVALID, "the split engine needs genome_size a multiple of %d", deac::kGeneStep);
     auto r = std::make_unique<RunHost>();
     r->cfg = *cfg;
     r->P = cfg->population_size;
@@ -1259,7 +1258,7 @@ int deac_batch_setup(deac_batch* b) {
             for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
                 if (b->runs[ri]->kgroup != g) continue;
                 nt = (uint32_t)b->runs[ri]->Nt;
-                chunks = (uint32_t)(b->runs[ri]->M / deac::kChunk);
+                chunks = deac::split_chunks(b->runs[ri]->M);
                 for (uint32_t m = 0; m < b->runs[ri]->P; ++m) grp.push_back({ri, m});
             }
             for (size_t r0 = 0; r0 < grp.size(); r0 += deac::kRowTile) {

@@ -579,21 +579,21 @@ __device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* wo
                         mutated = true;
                     }
                     qd[jj] = v;
-                    qs[part_slot(jj, s)] = v;
+                    qs[part_slot(jj)] = v;
                 }
             }
         }
         __syncthreads();
         if (S == 2 && j0 == 0 && threadIdx.x == 0) {
             // gpu_match_population_zero (deac_gpu.cu:541-549)
-            dst[PM] = part_s[part_slot(0, 0)];
-            part_s[len + part_slot(0, 1)] = part_s[part_slot(0, 0)];
+            dst[PM] = part_s[part_slot(0)];
+            part_s[len + part_slot(0)] = part_s[part_slot(0)];
         }
         __syncthreads();
         // (ends with a barrier after its last read of part_s)
         digitize_trial(part_s, len, S, len,
                        R.xdig + xdig_row_offset(R.xdig_row0 + i) + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_unit,
-                       R.xdig_side, R.xexp + (uint64_t)i * (M / kChunk) + j0 / kChunk,
+                       R.xdig_side, R.xexp + (uint64_t)i * split_chunks(M) + j0 / kChunk,
                        R.xexp_max + i, s_digit_max);
     }
     if (__syncthreads_or(mutated) && threadIdx.x == 0) R.changed[i] = 1;

@@ -69,28 +69,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// The digit-pair MMAs of one chunk (one thread): group g accumulates every
-// pair a+b = g of trial digit a and K digit g-a, both sides, two K steps of
-// 16 genes.  Descriptors are the planes' base descriptors plus constant
-// offsets (addresses in 16-byte units; the 14-bit field never carries).
-template <int S>
-__device__ __forceinline__ void issue_chunk_mmas(uint32_t tmem, uint64_t dA, uint64_t dB, uint32_t idesc) {
-    constexpr uint32_t a_plane = kTauTile * kChunk * 2 / 16, b_plane = kRowTile * kChunk * 2 / 16;
-    constexpr uint32_t a_step = 2 * kTauTile, b_step = 2 * kRowTile;  // two units of 8 genes
-#pragma unroll
-    for (int g = 0; g < kDigits; ++g)
-#pragma unroll
-        for (int a = 0; a <= g; ++a)
-#pragma unroll
-            for (int s = 0; s < S; ++s)
-#pragma unroll
-                for (int ks = 0; ks < kChunk / 16; ++ks) {
-                    const uint64_t da = dA + (uint64_t)(((g - a) * S + s) * a_plane + ks * a_step);
-                    const uint64_t db = dB + (uint64_t)((a * S + s) * b_plane + ks * b_step);
-                    mma_bf16(tmem + g * kRowTile, da, db, idesc, (a | s | ks) ? 1u : 0u);
-                }
-}
-
 // Error-free transformations in FP32 (IEEE round-to-nearest; the file is
 // compiled without FMA contraction): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -145,32 +123,32 @@ __device__ __forceinline__ double times_pow2(double x, int k) {
 // tile's summed double-float (hi, lo) and bound accumulator b (see below).
 __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, const SplitRow rw, uint32_t t,
                                                const SplitTile& tile, float hi, float lo, float b) {
-    const double M = (double)R.M, C = (double)(R.M / kChunk), ks = (double)tile.nsplit;
+    const double M = (double)R.M, C = (double)split_chunks(R.M), ks = (double)tile.nsplit;
     const int emax = X.xexp_max[rw.member] + X.kexp_max[t];
     // B >= sum_c 2^(e_x + e_K): FP32 sums of powers of two (relative error
     // below 2^-23 per addition), terms under 2^-126 dropped
     const double bsum = times_pow2(((double)b * (1.0 + (C + ks + 9.0) * 0x1p-23) + C * 0x1p-126), emax);
     // Error of the estimate against the FP64 chain value, in parts:
     //  digits: dropped digit pairs and remainders, 2^-45.9 2^(e_x+e_K) per
-    //    product, 64 products a chunk:                     2^-39 B
+    //    product, 128 products a chunk:                    2^-38 B
     //  digit-group sums in FP32 (TwoSum cascade of seven exact terms):
-    //    30 u^2 times the chunk's |terms| <= 64 2^(e_x+e_K):  2^-37 B
+    //    30 u^2 times the chunk's |terms| <= 128 2^(e_x+e_K): 2^-36 B
     //  double-float additions, 3 u^2 |partial| each, along the longest
     //    path (a split's chunks, then the combine):  depth 3 u^2 |sum|
     //  the FP64 chains themselves, 2^-53 per step of |partial sum|, and
     //    the final FP64 sum.
-    // |sum| is at most 64 B in general; when every product is >= 0 the
+    // |sum| is at most 128 B in general; when every product is >= 0 the
     // partial sums are at most the value itself, bounded by E' below.
     const double depth = (double)tile.per + (double)((tile.nsplit + 7) / 8) + 10.0;
     // (hi, lo) count in units of 2^emax (the fold's scaling)
     const double e = times_pow2((double)hi + (double)lo, emax);
-    const double gen = 0x1p-39 + 0x1p-37 + depth * 3.0 * 0x1p-42;  // units of B
+    const double gen = 0x1p-38 + 0x1p-36 + depth * 3.0 * 0x1p-41;  // units of B
     double eb;
     if (R.flags & kNonNegProducts) {
         const double Ep = (fabs(e) + bsum * gen * 1.01) * (1.0 + 0x1p-40);
-        eb = bsum * 0x1p-39 + Ep * ((M + 1.0) * 0x1p-53 + 0x1p-43 + depth * 3.0 * 0x1p-48 + 0x1p-51);
+        eb = bsum * 0x1p-38 + Ep * ((M + 1.0) * 0x1p-53 + 0x1p-43 + depth * 3.0 * 0x1p-48 + 0x1p-51);
     } else {
-        eb = bsum * (gen + M * 0x1p-47 + 0x1p-46);
+        eb = bsum * (gen + M * 0x1p-46 + 0x1p-45);
     }
     // Absolute terms: subnormal roundings of the scaled chunk sums (2^-149
     // each, a few per chunk, in units of 2^emax), and the values below the
@@ -261,14 +239,15 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     const RunDev& R0 = runs[tile.run0];
     const SplitRun& X0 = split[tile.run0];
     const uint32_t S = R0.S, M = R0.M, Nt = R0.Nt;
-    const uint32_t C = M / kChunk;
+    const uint32_t C = split_chunks(M);
     const uint32_t tau0 = tile.tau0;
     const uint32_t nchunks = wk.c1 - wk.c0;
     constexpr uint32_t kProducerWarp = kFoldWarps, kMmaWarp = kFoldWarps + 1;
     constexpr uint32_t kBufCols = 256;  // TMEM columns per half: 7 x 32 group sums, then the bound
     constexpr uint32_t kBoundCol = kKept * kHalfRows;
 
-    // shared memory: two stages of [K digits: 7S planes x 2 units x 128 x 16 B]
+    // shared memory: two operand stages (16 genes each; a chunk streams
+    // through them in four) of [K digits: 7S planes x 2 units x 128 x 16 B]
     // [trials: S x 2 units x 2 halves x 7 digits x 32 x 16 B], then two
     // buffers of the bound operands (128 x 16 and 64 x 16, canonical)
     const uint32_t a_stage = kDigits * S * (2 * kTauTile * 16);  // 56 KB for two sides
@@ -281,13 +260,19 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
     auto sBb = [&](uint32_t buf) { return sBound + buf * kBoundBytes + kTauTile * 16 * 2; };
     const CUtensorMap* map_k = maps + 2 * tile.group;
     const CUtensorMap* map_x = maps + 2 * tile.group + 1;
-    // stage ks of chunk c: units 4c + 2ks and 4c + 2ks + 1 of both operands
-    auto load_k = [&](uint32_t c, uint32_t ks) {
-        tma_load_3d(sA(ks), map_k, (int)(2 * tau0), (int)(c * (kChunk / 8) + 2 * ks), 0, &s_full[ks]);
+    // stage q of chunk c into buffer sb: units 8c + 2q and 8c + 2q + 1 of
+    // both operands
+    auto load_k = [&](uint32_t c, uint32_t q, uint32_t sb) {
+        tma_load_3d(sA(sb), map_k, (int)(2 * tau0), (int)(c * (kChunk / 8) + 2 * q), 0, &s_full[sb]);
     };
-    auto load_x = [&](uint32_t c, uint32_t ks) {
-        tma_load_5d(sB(ks), map_x, 0, 0, (int)(2 * (tile.grow0 / kRowTile)), (int)(c * (kChunk / 8) + 2 * ks), 0,
-                    &s_full[ks]);
+    auto load_x = [&](uint32_t c, uint32_t q, uint32_t sb) {
+        tma_load_5d(sB(sb), map_x, 0, 0, (int)(2 * (tile.grow0 / kRowTile)), (int)(c * (kChunk / 8) + 2 * q), 0,
+                    &s_full[sb]);
+    };
+    // operand stages of chunk c: four, or two for a final 32-gene chunk
+    auto chunk_stages = [&](uint32_t c) {
+        const uint32_t left = (M - c * kChunk) / kStage;
+        return left < (uint32_t)(kChunk / kStage) ? left : (uint32_t)(kChunk / kStage);
     };
 
     // the bound operands are written at k = 0 only: zero both buffers once
@@ -310,10 +295,11 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         s_abort = 0;
         s_armed[0] = s_armed[1] = 0;
-        // K is constant: the first chunk's K stages load while the trial kernel ends
-        for (uint32_t ks = 0; ks < 2; ++ks) {
-            mbar_add_tx(&s_full[ks], a_stage);
-            load_k(wk.c0, ks);
+        // K is constant: the first chunk's first two K stages load while
+        // the trial kernel ends
+        for (uint32_t q = 0; q < 2; ++q) {
+            mbar_add_tx(&s_full[q], a_stage);
+            load_k(wk.c0, q, q);
         }
     }
     if (tid < kTauTile) s_kmax[tid] = (tau0 + tid < Nt) ? X0.kexp_max[tau0 + tid] : 0;
@@ -390,25 +376,28 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
             return (uint16_t)(__float_as_uint(v) >> 16);
         };
         load_scales(wk.c0);
+        uint32_t n = 0;  // operand stages issued: stage n goes to buffer n & 1
         for (uint32_t it = 0; it < nchunks && ok; ++it) {
             const uint32_t c = wk.c0 + it, buf = it & 1u;
-            // the operand stages, each once the MMAs of the chunk before are
-            // done with it (the first stage while they work on the second)
+            // the chunk's operand stages, each once the MMAs are done with the
+            // stage two before (which used the same buffer)
             if (lane == 0) {
-                for (uint32_t ks = 0; ks < 2 && ok; ++ks) {
-                    if (it == 0) {
-                        mbar_expect_tx(&s_full[ks], b_stage);  // K in flight since the start
-                        load_x(c, ks);
+                const uint32_t nst = chunk_stages(c);
+                for (uint32_t q = 0; q < nst && ok; ++q, ++n) {
+                    const uint32_t sb = n & 1u;
+                    if (n < 2) {
+                        mbar_expect_tx(&s_full[sb], b_stage);  // K in flight since the start
+                        load_x(c, q, sb);
                     } else {
-                        if (!mbar_wait_or(&s_empty[ks], (it - 1) & 1u, abort)) {
+                        if (!mbar_wait_or(&s_empty[sb], ((n - 2) >> 1) & 1u, abort)) {
                             ok = false;
                             break;
                         }
-                        mbar_expect_tx(&s_full[ks], a_stage + b_stage);
-                        load_k(c, ks);
-                        load_x(c, ks);
+                        mbar_expect_tx(&s_full[sb], a_stage + b_stage);
+                        load_k(c, q, sb);
+                        load_x(c, q, sb);
                     }
-                    s_armed[ks] = it + 1;
+                    s_armed[sb] = (n >> 1) + 1;
                 }
                 // the exponents' buffer is free once the fold warps are done
                 // with the chunk before's second half (so with the chunk two
@@ -438,22 +427,26 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         // ---- MMA issue (one thread)
         if (lane == 0) {
             const uint32_t idesc_b = idesc_bf16(kTauTile, kHalfRows);
+            uint32_t n = 0;  // operand stages consumed (stage n in buffer n & 1)
             for (uint32_t it = 0; it < nchunks && ok; ++it) {
                 const uint32_t buf = it & 1u;
-                for (uint32_t ks = 0; ks < 2 && ok; ++ks) {
-                    ok = mbar_wait_or(&s_full[ks], it & 1u, abort);
-                    if (ok && ks == 1) ok = mbar_wait_or(&s_scales[buf], (it >> 1) & 1u, abort);
+                const uint32_t nst = chunk_stages(wk.c0 + it);
+                for (uint32_t q = 0; q < nst && ok; ++q, ++n) {
+                    const uint32_t sb = n & 1u;
+                    const bool last = q + 1 == nst;
+                    ok = mbar_wait_or(&s_full[sb], (n >> 1) & 1u, abort);
+                    if (ok && last) ok = mbar_wait_or(&s_scales[buf], (it >> 1) & 1u, abort);
                     for (uint32_t h = 0; h < 2 && ok; ++h) {
                         // the buffer of half h: read by the fold for the chunk before
-                        if (ks == 0 && it > 0) ok = mbar_wait_or(&s_tempty[h], (it - 1) & 1u, abort);
+                        if (q == 0 && it > 0) ok = mbar_wait_or(&s_tempty[h], (it - 1) & 1u, abort);
                         if (!ok) break;
                         asm volatile("tcgen05.fence::after_thread_sync;\n");
                         const uint32_t d_half = tmem + h * kBufCols;
                         // K planes: units 128 timeslice rows apart; trial
                         // digits of half h: units 2 x 7 x 32 rows apart,
                         // digits 32 rows apart, rows 16 bytes
-                        const uint64_t dA = smem_desc(smem_u32(sA(ks)), kTauTile * 16, 128);
-                        const uint64_t dB = smem_desc(smem_u32(sB(ks)) + h * kDigits * kHalfRows * 16,
+                        const uint64_t dA = smem_desc(smem_u32(sA(sb)), kTauTile * 16, 128);
+                        const uint64_t dB = smem_desc(smem_u32(sB(sb)) + h * kDigits * kHalfRows * 16,
                                                       2 * kDigits * kHalfRows * 16, 128);
                         constexpr uint32_t a_plane = 2 * kTauTile * 16 / 16;          // a K plane, 16-byte units
                         constexpr uint32_t b_side = 2 * 2 * kDigits * kHalfRows;     // a side of the trials
@@ -467,9 +460,9 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
                                 // groups d..6 (trial digits 0..6-d); the chunk's
                                 // first MMA of a half clears its groups
                                 mma_bf16(d_half + d * kHalfRows, da, db, idesc_bf16(kTauTile, kHalfRows * (kDigits - d)),
-                                         (ks | d | s2) ? 1u : 0u);
+                                         (q | d | s2) ? 1u : 0u);
                             }
-                        if (ks == 1) {
+                        if (last) {
                             // the bound: sum_c 2^(e_x-max_x) 2^(e_K-max_K), rank 1
                             const uint64_t dab = smem_desc(smem_u32(sAb(buf)), 128, 256);
                             const uint64_t dbb = smem_desc(smem_u32(sBb(buf)) + h * (kHalfRows / 8) * 256, 128, 256);
@@ -477,7 +470,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
                             mma_commit(&s_tfull[h]);
                         }
                     }
-                    if (ok) mma_commit(&s_empty[ks]);
+                    if (ok) mma_commit(&s_empty[sb]);
                 }
             }
             // every MMA issued completes before TMEM is released
@@ -975,24 +968,38 @@ __global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt,
                                 int16_t* kexp, int16_t* kexp_max) {
     __shared__ int s_max[8];
     const uint32_t t = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t S = kn ? 2u : 1u, C = M / kChunk, nw = blockDim.x >> 5;
+    const uint32_t S = kn ? 2u : 1u, C = split_chunks(M), nw = blockDim.x >> 5;
     int wmax = -1000;
+    // the exponents of the normal values (zeros, subnormals and non-finite
+    // values set no scale, as std::isnormal on the host)
+    auto ex = [](double v) { const int e = exp_of(v); return e > 1023 ? -2000 : e; };
     for (uint32_t c = warp; c < C; c += nw) {
-        const uint32_t j = c * kChunk + lane;
-        const double v0 = kp[(uint64_t)t * M + j], v1 = kn ? kn[(uint64_t)t * M + j] : 0.0;
-        // the exponents of the normal values (zeros, subnormals and
-        // non-finite values set no scale, as std::isnormal on the host)
-        auto ex = [](double v) { const int e = exp_of(v); return e > 1023 ? -2000 : e; };
-        int e = max(ex(v0), ex(v1));
+        // lane: genes 64c + lane and 64c + 32 + lane (the second absent in
+        // a final 32-gene chunk)
+        double v[2][2];
+        int e = -2000;
+#pragma unroll
+        for (uint32_t h = 0; h < 2; ++h) {
+            const uint32_t j = c * kChunk + h * 32 + lane;
+            const bool in = j < M;
+            v[h][0] = in ? kp[(uint64_t)t * M + j] : 0.0;
+            v[h][1] = in && kn ? kn[(uint64_t)t * M + j] : 0.0;
+            e = max(e, max(ex(v[h][0]), ex(v[h][1])));
+        }
         for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
         e = e <= -1500 ? -1000 : e + 1;  // scale 2^e above every |v| of the chunk
-        for (uint32_t sd = 0; sd < S; ++sd) {
-            const double v = sd ? v1 : v0;
-            const uint64_t f = frac_digits(v, e);
-            const bool neg = v < 0.0;
-            for (int d = 0; d < kDigits; ++d) {
-                const uint32_t dg = (uint32_t)(f >> (7 * (kDigits - 1 - d))) & 127u;
-                kdig[((((uint64_t)d * S + sd) * (M / 8) + j / 8) * Nt + t) * 8 + (j & 7u)] = bf16_digit(dg, neg);
+#pragma unroll
+        for (uint32_t h = 0; h < 2; ++h) {
+            const uint32_t j = c * kChunk + h * 32 + lane;
+            if (j >= M) continue;
+            for (uint32_t sd = 0; sd < S; ++sd) {
+                const double x = v[h][sd];
+                const uint64_t f = frac_digits(x, e);
+                const bool neg = x < 0.0;
+                for (int d = 0; d < kDigits; ++d) {
+                    const uint32_t dg = (uint32_t)(f >> (7 * (kDigits - 1 - d))) & 127u;
+                    kdig[((((uint64_t)d * S + sd) * (M / 8) + j / 8) * Nt + t) * 8 + (j & 7u)] = bf16_digit(dg, neg);
+                }
             }
         }
         if (lane == 0) kexp[(uint64_t)t * C + c] = (int16_t)e;
@@ -1004,31 +1011,6 @@ __global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt,
         int m = -1000;
         for (uint32_t k = 0; k < nw; ++k) m = max(m, s_max[k]);
         kexp_max[t] = (int16_t)m;
-    }
-}
-
-// ------------------------------------------------------------------ host
-void digits_of(double v, int e, uint16_t out[kDigits]) {
-    const double m = std::fabs(v);
-    uint64_t f = 0;
-    if (m > 0.0) {
-        int ev;
-        std::frexp(m, &ev);  // m = f * 2^ev, f in [0.5, 1)
-        const int ef = ev - 1;
-        if (ef >= -1022) {
-            uint64_t bits;
-            std::memcpy(&bits, &m, 8);
-            const uint64_t mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-            const int shift = (52 - kDigitBits) + e - ef;
-            f = shift >= 64 ? 0 : (mant >> shift);
-        }
-    }
-    for (int b = 0; b < kDigits; ++b) {
-        const uint32_t d = (uint32_t)(f >> (7 * (kDigits - 1 - b))) & 127u;
-        float fd = (float)d;
-        uint32_t fb;
-        std::memcpy(&fb, &fd, 4);
-        out[b] = (uint16_t)((fb >> 16) | ((v < 0.0 && d) ? 0x8000u : 0u));
     }
 }
 

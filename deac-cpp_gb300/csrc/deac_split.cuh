@@ -2,12 +2,14 @@
 // tcgen05 tensor cores, used by DEAC_ENGINE_SPLIT_BF16.
 //
 // E[i,t] = sum_k x[i,k] K[t,k] (both sides) is evaluated from exact BF16
-// digit slices:  every value v of a 32-gene chunk is written as
+// digit slices:  every value v of a 64-gene chunk is written as
 //     v = sign * 2^e * sum_{b=0..6} d_b 2^(-7(b+1)) + r,   0 <= d_b <= 127,
 // with one power-of-two scale 2^e per (row, chunk) shared by both sides
-// (|r| < 2^(e-49)).  Digit products d_a d'_b < 2^14 and a group of equal
-// weight (a+b = g, g <= 6) summed over 32 genes x 2 sides is < 2^23, so the
-// tensor core's FP32 accumulation of each group is exact.  Per chunk the
+// (|r| < 2^(e-49)).  Digit products d_a d'_b <= 127^2 and a group of equal
+// weight (a+b = g, g <= 6: at most 7 pairs) summed over 64 genes x 2 sides
+// is at most 7 * 128 * 127^2 = 14,451,584 < 2^24 in magnitude, so the
+// tensor core's FP32 accumulation of each group is exact (the last chunk of
+// a genome whose size is an odd multiple of 32 has 32 genes).  Per chunk the
 // seven group sums are combined into a double-float (FP32 pair) value,
 // scaled by 2^(e_x + e_K - 56) relative to the output's largest scale and
 // added to double-float accumulators; CTAs split the chunks of a tile and a
@@ -51,7 +53,12 @@ namespace deac {
 
 constexpr int kDigits = 7;         // 7-bit digits per value (49 bits)
 constexpr int kDigitBits = 7 * kDigits;
-constexpr int kChunk = 32;         // genes per scale chunk and per MMA stage
+constexpr int kChunk = 64;         // genes per scale chunk
+constexpr int kStage = 16;         // genes per operand stage (one MMA K step)
+constexpr int kGeneStep = 32;      // the split engine's genome sizes are multiples of this
+// scale chunks of a genome of M genes (the last one 32 genes when M is an
+// odd multiple of 32)
+__host__ __device__ inline uint32_t split_chunks(uint64_t M) { return (uint32_t)((M + kChunk - 1) / kChunk); }
 constexpr int kTauTile = 128;      // MMA M: timeslices, one TMEM lane each
 constexpr int kRowTile = 64;       // trial rows per output tile
 constexpr int kHalfRows = 32;      // rows per TMEM buffer (a tile's half)
@@ -67,19 +74,19 @@ __host__ __device__ inline uint64_t xdig_row_offset(uint32_t row) {
     return ((uint64_t)(row >> 5) * kDigits * kHalfRows + (row & 31u)) * 8;
 }
 constexpr int kSelectThreads = 512;
-// dynamic shared memory of split_contract_kernel for S sides: K digits
-// [7][S] x (128 x 32), trial digits [7][S] x (64 x 32) and two buffers of
-// the bound operands (128 x 16, 64 x 16)
+// dynamic shared memory of split_contract_kernel for S sides: two operand
+// stages of K digits [7][S] x (128 x 16) and trial digits [7][S] x (64 x 16),
+// and two buffers of the bound operands (128 x 16, 64 x 16)
 constexpr uint32_t split_smem_bytes(uint32_t S) {
-    return (uint32_t)kDigits * S * (kTauTile * kChunk * 2) + (uint32_t)kDigits * S * (kRowTile * kChunk * 2) +
+    return 2 * ((uint32_t)kDigits * S * (kTauTile * kStage * 2) + (uint32_t)kDigits * S * (kRowTile * kStage * 2)) +
            2 * (kTauTile + kRowTile) * 16 * 2;
 }
 
 // Split-engine buffers of one run (device pointers).
 struct SplitRun {
-    int16_t* xexp;       // [P][M/kChunk] chunk scale exponents of the trial
+    int16_t* xexp;       // [P][split_chunks(M)] chunk scale exponents of the trial
     const uint16_t* kdig;  // tiled digit planes of K, rows = timeslices (shared)
-    const int16_t* kexp;   // [Nt][M/kChunk]
+    const int16_t* kexp;   // [Nt][split_chunks(M)]
     const int16_t* kexp_max;  // [Nt] max over chunks
     int32_t* xexp_max;   // [P] max over chunks
     double* e_mp;        // [P][Nt] split estimate of the model ISF
@@ -136,7 +143,7 @@ __global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* w
 // per 32-gene chunk the scale exponent shared by both sides (kexp[t][c]),
 // seven 7-bit digits per value as BF16 in the tiled planes
 // [plane][unit of 8 genes][timeslice][8], and the timeslice's largest scale
-// exponent (kexp_max[t]); the same digits as digits_of on the host.
+// exponent (kexp_max[t]).
 __global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt, uint32_t M, uint16_t* kdig,
                                 int16_t* kexp, int16_t* kexp_max);
 constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
@@ -164,12 +171,13 @@ __device__ __forceinline__ uint16_t bf16_digit(uint32_t d, bool neg) {
     return (uint16_t)((f >> 16) | (neg && d ? 0x8000u : 0u));
 }
 
-// Position in shared memory of gene j (of a trial part) on side s, within
-// the side's row: the genes of each 8-gene unit permuted in pairs so that the
-// eight threads of a chunk in digitize_trial read their units' pairs from
-// eight distinct bank groups.
-__device__ __forceinline__ uint32_t part_slot(uint32_t j, uint32_t s) {
-    return j ^ ((((j >> 4) & 1u) << 2) | ((s & 1u) << 1));
+// Position in shared memory of gene j (of a trial part) within its side's
+// row: the 16-byte pairs of each 8-gene unit permuted (by bits 4 and 5 of j)
+// so that the eight threads of one side of a chunk in digitize_trial, which
+// read the same pair of eight consecutive units, hit eight distinct bank
+// groups.
+__device__ __forceinline__ uint32_t part_slot(uint32_t j) {
+    return j ^ ((((j >> 4) & 1u) << 2) | (((j >> 5) & 1u) << 1));
 }
 
 // BF16 bits (in the upper half of the word) of the 7-bit digit of f at bit
@@ -204,13 +212,13 @@ __device__ __forceinline__ void store_unit_digits(const double v[8], int e, uint
     }
 }
 
-// The digit planes of the `len` genes (a multiple of kChunk) of one trial
-// part, both sides, read from shared memory `x` (side s at s * side_stride,
-// gene j at part_slot(j, s)) by the calling CTA (blockDim.x a multiple of
-// 32): eight threads per 32-gene chunk, each one 16-byte unit of 8 genes of
-// one side.  A chunk's scale exponent is the maximum over both sides; each
-// gene gets seven 7-bit digits, written as one 16-byte store per digit plane;
-// the part's maximum exponent is raised into *xexp_max.  `xdig` points at the
+// The digit planes of the `len` genes (a multiple of 32) of one trial part,
+// both sides, read from shared memory `x` (side s at s * side_stride, gene j
+// at part_slot(j)) by the calling CTA (blockDim.x a multiple of 32): sixteen
+// threads per 64-gene chunk, each one 16-byte unit of 8 genes of one side.
+// A chunk's scale exponent is the maximum over both sides; each gene gets
+// seven 7-bit digits, written as one 16-byte store per digit plane; the
+// part's maximum exponent is raised into *xexp_max.  `xdig` points at the
 // trial's row in the tiled planes at the part's first unit; units are
 // unit_stride elements apart, sides xside_stride, digits kXdigDigit.
 // `s_max` is shared scratch of one int per warp.
@@ -218,20 +226,20 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
                                                uint16_t* xdig, uint64_t unit_stride, uint64_t xside_stride,
                                                int16_t* xexp, int32_t* xexp_max, int* s_max) {
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint32_t s = (threadIdx.x >> 2) & 1u, uq = threadIdx.x & 3u;
-    const uint32_t C = len / kChunk, per_pass = blockDim.x >> 3;
+    const uint32_t s = (threadIdx.x >> 3) & 1u, uq = threadIdx.x & 7u;
+    const uint32_t C = (len + kChunk - 1) / kChunk, per_pass = blockDim.x >> 4;
     int wmax = -2000;
     for (uint32_t c0 = 0; c0 < C; c0 += per_pass) {
-        const uint32_t c = c0 + (threadIdx.x >> 3);
-        const bool live = c < C && s < S;
-        const uint32_t u = c * 4 + uq;  // this thread's unit within the part
+        const uint32_t c = c0 + (threadIdx.x >> 4);
+        const uint32_t u = c * 8 + uq;  // this thread's unit within the part
+        const bool live = c < C && s < S && u * 8 < len;
         double v[8];
         int e = -2000;
         if (live) {
-            const double* row = x + s * side_stride + u * 8;
+            const double* row = x + s * side_stride;
 #pragma unroll
             for (uint32_t k = 0; k < 4; ++k) {
-                const double2 q = *reinterpret_cast<const double2*>(row + part_slot(u * 8 + 2 * k, s) - u * 8);
+                const double2 q = *reinterpret_cast<const double2*>(row + part_slot(u * 8 + 2 * k));
                 v[2 * k] = q.x;
                 v[2 * k + 1] = q.y;
             }
@@ -239,11 +247,11 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
             for (uint32_t k = 0; k < 8; ++k) e = max(e, exp_of(v[k]));
         }
 #pragma unroll
-        for (int o = 1; o < 8; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        for (int o = 1; o < 16; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
         e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
         if (live) {
             store_unit_digits(v, e, xdig + s * xside_stride + (uint64_t)u * unit_stride);
-            if ((threadIdx.x & 7u) == 0) xexp[c] = (int16_t)e;
+            if ((threadIdx.x & 15u) == 0) xexp[c] = (int16_t)e;
         }
         if (c < C) wmax = max(wmax, e);
     }
@@ -259,23 +267,35 @@ __device__ __forceinline__ void digitize_trial(const double* x, uint32_t side_st
 
 // ---- trial slices: the split engine's trials for batches on counter
 // streams, runs of at most kSliceRows members.  An item of a run is
-// slice_chunks(P) consecutive 32-gene chunks of every member, both sides.
-// trial_slice_kernel is persistent: each CTA walks its items (seg_start[b]
-// .. seg_start[b+1] of the segment list), staging the members' parent rows
-// of an item in shared memory by bulk copies, two items in flight, so each
-// parent gene leaves HBM once however many trials use it as a donor; then it
-// forms every trial gene of the item (written once, coalesced) and its
-// digit planes, whose stores cover consecutive members' 16-byte rows.
-constexpr int kSliceThreads = 256;
-constexpr uint32_t kSliceRows = 64;  // largest population of a sliced run
-// one stage: the parents of an item, [member][side][slice_chunks(P) x 32]
+// slice_chunks(P, S) consecutive 64-gene chunks of every member, both sides.
+// trial_slice_kernel is persistent, one CTA per SM: each CTA walks its items
+// (seg_start[b] .. seg_start[b+1] of the segment list) through three
+// shared-memory stages, each holding every member's parent rows of one item
+// (bulk copies, so each parent gene leaves HBM once however many trials use
+// it as a donor).  Warp w forms the trials of one group of members for one
+// chunk of the item: lane = (member, side, unit of 8 genes), so the chunk's
+// scale exponent is a shuffle maximum over the member's lanes, the digits
+// are made from registers, and each trial gene is written once.  The last
+// warp done with an item stages the item three ahead in its place.
+constexpr int kSliceThreads = 1024;
+constexpr uint32_t kSliceWarps = kSliceThreads / 32;
+constexpr uint32_t kSliceRows = 64;   // largest population of a sliced run
+constexpr uint32_t kSliceStages = 3;
+// one stage: the parents of an item, [member][side][slice_chunks x 64] --
+// at most 64 x 2 x 64 doubles (slice_chunks keeps P S chunks <= 128)
 constexpr uint32_t kSliceStageDoubles = kSliceRows * 2 * kChunk;
-// the item's trials, rows padded by 2 doubles (16 bytes: an odd number of
-// 16-byte units per row spreads the digit pass's row reads over the banks)
-constexpr uint32_t kSliceTrialDoubles = kSliceStageDoubles + 2 * kSliceRows;
-// two stages, the trials, and one chunk exponent per (member, chunk)
-constexpr uint32_t kSliceSmemBytes = (2 * kSliceStageDoubles + kSliceTrialDoubles) * 8 + kSliceRows * 4;
-__host__ __device__ inline uint32_t slice_chunks(uint32_t P) { return kSliceRows / P; }
+constexpr uint32_t kSliceSmemBytes = kSliceStages * kSliceStageDoubles * 8;
+// members per warp: 32 lanes over 8 units x S sides each
+__host__ __device__ inline uint32_t slice_rows_per_warp(uint32_t S) { return 4 / S; }
+// member groups of a run: one warp each per chunk
+__host__ __device__ inline uint32_t slice_groups(uint32_t P, uint32_t S) {
+    return (P + slice_rows_per_warp(S) - 1) / slice_rows_per_warp(S);
+}
+// chunks per item: the groups times the chunks fill at most the CTA's warps
+__host__ __device__ inline uint32_t slice_chunks(uint32_t P, uint32_t S) {
+    const uint32_t g = slice_groups(P, S);
+    return g >= kSliceWarps ? 1u : kSliceWarps / g;
+}
 struct SliceSeg {
     uint32_t run, item0, item1;  // items [item0, item1) of one run
 };
@@ -283,7 +303,5 @@ __global__ void trial_slice_kernel(RunDev* runs, const SliceSeg* segs, const uin
 // status value of a CTA whose bulk-copy wait gave up
 constexpr int kStatusSliceWait = 2;
 
-// host-side digit decomposition of one value for a given scale exponent
-void digits_of(double v, int e, uint16_t out[kDigits]);
 
 }  // namespace deac
