@@ -38,14 +38,21 @@ __device__ __forceinline__ void slice_settle(SliceCursor& c, const SliceSeg* seg
 
 // What the warps need of a staged item's run: this generation's CR / F
 // thresholds and weights, mutant indices, jDE step and parent buffer of
-// every member (written by the warp that stages the item).
+// every member, and the run's fields (written by the warp that stages the
+// item, only when the stage's table is of another run).
 struct SliceTable {
     uint64_t thr[2][kSliceRows];
     double fw[2][kSliceRows];
     uint64_t step[kSliceRows];
     uint8_t mut[3][kSliceRows];
     uint8_t cur[kSliceRows];
-    uint32_t run, item;  // run kNoItem: the CTA's items are exhausted
+    // the run's fields the warps use (a copy of its description)
+    double* pop;
+    uint16_t* xdig;
+    int16_t* xexp;
+    uint64_t key_x, xdig_unit, xdig_side;
+    uint32_t P, S, M, xdig_row0, keep_sign;
+    uint32_t run, item;  // item kNoItem: the CTA's items are exhausted
 };
 
 }  // namespace
@@ -67,6 +74,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
             mbar_init(&s_full[q], 1);
             s_done[q] = 0;
             s_armed[q] = 0;
+            s_tab[q].run = kNoItem;
         }
         mbar_init_fence();
         s_fail = 0;
@@ -85,39 +93,53 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
         SliceTable& T = s_tab[st];
         if (c.g >= se) {
             if (lane == 0) {
-                T.run = kNoItem;
+                T.item = kNoItem;
                 mbar_arrive(&s_full[st]);
             }
             __syncwarp();
             return;
         }
         const uint32_t run = segs[c.g].run;
-        const RunDev& R = runs[run];
-        const uint32_t P = R.P, S = R.S, M = R.M;
+        if (T.run != run) {
+            const RunDev& R = runs[run];
+            const uint32_t P = R.P, S = R.S;
+            for (uint32_t m = lane; m < P; m += 32) {
+                T.cur[m] = R.cur[m];
+                for (uint32_t s = 0; s < S; ++s) {
+                    T.thr[s][m] = crossover_threshold(R.cr[(uint64_t)S * P + s * P + m]);
+                    T.fw[s][m] = R.fw[(uint64_t)S * P + s * P + m];
+                }
+                for (uint32_t q = 0; q < 3; ++q) T.mut[q][m] = (uint8_t)R.mutants[3 * m + q];
+                T.step[m] = R.rng[m] - 1;  // the jDE step this trial's CR / F and mutants come from
+            }
+            if (lane == 0) {
+                T.pop = R.pop;
+                T.xdig = R.xdig;
+                T.xexp = R.xexp;
+                T.key_x = R.key_crossover;
+                T.xdig_unit = R.xdig_unit;
+                T.xdig_side = R.xdig_side;
+                T.P = P;
+                T.S = S;
+                T.M = R.M;
+                T.xdig_row0 = R.xdig_row0;
+                T.keep_sign = (R.flags & kSignedWeights) != 0;
+                T.run = run;
+            }
+        }
+        if (lane == 0) T.item = c.it;
+        __syncwarp();
+        const uint32_t P = T.P, S = T.S, M = T.M;
         const uint32_t L = slice_chunks(P, S) * kChunk;
         const uint32_t j0 = c.it * L;
         const uint32_t len = M - j0 < L ? M - j0 : L;
         const uint64_t PM = (uint64_t)P * M;
-        for (uint32_t m = lane; m < P; m += 32) {
-            T.cur[m] = R.cur[m];
-            for (uint32_t s = 0; s < S; ++s) {
-                T.thr[s][m] = crossover_threshold(R.cr[(uint64_t)S * P + s * P + m]);
-                T.fw[s][m] = R.fw[(uint64_t)S * P + s * P + m];
-            }
-            for (uint32_t q = 0; q < 3; ++q) T.mut[q][m] = (uint8_t)R.mutants[3 * m + q];
-            T.step[m] = R.rng[m] - 1;  // the jDE step this trial's CR / F and mutants come from
-        }
-        if (lane == 0) {
-            T.run = run;
-            T.item = c.it;
-        }
-        __syncwarp();
         if (lane == 0) mbar_expect_tx(&s_full[st], P * S * len * (uint32_t)sizeof(double));
         __syncwarp();
         double* dst = slice_s + (uint64_t)st * kSliceStageDoubles;
         for (uint32_t q = lane; q < P * S; q += 32) {
             const uint32_t m = q / S, s = q - m * S;
-            const double* src = R.pop + ((uint64_t)T.cur[m] * S + s) * PM + (uint64_t)m * M + j0;
+            const double* src = T.pop + ((uint64_t)T.cur[m] * S + s) * PM + (uint64_t)m * M + j0;
             bulk_load(dst + (uint64_t)q * L, src, len * (uint32_t)sizeof(double), &s_full[st]);
         }
         ++c.it;
@@ -171,87 +193,104 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
             break;
         }
         const SliceTable& T = s_tab[st];
+        if (T.item == kNoItem) break;
         const uint32_t rn = T.run;
-        if (rn == kNoItem) break;
-        RunDev& R = runs[rn];
         if (rn != run) {
             flush();
             run = rn;
-            P = R.P;
-            S = R.S;
+            P = T.P;
+            S = T.S;
         }
-        const uint32_t M = R.M;
+        const uint32_t M = T.M;
         const uint32_t cpi = slice_chunks(P, S), L = cpi * kChunk;
         const uint32_t j0 = T.item * L;
         const uint32_t len = M - j0 < L ? M - j0 : L;
         const uint32_t nch = (len + kChunk - 1) / kChunk;
         const uint32_t G = slice_groups(P, S);
         if (warp < G * nch) {
-            // ---- one chunk of one member group: lane = (member, side, unit)
-            const uint32_t LR = 8 * S;
+            // ---- one chunk of one member group
+            const uint32_t RW = slice_rows_per_warp(S), LR = 8 * S;
             const uint32_t c = warp / G;
-            const uint32_t row = (warp - c * G) * slice_rows_per_warp(S) + lane / LR;
-            const uint32_t s = (lane % LR) >> 3, u = lane & 7u;
-            const uint32_t jl = c * kChunk + u * 8;  // the unit's first gene within the item
-            const bool live = row < P && jl < len;
-            const uint32_t rr = row < P ? row : 0;
+            const uint32_t row0 = (warp - c * G) * RW;
+            const uint32_t jc = c * kChunk;                             // the chunk's first gene in the item
+            const uint32_t halves = len - jc < (uint32_t)kChunk ? 1u : 2u;  // 32-gene halves of the chunk
             const double* par = slice_s + (uint64_t)st * kSliceStageDoubles;
             const uint64_t PM = (uint64_t)P * M;
-            double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-            bool mutated = false;
-            int e = -2000;
-            if (live) {
-                const double* px = par + ((uint64_t)rr * S + s) * L + jl;
-                const double* pa = par + ((uint64_t)T.mut[0][rr] * S + s) * L + jl;
-                const double* pb = par + ((uint64_t)T.mut[1][rr] * S + s) * L + jl;
-                const double* pc = par + ((uint64_t)T.mut[2][rr] * S + s) * L + jl;
-                const uint64_t thr = T.thr[s][rr];
-                const double fw = T.fw[s][rr];
-                const bool keep_sign = (R.flags & kSignedWeights) != 0;
-                const uint64_t pos = ((T.step[rr] * P + rr) * S + s) * (uint64_t)M + j0 + jl;
-                const uint64_t key_x = R.key_crossover;
-#pragma unroll
-                for (uint32_t h = 0; h < 4; ++h) {
-                    const double2 x = reinterpret_cast<const double2*>(px)[h];
-                    const double2 a = reinterpret_cast<const double2*>(pa)[h];
-                    const double2 b = reinterpret_cast<const double2*>(pb)[h];
-                    const double2 cc = reinterpret_cast<const double2*>(pc)[h];
-#pragma unroll
-                    for (uint32_t q = 0; q < 2; ++q) {
-                        const uint32_t kk = 2 * h + q;
-                        const bool mutate = (stream_draw(key_x, pos + kk) >> 11) < thr;
-                        double w = q ? x.y : x.x;
+            const uint64_t key_x = T.key_x;
+            const bool keep_sign = T.keep_sign != 0;
+            // formation, lane = gene: per member of the group, side and half,
+            // 32 consecutive genes (conflict-free reads of the staged parents,
+            // coalesced trial stores); the chunk's exponent and mutation flag
+            // of the member this lane digitises below
+            int my_e = -2000;
+            bool my_mut = false;
+            for (uint32_t mm = 0; mm < RW; ++mm) {
+                const uint32_t row = row0 + mm;
+                if (row >= P) break;
+                const double* pa = par + (uint64_t)T.mut[0][row] * S * L;
+                const double* pb = par + (uint64_t)T.mut[1][row] * S * L;
+                const double* pc = par + (uint64_t)T.mut[2][row] * S * L;
+                const double* px = par + (uint64_t)row * S * L;
+                double* dst = T.pop + (uint64_t)(1u - T.cur[row]) * S * PM + (uint64_t)row * M + j0;
+                const uint64_t pos0 = (T.step[row] * P + row) * S;
+                int em = -2000;
+                bool mt = false;
+                double z = 0.0;  // side 0's gene 0 (lane 0 of the first half)
+                for (uint32_t s = 0; s < S; ++s) {
+                    const uint64_t thr = T.thr[s][row];
+                    const double fw = T.fw[s][row];
+                    for (uint32_t h = 0; h < halves; ++h) {
+                        const uint32_t jl = jc + h * 32 + lane;
+                        const uint32_t o = s * L + jl;
+                        const bool mutate = (stream_draw(key_x, (pos0 + s) * M + j0 + jl) >> 11) < thr;
+                        double v = px[o];
                         if (mutate) {
-                            w = fma(fw, (q ? b.y : b.x) - (q ? cc.y : cc.x), q ? a.y : a.x);
+                            v = fma(fw, pb[o] - pc[o], pa[o]);
                             if (!keep_sign)
-                                w = __longlong_as_double(__double_as_longlong(w) & 0x7FFFFFFFFFFFFFFFll);  // fabs
-                            mutated = true;
+                                v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
+                            mt = true;
                         }
-                        v[kk] = w;
+                        if (j0 + jl == 0) {
+                            if (s == 0) z = v;
+                            else v = z;  // gpu_match_population_zero
+                        }
+                        dst[(uint64_t)s * PM + jl] = v;
+                        em = max(em, exp_of(v));
                     }
                 }
+                em = __reduce_max_sync(0xffffffffu, em);
+                mt = __any_sync(0xffffffffu, mt);
+                if (lane / LR == mm) {
+                    my_e = em;
+                    my_mut = mt;
+                }
             }
-            // gpu_match_population_zero: side 1's gene 0 takes side 0's (held
-            // by the member's first lane)
-            const double z = __shfl_sync(0xffffffffu, v[0], lane & ~(LR - 1u));
-            if (live && s == 1 && j0 + jl == 0) v[0] = z;
-            if (live) {
-                double* dst = R.pop + ((uint64_t)(1u - T.cur[rr]) * S + s) * PM + (uint64_t)rr * M + j0 + jl;
+            // the warp's trial stores are visible to all its lanes (a
+            // warp-wide barrier orders memory among its threads)
+            __syncwarp();
+            // digits, lane = (member, side, unit of 8 genes): the unit's
+            // trial genes read back (from the caches) and sliced at the
+            // chunk's scale
+            const uint32_t row = row0 + lane / LR;
+            const uint32_t s = (lane % LR) >> 3, u = lane & 7u;
+            if (row < P && u < halves * 4) {
+                const uint32_t jl = jc + u * 8;
+                const double2* src = reinterpret_cast<const double2*>(
+                    T.pop + ((uint64_t)(1u - T.cur[row]) * S + s) * PM + (uint64_t)row * M + j0 + jl);
+                double v[8];
 #pragma unroll
-                for (uint32_t h = 0; h < 4; ++h)
-                    reinterpret_cast<double2*>(dst)[h] = make_double2(v[2 * h], v[2 * h + 1]);
-#pragma unroll
-                for (uint32_t kk = 0; kk < 8; ++kk) e = max(e, exp_of(v[kk]));
-            }
-            for (uint32_t o = 1; o < LR; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-            e = e <= -1500 ? -1000 : e + 1;  // scale 2^e > every |v| of the chunk
-            if (live) {
+                for (uint32_t q = 0; q < 4; ++q) {
+                    const double2 w = src[q];
+                    v[2 * q] = w.x;
+                    v[2 * q + 1] = w.y;
+                }
+                const int e = my_e <= -1500 ? -1000 : my_e + 1;  // scale 2^e > every |v| of the chunk
                 store_unit_digits(v, e,
-                                  R.xdig + xdig_row_offset(R.xdig_row0 + rr) + s * R.xdig_side +
-                                      (uint64_t)((j0 + jl) >> 3) * R.xdig_unit);
-                if (s == 0 && u == 0) R.xexp[(uint64_t)rr * split_chunks(M) + (j0 + jl) / kChunk] = (int16_t)e;
+                                  T.xdig + xdig_row_offset(T.xdig_row0 + row) + s * T.xdig_side +
+                                      (uint64_t)((j0 + jl) >> 3) * T.xdig_unit);
+                if (s == 0 && u == 0) T.xexp[(uint64_t)row * split_chunks(M) + (j0 + jc) / kChunk] = (int16_t)e;
                 lane_max = max(lane_max, e);
-                lane_mut = lane_mut || mutated;
+                lane_mut = lane_mut || my_mut;
             }
         }
         // the last warp done with the stage stages the item kSliceStages on
