@@ -41,11 +41,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// whether the phase with parity `phase` has completed
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t phase) {
+// whether the phase with parity `phase` has completed, the thread suspended
+// in the meantime (woken when the phase completes, or after a time limit
+// of the hardware's choosing)
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t phase) {
     uint32_t done;
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
         : "r"(smem_u32(bar)), "r"(phase)
         : "memory");
@@ -55,11 +57,11 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t phase) {
 // Wait for the completion of the mbarrier phase with parity `phase`, giving
 // up after kWaitNs of wall time (the caller then reports an error).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+    if (mbar_try(bar, phase)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
-        if (mbar_test(bar, phase)) return true;
+        if (mbar_try(bar, phase)) return true;
         if (global_ns() - t0 > kWaitNs) return false;
-        __nanosleep(64);
     }
 }
 

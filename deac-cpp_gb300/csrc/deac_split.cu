@@ -167,21 +167,15 @@ __device__ __forceinline__ void store_estimate(const RunDev& R, SplitRun& X, con
 // another role of the CTA gave up (*abort) or after kWaitNs (then setting
 // *abort, which makes every role of the CTA leave its loop).
 __device__ __forceinline__ bool mbar_wait_or(uint64_t* bar, uint32_t phase, volatile int* abort) {
+    if (mbar_try(bar, phase)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(phase)
-            : "memory");
-        if (done) return true;
+        if (mbar_try(bar, phase)) return true;
         if (*abort) return false;
         if (global_ns() - t0 > kWaitNs) {
             *abort = 1;
             return false;
         }
-        __nanosleep(32);
     }
 }
 
@@ -576,18 +570,7 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
         for (uint32_t ks = 0; ks < 2; ++ks) {
             const uint32_t n = s_armed[ks];
             if (n == 0) continue;
-            const uint64_t t0 = global_ns();
-            for (;;) {
-                uint32_t done;
-                asm volatile(
-                    "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, "
-                    "p;\n}\n"
-                    : "=r"(done)
-                    : "r"(smem_u32(&s_full[ks])), "r"((n - 1) & 1u)
-                    : "memory");
-                if (done || global_ns() - t0 > kWaitNs) break;
-                __nanosleep(64);
-            }
+            mbar_wait(&s_full[ks], (n - 1) & 1u);
         }
     }
     __syncthreads();
