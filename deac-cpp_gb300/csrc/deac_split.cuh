@@ -180,34 +180,36 @@ __device__ __forceinline__ uint32_t part_slot(uint32_t j) {
     return j ^ ((((j >> 4) & 1u) << 2) | (((j >> 5) & 1u) << 1));
 }
 
-// BF16 bits (in the upper half of the word) of the 7-bit digit of f at bit
-// `shift`, negated when sg = -1: (2^23 + d) - 2^23 in one exact FMA, which
-// gives +0 for d = 0 on either sign.
-__device__ __forceinline__ uint32_t digit_bits(uint64_t f, int shift, float sg) {
-    const uint32_t d = (uint32_t)(f >> shift) & 127u;
-    return __float_as_uint(__fmaf_rn(sg, __uint_as_float(0x4B000000u | d), -sg * 8388608.0f));
-}
-
 // The seven digit planes of one 16-byte unit (8 genes v) at scale 2^e:
-// one 16-byte store per plane at q, q + kXdigDigit, ...
+// one 16-byte store per plane at q, q + kXdigDigit, ...  Two genes' digits
+// d, d' (7 bits each) of a plane are made at once, as one exact packed BF16
+// FMA: sign * (128 + d) - sign * 128 = sign * d (128 + d and 128 are BF16
+// numbers; d = 0 gives +0 on either sign), the pair packed as the plane's
+// 32-bit word (gene 2k in the low half).
 __device__ __forceinline__ void store_unit_digits(const double v[8], int e, uint16_t* q) {
     uint64_t f[8];
-    float sg[8];
+    uint32_t sg[4], nb[4];  // per pair: the signs as BF16 +-1, and -sign * 128
 #pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) {
-        f[k] = frac_digits(v[k], e);
-        // the sign bit (integer test: FP64 compares share the narrow FP64
-        // pipe); -0 and zero digits give +0 either way
-        sg[k] = __double_as_longlong(v[k]) < 0 ? -1.0f : 1.0f;
+    for (uint32_t k = 0; k < 8; ++k) f[k] = frac_digits(v[k], e);
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        // the sign bits (integer tests: FP64 compares share the narrow FP64 pipe)
+        const uint32_t n0 = (uint32_t)((uint64_t)__double_as_longlong(v[2 * k]) >> 63);
+        const uint32_t n1 = (uint32_t)((uint64_t)__double_as_longlong(v[2 * k + 1]) >> 63);
+        const uint32_t m = (n0 << 15) | (n1 << 31);  // sign bits of the two halves
+        sg[k] = 0x3F803F80u | m;                      // +-1.0
+        nb[k] = 0xC300C300u ^ m;                      // -+128.0
     }
 #pragma unroll
     for (int b = 0; b < kDigits; ++b) {
         const int sh = 7 * (kDigits - 1 - b);
         uint32_t w[4];
 #pragma unroll
-        for (uint32_t k = 0; k < 4; ++k)
-            w[k] = __byte_perm(digit_bits(f[2 * k], sh, sg[2 * k]), digit_bits(f[2 * k + 1], sh, sg[2 * k + 1]),
-                               0x7632);
+        for (uint32_t k = 0; k < 4; ++k) {
+            const uint32_t lo = (uint32_t)(f[2 * k] >> sh) & 127u, hi = (uint32_t)(f[2 * k + 1] >> sh) & 127u;
+            const uint32_t x = 0x43004300u | lo | (hi << 16);  // BF16 pair (128 + d, 128 + d')
+            asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(w[k]) : "r"(sg[k]), "r"(x), "r"(nb[k]));
+        }
         *reinterpret_cast<uint4*>(q + b * kXdigDigit) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }

@@ -163,6 +163,9 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
     // this warp's bookkeeping of its members in the current run: the largest
     // chunk exponent and whether a gene mutated, per lane, raised into the
     // run's arrays when the warp leaves the run
+    // the stream's Weyl increment, and this lane's multiple of it
+    constexpr uint64_t kGamma = 0x9E3779B97F4A7C15ull;
+    const uint64_t lane_gamma = (uint64_t)lane * kGamma;
     uint32_t run = kNoItem, P = 0, S = 1;
     int lane_max = -2000;
     bool lane_mut = false;
@@ -239,13 +242,30 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                 for (uint32_t s = 0; s < S; ++s) {
                     const uint64_t thr = T.thr[s][row];
                     const double fw = T.fw[s][row];
-                    for (uint32_t h = 0; h < halves; ++h) {
+                    // the draws of this side's chunk genes are consecutive
+                    // stream outputs: the Weyl value of gene jc + 32 h + lane
+                    // is w0 + (32 h + lane) gamma
+                    const uint64_t w0 = key_x + ((pos0 + s) * M + j0 + jc + 1) * kGamma + lane_gamma;
+                    // both 32-gene halves at once (independent loads, draws
+                    // and FMAs in flight)
+                    double x[2], a[2], b[2], cc[2];
+#pragma unroll
+                    for (uint32_t h = 0; h < 2; ++h) {
+                        const uint32_t o = s * L + jc + h * 32 + lane;
+                        const bool in = h < halves;
+                        x[h] = in ? px[o] : 0.0;
+                        a[h] = in ? pa[o] : 0.0;
+                        b[h] = in ? pb[o] : 0.0;
+                        cc[h] = in ? pc[o] : 0.0;
+                    }
+#pragma unroll
+                    for (uint32_t h = 0; h < 2; ++h) {
+                        if (h >= halves) continue;
                         const uint32_t jl = jc + h * 32 + lane;
-                        const uint32_t o = s * L + jl;
-                        const bool mutate = (stream_draw(key_x, (pos0 + s) * M + j0 + jl) >> 11) < thr;
-                        double v = px[o];
+                        const bool mutate = (splitmix_mix(w0 + h * (32 * kGamma)) >> 11) < thr;
+                        double v = x[h];
                         if (mutate) {
-                            v = fma(fw, pb[o] - pc[o], pa[o]);
+                            v = fma(fw, b[h] - cc[h], a[h]);
                             if (!keep_sign)
                                 v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
                             mt = true;
