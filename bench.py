@@ -494,6 +494,7 @@ def engine_arm(args, world, rank, local):
     split, ms, clocks = timed_engine(deac_gb300.ENGINE_SPLIT_BF16, configs, args, local, stream, world, True, G,
                                      "counter")
     counts = [split.split_counts(r) for r in range(n)]
+    launches_per_generation = split.generation_launches()
     # per-kernel device time (kernels launched one by one, bracketed by
     # events on the batch stream), for the roofline of the dominant kernel
     split.enable_timing(True)
@@ -585,9 +586,9 @@ def engine_arm(args, world, rank, local):
                 "d2h_bytes_per_step": d2h // args.steps,
                 "includes": "batch creation, set-up from host arrays, K steps with a status read each, "
                             "every run's result fetched at the end"},
-        # per generation: trial parts, tensor contraction, combine, selection,
-        # the exact pass
-        "gpu_launches": 5 * G * args.steps,
+        # per generation: trial slices, tensor contraction, (the partial-sum
+        # combine where tiles are split), selection, the exact pass
+        "gpu_launches": launches_per_generation * G * args.steps,
         "clocks": clocks,
     }
     if early:

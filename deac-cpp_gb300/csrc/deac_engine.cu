@@ -343,6 +343,53 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
 
 int launch_generation_timed(deac_batch* b) { return launch_generation(b, b->stream, 0, true); }
 
+// Split engine, generation 0: the initial population's moments and
+// normalisation (trial_kernel's initial pass), its digit slices, the
+// tensor-core estimate of every parent and its fitness interval
+// (split_init_kernel), the exact FP64 fitness of the members the intervals
+// leave open and generation 0's bookkeeping (contract_kernel's initial pass,
+// which skips every other member), then the first generation's jDE.
+int launch_split_init(deac_batch* b) {
+    cudaStream_t s = b->stream;
+    std::vector<deac::PartWork> pw;
+    uint32_t smax = 1;
+    for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+        const RunHost& r = *b->runs[ri];
+        const uint32_t parts = (uint32_t)((r.M + deac::kTrialPart - 1) / deac::kTrialPart);
+        smax = std::max<uint32_t>(smax, (uint32_t)r.S);
+        for (uint32_t i = 0; i < r.dev.P; ++i)
+            for (uint32_t q = 0; q < parts; q += 8) pw.push_back({ri, i, q, std::min<uint32_t>(8, parts - q)});
+    }
+    deac::PartWork* d_pw = nullptr;
+    CUDA_TRY(cudaMalloc(&d_pw, pw.size() * sizeof(deac::PartWork)));
+    struct Free {
+        void* p;
+        ~Free() { cudaFree(p); }
+    } free_pw{d_pw};
+    CUDA_TRY(copy(b, d_pw, pw.data(), pw.size() * sizeof(deac::PartWork), cudaMemcpyHostToDevice));
+    deac::trial_kernel<<<b->n_trial_ctas, deac::kTrialThreads, b->trial_smem_bytes, s>>>(b->d_runs, b->d_trial_work,
+                                                                                          1, b->smem_doubles);
+    deac::parent_digits_kernel<<<(uint32_t)pw.size(), deac::kTrialPartThreads,
+                                 (size_t)smax * deac::kTrialPart * sizeof(double), s>>>(
+        b->d_runs, static_cast<const deac::PartWork*>(d_pw));
+    launch(deac::split_contract_kernel, b->n_split_ctas, deac::kSplitThreads, deac::split_smem_bytes(2), s, false,
+           b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
+           static_cast<const deac::SplitWork*>(b->d_split_work), static_cast<const deac::SplitRow*>(b->d_rows),
+           static_cast<const CUtensorMap*>(b->d_maps), b->d_partial, b->d_status);
+    if (b->n_combine_tiles)
+        launch(deac::split_combine_kernel, b->n_combine_tiles * deac::kCombineCtasPerTile, 256, 0, s, false,
+               b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
+               static_cast<const uint32_t*>(b->d_combine_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
+               static_cast<const float4*>(b->d_partial));
+    deac::split_init_kernel<<<b->n_trial_ctas, deac::kInitThreads, 0, s>>>(b->d_runs, b->d_split, b->d_trial_work);
+    launch_contract(b, s, deac::kModeInit);
+    deac::jde_kernel<<<(b->n_trial_ctas + 127) / 128, 128, 0, s>>>(
+        b->d_runs, static_cast<const deac::Work*>(b->d_trial_work), b->n_trial_ctas);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(s));  // before the work list is freed
+    return DEAC_OK;
+}
+
 // Take the snapshot the result and fetch calls read; nothing is done again
 // until the next launch.  Split engine: first make exact the fitness of the
 // parents that may hold each run's minimum (the best member, the reported
@@ -1286,7 +1333,12 @@ int deac_batch_setup(deac_batch* b) {
     }
     CUDA_TRY(cudaDeviceSynchronize());
     // initial fitness, statistics of generation 0 and the first stop test
-    launch_generation(b, b->stream, 1);
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        int rc = launch_split_init(b);
+        if (rc) return rc;
+    } else {
+        launch_generation(b, b->stream, 1);
+    }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->set_up = true;
@@ -1753,6 +1805,20 @@ int deac_batch_autotune(deac_batch* b, uint64_t generations, deac_tune_report* o
     out->ms_per_generation = best_ms;
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     g_tune_cache[key] = {best_parts, best_waves};
+    return DEAC_OK;
+}
+
+int deac_batch_generation_launches(const deac_batch* b, uint32_t* launches) {
+    if (!b || !launches) return fail(DEAC_E_INVALID, "null argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    // as launch_generation issues them
+    if (b->engine == DEAC_ENGINE_PLAIN_FP64) {
+        *launches = 2;  // trial_kernel, contract_kernel
+    } else {
+        *launches = (b->n_part_ctas ? 1u : 0u) + (b->n_slice_ctas ? 1u : 0u) + (b->n_norm_ctas ? 1u : 0u) +
+                    1u /* split_contract_kernel */ + (b->n_combine_tiles ? 1u : 0u) +
+                    1u /* split_select_kernel */ + 1u /* exact_pass_kernel */;
+    }
     return DEAC_OK;
 }
 

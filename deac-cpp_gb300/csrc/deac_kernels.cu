@@ -607,6 +607,33 @@ __global__ void __launch_bounds__(kTrialPartThreads, 4) trial_part_counter_kerne
     trial_part_body<true>(runs, work);
 }
 
+// Split engine, generation 0: the digit slices of member i's parent (the
+// initial population, normalised in place by trial_kernel), parts [part0,
+// part0 + nparts) of 512 genes per side, so that the tensor-core contraction
+// can estimate the initial fitness.  Raises the member's maximum chunk
+// exponent, which the generation-0 decision resets.
+__global__ void __launch_bounds__(kTrialPartThreads) parent_digits_kernel(RunDev* runs, const PartWork* work) {
+    extern __shared__ __align__(16) double part_s[];  // [S][len]
+    __shared__ int s_digit_max[kTrialPartThreads / 32];
+    const PartWork wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    const uint32_t i = wk.member, M = R.M, S = R.S;
+    const uint64_t PM = (uint64_t)R.P * M;
+    const double* src = R.pop + (uint64_t)R.cur[i] * S * PM + (uint64_t)i * M;
+    for (uint32_t part = wk.part0; part < wk.part0 + wk.nparts; ++part) {
+        const uint32_t j0 = part * kTrialPart;
+        const uint32_t len = M - j0 < kTrialPart ? M - j0 : kTrialPart;
+        for (uint32_t s = 0; s < S; ++s)
+            for (uint32_t j = threadIdx.x; j < len; j += blockDim.x)
+                part_s[s * len + part_slot(j)] = src[(uint64_t)s * PM + j0 + j];
+        __syncthreads();
+        // (ends with a barrier after its last read of part_s)
+        digitize_trial(part_s, len, S, len,
+                       R.xdig + xdig_row_offset(R.xdig_row0 + i) + (uint64_t)(j0 >> 3) * R.xdig_unit, R.xdig_unit,
+                       R.xdig_side, R.xexp + (uint64_t)i * split_chunks(M) + j0 / kChunk, R.xexp_max + i, s_digit_max);
+    }
+}
+
 // ---------------------------------------------------------------- norm
 // Split engine, runs that normalise (kDeferNorm) or have moment terms: one
 // CTA per raw trial forms its exact row sums (warps 0-7 the positive side,
@@ -743,7 +770,10 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
         __syncthreads();
     }
     auto wanted_in = [&](int pm, uint32_t m) -> bool {
-        if (pm == kModeGeneration || pm == kModeInit) return true;
+        if (pm == kModeGeneration) return true;
+        // split engine: the members generation 0's interval left open (all
+        // of them in runs whose statistics or terms need exact values)
+        if (pm == kModeInit) return R.f_lo == nullptr || R.recheck[m] != 0;
         if (pm == kModeTrials) return R.recheck[m] != 0;
         const bool inexact = R.f_lo[m] != R.f_hi[m];
         if (pm == kModeFinalBest) return inexact && R.f_lo[m] <= s_min_hi;

@@ -242,6 +242,9 @@ __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const PartWork* work);
 // the same for batches that draw from counter streams
 __global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
+// split engine, generation 0: the BF16 digit slices of every member's
+// initial parent (the trial planes' rows), parts as trial_part_kernel's
+__global__ void parent_digits_kernel(RunDev* runs, const PartWork* work);
 // split engine, runs that normalise (kDeferNorm) or have moment terms: the
 // exact normalisation row sums of one raw trial per CTA (both sides), the
 // reciprocal norm and the final `changed` flag, then its moment row sums

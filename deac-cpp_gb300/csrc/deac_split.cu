@@ -626,6 +626,62 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     store_estimate(R, X, rw, t, tile, hi, lo, b);
 }
 
+// ------------------------------------------------- chi^2 and its interval
+// One timeslice's term of chi^2 from the estimate em (of the raw trial when
+// `defer`, to be scaled by rc = 1/norm) with its bound eb0, and of the bound
+// on chi^2's distance from the value the FP64 engine computes (any summation
+// order: the rounding term covers n-term sums).  kDeferNorm: the kept trial
+// is RN(gene / norm) per gene; scaled estimate and bound: the raw bound twice
+// over (its FP64-chain term counts normalised genes, whose scale exponents
+// can exceed the raw ones times 1/norm by a factor two), 0.001 of it more
+// for the per-gene roundings (at most 2^-47 B while the raw bound is at
+// least 2^-33 B), and 2^-51 |E| for the product's rounding.  The bound is
+// formed in FP64 rounded upward (every term is non-negative, so each rounding
+// up keeps an upper bound): early in a run with sigma far below F's scale
+// the residuals reach 1e130 sigma and more, beyond the float range.
+__device__ __forceinline__ void chi_term(double em, double eb0, double f, double ie, bool defer, double rc,
+                                         double& chi, double& dchi) {
+    const double e = defer ? em * rc : em;
+    // r carries up to three roundings of 2^-53 each
+    const double r = (f - e) * ie;
+    chi = fma(r, r, chi);
+    const double ar = fabs(r);
+    const double eb =
+        defer ? __dadd_ru(__dmul_ru(__dmul_ru(2.001, eb0), fabs(rc)), __dmul_ru(fabs(e), 0x1p-51)) : eb0;
+    const double dr = __dadd_ru(__dmul_ru(__dmul_ru(eb, ie), 1.0 + 0x1p-20), __dmul_ru(ar, 0x1p-51));
+    dchi = __fma_ru(__dadd_ru(2.0 * ar, dr), dr, dchi);
+}
+
+// The interval [lo, hi] holding the FP64 engine's fitness, from the summed
+// chi (any order) and bound dchi: /Nt as a product with 1/Nt rounded once
+// (two roundings where a quotient has one, covered by two more units of the
+// slack), then the exact moment terms (mom1, mom3: the member's first and
+// third moments) added as contract_kernel adds them -- each step is
+// monotone in the fitness so far, so the interval's ends map to the ends.
+__device__ __forceinline__ void chi_interval(const RunDev& R, double chi, double dchi, double inv_nt, double mom1,
+                                             double mom3, double& lo, double& hi) {
+    const uint32_t Nt = R.Nt;
+    chi *= inv_nt;
+    const double dchi_d = __dadd_ru(__dmul_ru(__dmul_ru(dchi, inv_nt), 1.0 + 0x1p-50),
+                                    __dmul_ru(__dmul_ru(chi, (double)(Nt + 10)), 0x1p-52));
+    lo = __dsub_rd(chi, dchi_d);
+    hi = __dadd_ru(chi, dchi_d);
+    if (R.flags & kFirstMomentCpu) {
+        const double d = mom1 - R.first_target, q = (d * d) / R.first_target;
+        lo = lo + q;
+        hi = hi + q;
+    } else if (R.flags & kFirstMoment) {
+        const double t1 = (R.first_target - mom1) / 1.0;
+        lo = fma(t1, t1, lo);
+        hi = fma(t1, t1, hi);
+    }
+    if (R.flags & kThirdMoment) {
+        const double t3 = (R.third_target - mom3) / R.third_error;
+        lo = fma(t3, t3, lo);
+        hi = fma(t3, t3, hi);
+    }
+}
+
 // ---------------------------------------------------------------- select
 // One CTA per member, in two roles.  Warps 0-3 form the estimate's chi^2 and
 // its interval and make the selection decision the interval settles
@@ -794,36 +850,12 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         }
     } else {
         // chi^2 of the estimate and a bound on its distance from the value
-        // the FP64 engine computes (any summation order: the rounding term
-        // covers n-term sums)
-        // kDeferNorm: the estimate is of the raw trial; the kept trial is
-        // RN(gene / norm) per gene.  Scaled estimate and bound: the raw bound
-        // twice over (its FP64-chain term counts normalised genes, whose
-        // scale exponents can exceed the raw ones times 1/norm by a factor
-        // two), 0.001 of it more for the per-gene roundings (at most
-        // 2^-47 B while the raw bound is at least 2^-33 B), and 2^-51 |E|
-        // for the product's rounding.
-        // chi^2 in FP64, and its error bound in FP64 rounded upward (every
-        // term is non-negative, so each rounding up keeps an upper bound).
-        // Early in a run with sigma far below F's scale the residuals reach
-        // 1e130 sigma and more: the bound needs the double's range.
-        const double rc_abs = fabs(rc);
+        // the FP64 engine computes (chi_term)
         double chi = 0.0, dchi = 0.0;
-        auto term = [&](double em, double eb0, double f, double ie) {
-            const double e = defer ? em * rc : em;
-            // r carries up to three roundings of 2^-53 each
-            const double r = (f - e) * ie;
-            chi = fma(r, r, chi);
-            const double ar = fabs(r);
-            const double eb = defer ? __dadd_ru(__dmul_ru(__dmul_ru(2.001, eb0), rc_abs), __dmul_ru(fabs(e), 0x1p-51))
-                                    : eb0;
-            const double dr = __dadd_ru(__dmul_ru(__dmul_ru(eb, ie), 1.0 + 0x1p-20), __dmul_ru(ar, 0x1p-51));
-            dchi = __fma_ru(__dadd_ru(2.0 * ar, dr), dr, dchi);
-        };
-        if (t0_ok) term(em0, eb00, f0, ie0);
+        if (t0_ok) chi_term(em0, eb00, f0, ie0, defer, rc, chi, dchi);
         for (uint32_t t = tid + kChiThreads; t < Nt; t += kChiThreads) {
             const uint64_t o = (uint64_t)i * Nt + t;
-            term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t]);
+            chi_term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], defer, rc, chi, dchi);
         }
         for (int o = 16; o > 0; o >>= 1) {
             chi += __shfl_xor_sync(0xffffffffu, chi, o);
@@ -839,29 +871,8 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             chi = (s_chi[0] + s_chi[1]) + (s_chi[2] + s_chi[3]);
             dchi = __dadd_ru(__dadd_ru(s_dchi[0], s_dchi[1]), __dadd_ru(s_dchi[2], s_dchi[3]));
             X.recheck[i] = 0;
-            // /Nt as a product with 1/Nt rounded once: two roundings where a
-            // quotient has one, covered by two more units of the slack below
-            chi *= inv_nt;
-            const double dchi_d = __dadd_ru(__dmul_ru(__dmul_ru(dchi, inv_nt), 1.0 + 0x1p-50),
-                                            __dmul_ru(__dmul_ru(chi, (double)(Nt + 10)), 0x1p-52));
-            double lo = __dsub_rd(chi, dchi_d), hi = __dadd_ru(chi, dchi_d);
-            // the moment terms, exact (norm_kernel's sums equal trial_kernel's),
-            // added as contract_kernel adds them: each step is monotone in the
-            // fitness so far, so the interval's ends map to the ends
-            if (R.flags & kFirstMomentCpu) {
-                const double d = mom1 - R.first_target, q = (d * d) / R.first_target;
-                lo = lo + q;
-                hi = hi + q;
-            } else if (R.flags & kFirstMoment) {
-                const double t1 = (R.first_target - mom1) / 1.0;
-                lo = fma(t1, t1, lo);
-                hi = fma(t1, t1, hi);
-            }
-            if (R.flags & kThirdMoment) {
-                const double t3 = (R.third_target - mom3) / R.third_error;
-                lo = fma(t3, t3, lo);
-                hi = fma(t3, t3, hi);
-            }
+            double lo, hi;
+            chi_interval(R, chi, dchi, inv_nt, mom1, mom3, lo, hi);
             X.t_lo[i] = lo;
             X.t_hi[i] = hi;
             int outcome;
@@ -943,6 +954,67 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
                 R.done = 1;
             }
         }
+    }
+}
+
+// ------------------------------------------------------ generation 0
+// Split engine, generation 0: one CTA (kInitThreads) per member.  The
+// initial parent's fitness as the interval of the tensor-core estimate (its
+// digits by parent_digits_kernel; normalised in place already, so no 1/norm
+// is deferred) plus the exact moment terms of trial_kernel's initial pass.
+// An interval above the stop fitness stands as the parent's fitness (its
+// midpoint in fit_old); the others, and every member of a run whose
+// statistics or negative-first-moment term need exact values, are flagged
+// for contract_kernel's initial pass, which evaluates just those exactly
+// and does generation 0's bookkeeping.  Resets the member's `changed` flag
+// and maximum chunk exponent for the first generation's trials.
+__global__ void __launch_bounds__(kInitThreads) split_init_kernel(RunDev* runs, SplitRun* split, const Work* work) {
+    __shared__ double s_chi[kInitThreads / 32], s_dchi[kInitThreads / 32];
+    const Work wk = work[blockIdx.x];
+    RunDev& R = runs[wk.run];
+    SplitRun& X = split[wk.run];
+    const uint32_t i = wk.index, Nt = R.Nt;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const bool force_exact = (R.flags & (kTrackStats | kNegativeFirstMoment)) != 0;
+    double chi = 0.0, dchi = 0.0;
+    if (!force_exact)
+        for (uint32_t t = tid; t < Nt; t += kInitThreads) {
+            const uint64_t o = (uint64_t)i * Nt + t;
+            chi_term(X.e_mp[o], X.e_bound[o], R.isf[t], X.inv_err[t], false, 1.0, chi, dchi);
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        chi += __shfl_xor_sync(0xffffffffu, chi, o);
+        dchi = __dadd_ru(dchi, __shfl_xor_sync(0xffffffffu, dchi, o));
+    }
+    if (lane == 0) {
+        s_chi[warp] = chi;
+        s_dchi[warp] = dchi;
+    }
+    __syncthreads();
+    if (tid != 0) return;
+    X.changed[i] = 0;
+    X.xexp_max[i] = (int32_t)0x80808080;
+    if (force_exact) {
+        X.recheck[i] = 1;
+        return;
+    }
+    chi = (s_chi[0] + s_chi[1]) + (s_chi[2] + s_chi[3]);
+    dchi = __dadd_ru(__dadd_ru(s_dchi[0], s_dchi[1]), __dadd_ru(s_dchi[2], s_dchi[3]));
+    const double mom1 = (R.flags & kFirstMoment) ? R.moments[2 * i] : 0.0;
+    const double mom3 = (R.flags & kThirdMoment) ? R.moments[2 * i + 1] : 0.0;
+    double lo, hi;
+    chi_interval(R, chi, dchi, X.inv_nt, mom1, mom3, lo, hi);
+    if (lo > R.stop) {
+        X.f_lo[i] = lo;
+        X.f_hi[i] = hi;
+        R.fit_old[i] = 0.5 * (lo + hi);
+        if (R.pmoments) {
+            R.pmoments[2 * i] = mom1;
+            R.pmoments[2 * i + 1] = mom3;
+        }
+        X.recheck[i] = 0;
+    } else {
+        X.recheck[i] = 1;  // settle with the exact FP64 value
     }
 }
 

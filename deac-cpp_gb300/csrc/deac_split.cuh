@@ -139,6 +139,9 @@ __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const Split
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
                                      const uint32_t* combine_tiles, const SplitRow* rows, const float4* partial);
 __global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* work);
+// generation 0: the initial parents' fitness intervals, one CTA per member
+constexpr int kInitThreads = 128;
+__global__ void split_init_kernel(RunDev* runs, SplitRun* split, const Work* work);
 // The digit planes of K (kn null for one-sided K), one CTA per timeslice t:
 // per 32-gene chunk the scale exponent shared by both sides (kexp[t][c]),
 // seven 7-bit digits per value as BF16 in the tiled planes

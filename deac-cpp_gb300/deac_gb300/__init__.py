@@ -157,6 +157,7 @@ SIGNATURES = {
     "deac_batch_fetch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, ctypes.c_uint64]),
     "deac_batch_enable_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "deac_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(TuneReport)]),
+    "deac_batch_generation_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
     "deac_batch_transfer_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
                                                  ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_split_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]),
@@ -288,6 +289,12 @@ class Batch:
         r = TuneReport()
         _check(self._lib.deac_batch_autotune(self._h, generations, ctypes.byref(r)))
         return {k: getattr(r, k) for k, _ in TuneReport._fields_}
+
+    def generation_launches(self) -> int:
+        """Kernel launches per generation of this batch (after setup)."""
+        n = ctypes.c_uint32()
+        _check(self._lib.deac_batch_generation_launches(self._h, ctypes.byref(n)))
+        return n.value
 
     def transfer_bytes(self):
         """(host -> device, device -> host) bytes this batch has copied."""

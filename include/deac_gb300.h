@@ -280,6 +280,11 @@ int deac_batch_autotune(deac_batch* b, uint64_t generations, deac_tune_report* o
  * in the reference. */
 int deac_batch_transfer_bytes(const deac_batch* b, uint64_t* host_to_device, uint64_t* device_to_host);
 
+/* Kernel launches one generation of this batch makes (after set-up; the
+ * same for every generation, whichever runs are still going).  No
+ * counterpart in the reference. */
+int deac_batch_generation_launches(const deac_batch* b, uint32_t* launches);
+
 /* Device time of the kernels launched since timing was enabled, per kernel
  * kind, measured with CUDA events on the batch stream (ms): 0 trial kernel,
  * 1 contraction kernel (plain generation or the split engine's exact
