@@ -206,11 +206,14 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 //    MMA over the trial digits 0..6-d (N = 32(7-d)) into groups d..6, the
 //    half's bound MMA with the second stage; commits per half (accumulators
 //    full) and per stage (operands free);
-//  16 fold warps: per half, read the seven exact group sums, release the
-//    buffer and fold the sums into double-float accumulators while the tensor
-//    cores work on the other half.
+//  16 fold warps: per half, read all seven exact group sums of their rows
+//    into registers, release the buffer at once, and fold the sums into
+//    double-float accumulators while the tensor cores go on.
 // Every wait is bounded; a CTA that gives up reports it in *status.
-__global__ void __launch_bounds__(kSplitThreads, 1)
+// One CTA per SM: 18 warps, so two SM sub-partitions hold 5 warps each,
+// and a sub-partition's 16K registers cap a thread at 96 (5 x 32 x 96 <=
+// 16384; more is refused at launch).
+__global__ void __maxnreg__(96)
 split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, const SplitWork* work,
                       const SplitRow* rows, const CUtensorMap* maps, float4* partial, int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -491,44 +494,36 @@ split_contract_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles, con
                 ok = mbar_wait_or(&s_tfull[h], it & 1u, abort);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n");
-                // the half's 8 rows in two passes of 4 (the group sums of 4
-                // rows in registers at a time); the buffer is released after
-                // the second pass's loads, while the tensor cores work on the
-                // other half
+                // the half's 8 rows: all their group sums into registers at
+                // once, then the buffer is released -- the next chunk's MMAs
+                // of this half may start -- and folded meanwhile
+                uint32_t dg[kKept][8];
 #pragma unroll
-                for (uint32_t pass = 0; pass < 2; ++pass) {
-                    uint32_t dg[kKept][4];
+                for (int g = 0; g < kKept; ++g) tmem_ld8(lane_base + h * kBufCols + g * kHalfRows + 8 * slice, dg[g]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+                asm volatile("tcgen05.fence::before_thread_sync;\n");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&s_tempty[h]);  // the buffer is free for the next chunk
 #pragma unroll
-                    for (int g = 0; g < kKept; ++g)
-                        tmem_ld4(lane_base + h * kBufCols + g * kHalfRows + 8 * slice + 4 * pass, dg[g]);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-                    if (pass == 1) {
-                        asm volatile("tcgen05.fence::before_thread_sync;\n");
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&s_tempty[h]);  // the buffer is free for the next chunk
+                for (int j = 0; j < 8; ++j) {
+                    const uint32_t r = h * kHalfRows + 8 * slice + j;
+                    // sum_g D_g 2^(7(6-g)) as a double-float: every term is exact
+                    float sh = __uint_as_float(dg[0][j]) * exp2_int(7 * (kKept - 1)), sl = 0.0f;
+#pragma unroll
+                    for (int g = 1; g < kKept; ++g) {
+                        float e;
+                        two_sum(sh, __uint_as_float(dg[g][j]) * exp2_int(7 * (kKept - 1 - g)), sh, e);
+                        sl += e;
                     }
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const uint32_t jj = 4 * pass + j;
-                        const uint32_t r = h * kHalfRows + 8 * slice + jj;
-                        // sum_g D_g 2^(7(6-g)) as a double-float: every term is exact
-                        float sh = __uint_as_float(dg[0][j]) * exp2_int(7 * (kKept - 1)), sl = 0.0f;
-#pragma unroll
-                        for (int g = 1; g < kKept; ++g) {
-                            float e;
-                            two_sum(sh, __uint_as_float(dg[g][j]) * exp2_int(7 * (kKept - 1 - g)), sh, e);
-                            sl += e;
-                        }
-                        float hi, lo;
-                        fast_two_sum(sh, sl, hi, lo);
-                        // weight of the lowest kept group, 2^(e_x + e_K - 56), in
-                        // units of the output's largest scale 2^(max_x + max_K):
-                        // the accumulators stay inside the FP32 range whatever
-                        // the magnitude of K (e^{-tau omega} spans hundreds of
-                        // binades)
-                        scale_pow2(hi, lo, (s_ex[buf][r] - s_xmax[r]) + kd - 7 * (kKept + 1));
-                        dw_add(acc_hi[h * 8 + jj], acc_lo[h * 8 + jj], hi, lo);
-                    }
+                    float hi, lo;
+                    fast_two_sum(sh, sl, hi, lo);
+                    // weight of the lowest kept group, 2^(e_x + e_K - 56), in
+                    // units of the output's largest scale 2^(max_x + max_K):
+                    // the accumulators stay inside the FP32 range whatever
+                    // the magnitude of K (e^{-tau omega} spans hundreds of
+                    // binades)
+                    scale_pow2(hi, lo, (s_ex[buf][r] - s_xmax[r]) + kd - 7 * (kKept + 1));
+                    dw_add(acc_hi[h * 8 + j], acc_lo[h * 8 + j], hi, lo);
                 }
             }
         }
