@@ -178,6 +178,9 @@ struct deac_batch {
     uint32_t* d_combine_tiles = nullptr;     // their indices
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
+    uint64_t* d_jstep = nullptr;        // step_powers on the device (initial populations)
+    char* run_pool = nullptr;           // every run's arena, one allocation
+    char* split_pool = nullptr;         // every run's split-engine buffers, one allocation
     uint32_t* d_fit_off = nullptr;      // snapshot_kernel: each run's first fitness slot (and the total)
     uint64_t* d_gene_off = nullptr;     // snapshot_kernel: each run's first gene slot
     std::vector<uint64_t> gene_off;     // its host copy
@@ -484,6 +487,24 @@ const std::vector<uint64_t>& jump_powers(uint32_t bits) {
     return tab;
 }
 
+// The matrices J^(2^b), b < bits, of one generator step over GF(2), grown
+// on demand and kept for the process.
+const std::vector<uint64_t>& step_powers(uint32_t bits) {
+    static std::mutex mu;
+    static std::vector<uint64_t> tab;
+    std::lock_guard<std::mutex> lock(mu);
+    if (tab.empty()) {
+        tab.resize(1024);
+        deac::step_matrix(tab.data());
+    }
+    while (tab.size() < (size_t)bits * 1024) {
+        const size_t k = tab.size();
+        tab.resize(k + 1024);
+        deac::gf2_matmul(tab.data() + k - 1024, tab.data() + k - 1024, tab.data() + k);
+    }
+    return tab;
+}
+
 // Host part of one run's set-up: its constants (the kernel matrix is formed
 // once per distinct one, after this).
 void prepare_model(RunHost& r) {
@@ -495,7 +516,8 @@ struct ArenaLayout {
     uint64_t o_isf, o_err, o_tw, o_np, o_nn, o_fp, o_fn, o_tp, o_tn, o_pop, o_cur, o_rng, o_cr, o_fw, o_fo, o_fnw,
         o_E, o_E2, o_mom, o_stats, o_trace, size;
     // bytes of the host image copied to the device: everything before the
-    // population, buffer 0 of it, then the initial CR and F
+    // population, then the initial CR and F (the population is drawn on the
+    // device), then 1/sigma for the split engine's decisions
     uint64_t pop_bytes, image_bytes;
 };
 
@@ -517,39 +539,60 @@ ArenaLayout arena_layout(const RunHost& r) {
     L.o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
     L.size = a.size;
     L.pop_bytes = (uint64_t)S * P * M * 8;
-    L.image_bytes = L.o_pop + L.pop_bytes + 2ull * S * P * 8;
+    L.image_bytes = L.o_pop + 2ull * S * P * 8 + Nt * 8;
     return L;
 }
 
-// Host part of one run's set-up: initial population (into pop, S*P*M
-// doubles) and PRNG start state.
-void prepare_population(RunHost& r, int32_t streams, double* pop) {
-    const deac_config& c = r.cfg;
-    const uint64_t P = r.P, M = r.M;
-    const int S = r.S;
-    // initial population: one stream seeded with 1407513600 + seed
-    // (deac.cpp:2089-2091), member-major, a draw per side per gene
-    // (deac.cpp:429-446), zero frequency matched (deac.cpp:447-456)
-    deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + c.seed);
-    for (uint64_t i = 0; i < P; ++i)
-        for (uint64_t j = 0; j < M; ++j)
-            for (int s = 0; s < S; ++s) {
-                double v = deac::to_unit(g.next());
-                if (c.allow_negative_weight) v -= 0.5;
-                pop[(uint64_t)s * P * M + i * M + j] = v;
+// Byte offsets of a run's split-engine buffers (one region of the batch's
+// split pool).
+struct SplitLayout {
+    uint64_t o_xe, o_xm, o_mu, o_em, o_eb, o_ch, o_rc, o_fl, o_fh, o_tl, o_th, o_cnt, o_rcp, o_ie, o_pm, size;
+};
+
+SplitLayout split_layout(const RunHost& r) {
+    const uint64_t P = r.P, Nt = r.Nt, C = deac::split_chunks(r.M);
+    Arena sa;
+    SplitLayout L;
+    L.o_xe = sa.take(P * C * 2), L.o_xm = sa.take(P * 4), L.o_mu = sa.take(P * 3 * 4);
+    L.o_em = sa.take(P * Nt * 8), L.o_eb = sa.take(P * Nt * 8);
+    L.o_ch = sa.take(P), L.o_rc = sa.take(P);
+    L.o_fl = sa.take(P * 8), L.o_fh = sa.take(P * 8), L.o_tl = sa.take(P * 8), L.o_th = sa.take(P * 8);
+    L.o_cnt = sa.take(3 * 8);
+    L.o_rcp = sa.take(P * 8), L.o_ie = sa.take(Nt * 8);
+    L.o_pm = sa.take(2 * P * 8);
+    L.size = sa.size;
+    return L;
+}
+
+// Host part of one run's set-up: the PRNG start state.  The initial
+// population (population_kernel, on the device) takes P*M*S draws of the
+// stream seeded with 1407513600 + seed (deac.cpp:2089-2091); with reference
+// streams the per-gene states start from the generator after them
+// (deac.cpp:1114-1126): J^(PMS) s0, a product of the step matrices J^(2^b)
+// of PMS's set bits.  With counter streams one slot per member (its jDE
+// step count, from 0).
+void prepare_start(RunHost& r, int32_t streams) {
+    const uint64_t P = r.P, M = r.M, S = (uint64_t)r.S;
+    r.n_states = streams == DEAC_STREAMS_COUNTER ? P : P * (1 + S * M);
+    const deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + r.cfg.seed);
+    uint64_t v[4] = {g.s[0], g.s[1], g.s[2], g.s[3]};
+    if (streams != DEAC_STREAMS_COUNTER) {
+        const uint64_t n = P * M * S;
+        const uint32_t bits = jump_bits(n) + 1;
+        const std::vector<uint64_t>& J = step_powers(bits);
+        for (uint32_t b2 = 0; b2 < bits; ++b2)
+            if ((n >> b2) & 1u) {
+                uint64_t o[4];
+                deac::gf2_matvec(J.data() + (uint64_t)b2 * 1024, v, o);
+                for (int w = 0; w < 4; ++w) v[w] = o[w];
             }
-    if (S == 2)
-        for (uint64_t i = 0; i < P; ++i) pop[P * M + i * M] = pop[i * M];
-    // per-gene states: state k = jump^k(generator after the initial draws)
-    // (deac.cpp:1114-1126), formed on the device by rng_table_kernel; with
-    // counter streams one slot per member (its jDE step count, from 0)
-    r.n_states = streams == DEAC_STREAMS_COUNTER ? P : P * (1 + (uint64_t)S * M);
-    for (int w = 0; w < 4; ++w) r.rng_start[w] = g.s[w];
+    }
+    for (int w = 0; w < 4; ++w) r.rng_start[w] = v[w];
 }
 
 // The host image of a run's arena (pinned; ArenaLayout::image_bytes): the
-// inputs and the constant terms before the population, buffer 0 of the
-// population (drawn in place) and the initial CR / F after it.
+// inputs and the constant terms before the population, then the initial
+// CR / F and 1/sigma.
 void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
     const uint64_t P = r.P, S = (uint64_t)r.S;
     const deac::Model& m = r.model;
@@ -566,12 +609,15 @@ void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
     put(L.o_fn, m.first_neg);
     put(L.o_tp, m.third_pos);
     put(L.o_tn, m.third_neg);
-    prepare_population(r, streams, reinterpret_cast<double*>(img + L.o_pop));
-    double* crfw = reinterpret_cast<double*>(img + L.o_pop + L.pop_bytes);
+    prepare_start(r, streams);
+    double* crfw = reinterpret_cast<double*>(img + L.o_pop);
     for (uint64_t k = 0; k < S * P; ++k) {
         crfw[k] = r.cfg.crossover_probability;
         crfw[S * P + k] = r.cfg.differential_weight;
     }
+    // 1/sigma as the split engine's decisions use it (one rounding each)
+    double* ie = crfw + 2 * S * P;
+    for (uint64_t t = 0; t < r.Nt; ++t) ie[t] = 1.0 / r.err[t];
 }
 
 // Device part of one run's set-up from its host image `img` (pinned; the
@@ -619,15 +665,22 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
                    o_fn = L.o_fn, o_tp = L.o_tp, o_tn = L.o_tn, o_pop = L.o_pop, o_cur = L.o_cur, o_rng = L.o_rng,
                    o_cr = L.o_cr, o_fw = L.o_fw, o_fo = L.o_fo, o_fnw = L.o_fnw, o_E = L.o_E, o_E2 = L.o_E2,
                    o_mom = L.o_mom, o_stats = L.o_stats, o_trace = L.o_trace;
-    CUDA_TRY(cudaMalloc(&r.arena, L.size));
+    // the run's region of the batch's pool, zeroed on the device already;
+    // the initial parents (buffer 0) are drawn there too: only the inputs,
+    // the initial CR / F and 1/sigma cross the bus
     r.arena_bytes = L.size;
     char* base = r.arena;
     const bool counter = b->streams == DEAC_STREAMS_COUNTER;
-    // zeros are written on the device; only the inputs, the initial parents
-    // (buffer 0) and the initial CR / F cross the bus
-    CUDA_TRY(cudaMemsetAsync(base, 0, L.size, b->stream));
-    CUDA_TRY(copy_async(b, base, img, o_pop + L.pop_bytes, cudaMemcpyHostToDevice, b->stream));
-    const char* crfw = img + o_pop + L.pop_bytes;
+    CUDA_TRY(copy_async(b, base, img, o_pop, cudaMemcpyHostToDevice, b->stream));
+    {
+        const deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + r.cfg.seed);
+        const uint64_t threads = ((uint64_t)P * M * S + (1ull << deac::kPopBlockLog2) - 1) >> deac::kPopBlockLog2;
+        deac::population_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, b->stream>>>(
+            reinterpret_cast<double*>(base + o_pop), (uint32_t)P, (uint32_t)M, (uint32_t)S,
+            r.cfg.allow_negative_weight ? 1 : 0, g.s[0], g.s[1], g.s[2], g.s[3], b->d_jstep);
+        CUDA_TRY(cudaGetLastError());
+    }
+    const char* crfw = img + o_pop;
     CUDA_TRY(copy_async(b, base + o_cr, crfw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice, b->stream));
     CUDA_TRY(copy_async(b, base + o_fw, crfw + (uint64_t)S * P * 8, (uint64_t)S * P * 8, cudaMemcpyHostToDevice,
                         b->stream));
@@ -718,22 +771,18 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
     d.trace_cap = r.trace_cap;
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
         const uint64_t C = deac::split_chunks(M);
-        Arena sa;
-        const uint64_t o_xe = sa.take(P * C * 2), o_xm = sa.take(P * 4), o_mu = sa.take(P * 3 * 4);
-        const uint64_t o_em = sa.take(P * Nt * 8), o_eb = sa.take(P * Nt * 8);
-        const uint64_t o_ch = sa.take(P), o_rc = sa.take(P);
-        const uint64_t o_fl = sa.take(P * 8), o_fh = sa.take(P * 8), o_tl = sa.take(P * 8), o_th = sa.take(P * 8);
-        const uint64_t o_cnt = sa.take(3 * 8);
-        const uint64_t o_rcp = sa.take(P * 8), o_ie = sa.take(Nt * 8);
-        const uint64_t o_pm = sa.take(2 * P * 8);
-        CUDA_TRY(cudaMalloc(&r.split_arena, sa.size));
-        CUDA_TRY(cudaMemset(r.split_arena, 0, sa.size));
+        // the run's region of the batch's split pool (zeroed on the device)
+        const SplitLayout SL = split_layout(r);
+        const uint64_t o_xe = SL.o_xe, o_xm = SL.o_xm, o_mu = SL.o_mu, o_em = SL.o_em, o_eb = SL.o_eb,
+                       o_ch = SL.o_ch, o_rc = SL.o_rc, o_fl = SL.o_fl, o_fh = SL.o_fh, o_tl = SL.o_tl,
+                       o_th = SL.o_th, o_cnt = SL.o_cnt, o_rcp = SL.o_rcp, o_ie = SL.o_ie, o_pm = SL.o_pm;
         char* sb = r.split_arena;
         deac::SplitRun& x = r.split;
         x.sel_min_bits = ~0ull;  // no member tallied yet
         x.xexp = reinterpret_cast<int16_t*>(sb + o_xe);
         x.xexp_max = reinterpret_cast<int32_t*>(sb + o_xm);
-        CUDA_TRY(cudaMemset(x.xexp_max, 0x80, P * 4));  // below every exponent: no trial sliced yet
+        // below every exponent: no trial sliced yet
+        CUDA_TRY(cudaMemsetAsync(x.xexp_max, 0x80, P * 4, b->stream));
         x.kdig = it->second.kdig;
         x.kexp = it->second.kexp;
         x.kexp_max = it->second.kexp_max;
@@ -746,16 +795,11 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
         x.t_lo = reinterpret_cast<double*>(sb + o_tl);
         x.t_hi = reinterpret_cast<double*>(sb + o_th);
         x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
-        {
-            // 1/sigma as the decisions use it, and float upper bounds for
-            // their error bounds
-            // 1/sigma as the decisions use it
-            std::vector<double> ie(Nt);
-            for (uint64_t t = 0; t < Nt; ++t) ie[t] = 1.0 / r.err[t];
-            CUDA_TRY(copy(b, sb + o_ie, ie.data(), Nt * 8, cudaMemcpyHostToDevice));
-            x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
-            x.inv_nt = 1.0 / (double)Nt;
-        }
+        // 1/sigma as the decisions use it, from the image
+        CUDA_TRY(copy_async(b, sb + o_ie, img + o_pop + 2ull * S * P * 8, Nt * 8, cudaMemcpyHostToDevice,
+                            b->stream));
+        x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
+        x.inv_nt = 1.0 / (double)Nt;
         d.changed = x.changed;
         d.xexp = x.xexp;
         d.xexp_max = x.xexp_max;
@@ -1196,6 +1240,38 @@ int deac_batch_setup(deac_batch* b) {
         const std::vector<uint64_t>& jp = jump_powers(bits);
         CUDA_TRY(cudaMalloc(&b->d_jpow, (size_t)bits * 1024 * 8));
         CUDA_TRY(copy(b, b->d_jpow, jp.data(), (size_t)bits * 1024 * 8, cudaMemcpyHostToDevice));
+    }
+    {
+        // the step matrices the initial populations' threads jump with
+        uint32_t bits = 1;
+        for (auto& r : b->runs) bits = std::max(bits, jump_bits((uint64_t)r->P * r->M * r->S) + 1);
+        const std::vector<uint64_t>& J = step_powers(bits);
+        CUDA_TRY(cudaMalloc(&b->d_jstep, (size_t)bits * 1024 * 8));
+        CUDA_TRY(copy(b, b->d_jstep, J.data(), (size_t)bits * 1024 * 8, cudaMemcpyHostToDevice));
+    }
+    {
+        // every run's arena (and split-engine buffers) in one allocation,
+        // zeroed on the device
+        uint64_t run_bytes = 0, split_bytes = 0;
+        for (auto& r : b->runs) {
+            run_bytes += arena_layout(*r).size;
+            if (b->engine == DEAC_ENGINE_SPLIT_BF16) split_bytes += split_layout(*r).size;
+        }
+        CUDA_TRY(cudaMalloc(&b->run_pool, run_bytes));
+        CUDA_TRY(cudaMemsetAsync(b->run_pool, 0, run_bytes, b->stream));
+        if (split_bytes) {
+            CUDA_TRY(cudaMalloc(&b->split_pool, split_bytes));
+            CUDA_TRY(cudaMemsetAsync(b->split_pool, 0, split_bytes, b->stream));
+        }
+        uint64_t ro = 0, so = 0;
+        for (auto& r : b->runs) {
+            r->arena = b->run_pool + ro;
+            ro += arena_layout(*r).size;
+            if (split_bytes) {
+                r->split_arena = b->split_pool + so;
+                so += split_layout(*r).size;
+            }
+        }
     }
     uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
@@ -1851,10 +1927,8 @@ int deac_batch_destroy(deac_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    for (auto& r : b->runs) {
-        if (r->arena) cudaFree(r->arena);
-        if (r->split_arena) cudaFree(r->split_arena);
-    }
+    cudaFree(b->run_pool);
+    cudaFree(b->split_pool);
     for (auto& kv : b->kcache) {
         cudaFree(kv.second.k_pos);
         if (kv.second.k_neg) cudaFree(kv.second.k_neg);
@@ -1874,6 +1948,7 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_rows);
     cudaFree(b->d_status);
     cudaFree(b->d_jpow);
+    cudaFree(b->d_jstep);
     cudaFree(b->d_fit_off);
     cudaFree(b->d_gene_off);
     cudaFree(b->d_snap);

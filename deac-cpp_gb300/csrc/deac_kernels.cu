@@ -389,6 +389,48 @@ __global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* 
     }
 }
 
+// ------------------------------------------------------ initial population
+__global__ void __launch_bounds__(128) population_kernel(double* pop, uint32_t P, uint32_t M, uint32_t S,
+                                                         int signed_weights, uint64_t s0, uint64_t s1, uint64_t s2,
+                                                         uint64_t s3, const uint64_t* jstep) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t n = (uint64_t)P * M * S;
+    const uint64_t d0 = t << kPopBlockLog2;
+    if (d0 >= n) return;
+    uint64_t v[4] = {s0, s1, s2, s3};
+    for (uint32_t b = 0; (t >> b) != 0; ++b)
+        if ((t >> b) & 1u) {
+            uint64_t o[4];
+            gf2_matvec(jstep + (uint64_t)(b + kPopBlockLog2) * 1024, v, o);
+            v[0] = o[0];
+            v[1] = o[1];
+            v[2] = o[2];
+            v[3] = o[3];
+        }
+    const uint64_t d1 = d0 + (1ull << kPopBlockLog2) < n ? d0 + (1ull << kPopBlockLog2) : n;
+    const uint64_t MS = (uint64_t)M * S, PM = (uint64_t)P * M;
+    // draw d is gene j, side s of member i: d = (i M + j) S + s
+    uint64_t i = d0 / MS;
+    uint32_t j = (uint32_t)((d0 - i * MS) / S), s = (uint32_t)(d0 - i * MS - (uint64_t)j * S);
+    double first = 0.0;  // the member's positive-side gene 0 (its draw and the next are one thread's: d0 is even)
+    for (uint64_t d = d0; d < d1; ++d) {
+        double x = to_unit(xoshiro_next(v[0], v[1], v[2], v[3]));
+        if (signed_weights) x -= 0.5;
+        if (S == 2 && j == 0) {
+            if (s == 0) first = x;
+            else x = first;
+        }
+        pop[(uint64_t)s * PM + i * M + j] = x;
+        if (++s == S) {
+            s = 0;
+            if (++j == M) {
+                j = 0;
+                ++i;
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------ PRNG table
 __global__ void rng_table_kernel(uint64_t* rng, uint64_t n, const uint64_t* jpow, uint32_t bits, uint64_t s0,
                                  uint64_t s1, uint64_t s2, uint64_t s3, uint32_t P, uint32_t M, uint32_t S) {

@@ -242,6 +242,16 @@ __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const PartWork* work);
 // the same for batches that draw from counter streams
 __global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
+// The initial population of one run (deac.cpp:418-458) into its parent
+// buffer 0: the stream seeded with 1407513600 + seed, member-major, a draw
+// per side per gene, U[0,1) (-0.5 with signed weights), then each member's
+// negative-side gene 0 := its positive-side gene 0.  Thread t makes draws
+// [t 2^block_log2, (t+1) 2^block_log2) from the state J^(t 2^block_log2) s0,
+// J the generator's step as a GF(2)-linear map (jstep: the matrices
+// J^(2^b), 1024 words each).
+constexpr uint32_t kPopBlockLog2 = 10;
+__global__ void population_kernel(double* pop, uint32_t P, uint32_t M, uint32_t S, int signed_weights, uint64_t s0,
+                                  uint64_t s1, uint64_t s2, uint64_t s3, const uint64_t* jstep);
 // split engine, generation 0: the BF16 digit slices of every member's
 // initial parent (the trial planes' rows), parts as trial_part_kernel's
 __global__ void parent_digits_kernel(RunDev* runs, const PartWork* work);

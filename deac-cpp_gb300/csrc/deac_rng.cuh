@@ -150,6 +150,17 @@ inline void jump_matrix(uint64_t cols[1024]) {
     }
 }
 
+// One generator step (xoshiro256+'s state update) as the same kind of
+// matrix: column i = step(e_i).
+inline void step_matrix(uint64_t cols[1024]) {
+    for (uint32_t i = 0; i < 256; ++i) {
+        Xoshiro x{{0, 0, 0, 0}};
+        x.s[i >> 6] = 1ull << (i & 63u);
+        x.next();
+        for (int w = 0; w < 4; ++w) cols[4 * i + w] = x.s[w];
+    }
+}
+
 // C = A B (column j of C is A times column j of B)
 inline void gf2_matmul(const uint64_t* A, const uint64_t* B, uint64_t* C) {
     for (uint32_t j = 0; j < 256; ++j) gf2_matvec(A, B + 4 * j, C + 4 * j);

@@ -22,7 +22,9 @@ def test_host_chain_matches_sequential_fma(tmp_path):
 
 def test_prng_table_jump_powers_match_the_jump_chain(tmp_path):
     # the per-gene PRNG states come from GF(2) matrix powers of the jump
-    # (rng_table_kernel); on the host they must equal the chain of jumps
+    # (rng_table_kernel), the initial populations' draws from powers of one
+    # step (population_kernel); on the host they must equal the chain of
+    # jumps and the sequence of draws
     exe = tmp_path / "rng_jump_check"
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(REPO / "deac-cpp_gb300" / "csrc"),
                     str(REPO / "tests" / "rng_jump_check.cpp"), "-o", str(exe)], check=True)
