@@ -22,10 +22,15 @@ synchronize on both sides; value is the max over ranks.  With --gpus N
 (torchrun), each rank runs its own 1024 seeds (weak scaling, no data-path
 collective).
 
-Secondary keys: the single-run production scale (8 runs of N_tau = 128,
-M = 4096, P = 8, --normalize, reference streams) over an early window and
-over a long window of 100,000 generations, where the exact FP64 passes of a
-converging population weigh more.
+Secondary keys: `config4_full_size`, the batched split-precision form at
+full size (4096 runs of M = 16384 on [0, 1024], P = 64, N_tau = 512, 270 GB;
+the plain engine on 256 of the same runs, whose chi^2, best member and
+spectrum must match); the single-run production scale (8 runs of
+N_tau = 128, M = 4096, P = 8, --normalize, reference streams) over an early
+window and over a long window of 100,000 generations, where the exact FP64
+passes of a converging population weigh more.  `gpu_launches` counts the
+engine's kernel launches in the timed steps (its per-generation count, from
+the engine, times the generations).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 

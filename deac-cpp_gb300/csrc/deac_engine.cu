@@ -179,6 +179,7 @@ struct deac_batch {
     int* d_status = nullptr;            // set when a bounded wait gave up
     uint64_t* d_jpow = nullptr;         // jump_powers on the device
     uint64_t* d_jstep = nullptr;        // step_powers on the device (initial populations)
+    bool any_defer = false;             // a run normalises raw trials in the selection (kDeferNorm)
     char* run_pool = nullptr;           // every run's arena, one allocation
     char* split_pool = nullptr;         // every run's split-engine buffers, one allocation
     uint32_t* d_fit_off = nullptr;      // snapshot_kernel: each run's first fitness slot (and the total)
@@ -337,8 +338,12 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
                static_cast<const uint32_t*>(b->d_combine_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
                static_cast<const float4*>(b->d_partial));
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
-    deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
-                                                                               b->d_trial_work);
+    if (b->any_defer)
+        deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
+                                                                                   b->d_trial_work);
+    else
+        deac::split_select_lean_kernel<<<b->n_trial_ctas, deac::kSelectLeanThreads, 0, s>>>(b->d_runs, b->d_split,
+                                                                                            b->d_trial_work);
     if ((rc = mark(4))) return rc;
     launch_contract(b, s, deac::kModeRecheck, early);
     return mark(1);
@@ -665,21 +670,14 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
                    o_fn = L.o_fn, o_tp = L.o_tp, o_tn = L.o_tn, o_pop = L.o_pop, o_cur = L.o_cur, o_rng = L.o_rng,
                    o_cr = L.o_cr, o_fw = L.o_fw, o_fo = L.o_fo, o_fnw = L.o_fnw, o_E = L.o_E, o_E2 = L.o_E2,
                    o_mom = L.o_mom, o_stats = L.o_stats, o_trace = L.o_trace;
-    // the run's region of the batch's pool, zeroed on the device already;
-    // the initial parents (buffer 0) are drawn there too: only the inputs,
-    // the initial CR / F and 1/sigma cross the bus
+    // the run's region of the batch's pool, zeroed on the device already
+    // (the initial parents, buffer 0, are drawn there by population_kernel
+    // once every run is in place): only the inputs, the initial CR / F and
+    // 1/sigma cross the bus
     r.arena_bytes = L.size;
     char* base = r.arena;
     const bool counter = b->streams == DEAC_STREAMS_COUNTER;
     CUDA_TRY(copy_async(b, base, img, o_pop, cudaMemcpyHostToDevice, b->stream));
-    {
-        const deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + r.cfg.seed);
-        const uint64_t threads = ((uint64_t)P * M * S + (1ull << deac::kPopBlockLog2) - 1) >> deac::kPopBlockLog2;
-        deac::population_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, b->stream>>>(
-            reinterpret_cast<double*>(base + o_pop), (uint32_t)P, (uint32_t)M, (uint32_t)S,
-            r.cfg.allow_negative_weight ? 1 : 0, g.s[0], g.s[1], g.s[2], g.s[3], b->d_jstep);
-        CUDA_TRY(cudaGetLastError());
-    }
     const char* crfw = img + o_pop;
     CUDA_TRY(copy_async(b, base + o_cr, crfw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice, b->stream));
     CUDA_TRY(copy_async(b, base + o_fw, crfw + (uint64_t)S * P * 8, (uint64_t)S * P * 8, cudaMemcpyHostToDevice,
@@ -1315,6 +1313,38 @@ int deac_batch_setup(deac_batch* b) {
             deac::stage_doubles(r.dev.S, r.dev.member_tile, r.dev.tau_tile, r.dev.chunk) * 2 * sizeof(double);
         contract_bytes = std::max<uint64_t>(contract_bytes, stage);
     }
+    {
+        // every run's initial population, one launch
+        std::vector<deac::PopRun> pr;
+        std::vector<deac::PopWork> pwk;
+        for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
+            const RunHost& r = *b->runs[ri];
+            const deac::Xoshiro g = deac::Xoshiro::seeded(1407513600ULL + r.cfg.seed);
+            pr.push_back({reinterpret_cast<double*>(r.arena + arena_layout(r).o_pop),
+                          {g.s[0], g.s[1], g.s[2], g.s[3]}, (uint32_t)r.P, (uint32_t)r.M, (uint32_t)r.S,
+                          r.cfg.allow_negative_weight ? 1u : 0u});
+            const uint64_t threads =
+                ((uint64_t)r.P * r.M * r.S + (1ull << deac::kPopBlockLog2) - 1) >> deac::kPopBlockLog2;
+            for (uint64_t t0 = 0; t0 < threads; t0 += deac::kPopThreads) pwk.push_back({ri, (uint32_t)t0});
+        }
+        deac::PopRun* d_pr = nullptr;
+        deac::PopWork* d_pw = nullptr;
+        CUDA_TRY(cudaMalloc(&d_pr, pr.size() * sizeof(deac::PopRun)));
+        CUDA_TRY(cudaMalloc(&d_pw, pwk.size() * sizeof(deac::PopWork)));
+        struct Free {
+            void* a;
+            void* b;
+            ~Free() {
+                cudaFree(a);
+                cudaFree(b);
+            }
+        } free_pop{d_pr, d_pw};
+        CUDA_TRY(copy(b, d_pr, pr.data(), pr.size() * sizeof(deac::PopRun), cudaMemcpyHostToDevice));
+        CUDA_TRY(copy(b, d_pw, pwk.data(), pwk.size() * sizeof(deac::PopWork), cudaMemcpyHostToDevice));
+        deac::population_kernel<<<(unsigned)pwk.size(), deac::kPopThreads, 0, b->stream>>>(d_pr, d_pw, b->d_jstep);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(b->stream));  // before the lists are freed
+    }
     b->smem_doubles = (int)trial_doubles;
     b->trial_smem_bytes = trial_doubles * sizeof(double);
     b->contract_smem_bytes = contract_bytes;
@@ -1330,6 +1360,7 @@ int deac_batch_setup(deac_batch* b) {
         std::vector<deac::Work> nw;
         for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
             const RunHost& r = *b->runs[ri];
+            if (r.dev.flags & deac::kDeferNorm) b->any_defer = true;
             if (!(r.dev.flags & (deac::kDeferNorm | deac::kFirstMoment | deac::kThirdMoment))) continue;
             for (uint32_t i = 0; i < r.dev.P; ++i) nw.push_back({ri, i});
         }

@@ -390,14 +390,27 @@ __global__ void snapshot_kernel(const RunDev* runs, uint32_t n, const uint32_t* 
 }
 
 // ------------------------------------------------------ initial population
-__global__ void __launch_bounds__(128) population_kernel(double* pop, uint32_t P, uint32_t M, uint32_t S,
-                                                         int signed_weights, uint64_t s0, uint64_t s1, uint64_t s2,
-                                                         uint64_t s3, const uint64_t* jstep) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+// (x >> 11) 2^-53 (the reference's uniform, rng.hpp:129-131) from integer
+// operations: the 53-bit integer's leading bit gives the exponent, the bits
+// below it the fraction -- exact, and off the narrow FP64 pipe.
+__device__ __forceinline__ double unit_from_bits(uint64_t x) {
+    const uint64_t m = x >> 11;
+    if (m == 0) return 0.0;
+    const int e = 63 - __clzll((long long)m);  // 0 .. 52
+    const uint64_t frac = (m << (52 - e)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)(((uint64_t)(e - 53 + 1023) << 52) | frac));
+}
+
+__global__ void __launch_bounds__(kPopThreads) population_kernel(const PopRun* runs, const PopWork* work,
+                                                                const uint64_t* jstep) {
+    const PopWork w = work[blockIdx.x];
+    const PopRun R = runs[w.run];
+    const uint32_t P = R.P, M = R.M, S = R.S;
+    const uint64_t t = (uint64_t)w.t0 + threadIdx.x;
     const uint64_t n = (uint64_t)P * M * S;
     const uint64_t d0 = t << kPopBlockLog2;
     if (d0 >= n) return;
-    uint64_t v[4] = {s0, s1, s2, s3};
+    uint64_t v[4] = {R.s[0], R.s[1], R.s[2], R.s[3]};
     for (uint32_t b = 0; (t >> b) != 0; ++b)
         if ((t >> b) & 1u) {
             uint64_t o[4];
@@ -408,14 +421,15 @@ __global__ void __launch_bounds__(128) population_kernel(double* pop, uint32_t P
             v[3] = o[3];
         }
     const uint64_t d1 = d0 + (1ull << kPopBlockLog2) < n ? d0 + (1ull << kPopBlockLog2) : n;
-    const uint64_t MS = (uint64_t)M * S, PM = (uint64_t)P * M;
+    const uint64_t PM = (uint64_t)P * M, MS = (uint64_t)M * S;
+    double* const pop = R.pop;
     // draw d is gene j, side s of member i: d = (i M + j) S + s
     uint64_t i = d0 / MS;
     uint32_t j = (uint32_t)((d0 - i * MS) / S), s = (uint32_t)(d0 - i * MS - (uint64_t)j * S);
     double first = 0.0;  // the member's positive-side gene 0 (its draw and the next are one thread's: d0 is even)
     for (uint64_t d = d0; d < d1; ++d) {
-        double x = to_unit(xoshiro_next(v[0], v[1], v[2], v[3]));
-        if (signed_weights) x -= 0.5;
+        double x = unit_from_bits(xoshiro_next(v[0], v[1], v[2], v[3]));
+        if (R.signed_weights) x -= 0.5;
         if (S == 2 && j == 0) {
             if (s == 0) first = x;
             else x = first;

@@ -242,7 +242,7 @@ __global__ void jde_kernel(RunDev* runs, const Work* work, uint32_t n);
 __global__ void trial_part_kernel(RunDev* runs, const PartWork* work);
 // the same for batches that draw from counter streams
 __global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
-// The initial population of one run (deac.cpp:418-458) into its parent
+// The initial populations (deac.cpp:418-458), each into its run's parent
 // buffer 0: the stream seeded with 1407513600 + seed, member-major, a draw
 // per side per gene, U[0,1) (-0.5 with signed weights), then each member's
 // negative-side gene 0 := its positive-side gene 0.  Thread t makes draws
@@ -250,8 +250,18 @@ __global__ void trial_part_counter_kernel(RunDev* runs, const PartWork* work);
 // J the generator's step as a GF(2)-linear map (jstep: the matrices
 // J^(2^b), 1024 words each).
 constexpr uint32_t kPopBlockLog2 = 10;
-__global__ void population_kernel(double* pop, uint32_t P, uint32_t M, uint32_t S, int signed_weights, uint64_t s0,
-                                  uint64_t s1, uint64_t s2, uint64_t s3, const uint64_t* jstep);
+constexpr int kPopThreads = 128;
+struct PopRun {
+    double* pop;          // the run's parent buffer 0
+    uint64_t s[4];        // its stream's seeded state
+    uint32_t P, M, S, signed_weights;
+};
+struct PopWork {
+    uint32_t run;         // index into the PopRun list
+    uint32_t t0;          // the CTA's first thread within the run
+};
+// one CTA (kPopThreads) per entry of `work`, every run of the batch in one launch
+__global__ void population_kernel(const PopRun* runs, const PopWork* work, const uint64_t* jstep);
 // split engine, generation 0: the BF16 digit slices of every member's
 // initial parent (the trial planes' rows), parts as trial_part_kernel's
 __global__ void parent_digits_kernel(RunDev* runs, const PartWork* work);

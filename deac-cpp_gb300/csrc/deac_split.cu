@@ -45,12 +45,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t v[4]) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
-                 : "r"(taddr));
-}
-
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
@@ -678,7 +672,7 @@ __device__ __forceinline__ void chi_interval(const RunDev& R, double chi, double
 }
 
 // ---------------------------------------------------------------- select
-// One CTA per member, in two roles.  Warps 0-3 form the estimate's chi^2 and
+// One CTA per member, in roles.  Warps 0-3 form the estimate's chi^2 and
 // its interval and make the selection decision the interval settles
 // (undecided members are flagged for the exact FP64 evaluation,
 // contract_kernel's recheck mode); thread 0 then keeps the run's tallies,
@@ -687,8 +681,10 @@ __device__ __forceinline__ void chi_interval(const RunDev& R, double chi, double
 // kDeferNorm runs and, once the decision is known, normalise it when it is
 // kept or rechecked; the last warp's first thread draws the next
 // generation's jDE, which it stores once the decision is known.
-__global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* runs, SplitRun* split,
-                                                                     const Work* work) {
+// kThreads: kSelectThreads, or kSelectLeanThreads (no scaling warps) for
+// batches without kDeferNorm runs.
+template <uint32_t kThreads>
+__device__ __forceinline__ void split_select_body(RunDev* runs, SplitRun* split, const Work* work) {
     grid_dependency_wait();
     constexpr uint32_t kChiWarps = 4, kChiThreads = kChiWarps * 32;
     __shared__ double s_chi[kChiWarps];
@@ -706,7 +702,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     // moment is formed from the model ISF itself: both decided exactly
     const bool force_exact = (R.flags & (kTrackStats | kNegativeFirstMoment)) != 0;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    constexpr uint32_t kJdeThread = kSelectThreads - 32;
+    constexpr uint32_t kJdeThread = kThreads - 32;
     // read by every thread before thread 0 may change them, in one round
     // trip with the chi^2 warps' first timeslice and the generation index
     const uint32_t cur0 = R.cur[i];
@@ -778,7 +774,8 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         }
         return;
     }
-    if (warp >= kChiWarps) {
+    constexpr uint32_t NS = kThreads - kChiThreads - 32;  // threads of the scaling warps
+    if constexpr (NS > 0) if (warp >= kChiWarps) {
         // The trial (buffer 1 - cur) of kDeferNorm runs, kept or rechecked,
         // normalised: every gene times 1/norm, as trial_kernel does.  Its
         // genes are loaded while warps 0-3 decide (all loads of the first
@@ -788,7 +785,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
         const bool need = defer && changed;
         const uint64_t PM = (uint64_t)P * M;
         const uint32_t half = M / 2, pairs = S * half;  // M is a multiple of the 32-gene chunk: gene pairs
-        constexpr uint32_t NS = kSelectThreads - kChiThreads - 32, U = 12;
+        constexpr uint32_t U = 12;
         double2* const row0 = reinterpret_cast<double2*>(R.pop + (uint64_t)(1u - cur0) * S * PM + (uint64_t)i * M);
         // pair q of side 1 lies PM doubles (PM/2 pairs) beyond the same pair of side 0
         auto at = [&](uint32_t q) { return q < half ? row0 + q : row0 + PM / 2 + (q - half); };
@@ -902,7 +899,7 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
     __syncwarp();
     // the decision to the jDE warp and the scaling warps, without waiting
     asm volatile("barrier.arrive 2, 64;" ::: "memory");
-    asm volatile("barrier.arrive 3, %0;" ::"r"(kSelectThreads - kChiThreads - 32 + 32) : "memory");
+    if constexpr (NS > 0) asm volatile("barrier.arrive 3, %0;" ::"r"(NS + 32) : "memory");
     if (tid != 0) return;
     const int outcome = s_outcome;
     // the run's tallies: the members' fitness minimum (non-negative doubles
@@ -950,6 +947,15 @@ __global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* ru
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(kSelectThreads) split_select_kernel(RunDev* runs, SplitRun* split,
+                                                                     const Work* work) {
+    split_select_body<kSelectThreads>(runs, split, work);
+}
+__global__ void __launch_bounds__(kSelectLeanThreads) split_select_lean_kernel(RunDev* runs, SplitRun* split,
+                                                                              const Work* work) {
+    split_select_body<kSelectLeanThreads>(runs, split, work);
 }
 
 // ------------------------------------------------------ generation 0

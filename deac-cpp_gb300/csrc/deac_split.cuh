@@ -139,6 +139,9 @@ __global__ void split_contract_kernel(RunDev* runs, SplitRun* split, const Split
 __global__ void split_combine_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
                                      const uint32_t* combine_tiles, const SplitRow* rows, const float4* partial);
 __global__ void split_select_kernel(RunDev* runs, SplitRun* split, const Work* work);
+// the same without the scaling warps (batches without kDeferNorm runs)
+constexpr int kSelectLeanThreads = 160;
+__global__ void split_select_lean_kernel(RunDev* runs, SplitRun* split, const Work* work);
 // generation 0: the initial parents' fitness intervals, one CTA per member
 constexpr int kInitThreads = 128;
 __global__ void split_init_kernel(RunDev* runs, SplitRun* split, const Work* work);
