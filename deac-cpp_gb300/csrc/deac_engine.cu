@@ -1009,21 +1009,27 @@ int build_part_work(deac_batch* b) {
     return DEAC_OK;
 }
 
-// Split engine: every tile's chunks split over CTAs so that the launch has
-// about split_waves x the SMs the row sums leave free (one CTA per SM: the
-// kernel uses ~214 KB of shared memory and all of TMEM); partial-sum blocks
-// only for tiles split over several CTAs (a tile with one CTA has its
-// estimates formed by that CTA).
+// Split engine: the batch's chunks (summed over its tiles) shared out so that
+// no CTA takes more than total / (split_waves x the SMs the row sums leave
+// free) of them (one CTA per SM: the kernel uses ~214 KB of shared memory and
+// all of TMEM); a tile is split in proportion to its chunk count, so long
+// tiles (large M) no longer set the launch's tail. Partial-sum blocks only for
+// tiles split over several CTAs (a tile with one CTA has its estimates formed
+// by that CTA).
 int build_split_work(deac_batch* b) {
     std::vector<deac::SplitTile> tiles = b->tiles_host;
     const std::vector<uint32_t>& tile_chunks = b->tile_chunks;
-    const uint64_t want = std::max<uint64_t>(1, b->split_waves * b->free_sms / tiles.size());
+    uint64_t total = 0;
+    for (uint32_t C : tile_chunks) total += C;
+    const uint64_t ctas = std::max<uint64_t>(1, b->split_waves * b->free_sms);
+    const uint64_t target = std::max<uint64_t>(1, (total + ctas - 1) / ctas);
     std::vector<deac::SplitWork> work;
     std::vector<uint32_t> combine_tiles;
     uint32_t blocks = 0;
     for (uint32_t t = 0; t < tiles.size(); ++t) {
         const uint32_t C = tile_chunks[t];
-        const uint32_t per = (uint32_t)((C + std::min<uint64_t>(want, C) - 1) / std::min<uint64_t>(want, C));
+        const uint32_t want = (uint32_t)std::min<uint64_t>(C, (C + target - 1) / target);
+        const uint32_t per = (C + want - 1) / want;
         const uint32_t nsplit = (C + per - 1) / per;
         tiles[t].block0 = nsplit > 1 ? blocks : ~0u;
         tiles[t].nsplit = nsplit;
@@ -1032,6 +1038,11 @@ int build_split_work(deac_batch* b) {
             work.push_back({t, c0, std::min(C, c0 + per), nsplit > 1 ? blocks++ : ~0u});
         if (nsplit > 1) combine_tiles.push_back(t);
     }
+    // longest pieces first: the block scheduler hands CTAs out in index
+    // order, so this is longest-processing-time-first over the SMs
+    std::stable_sort(work.begin(), work.end(), [](const deac::SplitWork& a, const deac::SplitWork& b2) {
+        return a.c1 - a.c0 > b2.c1 - b2.c0;
+    });
     for (void* p : {(void*)b->d_combine_tiles, (void*)b->d_tiles, (void*)b->d_split_work, (void*)b->d_partial})
         cudaFree(p);
     b->d_combine_tiles = nullptr;
