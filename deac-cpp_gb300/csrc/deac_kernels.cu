@@ -277,7 +277,7 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
                     double v = x[h];
                     if (mutate) {
                         v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
-                        if (!keep_sign) v = fabs(v);
+                        if (!keep_sign) v = abs_bits(v);
                         mutated = true;
                     }
                     dst[(uint64_t)sd[h] * PM + jj[h]] = v;
@@ -630,8 +630,7 @@ __device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* wo
                     double v = x[h];
                     if (mutate) {
                         v = fma(fw, b[h] - c[h], a[h]);
-                        if (!keep_sign)
-                            v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
+                        if (!keep_sign) v = abs_bits(v);
                         mutated = true;
                     }
                     qd[jj] = v;

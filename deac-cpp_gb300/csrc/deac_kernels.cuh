@@ -202,6 +202,15 @@ __device__ __forceinline__ uint64_t crossover_threshold(double cr) {
     return (uint64_t)ceil(cr * 0x1.0p53);
 }
 
+// |v|: v with its sign bit cleared by an integer AND on the high word.  The
+// AND is inline PTX so that the compiler cannot turn it back into an FP64
+// absolute value, which GB300 runs on its narrow FP64 pipe.
+__device__ __forceinline__ double abs_bits(double v) {
+    uint32_t hi = (uint32_t)__double2hiint(v);
+    asm("and.b32 %0, %0, 0x7FFFFFFF;" : "+r"(hi));
+    return __hiloint2double((int)hi, __double2loint(v));
+}
+
 // Asynchronous L2 prefetch of the `count` elements at p, rounded out to the
 // 16-byte units a bulk copy addresses and clipped at `end` (one past the
 // buffer's last element), so that it never reaches beyond the buffer.

@@ -155,17 +155,19 @@ __global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt,
 constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
 
 // ---- digit slicing of one value (shared by trial_kernel and the host)
-// exponent field of |v| (unbiased), or -2000 for zero / subnormal
+// exponent field of |v| (unbiased), or -2000 for zero / subnormal.  The
+// field is read from the high word, without masking the sign off the whole
+// value: the compiler turns such a mask into an FP64 absolute value, a slot
+// of GB300's narrow FP64 pipe.
 __device__ __forceinline__ int exp_of(double v) {
-    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    const int ef = (int)(b >> 52);
+    const int ef = (int)(((uint32_t)__double2hiint(v) >> 20) & 0x7FFu);
     return ef == 0 ? -2000 : ef - 1023;
 }
 
 // fixed-point fraction floor(|v| * 2^(49-e)) for a scale 2^e > |v|
 __device__ __forceinline__ uint64_t frac_digits(double v, int e) {
-    const uint64_t b = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    const int ef = (int)(b >> 52);
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const int ef = (int)(((uint32_t)__double2hiint(v) >> 20) & 0x7FFu);
     if (ef == 0) return 0;  // zero or subnormal: below every scale used here
     const uint64_t mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const int shift = (52 - kDigitBits) + e - (ef - 1023);
@@ -200,8 +202,8 @@ __device__ __forceinline__ void store_unit_digits(const double v[8], int e, uint
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
         // the sign bits (integer tests: FP64 compares share the narrow FP64 pipe)
-        const uint32_t n0 = (uint32_t)((uint64_t)__double_as_longlong(v[2 * k]) >> 63);
-        const uint32_t n1 = (uint32_t)((uint64_t)__double_as_longlong(v[2 * k + 1]) >> 63);
+        const uint32_t n0 = (uint32_t)__double2hiint(v[2 * k]) >> 31;
+        const uint32_t n1 = (uint32_t)__double2hiint(v[2 * k + 1]) >> 31;
         const uint32_t m = (n0 << 15) | (n1 << 31);  // sign bits of the two halves
         sg[k] = 0x3F803F80u | m;                      // +-1.0
         nb[k] = 0xC300C300u ^ m;                      // -+128.0

@@ -239,7 +239,10 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                 int em = -2000;
                 bool mt = false;
                 double z = 0.0;  // side 0's gene 0 (lane 0 of the first half)
-                for (uint32_t s = 0; s < S; ++s) {
+                // (both sides unrolled: their loads, draws and FMAs overlap)
+#pragma unroll
+                for (uint32_t s = 0; s < 2; ++s) {
+                    if (s >= S) break;
                     const uint64_t thr = T.thr[s][row];
                     const double fw = T.fw[s][row];
                     // the draws of this side's chunk genes are consecutive
@@ -266,8 +269,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                         double v = x[h];
                         if (mutate) {
                             v = fma(fw, b[h] - cc[h], a[h]);
-                            if (!keep_sign)
-                                v = __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);  // fabs
+                            if (!keep_sign) v = abs_bits(v);
                             mt = true;
                         }
                         if (j0 + jl == 0) {
