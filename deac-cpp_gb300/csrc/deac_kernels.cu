@@ -275,8 +275,8 @@ __device__ __forceinline__ void trial_body(RunDev* runs, const Work* work, int i
                         store_state(R, base + 1 + (uint64_t)sd[h] * M + jj[h], st[h]);
                     }
                     double v = x[h];
+                    mutate_gene(v, a[h], b[h], cc[h], s_fw[sd[h]], mutate);
                     if (mutate) {
-                        v = fma(s_fw[sd[h]], b[h] - cc[h], a[h]);
                         if (!keep_sign) v = abs_bits(v);
                         mutated = true;
                     }
@@ -628,8 +628,8 @@ __device__ __forceinline__ void trial_part_body(RunDev* runs, const PartWork* wo
                         so[3 * n] = st[h][3];
                     }
                     double v = x[h];
+                    mutate_gene(v, a[h], b[h], c[h], fw, mutate);
                     if (mutate) {
-                        v = fma(fw, b[h] - c[h], a[h]);
                         if (!keep_sign) v = abs_bits(v);
                         mutated = true;
                     }

@@ -211,6 +211,18 @@ __device__ __forceinline__ double abs_bits(double v) {
     return __hiloint2double((int)hi, __double2loint(v));
 }
 
+// The DE/rand/1 mutation v = a + F (b - c) (one rounding for b - c, one for
+// the fused multiply-add: deac_gpu.cu:514-539) in lanes where `mutate` holds;
+// v keeps its value elsewhere.  Predicated in PTX so that the FP64 pipe (a
+// narrow one on GB300) sees only the mutating lanes of a warp, where the
+// compiler would compute every lane and select.
+__device__ __forceinline__ void mutate_gene(double& v, double a, double b, double c, double fw, bool mutate) {
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t@p sub.rn.f64 %0, %2, %3;\n\t"
+        "@p fma.rn.f64 %0, %5, %0, %1;\n\t}"
+        : "+d"(v)
+        : "d"(a), "d"(b), "d"(c), "r"((uint32_t)mutate), "d"(fw));
+}
+
 // Asynchronous L2 prefetch of the `count` elements at p, rounded out to the
 // 16-byte units a bulk copy addresses and clipped at `end` (one past the
 // buffer's last element), so that it never reaches beyond the buffer.

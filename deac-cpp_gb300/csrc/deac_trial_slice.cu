@@ -22,6 +22,12 @@ namespace {
 
 constexpr uint32_t kNoItem = 0xFFFFFFFFu;
 
+// A trial gene to global memory, kept in L1 (evict-last): the warp reads its
+// trial genes back at once, in the digit layout.
+__device__ __forceinline__ void st_keep_l1(double* p, double v) {
+    asm volatile("st.global.L1::evict_last.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
 // The CTA's position in its item sequence: segment g, item `it` of it.
 struct SliceCursor {
     uint32_t g, it;
@@ -267,8 +273,8 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                         const uint32_t jl = jc + h * 32 + lane;
                         const bool mutate = (splitmix_mix(w0 + h * (32 * kGamma)) >> 11) < thr;
                         double v = x[h];
+                        mutate_gene(v, a[h], b[h], cc[h], fw, mutate);
                         if (mutate) {
-                            v = fma(fw, b[h] - cc[h], a[h]);
                             if (!keep_sign) v = abs_bits(v);
                             mt = true;
                         }
@@ -276,7 +282,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                             if (s == 0) z = v;
                             else v = z;  // gpu_match_population_zero
                         }
-                        dst[(uint64_t)s * PM + jl] = v;
+                        st_keep_l1(dst + (uint64_t)s * PM + jl, v);
                         em = max(em, exp_of(v));
                     }
                 }
