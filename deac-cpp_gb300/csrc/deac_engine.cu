@@ -172,6 +172,10 @@ struct deac_batch {
     std::vector<deac::SplitTile> tiles_host;
     std::vector<uint32_t> tile_chunks;
     uint64_t free_sms = 1;
+    uint32_t* d_final_members = nullptr;     // split engine: the final evaluations' member lists,
+    uint64_t* d_final_items = nullptr;       // their items and its length
+    uint32_t* d_final_count = nullptr;
+    uint32_t final_capacity = 0;
     uint64_t* d_exact_list = nullptr;        // split engine: the exact pass's items
     uint32_t* d_exact_count = nullptr;
     uint32_t n_combine_tiles = 0;            // tiles split over several contraction CTAs
@@ -408,7 +412,16 @@ int launch_split_init(deac_batch* b) {
 int finalize_split(deac_batch* b, bool all = false) {
     if (b->snapped && (b->snapped_all || !all)) return DEAC_OK;
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        launch_contract(b, b->stream, all ? deac::kModeFinal : deac::kModeFinalBest);
+        // the parents to evaluate listed per run, then only their tiles
+        // (two CTAs of 96 KB per SM)
+        const int mode = all ? deac::kModeFinal : deac::kModeFinalBest;
+        CUDA_TRY(cudaMemsetAsync(b->d_final_count, 0, sizeof(uint32_t), b->stream));
+        deac::final_list_kernel<<<(unsigned)b->runs.size(), 32, 0, b->stream>>>(
+            b->d_runs, mode, b->d_final_items, b->d_final_count, b->final_capacity, b->d_status);
+        CUDA_TRY(cudaGetLastError());
+        const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(b->final_capacity, 2 * (uint32_t)b->sms));
+        deac::final_exact_kernel<<<grid, deac::kContractThreads, deac::kFinalSmemBytes, b->stream>>>(
+            b->d_runs, b->d_final_items, b->d_final_count, mode);
         CUDA_TRY(cudaGetLastError());
     }
     b->snapped_all = all || b->engine != DEAC_ENGINE_SPLIT_BF16;
@@ -434,6 +447,11 @@ int finalize_split(deac_batch* b, bool all = false) {
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(copy_async(b, b->h_snap, b->d_snap, b->snap_bytes, cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
+    if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
+        int st = 0;
+        CUDA_TRY(copy(b, &st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
+        if (st) return fail(DEAC_E_CUDA, "the final exact evaluations failed (status %d)", st);
+    }
     b->snap.resize(n);
     b->snap_fit.resize(n);
     b->snap_cur.resize(n);
@@ -1400,6 +1418,29 @@ int deac_batch_setup(deac_batch* b) {
             r->dev.exact_list = b->d_exact_list;
             r->dev.exact_count = b->d_exact_count;
         }
+        // the final exact evaluations: every run's member list, and room
+        // for the item list of the largest tiling of every run
+        uint64_t members = 0, cap = 0;
+        for (auto& r : b->runs) {
+            members += r->dev.P;
+            uint32_t most = 0;
+            for (uint32_t n = 1; n <= r->dev.P; ++n) {
+                uint32_t mt, tt, chunk, ctas;
+                deac::final_tiling(n, r->dev.S, r->dev.Nt, mt, tt, chunk, ctas);
+                most = std::max(most, ctas);
+            }
+            cap += most;
+        }
+        b->final_capacity = (uint32_t)cap;
+        CUDA_TRY(cudaMalloc(&b->d_final_members, members * sizeof(uint32_t)));
+        CUDA_TRY(cudaMalloc(&b->d_final_items, std::max<uint64_t>(cap, 1) * sizeof(uint64_t)));
+        CUDA_TRY(cudaMalloc(&b->d_final_count, sizeof(uint32_t)));
+        uint64_t off = 0;
+        for (auto& r : b->runs) {
+            r->dev.final_members = b->d_final_members + off;
+            off += r->dev.P;
+        }
+        CUDA_TRY(raise_smem_limit(deac::final_exact_kernel, deac::kFinalSmemBytes));
     }
     std::vector<deac::RunDev> descs;
     for (auto& r : b->runs) descs.push_back(r->dev);
@@ -1986,6 +2027,9 @@ int deac_batch_destroy(deac_batch* b) {
     cudaFree(b->d_partial);
     cudaFree(b->d_combine_tiles);
     cudaFree(b->d_exact_list);
+    cudaFree(b->d_final_members);
+    cudaFree(b->d_final_items);
+    cudaFree(b->d_final_count);
     cudaFree(b->d_exact_count);
     cudaFree(b->d_rows);
     cudaFree(b->d_status);

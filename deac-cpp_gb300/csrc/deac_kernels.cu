@@ -800,7 +800,11 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // slots.
 // One contraction item: tile w of run w.run in mode `mode`; in
 // kModeRecheck the item's pass `pmode` is kModeParents or kModeTrials.
-__device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mode, int pmode, double* dyn) {
+// `fin`: a tile of the final exact evaluations, over the run's listed
+// members (final_members, final_n) in the listed tiling instead of every
+// member in the run's own.
+__device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mode, int pmode, double* dyn,
+                                              bool fin = false) {
     __shared__ int s_last, s_any;
     const bool both = mode == kModeRecheck;
     RunDev& R = runs[w.run];
@@ -815,7 +819,7 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     // kModeFinalBest: the lowest upper end of the parents' intervals (a
     // parent whose interval starts above it cannot hold the minimum)
     __shared__ double s_min_hi;
-    if (mode == kModeFinalBest) {
+    if (mode == kModeFinalBest && !fin) {
         double mh = __longlong_as_double(0x7ff0000000000000ll);  // +inf
         for (uint32_t m = threadIdx.x; m < R.P; m += blockDim.x) mh = fmin(mh, R.f_hi[m]);
         for (int o = 16; o > 0; o >>= 1) mh = fmin(mh, __shfl_xor_sync(0xffffffffu, mh, o));
@@ -835,18 +839,23 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
         return pm == kModeFinal ? inexact : (R.recheck[m] != 0 && inexact);
     };
     const bool use_parent = parents_of(pmode);
-    auto wanted = [&](uint32_t m) -> bool { return wanted_in(pmode, m); };
+    // the tile's member slots: every member in order, or the listed ones
     const uint32_t P = R.P, M = R.M, Nt = R.Nt, S = R.S;
-    const uint32_t MT = R.member_tile, TT = R.tau_tile, CH = R.chunk;
+    const uint32_t NM = fin ? R.final_n : P;
+    auto member = [&](uint32_t slot) -> uint32_t { return fin ? R.final_members[slot] : slot; };
+    auto wanted = [&](uint32_t m) -> bool { return fin || wanted_in(pmode, m); };
+    const uint32_t MT = fin ? R.final_mt : R.member_tile, TT = fin ? R.final_tt : R.tau_tile,
+                   CH = fin ? R.final_chunk : R.chunk;
     const uint64_t PM = (uint64_t)P * M;
-    const uint32_t member_tiles = (P + MT - 1) / MT;
+    const uint32_t member_tiles = (NM + MT - 1) / MT;
     const uint32_t mt = w.index % member_tiles, tt = w.index / member_tiles;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t pair = S == 2 ? warp * 16 + (lane & 15u) : threadIdx.x;
     const uint32_t side = S == 2 ? (lane >> 4) : 0u;
     const uint32_t mi = pair % MT, ti = pair / MT;
-    const uint32_t i = mt * MT + mi, t = tt * TT + ti;
-    const bool valid = ti < TT && i < P && t < Nt && wanted(i);
+    const uint32_t slot = mt * MT + mi, t = tt * TT + ti;
+    const uint32_t i = slot < NM ? member(slot) : 0u;
+    const bool valid = ti < TT && slot < NM && t < Nt && wanted(i);
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     if (valid) s_any = 1;
@@ -874,8 +883,9 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
             if (r >= rows) break;
             dst_row[j] = r;
             if (r < S * MT) {
-                const uint32_t s = r / MT, m = mt * MT + (r - s * MT);
-                if (m < P && wanted(m)) {
+                const uint32_t s = r / MT, sl = mt * MT + (r - s * MT);
+                const uint32_t m = sl < NM ? member(sl) : 0u;
+                if (sl < NM && wanted(m)) {
                     const uint32_t bsel = use_parent ? R.cur[m] : 1u - R.cur[m];
                     src_row[j] = pop + ((uint64_t)bsel * S + s) * PM + (uint64_t)m * M;
                 }
@@ -937,7 +947,7 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t done_ctas = atomicAdd(&R.ticket, 1u) + 1u;
-        s_last = done_ctas == (both ? 2 * R.contract_ctas : R.contract_ctas);
+        s_last = done_ctas == (fin ? R.final_ctas : both ? 2 * R.contract_ctas : R.contract_ctas);
     }
     __syncthreads();
     if (!s_last) return;
@@ -956,8 +966,9 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     const bool fit_parent = parents_of(fmode);
     double* fit_dst = fit_parent ? R.fit_old : R.fit_new;
     const volatile double* E_all = both && pass == 1 ? R.model_isf2 : R.model_isf;
-    for (uint32_t m = warp; m < P; m += nwarps) {
-        if (!wanted_in(fmode, m)) continue;  // warp-uniform
+    for (uint32_t k = warp; k < NM; k += nwarps) {
+        const uint32_t m = member(k);
+        if (!fin && !wanted_in(fmode, m)) continue;  // warp-uniform
         for (uint32_t s = lane; s < width; s += 32) {
             double v = 0.0;
             for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
@@ -1111,6 +1122,56 @@ __global__ void __launch_bounds__(kContractThreads) exact_pass_kernel(RunDev* ru
         const uint64_t e = list[k];
         const Work w{(uint32_t)(e >> 32), (uint32_t)e & 0x7FFFFFFFu};
         contract_body(runs, w, kModeRecheck, (e >> 31) & 1u ? kModeTrials : kModeParents, dyn);
+        __syncthreads();  // shared memory is reused by the next item
+    }
+}
+
+__global__ void final_list_kernel(RunDev* runs, int mode, uint64_t* items, uint32_t* count, uint32_t capacity,
+                                  int* status) {
+    RunDev& R = runs[blockIdx.x];
+    const uint32_t lane = threadIdx.x, P = R.P;
+    // kModeFinalBest: the lowest upper end of the parents' intervals (a
+    // parent whose interval starts above it cannot hold the minimum)
+    double mh = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+    if (mode == kModeFinalBest) {
+        for (uint32_t m = lane; m < P; m += 32) mh = fmin(mh, R.f_hi[m]);
+        for (int o = 16; o > 0; o >>= 1) mh = fmin(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+    }
+    uint32_t n = 0;
+    for (uint32_t m0 = 0; m0 < P; m0 += 32) {
+        const uint32_t m = m0 + lane;
+        const bool want = m < P && R.f_lo[m] != R.f_hi[m] && (mode != kModeFinalBest || R.f_lo[m] <= mh);
+        const uint32_t mask = __ballot_sync(0xffffffffu, want);
+        if (want) R.final_members[n + __popc(mask & ((1u << lane) - 1u))] = m;
+        n += __popc(mask);
+    }
+    if (lane != 0) return;
+    uint32_t mt = 1, tt = 1, chunk = 8, ctas = 0;
+    if (n) final_tiling(n, R.S, R.Nt, mt, tt, chunk, ctas);
+    uint32_t base = 0;
+    if (ctas) {
+        base = atomicAdd(count, ctas);
+        if (base + ctas > capacity) {
+            // (capacity covers the largest tiling of every run: not reached)
+            atomicCAS(status, 0, kStatusFinalList);
+            ctas = 0;
+        }
+    }
+    R.final_n = ctas ? n : 0u;
+    R.final_mt = mt;
+    R.final_tt = tt;
+    R.final_chunk = chunk;
+    R.final_ctas = ctas;
+    for (uint32_t k = 0; k < ctas; ++k) items[base + k] = ((uint64_t)blockIdx.x << 32) | k;
+}
+
+__global__ void __launch_bounds__(kContractThreads) final_exact_kernel(RunDev* runs, const uint64_t* items,
+                                                                       const uint32_t* count, int mode) {
+    extern __shared__ __align__(16) double dyn[];
+    const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(count);
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint64_t e = items[k];
+        contract_body(runs, Work{(uint32_t)(e >> 32), (uint32_t)e}, mode, mode, dyn, true);
         __syncthreads();  // shared memory is reused by the next item
     }
 }

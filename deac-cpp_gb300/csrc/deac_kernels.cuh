@@ -111,6 +111,10 @@ struct RunDev {
     // runs; see exact_pass_kernel) and its length
     uint64_t* exact_list;
     uint32_t* exact_count;
+    // split engine: the final exact evaluations (final_list_kernel) -- the
+    // parents to evaluate, ascending, and the tiling of their contraction
+    uint32_t* final_members;  // [P]
+    uint32_t final_n, final_mt, final_tt, final_chunk, final_ctas;
     // status, owned by the kernels
     uint64_t ii;             // next generation index to execute
     uint64_t generation;     // generation reported when done
@@ -297,5 +301,28 @@ __global__ void contract_kernel(RunDev* runs, const Work* work, int mode);
 // split engine: the exact pass over the items split_select_kernel listed
 // (entry = run << 32 | pass << 31 | tile, pass 1 = the trials; count entries)
 __global__ void exact_pass_kernel(RunDev* runs, const uint64_t* list, const uint32_t* count);
+// The split engine's final exact evaluations (kModeFinal / kModeFinalBest):
+// final_list_kernel (one warp per run) lists the parents to evaluate and
+// appends the tiles of their contraction to `items` (run << 32 | tile);
+// final_exact_kernel evaluates the listed tiles, packed so that every chain
+// pair of a tile belongs to a listed parent.
+constexpr uint32_t kFinalSmemBytes = 96 * 1024;
+__host__ __device__ inline void final_tiling(uint32_t n, uint32_t S, uint32_t Nt, uint32_t& mt, uint32_t& tt,
+                                             uint32_t& chunk, uint32_t& ctas) {
+    const uint32_t pairs = contract_pairs(S);
+    mt = 1;
+    while (mt * 2 <= (n < pairs ? n : pairs)) mt *= 2;
+    tt = pairs / mt;
+    const uint32_t rows = S * (mt + tt);
+    uint32_t c = (kFinalSmemBytes / 8) / (2 * rows) - 2;
+    c = (c < 128 ? c : 128) & ~1u;
+    chunk = c > 8 ? c : 8;
+    ctas = ((n + mt - 1) / mt) * ((Nt + tt - 1) / tt);
+}
+__global__ void final_list_kernel(RunDev* runs, int mode, uint64_t* items, uint32_t* count, uint32_t capacity,
+                                  int* status);
+__global__ void final_exact_kernel(RunDev* runs, const uint64_t* items, const uint32_t* count, int mode);
+// status value of a final item list that would have overflowed
+constexpr int kStatusFinalList = 3;
 
 }  // namespace deac
