@@ -68,6 +68,11 @@ WORKLOAD = ("deac batching form: 1024 ragged runs in one batch (seeds 1-1024; M 
             "engine on the same runs beside it")
 DATA = ("synthetic (benchmark recipe per run: 0.7 N(5,1) + 0.3 N(20,3) at the run's temperature, sigma = 1e-4 F, "
         "numpy default_rng(seed))")
+# DRAM bytes per unit of the two main kernels, from one ncu capture each of
+# the first 64 runs (295.3 MB read + 757.6 MB written over 36.85 M genes;
+# 1.2986 GB + 17.5 MB over 4.716 G products)
+SLICE_DRAM_BYTES_PER_GENE = (295.264e6 + 757.633e6) / 36847616
+CONTRACT_DRAM_BYTES_PER_PRODUCT = (1.298555e9 + 17.477632e6) / 4716494848
 # the single-run production scale, for the secondary keys
 P1, M1, OMEGA1, T1 = 8, 4096, 512.0, 1.35
 LONG_WINDOW = 100_000
@@ -526,8 +531,15 @@ def engine_arm(args, world, rank, local):
     roof = kernel_roofline(dominant, ms_d / n_d / 1e3, peaks, configs)
     roof["peak_source"] = peaks["source"] + (" burst figure" if roof["bound"] != "fp64" else
                                              "; FP64: measured DFMA throughput")
-    # DRAM bytes per launch are read from an ncu capture, not from this run
-    roof["traffic"] = None
+    # DRAM bytes per launch: an ncu capture of the first 64 runs (too large
+    # to capture whole), scaled to this launch by its genes or products
+    rows_, genes_, products_ = workload_sizes(configs)
+    traffic = {0: genes_ * SLICE_DRAM_BYTES_PER_GENE, 3: products_ * CONTRACT_DRAM_BYTES_PER_PRODUCT}.get(dominant)
+    roof["traffic"] = traffic
+    if traffic is not None:
+        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the first 64 "
+                                  "runs, scaled by " + ("genes" if dominant == 0 else "products") +
+                                  " (profiles/*_cfg3_64runs.md)")
     roof["per_generation_us"] = {KERNEL_NAMES[k]: round(v, 1) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs
