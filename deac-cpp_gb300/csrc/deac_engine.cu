@@ -25,6 +25,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -1655,11 +1656,16 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
                                         total * 8 + (total + 7) / 8 * 8) +
         b->gene_off[run];
     const uint64_t L = res.spectrum_length;
-    std::vector<double> dsf(L), fr(L);
-    deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes, S == 2 ? &genes[M] : nullptr, dsf.data(),
-                        fr.data());
-    if (best_dsf) std::memcpy(best_dsf, dsf.data(), L * 8);
-    if (best_frequency) std::memcpy(best_frequency, fr.data(), L * 8);
+    if (best_dsf && best_frequency) {
+        deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes, S == 2 ? &genes[M] : nullptr, best_dsf,
+                            best_frequency);
+    } else if (best_dsf || best_frequency) {
+        std::vector<double> dsf(L), fr(L);
+        deac::best_spectrum(r.cfg, r.model, r.freq.data(), M, genes, S == 2 ? &genes[M] : nullptr, dsf.data(),
+                            fr.data());
+        if (best_dsf) std::memcpy(best_dsf, dsf.data(), L * 8);
+        if (best_frequency) std::memcpy(best_frequency, fr.data(), L * 8);
+    }
     if (r.cfg.track_stats && (stats_mean || stats_minimum || stats_squared_mean)) {
         const uint64_t N = r.cfg.number_of_generations, n = res.stats_length;
         std::vector<double> stats(3 * n);
@@ -1675,6 +1681,60 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf, double* best
         if (stats_mean) std::memcpy(stats_mean, stats.data(), n * 8);
         if (stats_minimum) std::memcpy(stats_minimum, stats.data() + n, n * 8);
         if (stats_squared_mean) std::memcpy(stats_squared_mean, stats.data() + 2 * n, n * 8);
+    }
+    return DEAC_OK;
+}
+
+int deac_batch_spectra_length(deac_batch* b, uint64_t* doubles) {
+    if (!b || !doubles) return fail(DEAC_E_INVALID, "bad argument");
+    uint64_t n = 0;
+    for (auto& r : b->runs) n += r->S == 2 ? 2 * r->M - 1 : r->M;
+    *doubles = n;
+    return DEAC_OK;
+}
+
+int deac_batch_fetch_all(deac_batch* b, deac_run_result* results, double* best_dsf, double* best_frequency) {
+    if (!b) return fail(DEAC_E_INVALID, "bad argument");
+    if (!b->set_up) return fail(DEAC_E_STATE, "deac_batch_setup has not run");
+    int rc0 = finalize_split(b);
+    if (rc0) return rc0;
+    const size_t n = b->runs.size();
+    size_t total = 0;
+    for (auto& rp : b->runs) total += rp->dev.P;
+    const double* const genes0 = reinterpret_cast<const double*>(
+        reinterpret_cast<const char*>(b->h_snap) + n * sizeof(deac::RunDev) + total * 8 + (total + 7) / 8 * 8);
+    std::vector<deac_run_result> res(n);
+    std::vector<uint64_t> off(n + 1, 0);
+    for (size_t r = 0; r < n; ++r) {
+        summarize(*b->runs[r], b->snap[r], b->snap_fit[r], &res[r]);
+        off[r + 1] = off[r] + res[r].spectrum_length;
+    }
+    if (results) std::memcpy(results, res.data(), n * sizeof(deac_run_result));
+    if (best_dsf || best_frequency) {
+        // runs shared out over host threads, by their spectrum lengths
+        const unsigned threads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+        std::atomic<size_t> next{0};
+        auto work = [&]() {
+            std::vector<double> scratch;
+            for (size_t r; (r = next.fetch_add(1)) < n;) {
+                const RunHost& rh = *b->runs[r];
+                const uint64_t M = rh.M, L = res[r].spectrum_length;
+                const double* genes = genes0 + b->gene_off[r];
+                double* d = best_dsf ? best_dsf + off[r] : nullptr;
+                double* f = best_frequency ? best_frequency + off[r] : nullptr;
+                if (!d || !f) {
+                    scratch.resize(L);
+                    if (!d) d = scratch.data();
+                    if (!f) f = scratch.data();
+                }
+                deac::best_spectrum(rh.cfg, rh.model, rh.freq.data(), M, genes, rh.S == 2 ? &genes[M] : nullptr, d,
+                                    f);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < threads; ++t) pool.emplace_back(work);
+        work();
+        for (auto& th : pool) th.join();
     }
     return DEAC_OK;
 }

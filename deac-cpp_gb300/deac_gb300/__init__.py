@@ -148,6 +148,8 @@ SIGNATURES = {
     "deac_batch_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
     "deac_batch_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(RunResult)]),
     "deac_batch_fetch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, _dp, _dp, _dp, _dp]),
+    "deac_batch_fetch_all": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RunResult), _dp, _dp]),
+    "deac_batch_spectra_length": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "deac_batch_fetch_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _dp, _dp, _dp, _dp]),
     "deac_batch_checkpoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                              ctypes.POINTER(ctypes.c_uint64)]),
@@ -323,6 +325,26 @@ class Batch:
         out = dict(res, dsf=spec, frequency=freq)
         if cfg.track_stats:
             out["stats_mean"], out["stats_minimum"], out["stats_squared_mean"] = st
+        return out
+
+    def fetch_all(self) -> list:
+        """Every run's summary and best spectrum (as fetch, without the
+        statistics arrays), in one call: the spectra are formed on host
+        threads into one array, each run's dsf and frequency a view of it."""
+        n = len(self._runs)
+        total = ctypes.c_uint64(0)
+        _check(self._lib.deac_batch_spectra_length(self._h, ctypes.byref(total)))
+        res = (RunResult * n)()
+        spec = np.empty(total.value)
+        freq = np.empty(total.value)
+        _check(self._lib.deac_batch_fetch_all(self._h, res, _ptr(spec), _ptr(freq)))
+        out, o = [], 0
+        for r in range(n):
+            d = {k: getattr(res[r], k) for k, _ in RunResult._fields_}
+            L = d["spectrum_length"]
+            d["dsf"], d["frequency"] = spec[o:o + L], freq[o:o + L]
+            o += L
+            out.append(d)
         return out
 
     def fetch_state(self, run: int) -> dict:

@@ -203,6 +203,16 @@ int deac_batch_fetch(deac_batch* b, uint32_t run, double* best_dsf,
                      double* best_frequency, double* stats_mean,
                      double* stats_minimum, double* stats_squared_mean);
 
+/* Every run's summary and best spectrum in one call (the batch form of
+ * deac_batch_result + deac_batch_fetch): results[r] for each run r, and the
+ * spectra concatenated in run order -- run r's best_dsf and best_frequency
+ * start at the sum of spectrum_length over the runs before it (size the
+ * arrays with deac_batch_spectra_length).  The spectra are formed on host
+ * threads.  Either array may be NULL. */
+int deac_batch_fetch_all(deac_batch* b, deac_run_result* results, double* best_dsf,
+                         double* best_frequency);
+int deac_batch_spectra_length(deac_batch* b, uint64_t* doubles);
+
 /* Current state of run `run`: population [side][member][gene] (S*P*M
  * doubles), fitness (P), crossover rates and differential weights
  * ([side][member], S*P each).  Any pointer may be NULL. */

@@ -191,3 +191,28 @@ def test_split_moment_terms_match_plain(name, engine):
     c = split["counts"]
     if not over.get("use_negative_first_moment"):
         assert c["interval"] > 0, c
+
+
+def test_fetch_all_matches_fetch(engine):
+    """The batch form of the outputs (every run's summary and best spectrum
+    in one call, spectra formed on host threads) equals the per-run fetch,
+    on both engines, over runs of every model, one- and two-sided."""
+    specs = []
+    for k, kw in enumerate([dict(spectra_type="bfull"), dict(model="hyperbolic", spectra_type="bfull"),
+                            dict(model="normalization", spectra_type="bfull"), dict(bosonic=True),
+                            dict(model="hyperbolic", bosonic=True), dict(spectra_type="spbsf")]):
+        cfg = engine.make_config(temperature=1.35, population_size=8 + 8 * (k % 3), number_of_generations=200,
+                                 seed=40 + k, **kw)
+        specs.append((cfg, config0_data(40 + k), uniform_grid(64 + 32 * k, 64.0)))
+    for kind in (engine.ENGINE_PLAIN_FP64, engine.ENGINE_SPLIT_BF16):
+        with engine.Batch(engine=kind) as b:
+            ids = [b.add_run(cfg, *data, freq) for cfg, data, freq in specs]
+            b.run()
+            every = b.fetch_all()
+            assert len(every) == len(ids)
+            for r in ids:
+                one = b.fetch(r)
+                for key in ("generation", "minimum_fitness", "best_index", "spectrum_length", "finished"):
+                    assert every[r][key] == one[key], key
+                assert np.array_equal(every[r]["dsf"], one["dsf"])
+                assert np.array_equal(every[r]["frequency"], one["frequency"])
