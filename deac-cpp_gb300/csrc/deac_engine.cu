@@ -264,7 +264,9 @@ void launch_contract(deac_batch* b, cudaStream_t s, int mode, bool early = false
     if (mode == deac::kModeRecheck) {
         // the listed items, over at most one CTA per SM (one fits per SM)
         const uint32_t grid = std::min<uint32_t>(2 * b->n_contract_ctas, (uint32_t)b->sms);
-        launch(deac::exact_pass_kernel, grid, deac::kContractThreads, b->contract_smem_bytes, s, early, b->d_runs,
+        // (a packed tile stages within kFinalSmemBytes)
+        const size_t smem = std::max<size_t>(b->contract_smem_bytes, deac::kFinalSmemBytes);
+        launch(deac::exact_pass_kernel, grid, deac::kContractThreads, smem, s, early, b->d_runs,
                static_cast<const uint64_t*>(b->d_exact_list), static_cast<const uint32_t*>(b->d_exact_count));
         return;
     }
@@ -1380,7 +1382,8 @@ int deac_batch_setup(deac_batch* b) {
     b->contract_smem_bytes = contract_bytes;
     CUDA_TRY(raise_smem_limit(deac::trial_kernel, std::max<size_t>(b->trial_smem_bytes, 1024)));
     CUDA_TRY(raise_smem_limit(deac::contract_kernel, b->contract_smem_bytes));
-    CUDA_TRY(raise_smem_limit(deac::exact_pass_kernel, b->contract_smem_bytes));
+    CUDA_TRY(raise_smem_limit(deac::exact_pass_kernel,
+                              std::max<size_t>(b->contract_smem_bytes, deac::kFinalSmemBytes)));
     CUDA_TRY(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
     b->n_trial_ctas = (uint32_t)tw.size();
     b->n_contract_ctas = (uint32_t)cw.size();
@@ -1412,7 +1415,19 @@ int deac_batch_setup(deac_batch* b) {
         if (rc) return rc;
     }
     if (b->engine == DEAC_ENGINE_SPLIT_BF16) {
-        CUDA_TRY(cudaMalloc(&b->d_exact_list, std::max<uint64_t>(2ull * b->n_contract_ctas, 1) * sizeof(uint64_t)));
+        // the exact pass lists both passes of a run, in the run's own tiles
+        // or packed with its open members (at most the largest packed tiling)
+        uint64_t exact_cap = 0;
+        for (auto& r : b->runs) {
+            uint32_t most = r->dev.contract_ctas;
+            for (uint32_t n = 1; n <= r->dev.P; ++n) {
+                uint32_t mt, tt, chunk, ctas;
+                deac::final_tiling(n, r->dev.S, r->dev.Nt, mt, tt, chunk, ctas, deac::kExactMinMembers);
+                most = std::max(most, ctas);
+            }
+            exact_cap += 2ull * most;
+        }
+        CUDA_TRY(cudaMalloc(&b->d_exact_list, std::max<uint64_t>(exact_cap, 1) * sizeof(uint64_t)));
         CUDA_TRY(cudaMalloc(&b->d_exact_count, sizeof(uint32_t)));
         CUDA_TRY(cudaMemset(b->d_exact_count, 0, sizeof(uint32_t)));
         for (auto& r : b->runs) {

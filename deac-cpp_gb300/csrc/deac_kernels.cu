@@ -800,9 +800,11 @@ __global__ void __launch_bounds__(kNormThreads) norm_kernel(RunDev* runs, const 
 // slots.
 // One contraction item: tile w of run w.run in mode `mode`; in
 // kModeRecheck the item's pass `pmode` is kModeParents or kModeTrials.
-// `fin`: a tile of the final exact evaluations, over the run's listed
-// members (final_members, final_n) in the listed tiling instead of every
-// member in the run's own.
+// `fin`: a packed tile, over the run's listed members (final_members,
+// final_n) in the listed tiling instead of every member in the run's own --
+// the final exact evaluations (the list is what they evaluate) and the exact
+// pass (the list holds the members left open; each pass still evaluates
+// only those it wants).
 __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mode, int pmode, double* dyn,
                                               bool fin = false) {
     __shared__ int s_last, s_any;
@@ -843,11 +845,11 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     const uint32_t P = R.P, M = R.M, Nt = R.Nt, S = R.S;
     const uint32_t NM = fin ? R.final_n : P;
     auto member = [&](uint32_t slot) -> uint32_t { return fin ? R.final_members[slot] : slot; };
-    auto wanted = [&](uint32_t m) -> bool { return fin || wanted_in(pmode, m); };
+    auto wanted = [&](uint32_t m) -> bool { return (fin && final_mode) || wanted_in(pmode, m); };
     const uint32_t MT = fin ? R.final_mt : R.member_tile, TT = fin ? R.final_tt : R.tau_tile,
                    CH = fin ? R.final_chunk : R.chunk;
     const uint64_t PM = (uint64_t)P * M;
-    const uint32_t member_tiles = (NM + MT - 1) / MT;
+    const uint32_t member_tiles = NM ? (NM + MT - 1) / MT : 1u;
     const uint32_t mt = w.index % member_tiles, tt = w.index / member_tiles;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t pair = S == 2 ? warp * 16 + (lane & 15u) : threadIdx.x;
@@ -947,7 +949,7 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t done_ctas = atomicAdd(&R.ticket, 1u) + 1u;
-        s_last = done_ctas == (fin ? R.final_ctas : both ? 2 * R.contract_ctas : R.contract_ctas);
+        s_last = done_ctas == (both ? 2u : 1u) * (fin ? R.final_ctas : R.contract_ctas);
     }
     __syncthreads();
     if (!s_last) return;
@@ -968,7 +970,7 @@ __device__ __forceinline__ void contract_body(RunDev* runs, const Work w, int mo
     const volatile double* E_all = both && pass == 1 ? R.model_isf2 : R.model_isf;
     for (uint32_t k = warp; k < NM; k += nwarps) {
         const uint32_t m = member(k);
-        if (!fin && !wanted_in(fmode, m)) continue;  // warp-uniform
+        if (!(fin && final_mode) && !wanted_in(fmode, m)) continue;  // warp-uniform
         for (uint32_t s = lane; s < width; s += 32) {
             double v = 0.0;
             for (uint32_t idx = s; idx < Nt; idx += kTreeSlots) {
@@ -1107,9 +1109,10 @@ __global__ void __launch_bounds__(kContractThreads) contract_kernel(RunDev* runs
 }
 
 // The split engine's exact pass: the items the selections left open, listed
-// by split_select_kernel (run << 32 | pass << 31 | tile, both passes of each
-// listed run), shared out over a grid of at most one CTA per SM; with nothing
-// listed every CTA returns at once.
+// by split_select_kernel (run << 32 | pass << 31 | packed << 30 | tile, both
+// passes of each listed run; packed: a tile of the run's listed members),
+// shared out over a grid of at most one CTA per SM; with nothing listed
+// every CTA returns at once.
 __global__ void __launch_bounds__(kContractThreads) exact_pass_kernel(RunDev* runs, const uint64_t* list,
                                                                       const uint32_t* count) {
     // the next generation's trial parts read nothing before their own wait:
@@ -1120,8 +1123,8 @@ __global__ void __launch_bounds__(kContractThreads) exact_pass_kernel(RunDev* ru
     const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(count);
     for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
         const uint64_t e = list[k];
-        const Work w{(uint32_t)(e >> 32), (uint32_t)e & 0x7FFFFFFFu};
-        contract_body(runs, w, kModeRecheck, (e >> 31) & 1u ? kModeTrials : kModeParents, dyn);
+        const Work w{(uint32_t)(e >> 32), (uint32_t)e & 0x3FFFFFFFu};
+        contract_body(runs, w, kModeRecheck, (e >> 31) & 1u ? kModeTrials : kModeParents, dyn, (e >> 30) & 1u);
         __syncthreads();  // shared memory is reused by the next item
     }
 }

@@ -307,11 +307,18 @@ __global__ void exact_pass_kernel(RunDev* runs, const uint64_t* list, const uint
 // final_exact_kernel evaluates the listed tiles, packed so that every chain
 // pair of a tile belongs to a listed parent.
 constexpr uint32_t kFinalSmemBytes = 96 * 1024;
+// The tiling of n listed members: mt members (a power of two, at least
+// min_mt) times tt timeslices fill the CTA's chain pairs.  Few members in few
+// tiles suit a batch-wide pass, where the FP64 pipe (charged per warp
+// instruction) is the limit; the exact pass of a generation is bound by the
+// latency of its chains instead, and takes min_mt = 8: fewer staged rows,
+// longer stages, fewer stage waits along each chain.
 __host__ __device__ inline void final_tiling(uint32_t n, uint32_t S, uint32_t Nt, uint32_t& mt, uint32_t& tt,
-                                             uint32_t& chunk, uint32_t& ctas) {
+                                             uint32_t& chunk, uint32_t& ctas, uint32_t min_mt = 1) {
     const uint32_t pairs = contract_pairs(S);
     mt = 1;
     while (mt * 2 <= (n < pairs ? n : pairs)) mt *= 2;
+    while (mt < min_mt && mt * 2 <= pairs) mt *= 2;
     tt = pairs / mt;
     const uint32_t rows = S * (mt + tt);
     uint32_t c = (kFinalSmemBytes / 8) / (2 * rows) - 2;
@@ -322,6 +329,8 @@ __host__ __device__ inline void final_tiling(uint32_t n, uint32_t S, uint32_t Nt
 __global__ void final_list_kernel(RunDev* runs, int mode, uint64_t* items, uint32_t* count, uint32_t capacity,
                                   int* status);
 __global__ void final_exact_kernel(RunDev* runs, const uint64_t* items, const uint32_t* count, int mode);
+// members per packed tile of the exact pass, at least
+constexpr uint32_t kExactMinMembers = 8;
 // status value of a final item list that would have overflowed
 constexpr int kStatusFinalList = 3;
 

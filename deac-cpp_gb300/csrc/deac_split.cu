@@ -927,12 +927,30 @@ __device__ __forceinline__ void split_select_body(RunDev* runs, SplitRun* split,
         const bool idle = nre == 0 && !force_exact;
         R.exact_idle = idle ? 1 : 0;
         if (!idle) {
-            // list both passes of every tile of this run for the exact pass
-            const uint32_t n = R.contract_ctas;
-            const uint32_t base = atomicAdd(R.exact_count, 2 * n);
-            for (uint32_t k = 0; k < 2 * n; ++k) {
-                const uint64_t pass = k >= n ? 1u : 0u;
-                R.exact_list[base + k] = ((uint64_t)wk.run << 32) | (pass << 31) | (pass ? k - n : k);
+            // list both passes of the run for the exact pass: tiles packed
+            // with the members left open (ascending), so that the FP64
+            // chains run on them alone -- or, with none left open (a run that
+            // keeps the exact pass for its statistics), the run's own tiles,
+            // whose last CTA does the bookkeeping
+            uint32_t n = 0;
+            for (uint32_t m = 0; m < P; ++m)
+                if (*reinterpret_cast<const volatile uint8_t*>(X.recheck + m)) R.final_members[n++] = m;
+            uint32_t ctas = R.contract_ctas, packed = 0;
+            if (n) {
+                uint32_t mt, tt, chunk;
+                final_tiling(n, S, R.Nt, mt, tt, chunk, ctas, kExactMinMembers);
+                R.final_n = n;
+                R.final_mt = mt;
+                R.final_tt = tt;
+                R.final_chunk = chunk;
+                R.final_ctas = ctas;
+                packed = 1;
+            }
+            const uint32_t base = atomicAdd(R.exact_count, 2 * ctas);
+            for (uint32_t k = 0; k < 2 * ctas; ++k) {
+                const uint64_t pass = k >= ctas ? 1u : 0u;
+                R.exact_list[base + k] =
+                    ((uint64_t)wk.run << 32) | (pass << 31) | ((uint64_t)packed << 30) | (pass ? k - ctas : k);
             }
         }
         if (idle) {
