@@ -538,8 +538,7 @@ def engine_arm(args, world, rank, local):
     roof["traffic"] = traffic
     if traffic is not None:
         roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the first 64 "
-                                  "runs, scaled by " + ("genes" if dominant == 0 else "products") +
-                                  " (profiles/*_cfg3_64runs.md)")
+                                  "runs, scaled by " + ("genes" if dominant == 0 else "products"))
     roof["per_generation_us"] = {KERNEL_NAMES[k]: round(v, 1) for k, v in per_gen_us.items()}
 
     # end to end through the public API with host buffers: create + add runs
