@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
             const uint32_t row0 = (warp - c * G) * RW;
             const uint32_t jc = c * kChunk;                             // the chunk's first gene in the item
             const uint32_t halves = len - jc < (uint32_t)kChunk ? 1u : 2u;  // 32-gene halves of the chunk
+            const bool first_chunk = j0 + jc == 0;  // holds gene 0
             const double* par = slice_s + (uint64_t)st * kSliceStageDoubles;
             const uint64_t PM = (uint64_t)P * M;
             const uint64_t key_x = T.key_x;
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                 const double* px = par + (uint64_t)row * S * L;
                 double* dst = T.pop + (uint64_t)(1u - T.cur[row]) * S * PM + (uint64_t)row * M + j0;
                 const uint64_t pos0 = (T.step[row] * P + row) * S;
-                int em = -2000;
+                uint32_t ef_max = 0;
                 bool mt = false;
                 double z = 0.0;  // side 0's gene 0 (lane 0 of the first half)
                 // (both sides unrolled: their loads, draws and FMAs overlap)
@@ -257,15 +258,16 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                     const uint64_t w0 = key_x + ((pos0 + s) * M + j0 + jc + 1) * kGamma + lane_gamma;
                     // both 32-gene halves at once (independent loads, draws
                     // and FMAs in flight)
+                    // (a 32-gene last chunk reads the stage's stale second
+                    // half too: inside the staged row, and never used)
                     double x[2], a[2], b[2], cc[2];
 #pragma unroll
                     for (uint32_t h = 0; h < 2; ++h) {
                         const uint32_t o = s * L + jc + h * 32 + lane;
-                        const bool in = h < halves;
-                        x[h] = in ? px[o] : 0.0;
-                        a[h] = in ? pa[o] : 0.0;
-                        b[h] = in ? pb[o] : 0.0;
-                        cc[h] = in ? pc[o] : 0.0;
+                        x[h] = px[o];
+                        a[h] = pa[o];
+                        b[h] = pb[o];
+                        cc[h] = pc[o];
                     }
 #pragma unroll
                     for (uint32_t h = 0; h < 2; ++h) {
@@ -278,15 +280,17 @@ __global__ void __launch_bounds__(kSliceThreads, 1)
                             if (!keep_sign) v = abs_bits(v);
                             mt = true;
                         }
-                        if (j0 + jl == 0) {
+                        if (first_chunk && h == 0 && lane == 0) {
                             if (s == 0) z = v;
                             else v = z;  // gpu_match_population_zero
                         }
                         st_keep_l1(dst + (uint64_t)s * PM + jl, v);
-                        em = max(em, exp_of(v));
+                        // the exponent field of |v| (0: zero or subnormal)
+                        ef_max = max(ef_max, ((uint32_t)__double2hiint(v) >> 20) & 0x7FFu);
                     }
                 }
-                em = __reduce_max_sync(0xffffffffu, em);
+                ef_max = __reduce_max_sync(0xffffffffu, ef_max);
+                const int em = ef_max == 0 ? -2000 : (int)ef_max - 1023;  // as exp_of
                 mt = __any_sync(0xffffffffu, mt);
                 if (lane / LR == mm) {
                     my_e = em;
