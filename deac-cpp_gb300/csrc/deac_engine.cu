@@ -622,7 +622,9 @@ void prepare_start(RunHost& r, int32_t streams) {
 void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
     const uint64_t P = r.P, S = (uint64_t)r.S;
     const deac::Model& m = r.model;
-    std::memset(img, 0, L.o_pop);
+    // (only the data, the weight rows a run has and the initial CR / F and
+    // 1/sigma are copied: the arena is zeroed on the device)
+    std::memset(img, 0, L.o_np);
     auto put = [&](uint64_t off, const std::vector<double>& v) {
         if (!v.empty()) std::memcpy(img + off, v.data(), v.size() * 8);
     };
@@ -698,7 +700,16 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
     r.arena_bytes = L.size;
     char* base = r.arena;
     const bool counter = b->streams == DEAC_STREAMS_COUNTER;
-    CUDA_TRY(copy_async(b, base, img, o_pop, cudaMemcpyHostToDevice, b->stream));
+    // the ISF, its errors and the tau weights, then each weight row the run
+    // has (an absent one stays zero: the pool was zeroed on the device)
+    CUDA_TRY(copy_async(b, base, img, o_np, cudaMemcpyHostToDevice, b->stream));
+    const std::pair<uint64_t, const std::vector<double>*> rows_present[] = {
+        {o_np, &m.norm_pos}, {o_nn, &m.norm_neg}, {o_fp, &m.first_pos},
+        {o_fn, &m.first_neg}, {o_tp, &m.third_pos}, {o_tn, &m.third_neg}};
+    for (const auto& rp : rows_present)
+        if (!rp.second->empty())
+            CUDA_TRY(copy_async(b, base + rp.first, img + rp.first, rp.second->size() * 8, cudaMemcpyHostToDevice,
+                                b->stream));
     const char* crfw = img + o_pop;
     CUDA_TRY(copy_async(b, base + o_cr, crfw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice, b->stream));
     CUDA_TRY(copy_async(b, base + o_fw, crfw + (uint64_t)S * P * 8, (uint64_t)S * P * 8, cudaMemcpyHostToDevice,
@@ -1249,18 +1260,26 @@ int deac_batch_setup(deac_batch* b) {
         // its rows spread over the host's threads
         std::map<std::string, RunHost*> owners;
         for (auto& rp : b->runs) owners.emplace(kernel_key(*rp), rp.get());
+        // blocks of 8 rows of every matrix, taken from one list by all the
+        // host's threads
+        std::vector<std::pair<RunHost*, uint64_t>> blocks;
         for (auto& kv : owners) {
             RunHost& r = *kv.second;
             r.model.k_pos.assign(r.Nt * r.M, 0.0);
             if (r.S == 2) r.model.k_neg.assign(r.Nt * r.M, 0.0);
-            const uint64_t per = (r.Nt + hw - 1) / hw;
-            pool.clear();
-            for (uint64_t i0 = 0; i0 < r.Nt; i0 += per)
-                pool.emplace_back([&r, i0, per] {
-                    deac::kernel_rows(r.cfg, r.model, r.tau.data(), r.freq.data(), r.M, i0, std::min(r.Nt, i0 + per));
-                });
-            for (auto& th : pool) th.join();
+            for (uint64_t i0 = 0; i0 < r.Nt; i0 += 8) blocks.emplace_back(&r, i0);
         }
+        std::atomic<size_t> next{0};
+        pool.clear();
+        for (unsigned t = 0; t < hw && t < blocks.size(); ++t)
+            pool.emplace_back([&blocks, &next] {
+                for (size_t k; (k = next.fetch_add(1)) < blocks.size();) {
+                    RunHost& r = *blocks[k].first;
+                    const uint64_t i0 = blocks[k].second;
+                    deac::kernel_rows(r.cfg, r.model, r.tau.data(), r.freq.data(), r.M, i0, std::min(r.Nt, i0 + 8));
+                }
+            });
+        for (auto& th : pool) th.join();
     }
     for (auto& r : b->runs)
         r->n_states = b->streams == DEAC_STREAMS_COUNTER ? r->P : r->P * (1 + (uint64_t)r->S * r->M);
