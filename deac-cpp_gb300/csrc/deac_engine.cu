@@ -177,6 +177,7 @@ struct deac_batch {
     uint64_t* d_final_items = nullptr;       // their items and its length
     uint32_t* d_final_count = nullptr;
     uint32_t final_capacity = 0;
+    bool combine_wide = false;               // split_combine_wide_kernel sums the partials
     uint64_t* d_exact_list = nullptr;        // split engine: the exact pass's items
     uint32_t* d_exact_count = nullptr;
     uint32_t n_combine_tiles = 0;            // tiles split over several contraction CTAs
@@ -260,6 +261,21 @@ void launch(void (*kernel)(Params...), uint32_t grid, uint32_t block, size_t sme
     cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
 }
 
+// The partial sums of the split tiles: a thread per output when no tile is
+// split over more than kCombineWideSplits CTAs, else warps sharing the splits.
+void launch_combine(deac_batch* b, cudaStream_t s, bool early) {
+    const deac::SplitTile* tiles = b->d_tiles;
+    const uint32_t* ct = b->d_combine_tiles;
+    const deac::SplitRow* rows = b->d_rows;
+    const float4* partial = b->d_partial;
+    if (b->combine_wide)
+        launch(deac::split_combine_wide_kernel, b->n_combine_tiles * deac::kCombineWideCtasPerTile, 256, 0, s, early,
+               b->d_runs, b->d_split, tiles, ct, rows, partial);
+    else
+        launch(deac::split_combine_kernel, b->n_combine_tiles * deac::kCombineCtasPerTile, 256, 0, s, early,
+               b->d_runs, b->d_split, tiles, ct, rows, partial);
+}
+
 void launch_contract(deac_batch* b, cudaStream_t s, int mode, bool early = false) {
     if (mode == deac::kModeRecheck) {
         // the listed items, over at most one CTA per SM (one fits per SM)
@@ -339,11 +355,7 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     if ((rc = mark(3))) return rc;
     // not scheduled early: its waiting CTAs would hold the SMs that the
     // normalisation row sums need
-    if (b->n_combine_tiles)
-        launch(deac::split_combine_kernel, b->n_combine_tiles * deac::kCombineCtasPerTile, 256, 0, s, early && !fork,
-               b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
-               static_cast<const uint32_t*>(b->d_combine_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
-               static_cast<const float4*>(b->d_partial));
+    if (b->n_combine_tiles) launch_combine(b, s, early && !fork);
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     if (b->any_defer)
         deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
@@ -391,11 +403,7 @@ int launch_split_init(deac_batch* b) {
            b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
            static_cast<const deac::SplitWork*>(b->d_split_work), static_cast<const deac::SplitRow*>(b->d_rows),
            static_cast<const CUtensorMap*>(b->d_maps), b->d_partial, b->d_status);
-    if (b->n_combine_tiles)
-        launch(deac::split_combine_kernel, b->n_combine_tiles * deac::kCombineCtasPerTile, 256, 0, s, false,
-               b->d_runs, b->d_split, static_cast<const deac::SplitTile*>(b->d_tiles),
-               static_cast<const uint32_t*>(b->d_combine_tiles), static_cast<const deac::SplitRow*>(b->d_rows),
-               static_cast<const float4*>(b->d_partial));
+    if (b->n_combine_tiles) launch_combine(b, s, false);
     deac::split_init_kernel<<<b->n_trial_ctas, deac::kInitThreads, 0, s>>>(b->d_runs, b->d_split, b->d_trial_work);
     launch_contract(b, s, deac::kModeInit);
     deac::jde_kernel<<<(b->n_trial_ctas + 127) / 128, 128, 0, s>>>(
@@ -1057,7 +1065,7 @@ int build_split_work(deac_batch* b) {
     const uint64_t target = std::max<uint64_t>(1, (total + ctas - 1) / ctas);
     std::vector<deac::SplitWork> work;
     std::vector<uint32_t> combine_tiles;
-    uint32_t blocks = 0;
+    uint32_t blocks = 0, max_split = 1;
     for (uint32_t t = 0; t < tiles.size(); ++t) {
         const uint32_t C = tile_chunks[t];
         const uint32_t want = (uint32_t)std::min<uint64_t>(C, (C + target - 1) / target);
@@ -1069,7 +1077,9 @@ int build_split_work(deac_batch* b) {
         for (uint32_t c0 = 0; c0 < C; c0 += per)
             work.push_back({t, c0, std::min(C, c0 + per), nsplit > 1 ? blocks++ : ~0u});
         if (nsplit > 1) combine_tiles.push_back(t);
+        max_split = std::max(max_split, nsplit);
     }
+    b->combine_wide = max_split <= deac::kCombineWideSplits;
     // longest pieces first: the block scheduler hands CTAs out in index
     // order, so this is longest-processing-time-first over the SMs
     std::stable_sort(work.begin(), work.end(), [](const deac::SplitWork& a, const deac::SplitWork& b2) {

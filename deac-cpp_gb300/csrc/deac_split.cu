@@ -615,6 +615,37 @@ __global__ void __launch_bounds__(256) split_combine_kernel(RunDev* runs, SplitR
     store_estimate(R, X, rw, t, tile, hi, lo, b);
 }
 
+// The same sums for batches whose tiles are split over at most
+// kCombineWideSplits CTAs: a thread per output adds its tile's partial
+// sums in order (no warp has to share the splits), 256 outputs a CTA.
+__global__ void __launch_bounds__(256) split_combine_wide_kernel(RunDev* runs, SplitRun* split,
+                                                                 const SplitTile* tiles,
+                                                                 const uint32_t* combine_tiles,
+                                                                 const SplitRow* rows, const float4* partial) {
+    grid_dependency_wait();
+    const SplitTile tile = tiles[combine_tiles[blockIdx.x / kCombineWideCtasPerTile]];
+    const uint32_t idx = (blockIdx.x % kCombineWideCtasPerTile) * 256 + threadIdx.x;
+    const uint32_t r = idx / kTauTile, tl = idx % kTauTile;
+    if (r >= tile.rows) return;
+    float hi = 0.0f, lo = 0.0f, b = 0.0f;
+    const float4* p = partial + (uint64_t)tile.block0 * kPartialBlock + idx;
+    float4 v[kCombineWideSplits];
+#pragma unroll
+    for (uint32_t u = 0; u < kCombineWideSplits; ++u)
+        v[u] = u < tile.nsplit ? p[(uint64_t)u * kPartialBlock] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (uint32_t u = 0; u < kCombineWideSplits; ++u) {
+        dw_add(hi, lo, v[u].x, v[u].y);
+        b += v[u].z;
+    }
+    const SplitRow rw = rows[tile.first_row + r];
+    const RunDev& R = runs[rw.run];
+    SplitRun& X = split[rw.run];
+    const uint32_t t = tile.tau0 + tl;
+    if (R.done || t >= R.Nt) return;
+    store_estimate(R, X, rw, t, tile, hi, lo, b);
+}
+
 // ------------------------------------------------- chi^2 and its interval
 // One timeslice's term of chi^2 from the estimate em (of the raw trial when
 // `defer`, to be scaled by rc = 1/norm) with its bound eb0, and of the bound

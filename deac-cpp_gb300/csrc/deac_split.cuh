@@ -153,6 +153,13 @@ __global__ void split_init_kernel(RunDev* runs, SplitRun* split, const Work* wor
 __global__ void k_digits_kernel(const double* kp, const double* kn, uint32_t Nt, uint32_t M, uint16_t* kdig,
                                 int16_t* kexp, int16_t* kexp_max);
 constexpr int kCombineCtasPerTile = (int)(kPartialBlock / 32);  // 32 outputs per CTA
+// split_combine_wide_kernel: tiles split over at most this many CTAs, 256
+// outputs per CTA
+constexpr uint32_t kCombineWideSplits = 8;
+constexpr int kCombineWideCtasPerTile = (int)(kPartialBlock / 256);
+__global__ void split_combine_wide_kernel(RunDev* runs, SplitRun* split, const SplitTile* tiles,
+                                          const uint32_t* combine_tiles, const SplitRow* rows,
+                                          const float4* partial);
 
 // ---- digit slicing of one value (shared by trial_kernel and the host)
 // exponent field of |v| (unbiased), or -2000 for zero / subnormal.  The
