@@ -357,12 +357,15 @@ int launch_generation(deac_batch* b, cudaStream_t s, int init_mode, bool timed =
     // normalisation row sums need
     if (b->n_combine_tiles) launch_combine(b, s, early && !fork);
     if (fork) CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
+    // (scheduled early behind the contraction or the combine: the selection
+    // waits for them in its first instruction)
+    const deac::Work* tw = static_cast<const deac::Work*>(b->d_trial_work);
     if (b->any_defer)
-        deac::split_select_kernel<<<b->n_trial_ctas, deac::kSelectThreads, 0, s>>>(b->d_runs, b->d_split,
-                                                                                   b->d_trial_work);
+        launch(deac::split_select_kernel, b->n_trial_ctas, deac::kSelectThreads, 0, s, early && !fork, b->d_runs,
+               b->d_split, tw);
     else
-        deac::split_select_lean_kernel<<<b->n_trial_ctas, deac::kSelectLeanThreads, 0, s>>>(b->d_runs, b->d_split,
-                                                                                            b->d_trial_work);
+        launch(deac::split_select_lean_kernel, b->n_trial_ctas, deac::kSelectLeanThreads, 0, s, early && !fork,
+               b->d_runs, b->d_split, tw);
     if ((rc = mark(4))) return rc;
     launch_contract(b, s, deac::kModeRecheck, early);
     return mark(1);
