@@ -552,10 +552,7 @@ void prepare_model(RunHost& r) {
 struct ArenaLayout {
     uint64_t o_isf, o_err, o_tw, o_np, o_nn, o_fp, o_fn, o_tp, o_tn, o_pop, o_cur, o_rng, o_cr, o_fw, o_fo, o_fnw,
         o_E, o_E2, o_mom, o_stats, o_trace, size;
-    // bytes of the host image copied to the device: everything before the
-    // population, then the initial CR and F (the population is drawn on the
-    // device), then 1/sigma for the split engine's decisions
-    uint64_t pop_bytes, image_bytes;
+    uint64_t pop_bytes;  // bytes of one population buffer (S P M doubles)
 };
 
 ArenaLayout arena_layout(const RunHost& r) {
@@ -576,7 +573,6 @@ ArenaLayout arena_layout(const RunHost& r) {
     L.o_trace = a.take(std::max<uint64_t>(r.trace_cap * P * 8, 8));
     L.size = a.size;
     L.pop_bytes = (uint64_t)S * P * M * 8;
-    L.image_bytes = L.o_pop + 2ull * S * P * 8 + Nt * 8;
     return L;
 }
 
@@ -627,14 +623,41 @@ void prepare_start(RunHost& r, int32_t streams) {
     for (int w = 0; w < 4; ++w) r.rng_start[w] = v[w];
 }
 
-// The host image of a run's arena (pinned; ArenaLayout::image_bytes): the
-// inputs and the constant terms before the population, then the initial
-// CR / F and 1/sigma.
-void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
+// A run's host image, what crosses the bus at set-up (the arena is zeroed on
+// the device): the ISF, its errors and the tau weights at their arena
+// offsets ([0, o_np)), then packed: each weight row the run has, the
+// initial CR / F and 1/sigma.
+struct ImageLayout {
+    uint64_t rows[6];  // norm +/-, first moment +/-, third moment +/- (~0: absent)
+    uint64_t crfw, ie, size;
+};
+
+const std::vector<double>* weight_rows(const RunHost& r, int k) {
+    const deac::Model& m = r.model;
+    const std::vector<double>* v[6] = {&m.norm_pos, &m.norm_neg, &m.first_pos, &m.first_neg, &m.third_pos,
+                                       &m.third_neg};
+    return v[k];
+}
+
+ImageLayout image_layout(const RunHost& r, const ArenaLayout& L) {
+    ImageLayout I;
+    uint64_t o = L.o_np;
+    for (int k = 0; k < 6; ++k) {
+        const std::vector<double>& v = *weight_rows(r, k);
+        I.rows[k] = v.empty() ? ~0ull : o;
+        if (!v.empty()) o += (v.size() * 8 + 15) / 16 * 16;
+    }
+    I.crfw = o;
+    o += 2ull * r.S * r.P * 8;
+    I.ie = o;
+    o += r.Nt * 8;
+    I.size = (o + 255) / 256 * 256;
+    return I;
+}
+
+void fill_image(RunHost& r, const ArenaLayout& L, const ImageLayout& I, int32_t streams, char* img) {
     const uint64_t P = r.P, S = (uint64_t)r.S;
     const deac::Model& m = r.model;
-    // (only the data, the weight rows a run has and the initial CR / F and
-    // 1/sigma are copied: the arena is zeroed on the device)
     std::memset(img, 0, L.o_np);
     auto put = [&](uint64_t off, const std::vector<double>& v) {
         if (!v.empty()) std::memcpy(img + off, v.data(), v.size() * 8);
@@ -642,20 +665,16 @@ void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
     put(L.o_isf, r.isf);
     put(L.o_err, r.err);
     put(L.o_tw, m.tau_weight);
-    put(L.o_np, m.norm_pos);
-    put(L.o_nn, m.norm_neg);
-    put(L.o_fp, m.first_pos);
-    put(L.o_fn, m.first_neg);
-    put(L.o_tp, m.third_pos);
-    put(L.o_tn, m.third_neg);
+    for (int k = 0; k < 6; ++k)
+        if (I.rows[k] != ~0ull) put(I.rows[k], *weight_rows(r, k));
     prepare_start(r, streams);
-    double* crfw = reinterpret_cast<double*>(img + L.o_pop);
+    double* crfw = reinterpret_cast<double*>(img + I.crfw);
     for (uint64_t k = 0; k < S * P; ++k) {
         crfw[k] = r.cfg.crossover_probability;
         crfw[S * P + k] = r.cfg.differential_weight;
     }
     // 1/sigma as the split engine's decisions use it (one rounding each)
-    double* ie = crfw + 2 * S * P;
+    double* ie = reinterpret_cast<double*>(img + I.ie);
     for (uint64_t t = 0; t < r.Nt; ++t) ie[t] = 1.0 / r.err[t];
 }
 
@@ -663,6 +682,7 @@ void fill_image(RunHost& r, const ArenaLayout& L, int32_t streams, char* img) {
 // copies are asynchronous on the batch stream: the image stays untouched
 // until the stream has been synchronised).
 int upload_run(deac_batch* b, RunHost& r, const char* img) {
+    const ImageLayout I = image_layout(r, arena_layout(r));
     const uint64_t P = r.P, M = r.M, Nt = r.Nt, N = r.cfg.number_of_generations;
     const int S = r.S;
     const deac::Model& m = r.model;
@@ -714,14 +734,12 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
     // the ISF, its errors and the tau weights, then each weight row the run
     // has (an absent one stays zero: the pool was zeroed on the device)
     CUDA_TRY(copy_async(b, base, img, o_np, cudaMemcpyHostToDevice, b->stream));
-    const std::pair<uint64_t, const std::vector<double>*> rows_present[] = {
-        {o_np, &m.norm_pos}, {o_nn, &m.norm_neg}, {o_fp, &m.first_pos},
-        {o_fn, &m.first_neg}, {o_tp, &m.third_pos}, {o_tn, &m.third_neg}};
-    for (const auto& rp : rows_present)
-        if (!rp.second->empty())
-            CUDA_TRY(copy_async(b, base + rp.first, img + rp.first, rp.second->size() * 8, cudaMemcpyHostToDevice,
-                                b->stream));
-    const char* crfw = img + o_pop;
+    const uint64_t row_offsets[6] = {o_np, o_nn, o_fp, o_fn, o_tp, o_tn};
+    for (int k = 0; k < 6; ++k)
+        if (I.rows[k] != ~0ull)
+            CUDA_TRY(copy_async(b, base + row_offsets[k], img + I.rows[k], weight_rows(r, k)->size() * 8,
+                                cudaMemcpyHostToDevice, b->stream));
+    const char* crfw = img + I.crfw;
     CUDA_TRY(copy_async(b, base + o_cr, crfw, (uint64_t)S * P * 8, cudaMemcpyHostToDevice, b->stream));
     CUDA_TRY(copy_async(b, base + o_fw, crfw + (uint64_t)S * P * 8, (uint64_t)S * P * 8, cudaMemcpyHostToDevice,
                         b->stream));
@@ -837,8 +855,7 @@ int upload_run(deac_batch* b, RunHost& r, const char* img) {
         x.t_hi = reinterpret_cast<double*>(sb + o_th);
         x.counts = reinterpret_cast<unsigned long long*>(sb + o_cnt);
         // 1/sigma as the decisions use it, from the image
-        CUDA_TRY(copy_async(b, sb + o_ie, img + o_pop + 2ull * S * P * 8, Nt * 8, cudaMemcpyHostToDevice,
-                            b->stream));
+        CUDA_TRY(copy_async(b, sb + o_ie, img + I.ie, Nt * 8, cudaMemcpyHostToDevice, b->stream));
         x.inv_err = reinterpret_cast<const double*>(sb + o_ie);
         x.inv_nt = 1.0 / (double)Nt;
         d.changed = x.changed;
@@ -1337,34 +1354,35 @@ int deac_batch_setup(deac_batch* b) {
     }
     uint64_t trial_doubles = 0, contract_bytes = std::max<uint64_t>(kTailSlotsBytes, deac::kContractMinSmemBytes);
     std::vector<deac::Work> tw, cw;
-    // pinned host images, one per host thread: a window of runs is drawn in
-    // parallel straight into them, then copied asynchronously (the next
-    // window waits for the copies)
-    uint64_t image_max = 0;
-    for (auto& rp : b->runs) image_max = std::max(image_max, arena_layout(*rp).image_bytes);
-    const uint32_t window = std::min<uint32_t>(hw, (uint32_t)b->runs.size());
-    std::vector<char*> images(window, nullptr);
+    // every run's host image in one pinned buffer, filled by all the host's
+    // threads, then copied asynchronously run by run
+    std::vector<uint64_t> image_off(b->runs.size() + 1, 0);
+    for (size_t k = 0; k < b->runs.size(); ++k)
+        image_off[k + 1] = image_off[k] + image_layout(*b->runs[k], arena_layout(*b->runs[k])).size;
+    char* images = nullptr;
     struct PinnedFree {
-        std::vector<char*>* v;
+        char** p;
         ~PinnedFree() {
-            for (char* p : *v)
-                if (p) cudaFreeHost(p);
+            if (*p) cudaFreeHost(*p);
         }
     } pinned_free{&images};
-    for (auto& p : images) CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&p), image_max));
+    CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&images), std::max<uint64_t>(image_off.back(), 256)));
+    {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < hw && t < b->runs.size(); ++t)
+            pool.emplace_back([b, &next, &image_off, images] {
+                for (size_t k; (k = next.fetch_add(1)) < b->runs.size();) {
+                    RunHost& rk = *b->runs[k];
+                    const ArenaLayout L = arena_layout(rk);
+                    fill_image(rk, L, image_layout(rk, L), b->streams, images + image_off[k]);
+                }
+            });
+        for (auto& th : pool) th.join();
+    }
     for (uint32_t ri = 0; ri < b->runs.size(); ++ri) {
         RunHost& r = *b->runs[ri];
-        if (ri % window == 0) {
-            CUDA_TRY(cudaStreamSynchronize(b->stream));  // the window before has been copied
-            std::vector<std::thread> pool;
-            for (uint32_t k = ri; k < b->runs.size() && k < ri + window; ++k)
-                pool.emplace_back([b, k, ri, &images] {
-                    RunHost& rk = *b->runs[k];
-                    fill_image(rk, arena_layout(rk), b->streams, images[k - ri]);
-                });
-            for (auto& th : pool) th.join();
-        }
-        int rc = upload_run(b, r, images[ri % window]);
+        int rc = upload_run(b, r, images + image_off[ri]);
         if (rc) return rc;
         for (uint32_t i = 0; i < r.dev.P; ++i) tw.push_back({ri, i});
         for (uint32_t k = 0; k < r.dev.contract_ctas; ++k) cw.push_back({ri, k});
